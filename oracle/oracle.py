@@ -1,0 +1,294 @@
+"""ctypes binding of the CPU oracle (oracle/wt_oracle.c) and of the
+reference-built WT() libraries (oracle/_ref/).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by the smoke entry and by the
+benchmark's CPU-baseline leg, always as the checker or the timed CPU
+baseline -- never as the product path.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+REF_DIR = os.path.join(HERE, "_ref")
+
+u64 = ctypes.c_uint64
+vp = ctypes.c_void_p
+NONE = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+
+def build(ref=True):
+    """Compile the oracle (and, when the reference checkout exists, the
+    reference's own builders into _ref/)."""
+    subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+    if ref and os.path.isdir("/root/reference"):
+        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build(ref=False)
+        L = ctypes.CDLL(LIB_PATH)
+        L.or_log2_up.argtypes = [u64]
+        L.or_hi.argtypes = [u64]
+        L.or_levels_for_sigma.argtypes = [u64]
+        L.or_wt_levelwt.argtypes = [vp, ctypes.c_int, u64, ctypes.c_int, vp, vp, u64]
+        L.or_wt_serial.argtypes = [vp, ctypes.c_int, u64, ctypes.c_int, vp, vp, u64]
+        L.or_remap_alphabet.argtypes = [vp, ctypes.c_int, u64]
+        L.or_remap_alphabet.restype = u64
+        L.or_rank_words.argtypes = [u64]
+        L.or_rank_words.restype = u64
+        L.or_rank_build.argtypes = [vp, u64, vp]
+        L.or_rank1.argtypes = [vp, vp, u64]
+        L.or_rank1.restype = u64
+        L.or_select_new.argtypes = [vp, u64, ctypes.c_int, ctypes.c_int]
+        L.or_select_new.restype = vp
+        L.or_select_info.argtypes = [vp, vp]
+        L.or_select_copy.argtypes = [vp, vp, vp, vp]
+        L.or_select_query.argtypes = [vp, vp, u64]
+        L.or_select_query.restype = u64
+        L.or_select_batch.argtypes = [vp, vp, vp, u64, vp]
+        L.or_select_free.argtypes = [vp]
+        L.or_wt_access.argtypes = [vp, vp, u64, ctypes.c_int, u64]
+        L.or_wt_access.restype = u64
+        L.or_wt_rank.argtypes = [vp, vp, u64, ctypes.c_int, u64, u64]
+        L.or_wt_rank.restype = u64
+        L.or_wt_inverse_select.argtypes = [vp, vp, u64, ctypes.c_int, u64, vp]
+        L.or_wt_inverse_select.restype = u64
+        L.or_wt_select.argtypes = [vp, vp, vp, vp, u64, ctypes.c_int, u64, u64]
+        L.or_wt_select.restype = u64
+        L.or_wt_access_batch.argtypes = [vp, vp, u64, ctypes.c_int, vp, u64, vp]
+        L.or_wt_rank_batch.argtypes = [vp, vp, u64, ctypes.c_int, vp, vp, u64, vp]
+        L.or_num_threads.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None else None
+
+
+def num_threads():
+    return lib().or_num_threads()
+
+
+def levels_for_sigma(sigma):
+    return lib().or_levels_for_sigma(int(sigma))
+
+
+def log2_up(x):
+    return lib().or_log2_up(int(x))
+
+
+def hi(x):
+    return lib().or_hi(int(x))
+
+
+def wt_words(n, levels):
+    return (n * levels + 63) // 64
+
+
+def wt_build(sym, levels, n_nodes=None, serial=False):
+    """levelWT (or serialWT) build. Returns (words u64[], nodes u64[n_nodes,5] or None)."""
+    sym = np.ascontiguousarray(sym)
+    n = sym.size
+    words = np.zeros(max(wt_words(n, levels), 1), dtype=np.uint64)
+    nodes = None
+    if n_nodes:
+        nodes = np.zeros((n_nodes, 5), dtype=np.uint64)
+    fn = lib().or_wt_serial if serial else lib().or_wt_levelwt
+    rc = fn(_p(sym), sym.dtype.itemsize, n, levels, _p(words), _p(nodes), n_nodes or 0)
+    if rc != 0:
+        raise RuntimeError(f"oracle wt build failed rc={rc}")
+    return words[: wt_words(n, levels)], nodes
+
+
+def remap_alphabet(sym):
+    s = np.array(sym, copy=True)
+    sigma = lib().or_remap_alphabet(_p(s), s.dtype.itemsize, s.size)
+    return s, int(sigma)
+
+
+def rank_build(words, size_bits):
+    words = np.ascontiguousarray(words, dtype=np.uint64)
+    tbl = np.zeros(lib().or_rank_words(size_bits), dtype=np.uint64)
+    lib().or_rank_build(_p(words), size_bits, _p(tbl))
+    return tbl
+
+
+def rank1(tbl, words, idx):
+    return lib().or_rank1(_p(tbl), _p(words), int(idx))
+
+
+class Select:
+    """select_support_mcl<t_b> built by the oracle, in the flat packed layout."""
+
+    def __init__(self, words, size_bits, t_b, rule=0):
+        self.words = np.ascontiguousarray(words, dtype=np.uint64)
+        self.h = lib().or_select_new(_p(self.words), size_bits, t_b, rule)
+        info = np.zeros(8, dtype=np.uint64)
+        lib().or_select_info(self.h, _p(info))
+        (self.size, self.arg_cnt, self.logn, self.logn4, self.nsb, self.has_long,
+         self.sb_nwords, self.pool_nwords) = [int(x) for x in info]
+        self.sb_words = np.zeros(max(self.sb_nwords, 1), dtype=np.uint64)
+        self.desc = np.zeros(max(self.nsb, 1), dtype=np.uint64)
+        self.pool = np.zeros(max(self.pool_nwords, 1), dtype=np.uint64)
+        lib().or_select_copy(self.h, _p(self.sb_words), _p(self.desc), _p(self.pool))
+        self.sb_words = self.sb_words[: self.sb_nwords]
+        self.desc = self.desc[: self.nsb]
+        self.pool = self.pool[: self.pool_nwords]
+
+    def query(self, i):
+        return lib().or_select_query(self.h, _p(self.words), int(i))
+
+    def query_batch(self, q):
+        q = np.ascontiguousarray(q, dtype=np.uint64)
+        out = np.zeros(q.size, dtype=np.uint64)
+        lib().or_select_batch(self.h, _p(self.words), _p(q), q.size, _p(out))
+        return out
+
+    def __del__(self):
+        try:
+            if self.h:
+                lib().or_select_free(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+
+def wt_access(tree, rtbl, n, levels, idx):
+    idx = np.ascontiguousarray(idx, dtype=np.uint64)
+    out = np.zeros(idx.size, dtype=np.uint64)
+    lib().or_wt_access_batch(_p(tree), _p(rtbl), n, levels, _p(idx), idx.size, _p(out))
+    return out
+
+
+def wt_rank(tree, rtbl, n, levels, idx, sym):
+    idx = np.ascontiguousarray(idx, dtype=np.uint64)
+    sym = np.ascontiguousarray(sym, dtype=np.uint64)
+    out = np.zeros(idx.size, dtype=np.uint64)
+    lib().or_wt_rank_batch(_p(tree), _p(rtbl), n, levels, _p(idx), _p(sym), idx.size, _p(out))
+    return out
+
+
+def wt_inverse_select(tree, rtbl, n, levels, i):
+    c = ctypes.c_uint64(0)
+    r = lib().or_wt_inverse_select(_p(tree), _p(rtbl), n, levels, int(i), ctypes.byref(c))
+    return int(r), int(c.value)
+
+
+def wt_select(tree, rtbl, sel1, sel0, n, levels, i, c):
+    return lib().or_wt_select(_p(tree), _p(rtbl), ctypes.c_void_p(sel1.h), ctypes.c_void_p(sel0.h),
+                              n, levels, int(i), int(c))
+
+
+# ---------------------------------------------------------------- reference
+
+_ref_libs = {}
+
+
+def ref_available(variant="levelwt_u8"):
+    return os.path.exists(os.path.join(REF_DIR, f"libref_{variant}.so"))
+
+
+def ref_wt(sym, sigma, variant="levelwt_u8"):
+    """The reference's own WT(s, n, sigma) (built from its sources into _ref/).
+    Returns (words u64[], nodes as a structured u32/u64 array [2*sigma,5])."""
+    if variant not in _ref_libs:
+        L = ctypes.CDLL(os.path.join(REF_DIR, f"libref_{variant}.so"))
+        L.ref_wt.argtypes = [vp, u64, u64, vp, u64, vp]
+        _ref_libs[variant] = L
+    L = _ref_libs[variant]
+    sb, ub = L.ref_symbol_bytes(), L.ref_uint_bytes()
+    sym = np.ascontiguousarray(sym, dtype={1: np.uint8, 4: np.uint32, 8: np.uint64}[sb])
+    n = sym.size
+    levels = levels_for_sigma(sigma)
+    nw = wt_words(n, levels)
+    words = np.zeros(max(nw, 1), dtype=np.uint64)
+    nodes = np.zeros((2 * sigma, 5), dtype=np.uint32 if ub == 4 else np.uint64)
+    rc = L.ref_wt(_p(sym), n, sigma, _p(words), nw, _p(nodes))
+    if rc != 0:
+        raise RuntimeError("reference WT failed")
+    return words[:nw], nodes
+
+
+def reachable_nodes(nodes, none_value):
+    """Heap ids reachable from the root through the child links."""
+    seen = []
+    stack = [0]
+    while stack:
+        h = stack.pop()
+        seen.append(h)
+        for c in (int(nodes[h, 3]), int(nodes[h, 4])):
+            if c != int(none_value):
+                stack.append(c)
+    return sorted(seen)
+
+
+_ref_rs = None
+
+
+def _ref_rank_select():
+    global _ref_rs
+    if _ref_rs is None:
+        L = ctypes.CDLL(os.path.join(REF_DIR, "libref_rank_select.so"))
+        L.ref_rank_build.argtypes = [vp, u64, vp, u64]
+        L.ref_rank_query.argtypes = [vp, u64, u64]
+        L.ref_rank_query.restype = u64
+        L.ref_select_new.argtypes = [vp, u64, ctypes.c_int]
+        L.ref_select_new.restype = vp
+        L.ref_select_info.argtypes = [vp, vp]
+        L.ref_select_copy.argtypes = [vp, vp, vp, vp]
+        L.ref_select_query.argtypes = [vp, u64]
+        L.ref_select_query.restype = u64
+        L.ref_select_free.argtypes = [vp]
+        _ref_rs = L
+    return _ref_rs
+
+
+def ref_rank_build(words, size_bits):
+    """The reference's rank_support_v<1> table (m_basic_block)."""
+    words = np.ascontiguousarray(words, dtype=np.uint64)
+    tbl = np.zeros(lib().or_rank_words(size_bits), dtype=np.uint64)
+    if _ref_rank_select().ref_rank_build(_p(words), size_bits, _p(tbl), tbl.size) != 0:
+        raise RuntimeError("reference rank table size mismatch")
+    return tbl
+
+
+class RefSelect:
+    """The reference's select_support_mcl<t_b>, exported in the flat packed layout."""
+
+    def __init__(self, words, size_bits, t_b):
+        L = _ref_rank_select()
+        self.words = np.ascontiguousarray(words, dtype=np.uint64)
+        self.h = L.ref_select_new(_p(self.words), size_bits, t_b)
+        info = np.zeros(8, dtype=np.uint64)
+        L.ref_select_info(self.h, _p(info))
+        (self.size, self.arg_cnt, self.logn, self.logn4, self.nsb, self.has_long,
+         self.sb_nwords, self.pool_nwords) = [int(x) for x in info]
+        self.sb_words = np.zeros(max(self.sb_nwords, 1), dtype=np.uint64)
+        self.desc = np.zeros(max(self.nsb, 1), dtype=np.uint64)
+        self.pool = np.zeros(max(self.pool_nwords, 1), dtype=np.uint64)
+        L.ref_select_copy(self.h, _p(self.sb_words), _p(self.desc), _p(self.pool))
+        self.sb_words = self.sb_words[: self.sb_nwords]
+        self.desc = self.desc[: self.nsb]
+        self.pool = self.pool[: self.pool_nwords]
+
+    def query(self, i):
+        return _ref_rank_select().ref_select_query(self.h, int(i))
+
+    def __del__(self):
+        try:
+            if self.h:
+                _ref_rank_select().ref_select_free(self.h)
+                self.h = None
+        except Exception:
+            pass

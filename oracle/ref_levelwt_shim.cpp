@@ -1,0 +1,42 @@
+// ref_levelwt_shim.cpp -- exposes the reference's own WT() builder over a C ABI
+// so the tests can pin the oracle against it.
+//
+// TEST INFRASTRUCTURE ONLY.  oracle/Makefile compiles this file together with
+// the unmodified reference sources (wavelet/levelWT/WT.C, or serialWT/WT.C)
+// found under the read-only reference checkout, with the reference directory on
+// the include path; the result goes to oracle/_ref/ and is never shipped.
+// The symbol and index widths follow the reference's own compile-time knobs:
+// -DINT makes symbols uintT, -DLONG makes uintT 64-bit (wavelet/levelWT/WT.h:24-43,
+// parallel.h:71-81).
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <utility>
+#include "parallel.h"
+#include "utils.h"
+#include "WT.h"
+
+extern "C" {
+
+// Width in bytes of the reference's symbol and uintT types in this build.
+int ref_symbol_bytes(void) { return (int)sizeof(symbol); }
+int ref_uint_bytes(void) { return (int)sizeof(uintT); }
+
+// Calls WT(s, n, sigma) and copies its outputs: `words` receives
+// ceil(n*levels/64) words; `nodes` receives 2*sigma WTnode records in the
+// reference's own struct layout (5 x uintT).  Node records the reference never
+// writes hold whatever malloc returned; callers compare reachable nodes only.
+int ref_wt(const void* s, uint64_t n, uint64_t sigma, uint64_t* words, uint64_t nwords,
+           void* nodes) {
+  symbol* in = (symbol*)malloc(sizeof(symbol) * (n ? n : 1));
+  if (!in) return -1;
+  memcpy(in, s, sizeof(symbol) * n);
+  std::pair<WTnode*, long*> R = WT(in, (uintT)n, (uintT)sigma);
+  memcpy(words, R.second, nwords * sizeof(uint64_t));
+  if (nodes) memcpy(nodes, R.first, 2 * sigma * sizeof(WTnode));
+  free(R.first);
+  free(R.second);
+  free(in);
+  return 0;
+}
+}
