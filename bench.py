@@ -1,0 +1,356 @@
+"""Benchmark: wavelet-tree + rank/select build throughput on GB300.
+
+Workload (one step): a full build of the integer wavelet tree over
+n = 2^30 uint32 symbols drawn as min(floor(Exp(mean 2^14)), 2^20 - 1)
+(seeded), 20 levels (sigma 2^20, wt_int max_level semantics), with
+rank_support_v<1>, select_support_mcl<1> and select_support_mcl<0> over the
+concatenated 20 x 2^30-bit level bitvector.
+
+  value : algorithmic GB/s of the whole build with the input resident in HBM
+  e2e   : the same through the host API (wtg_tree_build from pinned host
+          memory, plus the copy of bits, rank and select tables back)
+The algorithmic bytes of one build are
+  L*n*w (level reads) + (L-1)*n*w (next-level writes) + L*n/8 (bits)
+  + [L*n/8 + 16*((L*n>>9)+1)] (rank: read bits, write table)
+  + 2 * [L*n/8 + select sample bytes written] (select1, select0).
+
+--impl reference times the reference algorithm on the host cores instead (the
+CPU restatement of levelWT + rank_support_v_par + select_support_mcl_par, all
+threads), on a bounded sample per step.
+
+Run: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl wtg|reference]
+Multi-GPU (torchrun): every rank builds its own independent sequence; no
+collective touches the data path (weak scaling).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "wavelet-suffix-fm-index_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "WT+rank/select build GB/s (% HBM peak); select Mq/s learned vs plain, exact"
+WORKLOAD = "wt_int build, n=2^30 uint32, Exp(mean 2^14) clamped to 2^20-1, 20 levels, rank + select1 + select0"
+MEAN, CAP, LEVELS, SEED = 2 ** 14, 2 ** 20 - 1, 20, 20240611
+
+
+def algorithmic_bytes(n, L, w, sel_words=0):
+    nb = n * L
+    bits = nb / 8
+    return (L * n * w + (L - 1) * n * w + bits + (bits + 16 * ((nb >> 9) + 1)) + 2 * bits + 8 * sel_words)
+
+
+def level_launch_bytes(n, w):
+    """Algorithmic bytes of one partitioning level pass: read n symbols,
+    write n symbols, write n bits."""
+    return 2 * n * w + n / 8
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.tmp = None
+
+    def __enter__(self):
+        try:
+            self.tmp = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.tmp, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or self.tmp is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.tmp.flush()
+        rows = []
+        with open(self.tmp.name) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.tmp.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in rows if num(r[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_build_seconds(n, threads_note=True):
+    """One full CPU build (oracle restatement, all OpenMP threads) of an n-symbol
+    sample of the workload; returns (seconds, sample bytes, cores)."""
+    import datagen
+    from oracle import oracle as O
+    sym = datagen.exp_u32(n, mean=MEAN, cap=CAP, seed=SEED)
+    t0 = time.perf_counter()
+    bits, _ = O.wt_build(sym, LEVELS)
+    w = np.concatenate([bits, np.zeros(1, np.uint64)])
+    O.rank_build(w, n * LEVELS)
+    s1 = O.Select(w, n * LEVELS, 1)
+    s0 = O.Select(w, n * LEVELS, 0)
+    dt = time.perf_counter() - t0
+    sel_words = s1.sb_nwords + s1.nsb + s1.pool_nwords + s0.sb_nwords + s0.nsb + s0.pool_nwords
+    return dt, algorithmic_bytes(n, LEVELS, 4, sel_words), O.num_threads()
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    O.build(ref=False)
+    n = 1 << args.cpu_log2
+    for _ in range(args.warmup):
+        cpu_build_seconds(n)
+    tot_t, tot_b, cores = 0.0, 0.0, 1
+    for _ in range(args.steps):
+        dt, b, cores = cpu_build_seconds(n)
+        tot_t += dt
+        tot_b += b
+    gbs = tot_b / tot_t / 1e9
+    sample = f"n=2^{args.cpu_log2} uint32 symbols of the same distribution, 20 levels, full build per step"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": gbs, "unit": "GB/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n": 1 << 30, "levels": LEVELS, "sample_n": n},
+        "cpu_baseline": {"value": gbs, "unit": "GB/s", "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": gbs, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_wtg(args, rank, world, local_rank):
+    import torch
+    import wtg
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local_rank)
+    n = 1 << args.n_log2
+    L = LEVELS
+    wtg.lib()
+
+    # input, generated on the device (seeded per rank), then resident in HBM
+    g = torch.Generator(device=dev)
+    g.manual_seed(SEED + rank)
+    x = torch.empty(n, device=dev, dtype=torch.float32)
+    x.exponential_(1.0 / MEAN, generator=g)
+    seq = torch.clamp(torch.floor(x), max=CAP).to(torch.int32)
+    del x
+    torch.cuda.synchronize()
+
+    stream = torch.cuda.current_stream(dev)
+    sp = stream.cuda_stream
+
+    tree = None
+    for _ in range(args.warmup):
+        tree = wtg.WaveletTree.from_device(seq.data_ptr(), n, 4, L, wtg.ALL, sp, tree=tree)
+    torch.cuda.synchronize()
+    tree.sync()
+
+    sel = [tree.select_tables(t_b) for t_b in (0, 1)]
+    sel_words = sum(s.sb_nwords + s.nsb + s.pool_nwords for s in sel)
+    step_bytes = algorithmic_bytes(n, L, 4, sel_words)
+
+    # ---- timed region: device-resident input
+    wtg.profile_read()
+    wtg.profile_enable(True)
+    launches0 = wtg.launch_count()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clocks:
+        start.record(stream)
+        for _ in range(args.steps):
+            tree = wtg.WaveletTree.from_device(seq.data_ptr(), n, 4, L, wtg.ALL, sp, tree=tree)
+        end.record(stream)
+        torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    tree.sync()
+    launches = wtg.launch_count() - launches0
+    wtg.profile_enable(False)
+    prof = wtg.profile_read()
+    ms = start.elapsed_time(end)
+    if dist:
+        t = torch.tensor([ms], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * args.steps * step_bytes / (ms / 1e3) / 1e9
+
+    peak, peak_kind = measured_peaks()
+    lv_n, lv_ms = prof["level"]
+    lv_avg = lv_ms / max(lv_n, 1)
+    lv_bytes = level_launch_bytes(n, 4)
+    roofline = {
+        "bound": "hbm", "kernel": "level_kernel<uint32,partition>", "achieved": lv_bytes / (lv_avg / 1e3) / 1e9,
+        "peak": peak, "unit": "GB/s", "peak_kind": peak_kind, "traffic": args.traffic,
+        "launch_ms": lv_avg, "launches": lv_n, "bytes_per_launch": lv_bytes,
+    }
+    roofline["frac"] = roofline["achieved"] / peak
+    kernel_share = {k: {"launches": v[0], "ms": v[1]} for k, v in prof.items()}
+
+    # ---- e2e: host API with pinned host buffers, outputs copied back
+    e2e = None
+    if not args.no_e2e:
+        import ctypes
+        host_in = torch.empty(n, dtype=torch.int32, pin_memory=True)
+        host_in.copy_(seq)
+        del seq
+        torch.cuda.empty_cache()
+        tree.free()
+        tree = None
+        h = ctypes.c_void_p()
+        L_ = wtg.lib()
+        wtg._ck(L_.wtg_tree_build(ctypes.c_void_p(host_in.data_ptr()), n, 4, L, wtg.ALL, ctypes.byref(h)))
+        t_e = wtg.WaveletTree(_handle=h)
+        s1, s0 = t_e.select_tables(1), t_e.select_tables(0)
+        outs = {
+            "bits": torch.empty(t_e.bit_words, dtype=torch.int64, pin_memory=True),
+            "rank": torch.empty(t_e.rank_words, dtype=torch.int64, pin_memory=True),
+        }
+        for tb, s in ((1, s1), (0, s0)):
+            outs[f"sb{tb}"] = torch.empty(max(s.sb_nwords, 1), dtype=torch.int64, pin_memory=True)
+            outs[f"desc{tb}"] = torch.empty(max(s.nsb, 1), dtype=torch.int64, pin_memory=True)
+            outs[f"pool{tb}"] = torch.empty(max(s.pool_nwords, 1), dtype=torch.int64, pin_memory=True)
+        d2h = 8 * (t_e.bit_words + t_e.rank_words + sum(s.sb_nwords + s.nsb + s.pool_nwords for s in (s1, s0)))
+        vp = ctypes.c_void_p
+
+        def e2e_step():
+            wtg._ck(L_.wtg_tree_build(vp(host_in.data_ptr()), n, 4, L, wtg.ALL, ctypes.byref(h)))
+            wtg._ck(L_.wtg_tree_get_bits(h, vp(outs["bits"].data_ptr()), t_e.bit_words))
+            wtg._ck(L_.wtg_tree_get_rank(h, vp(outs["rank"].data_ptr()), t_e.rank_words))
+            for tb in (1, 0):
+                wtg._ck(L_.wtg_tree_get_select(h, tb, vp(outs[f"sb{tb}"].data_ptr()),
+                                               vp(outs[f"desc{tb}"].data_ptr()), vp(outs[f"pool{tb}"].data_ptr())))
+
+        e2e_step()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e_steps = max(1, args.steps)
+        for _ in range(e_steps):
+            e2e_step()
+        torch.cuda.synchronize()
+        e_s = time.perf_counter() - t0
+        if dist:
+            t = torch.tensor([e_s], device=dev, dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e_s = float(t.item())
+        e2e = {"value": world * e_steps * step_bytes / e_s / 1e9, "unit": "GB/s",
+               "h2d_bytes_per_step": 4 * n, "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e_s / e_steps}
+        t_e.free()
+
+    if rank != 0:
+        if dist:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+
+    cpu = None
+    if not args.no_cpu:
+        from oracle import oracle as O
+        O.build(ref=False)
+        cn = 1 << args.cpu_log2
+        dt, b, cores = cpu_build_seconds(cn)
+        cpu = {"value": b / dt / 1e9, "unit": "GB/s", "cores": cores, "kind": "port",
+               "sample": f"n=2^{args.cpu_log2} of the same distribution, 20 levels, one full build ({dt:.2f} s)"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n": n, "levels": L, "sigma": 1 << L, "elem_bytes": 4,
+                   "algorithmic_bytes_per_step": step_bytes,
+                   "l2": "inputs larger than L2 (4 GiB per level pass, 2.5 GiB of bits)",
+                   "parallelism": f"replicas x{world} (independent sequences)"},
+        "hbm_frac": value / peak,
+        "roofline": roofline,
+        "kernel_time": kernel_share,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "clocks": clocks.summary(),
+        "gpu_launches": launches,
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="wtg", choices=["wtg", "reference"])
+    ap.add_argument("--n-log2", type=int, default=30)
+    ap.add_argument("--cpu-log2", type=int, default=27)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--traffic", type=float, default=None,
+                    help="DRAM bytes per level launch from an ncu capture, reported as roofline.traffic")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        args.cpu_log2 = min(args.cpu_log2, 26)
+        run_reference(args, rank)
+    else:
+        run_wtg(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,169 @@
+/*
+ * wtg.h -- C ABI of the GB300 wavelet-tree / rank / select library (libwtg.so).
+ *
+ * Drop-in boundary for the wavelet-tree construction path of
+ * jlabeit/wavelet-suffix-fm-index.  Every entry point is extern "C", takes
+ * plain pointers and sizes, never throws, and returns an int status
+ * (WTG_OK = 0).  wtg_last_error() gives the message of the calling thread's
+ * last failure.  All compute runs as hand-written CUDA kernels on the current
+ * CUDA device; there is no CPU fallback: without a usable GPU every build
+ * fails with WTG_ERR_CUDA.
+ *
+ * Layouts (bit-exact with the reference):
+ *   bits   : level l of the tree occupies bits [l*n, (l+1)*n) of one array of
+ *            ceil(n*levels/64) 64-bit words, LSB first
+ *            (wavelet/levelWT/WT.C:97,104,136; wt_int/wt_int_par.hpp:397-398).
+ *   nodes  : WTnode records {bitmapPtr, length, parent, leftChild, rightChild}
+ *            in heap order, with 4-byte (uintT) or 8-byte (-DLONG) fields and
+ *            UINT_T_MAX for absent links (wavelet/levelWT/WT.h:30-35).  Node
+ *            records the reference never writes are zero here.
+ *   rank   : rank_support_v<1> m_basic_block, ((capacity>>9)+1)*2 words
+ *            (rank/rank_support_v_par.hpp:78-113).
+ *   select : select_support_mcl<t_b> as three flat arrays:
+ *            sb_words = the int_vector<0> data of m_superblock (width logn);
+ *            desc[i]  = (pool_word_offset << 8) | (is_long << 7) | width for
+ *                       superblock i;
+ *            pool     = the int_vector<0> data of each superblock's mini block
+ *                       (64 entries) or long block (4096 entries), in order
+ *            (select/select_support_mcl_par.hpp:83-90,483-561).
+ *            info[8]  = size, arg_cnt, logn, logn4, nsb, has_long, sb_nwords,
+ *                       pool_nwords (has_long: m_longsuperblock != nullptr).
+ */
+#ifndef WTG_H
+#define WTG_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define WTG_OK 0
+#define WTG_ERR_INVALID 1   /* bad argument */
+#define WTG_ERR_OOM 2       /* device allocation failed */
+#define WTG_ERR_CUDA 3      /* CUDA runtime error (including: no GPU) */
+#define WTG_ERR_TIMEOUT 4   /* a bounded device-side wait gave up; results invalid */
+#define WTG_ERR_RANGE 5     /* symbol or index outside the structure */
+
+/* build flags */
+#define WTG_RANK 1u     /* rank_support_v<1> over the (concatenated) bitvector */
+#define WTG_SELECT1 2u  /* select_support_mcl<1> */
+#define WTG_SELECT0 4u  /* select_support_mcl<0> */
+#define WTG_ALL 7u
+
+typedef struct wtg_tree wtg_tree; /* wavelet tree + supports, owns device memory */
+typedef struct wtg_bv wtg_bv;     /* rank/select supports over a caller bitvector */
+
+const char* wtg_last_error(void);
+int wtg_version(void);
+/* Number of kernel launches issued by this process so far (all entry points). */
+uint64_t wtg_launch_count(void);
+
+/* ------------------------------------------------------------ tree build
+ * Replaces WT(symbol* s, uintT n, uintT sigma) (wavelet/levelWT/WT.h:43,
+ * levelWT/WT.C:86-270; same contract in ddWT/recWT/serialWT) and the
+ * sdsl::wt_int<> constructor (wt_int/wt_int_par.hpp:368-406) with its
+ * util::init_support calls for rank and select (:402-404).
+ *   seq        : n symbols of elem_bytes (1, 2, 4 or 8) bytes, host memory
+ *   levels     : tree height; symbols are read through their low `levels`
+ *                bits, bit (levels-1-l) at level l (levelWT/WT.C:105,
+ *                wt_int_par.hpp:173).  levels = max(1, log2Up(sigma)) gives
+ *                levelWT's tree; 0 derives wt_int's hi(max(1,max symbol))+1
+ *                (wt_int_par.hpp:385-395).  1..24 supported.
+ *   flags      : WTG_RANK | WTG_SELECT1 | WTG_SELECT0 supports to build over
+ *                the concatenated bitvector.
+ * The input is copied to the device inside the call. */
+int wtg_tree_build(const void* seq, uint64_t n, int elem_bytes, int levels, uint32_t flags,
+                   wtg_tree** out);
+
+/* When *out is non-NULL on entry, wtg_tree_build rebuilds that handle in place
+ * (reusing its device buffers) instead of creating a new one. */
+
+/* Same, from device memory, enqueued on `stream` (a cudaStream_t, NULL for
+ * the legacy default stream).  When *out is non-NULL the handle is rebuilt in
+ * place, reusing its device buffers.  Returns once the work is enqueued and
+ * the output sizes are known; call wtg_tree_sync() before trusting results. */
+int wtg_tree_build_device(const void* d_seq, uint64_t n, int elem_bytes, int levels, uint32_t flags,
+                          void* stream, wtg_tree** out);
+
+/* Waits for the handle's stream and reports device-side failures
+ * (WTG_ERR_TIMEOUT when a bounded wait expired). */
+int wtg_tree_sync(wtg_tree* t);
+int wtg_tree_free(wtg_tree* t);
+
+/* n, levels, bit words, rank words */
+int wtg_tree_info(wtg_tree* t, uint64_t info[4]);
+/* select info[8] (see above) for t_b in {0,1} */
+int wtg_tree_select_info(wtg_tree* t, int t_b, uint64_t info[8]);
+
+/* ------------------------------------------------------- tree outputs
+ * Host destinations; sizes must match wtg_tree_info / wtg_tree_select_info. */
+int wtg_tree_get_bits(wtg_tree* t, uint64_t* dst, uint64_t nwords);
+/* WTnode records for heap ids [0, n_entries) with index_bytes (4 or 8) per
+ * field: the reference's 2*sigma-entry node array (levelWT/WT.C:89). */
+int wtg_tree_get_nodes(wtg_tree* t, int index_bytes, uint64_t n_entries, void* dst);
+int wtg_tree_get_rank(wtg_tree* t, uint64_t* dst, uint64_t nwords);
+int wtg_tree_get_select(wtg_tree* t, int t_b, uint64_t* sb_words, uint64_t* desc, uint64_t* pool);
+/* Device pointers of the outputs (valid until the next rebuild or free):
+ * ptrs[0]=bits, [1]=rank, [2]=select1 sb_words, [3]=select1 desc,
+ * [4]=select1 pool, [5..7]=the same for select0. */
+int wtg_tree_device_ptrs(wtg_tree* t, uint64_t ptrs[8]);
+
+/* ------------------------------------------------------------ queries
+ * Batched wt_int queries (wt_int/wt_int_par.hpp:519-660), one answer per
+ * query.  Host arrays; the _device variants take device arrays and a stream. */
+/* operator[](i) (wt_int_par.hpp:519-541) */
+int wtg_query_access(wtg_tree* t, const uint64_t* idx, uint64_t nq, uint64_t* out);
+/* rank(i, c): occurrences of c in [0, i) (wt_int_par.hpp:553-577) */
+int wtg_query_rank(wtg_tree* t, const uint64_t* idx, const uint64_t* sym, uint64_t nq, uint64_t* out);
+/* inverse_select(i) -> (rank, symbol) (wt_int_par.hpp:588-611) */
+int wtg_query_inverse_select(wtg_tree* t, const uint64_t* idx, uint64_t nq, uint64_t* rank_out,
+                             uint64_t* sym_out);
+/* select(i, c): position of the i-th c (1-based i); UINT64_MAX where c occurs
+ * fewer than i times (the reference throws std::logic_error,
+ * wt_int_par.hpp:644-646).  Needs WTG_RANK|WTG_SELECT1|WTG_SELECT0. */
+int wtg_query_select(wtg_tree* t, const uint64_t* i, const uint64_t* sym, uint64_t nq, uint64_t* out);
+int wtg_query_access_device(wtg_tree* t, const uint64_t* d_idx, uint64_t nq, uint64_t* d_out, void* stream);
+int wtg_query_rank_device(wtg_tree* t, const uint64_t* d_idx, const uint64_t* d_sym, uint64_t nq,
+                          uint64_t* d_out, void* stream);
+
+/* --------------------------------------------- standalone bitvector supports
+ * rank_support_v<1> (rank/rank_support_v_par.hpp:69-123) and
+ * select_support_mcl<1>/<0> (select/select_support_mcl_par.hpp:120-129,
+ * 483-561) over the first size_bits bits of a caller bitvector. */
+int wtg_bv_build(const uint64_t* words, uint64_t size_bits, uint32_t flags, wtg_bv** out);
+int wtg_bv_build_device(const uint64_t* d_words, uint64_t size_bits, uint32_t flags, void* stream,
+                        wtg_bv** out);
+int wtg_bv_sync(wtg_bv* b);
+int wtg_bv_free(wtg_bv* b);
+int wtg_bv_rank_words(wtg_bv* b, uint64_t* nwords);
+int wtg_bv_get_rank(wtg_bv* b, uint64_t* dst, uint64_t nwords);
+int wtg_bv_select_info(wtg_bv* b, int t_b, uint64_t info[8]);
+int wtg_bv_get_select(wtg_bv* b, int t_b, uint64_t* sb_words, uint64_t* desc, uint64_t* pool);
+/* rank_support_v::rank(idx) (rank_support_v_par.hpp:131-142), idx <= size */
+int wtg_bv_rank(wtg_bv* b, const uint64_t* idx, uint64_t nq, uint64_t* out);
+/* select_support_mcl::select(i) (select_support_mcl_par.hpp:564-611), 1 <= i <= args */
+int wtg_bv_select(wtg_bv* b, int t_b, const uint64_t* i, uint64_t nq, uint64_t* out);
+int wtg_bv_select_device(wtg_bv* b, int t_b, const uint64_t* d_i, uint64_t nq, uint64_t* d_out,
+                         void* stream);
+
+/* ------------------------------------------------------------ profiling
+ * When enabled, every build records a CUDA event pair around each kernel it
+ * launches, on the launching stream.  wtg_profile_read waits for those events
+ * and returns, per kernel class, the number of launches and their summed
+ * device time in ms, then clears the record.  Classes: 0 level pass with
+ * partition, 1 last level pass, 2 key histogram, 3 node tables and scans,
+ * 4 bitvector pass (rank + select samples), 5 select finishing kernels. */
+#define WTG_PROF_CLASSES 6
+int wtg_profile_enable(int on);
+int wtg_profile_read(uint64_t launches[WTG_PROF_CLASSES], double ms[WTG_PROF_CLASSES]);
+
+/* --------------------------------------------------------------- helpers */
+/* Alphabet remap of levelWT/WTTime.C:80-94: every symbol becomes its rank
+ * among the distinct values present; *sigma_out = number of distinct values.
+ * In place on host memory. */
+int wtg_remap_alphabet(void* seq, uint64_t n, int elem_bytes, uint64_t* sigma_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

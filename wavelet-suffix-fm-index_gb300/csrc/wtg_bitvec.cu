@@ -1,0 +1,450 @@
+// wtg_bitvec.cu -- rank_support_v<1> and select_support_mcl<1>/<0>
+// construction over one bitvector, on the GPU.
+//
+// One pass over the bitvector (bv_pass_kernel) reads each 512-bit superblock
+// once and produces, through a single decoupled look-back scan of the
+// superblock one-counts:
+//   * the rank_support_v table (rank/rank_support_v_par.hpp:69-123): the
+//     absolute count before each superblock (the exclusive scan of :112-113)
+//     and the seven 9-bit in-superblock counts (:95-110), including the
+//     reference's final-superblock rule (:99-108, and the (total, 0) pair when
+//     the capacity is a multiple of 512);
+//   * for select_support_mcl, the position of every 64th arg (its
+//     superblock starts are every 64th of those) and of every arg that ends a
+//     superblock (select_support_mcl_par.hpp:492-523);
+// The select structure is then finished per superblock: the long/mini choice
+// (span > log^4 n) and widths (:525-543), the pool offsets (a scan), the mini
+// blocks from the samples (init_miniblock_serial :440-481), the long blocks by
+// re-reading their span (init_longblock_serial :401-438) and m_superblock
+// (:546-549).
+#include <algorithm>
+
+#include "wtg_internal.cuh"
+
+namespace wtg {
+
+constexpr int BV_THREADS = 256;  // one 512-bit superblock per thread
+constexpr int BV_SB_PER_TILE = BV_THREADS;
+
+enum {
+  INF_M1 = 0,   // number of ones
+  INF_M0,       // number of zeros
+  INF_LAST1,    // position of the last one + 1
+  INF_LAST0,    // position of the last zero + 1
+  INF_NLONG1,   // long superblocks of select1
+  INF_NLONG0,
+  INF_POOL1,    // pool words of select1
+  INF_POOL0,
+  INF_N = 16
+};
+
+__device__ __forceinline__ uint64_t warp_max_u64(uint64_t v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    uint64_t t = __shfl_xor_sync(0xffffffffu, v, o);
+    v = t > v ? t : v;
+  }
+  return v;
+}
+
+// records the sample / superblock-end positions of args [K, K+c) that sit in
+// word wi (x = the word's arg mask)
+__device__ __forceinline__ void select_marks(uint64_t x, uint32_t c, uint64_t K, uint64_t wi,
+                                             uint64_t* __restrict__ samp, int64_t samp_dir,
+                                             uint64_t* __restrict__ ends) {
+  uint64_t q = (K + 63) & ~63ull;  // next multiple of 64
+  if (q < K + c) samp[samp_dir * (int64_t)(q >> 6)] = (wi << 6) + sel64(x, (uint32_t)(q - K + 1));
+  uint64_t e = K | 4095ull;  // next index with e % 4096 == 4095
+  if (e < K + c) ends[e >> 12] = (wi << 6) + sel64(x, (uint32_t)(e - K + 1));
+}
+
+__global__ void __launch_bounds__(BV_THREADS)
+    bv_pass_kernel(const uint64_t* __restrict__ words, uint64_t size, uint64_t W, uint64_t NB, uint32_t flags,
+                   uint64_t* __restrict__ rank, uint64_t* __restrict__ samples, uint64_t samp_last,
+                   uint64_t* __restrict__ ends1, uint64_t* __restrict__ ends0, unsigned long long* info,
+                   uint64_t* status, uint32_t* counter, uint32_t* err) {
+  __shared__ uint32_t s_tile;
+  __shared__ uint64_t s_wsum[BV_THREADS / 32];
+  __shared__ uint64_t s_prefix;
+  if (threadIdx.x == 0) s_tile = atomicAdd(counter, 1u);
+  __syncthreads();
+  const uint32_t tile = s_tile;
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint64_t b = (uint64_t)tile * BV_SB_PER_TILE + threadIdx.x;
+  const uint64_t tailmask = (size & 63) ? ((1ull << (size & 63)) - 1) : ~0ull;
+
+  uint64_t w[8];
+  uint32_t c[8];
+  uint32_t tot = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    uint64_t wi = 8 * b + k;
+    uint64_t x = (b <= NB && wi < W) ? __ldg(&words[wi]) : 0ull;
+    if (wi == W - 1) x &= tailmask;
+    w[k] = x;
+    c[k] = __popcll(x);
+    tot += c[k];
+  }
+
+  // block exclusive scan of the superblock one-counts
+  uint64_t incl = tot;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint64_t t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= (uint32_t)o) incl += t;
+  }
+  if (lane == 31) s_wsum[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    uint64_t v = lane < BV_THREADS / 32 ? s_wsum[lane] : 0;
+    uint64_t vinc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint64_t t = __shfl_up_sync(0xffffffffu, vinc, o);
+      if (lane >= (uint32_t)o) vinc += t;
+    }
+    if (lane < BV_THREADS / 32) s_wsum[lane] = vinc - v;
+    uint64_t total = __shfl_sync(0xffffffffu, vinc, BV_THREADS / 32 - 1);
+    uint64_t prefix = 0;
+    if (tile == 0) {
+      if (lane == 0) lb_publish(status, tile, LB_FLAG_INC, total);
+    } else {
+      if (lane == 0) lb_publish(status, tile, LB_FLAG_AGG, total);
+      prefix = lb_lookback_warp(status, tile, err);
+      if (lane == 0) lb_publish(status, tile, LB_FLAG_INC, prefix + total);
+    }
+    if (lane == 0) s_prefix = prefix;
+  }
+  __syncthreads();
+  const uint64_t ones_before = s_prefix + s_wsum[warp] + incl - tot;
+
+  if (b <= NB) {
+    if (flags & WTG_RANK) {
+      // fields 1..7 hold the count before block k of the superblock; in the
+      // final superblock only fields 1..max(r,1) are written (r = its words)
+      const uint64_t r = W - 8 * NB;
+      const uint32_t kmax = (b < NB) ? 7u : (r > 1 ? (uint32_t)r : 1u);
+      uint64_t second = 0;
+      uint64_t cum = 0;
+#pragma unroll
+      for (int k = 1; k < 8; ++k) {
+        cum += c[k - 1];
+        if ((uint32_t)k <= kmax) second |= cum << (63 - 9 * k);
+      }
+      rank[2 * b] = ones_before;
+      rank[2 * b + 1] = second;
+    }
+    if (b == NB) {
+      info[INF_M1] = ones_before + tot;
+      info[INF_M0] = size - (ones_before + tot);
+    }
+  }
+
+  uint64_t last1 = 0, last0 = 0;
+  if (flags & WTG_SELECT1) {
+    uint64_t K = ones_before;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      if (c[k]) {
+        uint64_t wi = 8 * b + k;
+        select_marks(w[k], c[k], K, wi, samples, 1, ends1);
+        last1 = (wi << 6) + hi64(w[k]) + 1;
+        K += c[k];
+      }
+    }
+  }
+  if (flags & WTG_SELECT0) {
+    uint64_t K = 8 * b * 64 - ones_before;  // zeros before the superblock
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      uint64_t wi = 8 * b + k;
+      uint64_t z = 0;
+      if (b <= NB && wi < W) z = (wi == W - 1) ? (~w[k] & tailmask) : ~w[k];
+      uint32_t cz = __popcll(z);
+      if (cz) {
+        select_marks(z, cz, K, wi, samples + samp_last, -1, ends0);
+        last0 = (wi << 6) + hi64(z) + 1;
+        K += cz;
+      }
+    }
+  }
+  last1 = warp_max_u64(last1);
+  last0 = warp_max_u64(last0);
+  if (lane == 0) {
+    if (last1) atomicMax(&info[INF_LAST1], (unsigned long long)last1);
+    if (last0) atomicMax(&info[INF_LAST0], (unsigned long long)last0);
+  }
+}
+
+// per superblock: long/mini choice, width and pool words
+__global__ void select_desc_kernel(int t_b, const uint64_t* __restrict__ samples, uint64_t samp_last,
+                                   const uint64_t* __restrict__ ends, unsigned long long* info, uint64_t logn4,
+                                   uint64_t nsb_cap, uint64_t* __restrict__ descw, uint64_t* __restrict__ sizes,
+                                   uint64_t* __restrict__ long_list) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nsb_cap) return;
+  const uint64_t m = info[t_b ? INF_M1 : INF_M0];
+  const uint64_t nsb = (m + 4095) >> 12;
+  if (i >= nsb) {
+    sizes[i] = 0;
+    return;
+  }
+  const uint64_t start = t_b ? samples[64 * i] : samples[samp_last - 64 * i];
+  const uint64_t end = (i + 1 < nsb) ? ends[i] : (uint64_t)info[t_b ? INF_LAST1 : INF_LAST0] - 1;
+  const uint64_t span = end - start;
+  const uint64_t lng = span > logn4;
+  const uint64_t wdt = lng ? hi64(end) + 1 : hi64(span) + 1;
+  descw[i] = (lng << 7) | wdt;
+  sizes[i] = lng ? 64 * wdt : wdt;
+  if (lng) {
+    unsigned long long slot = atomicAdd(&info[t_b ? INF_NLONG1 : INF_NLONG0], 1ull);
+    long_list[slot] = i;
+  }
+}
+
+__global__ void select_pool_total_kernel(int t_b, unsigned long long* info, const uint64_t* sizes,
+                                         const uint64_t* offs) {
+  const uint64_t m = info[t_b ? INF_M1 : INF_M0];
+  const uint64_t nsb = (m + 4095) >> 12;
+  info[t_b ? INF_POOL1 : INF_POOL0] = nsb ? offs[nsb - 1] + sizes[nsb - 1] : 0;
+}
+
+// warp per superblock: final descriptors, and the 64-entry mini blocks
+__global__ void __launch_bounds__(256)
+    select_mini_kernel(int t_b, uint64_t nsb, uint64_t m, const uint64_t* __restrict__ samples, uint64_t samp_last,
+                       const uint64_t* __restrict__ descw, const uint64_t* __restrict__ offs,
+                       uint64_t* __restrict__ desc, uint64_t* __restrict__ pool) {
+  __shared__ uint64_t ent[256 / 32][64];
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (i >= nsb) return;
+  const uint64_t d = descw[i];
+  const uint64_t off = offs[i];
+  if (lane == 0) desc[i] = (off << 8) | (d & 255);
+  if ((d >> 7) & 1) return;  // long block
+  const uint32_t wdt = (uint32_t)(d & 127);
+  auto samp = [&](uint64_t k) { return t_b ? samples[k] : samples[samp_last - k]; };
+  const uint64_t start = samp(64 * i);
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    uint32_t j = lane + 32 * h;
+    uint64_t k = 4096 * i + 64 * (uint64_t)j;
+    ent[warp][j] = (k < m) ? samp(64 * i + j) - start : 0;
+  }
+  __syncwarp();
+  if (lane < wdt) pool[off + lane] = packed_word(lane, wdt, 64, [&](uint64_t j) { return ent[warp][j]; });
+}
+
+// m_superblock: entry i = position of arg 4096*i, width logn
+__global__ void select_sb_pack_kernel(int t_b, uint64_t nsb, uint32_t logn, const uint64_t* __restrict__ samples,
+                                      uint64_t samp_last, uint64_t nwords, uint64_t* __restrict__ sb_words) {
+  uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nwords) return;
+  sb_words[q] = packed_word(q, logn, nsb, [&](uint64_t i) {
+    return t_b ? samples[64 * i] : samples[samp_last - 64 * i];
+  });
+}
+
+// block per long superblock: all 4096 arg positions, packed
+__global__ void __launch_bounds__(256)
+    select_long_kernel(int t_b, const uint64_t* __restrict__ words, uint64_t size, uint64_t W,
+                       const uint64_t* __restrict__ samples, uint64_t samp_last, const uint64_t* __restrict__ ends,
+                       const unsigned long long* info, const uint64_t* __restrict__ long_list,
+                       const uint64_t* __restrict__ descw, const uint64_t* __restrict__ offs,
+                       uint64_t* __restrict__ pool, uint32_t* err) {
+  __shared__ uint64_t ent[4096];
+  __shared__ uint32_t s_wsum[8];
+  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint64_t m = info[t_b ? INF_M1 : INF_M0];
+  const uint64_t nsb = (m + 4095) >> 12;
+  const uint64_t nlong = info[t_b ? INF_NLONG1 : INF_NLONG0];
+  const uint64_t tailmask = (size & 63) ? ((1ull << (size & 63)) - 1) : ~0ull;
+  for (uint64_t li = blockIdx.x; li < nlong; li += gridDim.x) {
+    const uint64_t i = long_list[li];
+    const uint64_t start = t_b ? samples[64 * i] : samples[samp_last - 64 * i];
+    const uint64_t end = (i + 1 < nsb) ? ends[i] : (uint64_t)info[t_b ? INF_LAST1 : INF_LAST0] - 1;
+    const uint32_t wdt = (uint32_t)(descw[i] & 127);
+    const uint64_t off = offs[i];
+    for (uint32_t j = tid; j < 4096; j += 256) ent[j] = 0;
+    __syncthreads();
+    uint64_t count = 0;
+    for (uint64_t wb = start >> 6; wb <= (end >> 6); wb += 256) {
+      const uint64_t wi = wb + tid;
+      uint64_t x = 0;
+      if (wi <= (end >> 6) && wi < W) {
+        x = words[wi];
+        if (!t_b) x = ~x;
+        if (wi == W - 1) x &= tailmask;
+        if (wi == (start >> 6)) x &= ~0ull << (start & 63);
+        if (wi == (end >> 6) && (end & 63) != 63) x &= (1ull << ((end & 63) + 1)) - 1;
+      }
+      uint32_t cx = __popcll(x);
+      uint32_t inc = cx;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= (uint32_t)o) inc += t;
+      }
+      if (lane == 31) s_wsum[warp] = inc;
+      __syncthreads();
+      uint32_t before = 0, total = 0;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        uint32_t t = s_wsum[k];
+        if ((uint32_t)k < warp) before += t;
+        total += t;
+      }
+      uint64_t p = count + before + inc - cx;
+      while (x) {
+        if (p < 4096) ent[p] = (wi << 6) + __ffsll((long long)x) - 1;
+        ++p;
+        x &= x - 1;
+      }
+      count += total;
+      __syncthreads();
+    }
+    if (count > 4096 && tid == 0) atomicCAS(err, 0u, (uint32_t)DERR_SELECT_OVERFLOW);
+    for (uint64_t q = tid; q < 64ull * wdt; q += 256)
+      pool[off + q] = packed_word(q, wdt, 4096, [&](uint64_t j) { return ent[j]; });
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------ host
+
+static uint32_t logn_of(uint64_t size) {
+  uint64_t cap = (size + 63) / 64 * 64;
+  return hi64(cap) + 1;
+}
+
+void bv_release(BvSupport& bv, cudaStream_t s) {
+  bv.rank.release(s);
+  bv.samples.release(s);
+  bv.info.release(s);
+  bv.status.release(s);
+  bv.scan_tmp.release(s);
+  for (auto& sd : bv.sel) {
+    sd.ends.release(s);
+    sd.desc.release(s);
+    sd.sizes.release(s);
+    sd.sb_words.release(s);
+    sd.pool.release(s);
+    sd.long_list.release(s);
+  }
+}
+
+int bv_build(BvSupport& bv, const uint64_t* d_words, uint64_t size, uint32_t flags, uint32_t* d_err,
+             cudaStream_t s) {
+  int rc;
+  bv.size = size;
+  bv.words = d_words;
+  bv.flags = flags;
+  const uint64_t W = (size + 63) / 64;
+  const uint64_t NB = W >> 3;
+  const uint64_t nsb_cap = size / 4096 + 2;
+  const uint64_t samp_n = W + 2;
+  const uint32_t logn = logn_of(size);
+  const uint64_t logn4 = (uint64_t)(uint32_t)(logn * logn * logn * logn);  // uint32 as in initData
+
+  if ((rc = bv.info.ensure(INF_N * sizeof(uint64_t), s))) return rc;
+  WTG_CK(cudaMemsetAsync(bv.info.p, 0, INF_N * sizeof(uint64_t), s));
+  if (flags & WTG_RANK)
+    if ((rc = bv.rank.ensure(2 * (NB + 1) * sizeof(uint64_t), s))) return rc;
+  if (flags & (WTG_SELECT1 | WTG_SELECT0))
+    if ((rc = bv.samples.ensure(samp_n * sizeof(uint64_t), s))) return rc;
+  for (int t_b = 0; t_b < 2; ++t_b) {
+    if (!(flags & (t_b ? WTG_SELECT1 : WTG_SELECT0))) continue;
+    SelectDev& sd = bv.sel[t_b];
+    if ((rc = sd.ends.ensure(nsb_cap * sizeof(uint64_t), s))) return rc;
+    if ((rc = sd.desc.ensure(2 * nsb_cap * sizeof(uint64_t), s))) return rc;   // [final | working]
+    if ((rc = sd.sizes.ensure(2 * nsb_cap * sizeof(uint64_t), s))) return rc;  // [sizes | offsets]
+    if ((rc = sd.long_list.ensure(nsb_cap * sizeof(uint64_t), s))) return rc;
+  }
+  const uint64_t tiles = (NB + 1 + BV_SB_PER_TILE - 1) / BV_SB_PER_TILE;
+  if (tiles > 0x7fffffffull) return fail(WTG_ERR_INVALID, "bitvector too large");
+  if ((rc = bv.status.ensure((tiles + 1) * sizeof(uint64_t), s))) return rc;
+  WTG_CK(cudaMemsetAsync(bv.status.p, 0, (tiles + 1) * sizeof(uint64_t), s));
+
+  unsigned long long* info = bv.info.as<unsigned long long>();
+  uint64_t* samples = bv.samples.as<uint64_t>();
+  prof_begin(PROF_BVPASS, s);
+  bv_pass_kernel<<<(unsigned)tiles, BV_THREADS, 0, s>>>(
+      d_words, size, W, NB, flags, bv.rank.as<uint64_t>(), samples, samp_n - 1, bv.sel[1].ends.as<uint64_t>(),
+      bv.sel[0].ends.as<uint64_t>(), info, bv.status.as<uint64_t>() + 1, bv.status.as<uint32_t>(), d_err);
+  prof_end(PROF_BVPASS, s);
+  count_launch();
+  WTG_CK(cudaGetLastError());
+
+  if (!(flags & (WTG_SELECT1 | WTG_SELECT0))) return WTG_OK;
+
+  for (int t_b = 0; t_b < 2; ++t_b) {
+    if (!(flags & (t_b ? WTG_SELECT1 : WTG_SELECT0))) continue;
+    SelectDev& sd = bv.sel[t_b];
+    uint64_t* descw = sd.desc.as<uint64_t>() + nsb_cap;
+    uint64_t* sizes = sd.sizes.as<uint64_t>();
+    uint64_t* offs = sizes + nsb_cap;
+    prof_begin(PROF_SELECT, s);
+    select_desc_kernel<<<(unsigned)((nsb_cap + 255) / 256), 256, 0, s>>>(
+        t_b, samples, samp_n - 1, sd.ends.as<uint64_t>(), info, logn4, nsb_cap, descw, sizes,
+        sd.long_list.as<uint64_t>());
+    prof_end(PROF_SELECT, s);
+    count_launch();
+    WTG_CK(cudaGetLastError());
+    if ((rc = scan_exclusive_u64(sizes, offs, nsb_cap, bv.scan_tmp, d_err, s))) return rc;
+    prof_begin(PROF_SELECT, s);
+    select_pool_total_kernel<<<1, 1, 0, s>>>(t_b, info, sizes, offs);
+    prof_end(PROF_SELECT, s);
+    count_launch();
+    WTG_CK(cudaGetLastError());
+  }
+
+  // the pool sizes decide the allocations: one small read-back
+  uint64_t h[INF_N];
+  WTG_CK(cudaMemcpyAsync(h, info, sizeof(h), cudaMemcpyDeviceToHost, s));
+  WTG_CK(cudaStreamSynchronize(s));
+
+  for (int t_b = 0; t_b < 2; ++t_b) {
+    if (!(flags & (t_b ? WTG_SELECT1 : WTG_SELECT0))) continue;
+    SelectDev& sd = bv.sel[t_b];
+    const uint64_t m = h[t_b ? INF_M1 : INF_M0];
+    sd.arg_cnt = m;
+    sd.logn = logn;
+    sd.logn4 = logn4;
+    sd.nsb = (m + 4095) >> 12;
+    sd.has_long = h[t_b ? INF_NLONG1 : INF_NLONG0] ? 1 : 0;
+    sd.pool_nwords = h[t_b ? INF_POOL1 : INF_POOL0];
+    sd.sb_nwords = (sd.nsb * logn + 63) / 64;
+    if ((rc = sd.pool.ensure((sd.pool_nwords + 1) * sizeof(uint64_t), s))) return rc;
+    if ((rc = sd.sb_words.ensure((sd.sb_nwords + 1) * sizeof(uint64_t), s))) return rc;
+    if (sd.nsb == 0) continue;
+    uint64_t* descw = sd.desc.as<uint64_t>() + nsb_cap;
+    uint64_t* offs = sd.sizes.as<uint64_t>() + nsb_cap;
+    const uint64_t warps = sd.nsb;
+    prof_begin(PROF_SELECT, s);
+    select_mini_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(
+        t_b, sd.nsb, m, samples, samp_n - 1, descw, offs, sd.desc.as<uint64_t>(), sd.pool.as<uint64_t>());
+    prof_end(PROF_SELECT, s);
+    count_launch();
+    WTG_CK(cudaGetLastError());
+    prof_begin(PROF_SELECT, s);
+    select_sb_pack_kernel<<<(unsigned)((sd.sb_nwords + 255) / 256), 256, 0, s>>>(
+        t_b, sd.nsb, logn, samples, samp_n - 1, sd.sb_nwords, sd.sb_words.as<uint64_t>());
+    prof_end(PROF_SELECT, s);
+    count_launch();
+    WTG_CK(cudaGetLastError());
+    const uint64_t nlong = h[t_b ? INF_NLONG1 : INF_NLONG0];
+    if (nlong) {
+      unsigned grid = (unsigned)std::min<uint64_t>(nlong, 4 * 152);
+      prof_begin(PROF_SELECT, s);
+      select_long_kernel<<<grid, 256, 0, s>>>(t_b, d_words, size, W, samples, samp_n - 1, sd.ends.as<uint64_t>(),
+                                              info, sd.long_list.as<uint64_t>(), descw, offs,
+                                              sd.pool.as<uint64_t>(), d_err);
+      prof_end(PROF_SELECT, s);
+      count_launch();
+      WTG_CK(cudaGetLastError());
+    }
+  }
+  return WTG_OK;
+}
+
+}  // namespace wtg

@@ -1,0 +1,488 @@
+// wtg_capi.cu -- the extern "C" boundary (include/wtg.h): handles, argument
+// checks, host<->device copies and error reporting around the kernels.
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "wtg_tree.cuh"
+
+struct wtg_tree {
+  wtg::TreeImpl t;
+};
+
+struct wtg_bv {
+  wtg::BvSupport bv;
+  wtg::DevBuf words;  // device copy for host-input builds
+  wtg::DevBuf err;
+  wtg::DevBuf qbuf;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+};
+
+using namespace wtg;
+
+namespace {
+
+constexpr int MAX_LEVELS = 24;
+
+int check_device() {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0)
+    return fail(WTG_ERR_CUDA, std::string("no usable CUDA device: ") + cudaGetErrorString(e));
+  return WTG_OK;
+}
+
+int check_seq_args(uint64_t n, int eb, int levels, uint32_t flags) {
+  if (eb != 1 && eb != 2 && eb != 4 && eb != 8) return fail(WTG_ERR_INVALID, "elem_bytes must be 1, 2, 4 or 8");
+  if (levels < 0 || levels > MAX_LEVELS) return fail(WTG_ERR_INVALID, "levels must be 0 (derive) or 1..24");
+  if (n >= (1ull << 32)) return fail(WTG_ERR_INVALID, "n must be below 2^32");
+  if (flags & ~WTG_ALL) return fail(WTG_ERR_INVALID, "unknown flags");
+  return WTG_OK;
+}
+
+int sync_and_check(cudaStream_t s, const uint32_t* d_err) {
+  WTG_CK(cudaStreamSynchronize(s));
+  uint32_t e = 0;
+  if (d_err) {
+    WTG_CK(cudaMemcpy(&e, d_err, sizeof(e), cudaMemcpyDeviceToHost));
+  }
+  if (e == DERR_LOOKBACK_TIMEOUT) return fail(WTG_ERR_TIMEOUT, "a device-side wait timed out; results are invalid");
+  if (e == DERR_BAD_INDEX) return fail(WTG_ERR_CUDA, "a computed index fell outside its buffer (inconsistent tables)");
+  if (e) return fail(WTG_ERR_CUDA, "device reported error code " + std::to_string(e));
+  return WTG_OK;
+}
+
+uint64_t rank_words_of(uint64_t size) {
+  if (size == 0) return 2;
+  uint64_t cap = (size + 63) / 64 * 64;
+  return ((cap >> 9) + 1) << 1;
+}
+
+int build_tree_common(wtg_tree* T, const void* d_seq, uint64_t n, int eb, int levels, uint32_t flags) {
+  TreeImpl& t = T->t;
+  int rc;
+  if (levels == 0) {
+    if ((rc = tree_levels_from_max(t, d_seq, n, eb, &levels))) return rc;
+    if (levels > MAX_LEVELS) return fail(WTG_ERR_RANGE, "derived levels exceed 24");
+  }
+  return tree_build(t, d_seq, n, eb, levels, flags);
+}
+
+// runs `launch` on device copies of host query arrays
+template <typename F>
+int host_query(DevBuf& qbuf, cudaStream_t s, const uint64_t* const* ins, int nin, uint64_t nq,
+               uint64_t* const* outs, int nout, const uint32_t* d_err, F launch) {
+  int rc;
+  if (nq == 0) return WTG_OK;
+  if ((rc = qbuf.ensure((size_t)(nin + nout) * nq * sizeof(uint64_t), s))) return rc;
+  uint64_t* d = qbuf.as<uint64_t>();
+  for (int k = 0; k < nin; ++k)
+    WTG_CK(cudaMemcpyAsync(d + k * nq, ins[k], nq * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+  const uint64_t* din[4];
+  uint64_t* dout[4];
+  for (int k = 0; k < nin; ++k) din[k] = d + k * nq;
+  for (int k = 0; k < nout; ++k) dout[k] = d + (nin + k) * nq;
+  if ((rc = launch(din, dout))) return rc;
+  for (int k = 0; k < nout; ++k)
+    WTG_CK(cudaMemcpyAsync(outs[k], dout[k], nq * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+  return sync_and_check(s, d_err);
+}
+
+void fill_select_info(const BvSupport& bv, int t_b, uint64_t info[8]) {
+  const SelectDev& sd = bv.sel[t_b];
+  info[0] = bv.size;
+  info[1] = sd.arg_cnt;
+  info[2] = sd.logn;
+  info[3] = sd.logn4;
+  info[4] = sd.nsb;
+  info[5] = sd.has_long;
+  info[6] = sd.sb_nwords;
+  info[7] = sd.pool_nwords;
+}
+
+int copy_select(const BvSupport& bv, int t_b, uint64_t* sb_words, uint64_t* desc, uint64_t* pool, cudaStream_t s) {
+  if (!(bv.flags & (t_b ? WTG_SELECT1 : WTG_SELECT0))) return fail(WTG_ERR_INVALID, "select support not built");
+  const SelectDev& sd = bv.sel[t_b];
+  if (sd.sb_nwords && sb_words)
+    WTG_CK(cudaMemcpyAsync(sb_words, sd.sb_words.p, sd.sb_nwords * 8, cudaMemcpyDeviceToHost, s));
+  if (sd.nsb && desc) WTG_CK(cudaMemcpyAsync(desc, sd.desc.p, sd.nsb * 8, cudaMemcpyDeviceToHost, s));
+  if (sd.pool_nwords && pool) WTG_CK(cudaMemcpyAsync(pool, sd.pool.p, sd.pool_nwords * 8, cudaMemcpyDeviceToHost, s));
+  WTG_CK(cudaStreamSynchronize(s));
+  return WTG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+// ------------------------------------------------------------------ trees
+
+int wtg_tree_build(const void* seq, uint64_t n, int elem_bytes, int levels, uint32_t flags, wtg_tree** out) {
+  int rc;
+  if (!out || (!seq && n)) return fail(WTG_ERR_INVALID, "null argument");
+  if ((rc = check_seq_args(n, elem_bytes, levels, flags))) return rc;
+  if ((rc = check_device())) return rc;
+  wtg_tree* T = *out;
+  const bool fresh = (T == nullptr);
+  if (fresh) {
+    T = new (std::nothrow) wtg_tree();
+    if (!T) return fail(WTG_ERR_OOM, "host allocation failed");
+  }
+  TreeImpl& t = T->t;
+  if (!t.own_stream) {
+    cudaError_t e = cudaStreamCreateWithFlags(&t.stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+      if (fresh) delete T;
+      return cuda_fail(e, "cudaStreamCreate");
+    }
+    t.own_stream = true;
+  }
+  if ((rc = t.seq.ensure(n * elem_bytes, t.stream)) == WTG_OK) {
+    cudaError_t ce = cudaSuccess;
+    if (n) ce = cudaMemcpyAsync(t.seq.p, seq, n * elem_bytes, cudaMemcpyHostToDevice, t.stream);
+    if (ce != cudaSuccess) rc = cuda_fail(ce, "cudaMemcpyAsync(seq)");
+  }
+  if (rc == WTG_OK) rc = build_tree_common(T, t.seq.p, n, elem_bytes, levels, flags);
+  if (rc == WTG_OK) rc = sync_and_check(t.stream, t.err.as<uint32_t>());
+  if (rc != WTG_OK) {
+    if (fresh) wtg_tree_free(T);
+    return rc;
+  }
+  *out = T;
+  return WTG_OK;
+}
+
+int wtg_tree_build_device(const void* d_seq, uint64_t n, int elem_bytes, int levels, uint32_t flags, void* stream,
+                          wtg_tree** out) {
+  int rc;
+  if (!out || (!d_seq && n)) return fail(WTG_ERR_INVALID, "null argument");
+  if ((rc = check_seq_args(n, elem_bytes, levels, flags))) return rc;
+  if ((rc = check_device())) return rc;
+  wtg_tree* T = *out;
+  bool fresh = false;
+  if (!T) {
+    T = new (std::nothrow) wtg_tree();
+    if (!T) return fail(WTG_ERR_OOM, "host allocation failed");
+    fresh = true;
+  }
+  if (T->t.own_stream) {
+    cudaStreamSynchronize(T->t.stream);
+    cudaStreamDestroy(T->t.stream);
+    T->t.own_stream = false;
+  }
+  T->t.stream = (cudaStream_t)stream;
+  rc = build_tree_common(T, d_seq, n, elem_bytes, levels, flags);
+  if (rc != WTG_OK) {
+    if (fresh) wtg_tree_free(T);
+    return rc;
+  }
+  *out = T;
+  return WTG_OK;
+}
+
+int wtg_tree_sync(wtg_tree* T) {
+  if (!T) return fail(WTG_ERR_INVALID, "null tree");
+  return sync_and_check(T->t.stream, T->t.err.as<uint32_t>());
+}
+
+int wtg_tree_free(wtg_tree* T) {
+  if (!T) return WTG_OK;
+  cudaStream_t s = T->t.stream;
+  tree_release(T->t);
+  cudaStreamSynchronize(s);
+  if (T->t.own_stream) cudaStreamDestroy(s);
+  delete T;
+  return WTG_OK;
+}
+
+int wtg_tree_info(wtg_tree* T, uint64_t info[4]) {
+  if (!T || !info) return fail(WTG_ERR_INVALID, "null argument");
+  info[0] = T->t.n;
+  info[1] = (uint64_t)T->t.levels;
+  info[2] = T->t.bit_words;
+  info[3] = (T->t.flags & WTG_RANK) ? rank_words_of(T->t.n * (uint64_t)T->t.levels) : 0;
+  return WTG_OK;
+}
+
+int wtg_tree_select_info(wtg_tree* T, int t_b, uint64_t info[8]) {
+  if (!T || !info || (t_b != 0 && t_b != 1)) return fail(WTG_ERR_INVALID, "bad argument");
+  if (!(T->t.flags & (t_b ? WTG_SELECT1 : WTG_SELECT0))) return fail(WTG_ERR_INVALID, "select support not built");
+  fill_select_info(T->t.bv, t_b, info);
+  return WTG_OK;
+}
+
+int wtg_tree_get_bits(wtg_tree* T, uint64_t* dst, uint64_t nwords) {
+  if (!T || (!dst && nwords)) return fail(WTG_ERR_INVALID, "null argument");
+  if (nwords != T->t.bit_words) return fail(WTG_ERR_INVALID, "nwords does not match the tree");
+  if (nwords) WTG_CK(cudaMemcpyAsync(dst, T->t.bits.p, nwords * 8, cudaMemcpyDeviceToHost, T->t.stream));
+  return sync_and_check(T->t.stream, T->t.err.as<uint32_t>());
+}
+
+int wtg_tree_get_nodes(wtg_tree* T, int index_bytes, uint64_t n_entries, void* dst) {
+  int rc;
+  if (!T || (!dst && n_entries)) return fail(WTG_ERR_INVALID, "null argument");
+  if (index_bytes != 4 && index_bytes != 8) return fail(WTG_ERR_INVALID, "index_bytes must be 4 or 8");
+  TreeImpl& t = T->t;
+  const size_t bytes = n_entries * 5 * (size_t)index_bytes;
+  if ((rc = t.nodes.ensure(bytes, t.stream))) return rc;
+  if ((rc = tree_nodes(t, index_bytes, n_entries, t.nodes.p))) return rc;
+  if (bytes) WTG_CK(cudaMemcpyAsync(dst, t.nodes.p, bytes, cudaMemcpyDeviceToHost, t.stream));
+  return sync_and_check(t.stream, t.err.as<uint32_t>());
+}
+
+int wtg_tree_get_rank(wtg_tree* T, uint64_t* dst, uint64_t nwords) {
+  if (!T || !dst) return fail(WTG_ERR_INVALID, "null argument");
+  if (!(T->t.flags & WTG_RANK)) return fail(WTG_ERR_INVALID, "rank support not built");
+  if (nwords != rank_words_of(T->t.n * (uint64_t)T->t.levels)) return fail(WTG_ERR_INVALID, "nwords mismatch");
+  WTG_CK(cudaMemcpyAsync(dst, T->t.bv.rank.p, nwords * 8, cudaMemcpyDeviceToHost, T->t.stream));
+  return sync_and_check(T->t.stream, T->t.err.as<uint32_t>());
+}
+
+int wtg_tree_get_select(wtg_tree* T, int t_b, uint64_t* sb_words, uint64_t* desc, uint64_t* pool) {
+  if (!T || (t_b != 0 && t_b != 1)) return fail(WTG_ERR_INVALID, "bad argument");
+  int rc = copy_select(T->t.bv, t_b, sb_words, desc, pool, T->t.stream);
+  if (rc) return rc;
+  return sync_and_check(T->t.stream, T->t.err.as<uint32_t>());
+}
+
+int wtg_tree_device_ptrs(wtg_tree* T, uint64_t ptrs[8]) {
+  if (!T || !ptrs) return fail(WTG_ERR_INVALID, "null argument");
+  const BvSupport& bv = T->t.bv;
+  ptrs[0] = (uint64_t)T->t.bits.p;
+  ptrs[1] = (uint64_t)bv.rank.p;
+  ptrs[2] = (uint64_t)bv.sel[1].sb_words.p;
+  ptrs[3] = (uint64_t)bv.sel[1].desc.p;
+  ptrs[4] = (uint64_t)bv.sel[1].pool.p;
+  ptrs[5] = (uint64_t)bv.sel[0].sb_words.p;
+  ptrs[6] = (uint64_t)bv.sel[0].desc.p;
+  ptrs[7] = (uint64_t)bv.sel[0].pool.p;
+  return WTG_OK;
+}
+
+// ---------------------------------------------------------------- queries
+
+int wtg_query_access(wtg_tree* T, const uint64_t* idx, uint64_t nq, uint64_t* out) {
+  if (!T || (nq && (!idx || !out))) return fail(WTG_ERR_INVALID, "null argument");
+  TreeImpl& t = T->t;
+  const uint64_t* ins[1] = {idx};
+  uint64_t* outs[1] = {out};
+  return host_query(t.qbuf, t.stream, ins, 1, nq, outs, 1, t.err.as<uint32_t>(),
+                    [&](const uint64_t** din, uint64_t** dout) {
+                      return launch_wt_access(t, din[0], nq, dout[0], t.stream);
+                    });
+}
+
+int wtg_query_rank(wtg_tree* T, const uint64_t* idx, const uint64_t* sym, uint64_t nq, uint64_t* out) {
+  if (!T || (nq && (!idx || !sym || !out))) return fail(WTG_ERR_INVALID, "null argument");
+  TreeImpl& t = T->t;
+  const uint64_t* ins[2] = {idx, sym};
+  uint64_t* outs[1] = {out};
+  return host_query(t.qbuf, t.stream, ins, 2, nq, outs, 1, t.err.as<uint32_t>(),
+                    [&](const uint64_t** din, uint64_t** dout) {
+                      return launch_wt_rank(t, din[0], din[1], nq, dout[0], t.stream);
+                    });
+}
+
+int wtg_query_inverse_select(wtg_tree* T, const uint64_t* idx, uint64_t nq, uint64_t* rank_out, uint64_t* sym_out) {
+  if (!T || (nq && (!idx || !rank_out || !sym_out))) return fail(WTG_ERR_INVALID, "null argument");
+  TreeImpl& t = T->t;
+  const uint64_t* ins[1] = {idx};
+  uint64_t* outs[2] = {rank_out, sym_out};
+  return host_query(t.qbuf, t.stream, ins, 1, nq, outs, 2, t.err.as<uint32_t>(),
+                    [&](const uint64_t** din, uint64_t** dout) {
+                      return launch_wt_inverse_select(t, din[0], nq, dout[0], dout[1], t.stream);
+                    });
+}
+
+int wtg_query_select(wtg_tree* T, const uint64_t* i, const uint64_t* sym, uint64_t nq, uint64_t* out) {
+  if (!T || (nq && (!i || !sym || !out))) return fail(WTG_ERR_INVALID, "null argument");
+  TreeImpl& t = T->t;
+  const uint64_t* ins[2] = {i, sym};
+  uint64_t* outs[1] = {out};
+  return host_query(t.qbuf, t.stream, ins, 2, nq, outs, 1, t.err.as<uint32_t>(),
+                    [&](const uint64_t** din, uint64_t** dout) {
+                      return launch_wt_select(t, din[0], din[1], nq, dout[0], t.stream);
+                    });
+}
+
+int wtg_query_access_device(wtg_tree* T, const uint64_t* d_idx, uint64_t nq, uint64_t* d_out, void* stream) {
+  if (!T) return fail(WTG_ERR_INVALID, "null tree");
+  return launch_wt_access(T->t, d_idx, nq, d_out, (cudaStream_t)stream);
+}
+
+int wtg_query_rank_device(wtg_tree* T, const uint64_t* d_idx, const uint64_t* d_sym, uint64_t nq, uint64_t* d_out,
+                          void* stream) {
+  if (!T) return fail(WTG_ERR_INVALID, "null tree");
+  return launch_wt_rank(T->t, d_idx, d_sym, nq, d_out, (cudaStream_t)stream);
+}
+
+// ----------------------------------------------------- standalone bitvectors
+
+static int bv_common(wtg_bv* B, const uint64_t* d_words, uint64_t size, uint32_t flags) {
+  int rc;
+  if ((rc = B->err.ensure(sizeof(uint32_t), B->stream))) return rc;
+  WTG_CK(cudaMemsetAsync(B->err.p, 0, sizeof(uint32_t), B->stream));
+  return bv_build(B->bv, d_words, size, flags, B->err.as<uint32_t>(), B->stream);
+}
+
+int wtg_bv_build(const uint64_t* words, uint64_t size_bits, uint32_t flags, wtg_bv** out) {
+  int rc;
+  if (!out || (!words && size_bits)) return fail(WTG_ERR_INVALID, "null argument");
+  *out = nullptr;
+  if (flags & ~WTG_ALL) return fail(WTG_ERR_INVALID, "unknown flags");
+  if (size_bits >= (1ull << 40)) return fail(WTG_ERR_INVALID, "bitvector too large");
+  if ((rc = check_device())) return rc;
+  wtg_bv* B = new (std::nothrow) wtg_bv();
+  if (!B) return fail(WTG_ERR_OOM, "host allocation failed");
+  cudaError_t e = cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete B;
+    return cuda_fail(e, "cudaStreamCreate");
+  }
+  B->own_stream = true;
+  const uint64_t W = (size_bits + 63) / 64;
+  rc = B->words.ensure((W + 2) * 8, B->stream);
+  if (rc == WTG_OK) {
+    cudaError_t ce = cudaMemsetAsync(B->words.p, 0, (W + 2) * 8, B->stream);
+    if (ce == cudaSuccess && W) ce = cudaMemcpyAsync(B->words.p, words, W * 8, cudaMemcpyHostToDevice, B->stream);
+    if (ce != cudaSuccess) rc = cuda_fail(ce, "copy bitvector");
+  }
+  if (rc == WTG_OK) rc = bv_common(B, B->words.as<uint64_t>(), size_bits, flags);
+  if (rc == WTG_OK) rc = sync_and_check(B->stream, B->err.as<uint32_t>());
+  if (rc != WTG_OK) {
+    wtg_bv_free(B);
+    return rc;
+  }
+  *out = B;
+  return WTG_OK;
+}
+
+int wtg_bv_build_device(const uint64_t* d_words, uint64_t size_bits, uint32_t flags, void* stream, wtg_bv** out) {
+  int rc;
+  if (!out || (!d_words && size_bits)) return fail(WTG_ERR_INVALID, "null argument");
+  if (flags & ~WTG_ALL) return fail(WTG_ERR_INVALID, "unknown flags");
+  if (size_bits >= (1ull << 40)) return fail(WTG_ERR_INVALID, "bitvector too large");
+  if ((rc = check_device())) return rc;
+  wtg_bv* B = *out;
+  bool fresh = false;
+  if (!B) {
+    B = new (std::nothrow) wtg_bv();
+    if (!B) return fail(WTG_ERR_OOM, "host allocation failed");
+    fresh = true;
+  }
+  B->stream = (cudaStream_t)stream;
+  rc = bv_common(B, d_words, size_bits, flags);
+  if (rc != WTG_OK) {
+    if (fresh) wtg_bv_free(B);
+    return rc;
+  }
+  *out = B;
+  return WTG_OK;
+}
+
+int wtg_bv_sync(wtg_bv* B) {
+  if (!B) return fail(WTG_ERR_INVALID, "null bitvector");
+  return sync_and_check(B->stream, B->err.as<uint32_t>());
+}
+
+int wtg_bv_free(wtg_bv* B) {
+  if (!B) return WTG_OK;
+  cudaStream_t s = B->stream;
+  bv_release(B->bv, s);
+  B->words.release(s);
+  B->err.release(s);
+  B->qbuf.release(s);
+  cudaStreamSynchronize(s);
+  if (B->own_stream) cudaStreamDestroy(s);
+  delete B;
+  return WTG_OK;
+}
+
+int wtg_bv_rank_words(wtg_bv* B, uint64_t* nwords) {
+  if (!B || !nwords) return fail(WTG_ERR_INVALID, "null argument");
+  *nwords = rank_words_of(B->bv.size);
+  return WTG_OK;
+}
+
+int wtg_bv_get_rank(wtg_bv* B, uint64_t* dst, uint64_t nwords) {
+  if (!B || !dst) return fail(WTG_ERR_INVALID, "null argument");
+  if (!(B->bv.flags & WTG_RANK)) return fail(WTG_ERR_INVALID, "rank support not built");
+  if (nwords != rank_words_of(B->bv.size)) return fail(WTG_ERR_INVALID, "nwords mismatch");
+  WTG_CK(cudaMemcpyAsync(dst, B->bv.rank.p, nwords * 8, cudaMemcpyDeviceToHost, B->stream));
+  return sync_and_check(B->stream, B->err.as<uint32_t>());
+}
+
+int wtg_bv_select_info(wtg_bv* B, int t_b, uint64_t info[8]) {
+  if (!B || !info || (t_b != 0 && t_b != 1)) return fail(WTG_ERR_INVALID, "bad argument");
+  if (!(B->bv.flags & (t_b ? WTG_SELECT1 : WTG_SELECT0))) return fail(WTG_ERR_INVALID, "select support not built");
+  fill_select_info(B->bv, t_b, info);
+  return WTG_OK;
+}
+
+int wtg_bv_get_select(wtg_bv* B, int t_b, uint64_t* sb_words, uint64_t* desc, uint64_t* pool) {
+  if (!B || (t_b != 0 && t_b != 1)) return fail(WTG_ERR_INVALID, "bad argument");
+  int rc = copy_select(B->bv, t_b, sb_words, desc, pool, B->stream);
+  if (rc) return rc;
+  return sync_and_check(B->stream, B->err.as<uint32_t>());
+}
+
+int wtg_bv_rank(wtg_bv* B, const uint64_t* idx, uint64_t nq, uint64_t* out) {
+  if (!B || (nq && (!idx || !out))) return fail(WTG_ERR_INVALID, "null argument");
+  const uint64_t* ins[1] = {idx};
+  uint64_t* outs[1] = {out};
+  return host_query(B->qbuf, B->stream, ins, 1, nq, outs, 1, B->err.as<uint32_t>(),
+                    [&](const uint64_t** din, uint64_t** dout) {
+                      return launch_bv_rank(B->bv, din[0], nq, dout[0], B->stream);
+                    });
+}
+
+int wtg_bv_select(wtg_bv* B, int t_b, const uint64_t* i, uint64_t nq, uint64_t* out) {
+  if (!B || (t_b != 0 && t_b != 1) || (nq && (!i || !out))) return fail(WTG_ERR_INVALID, "bad argument");
+  const uint64_t* ins[1] = {i};
+  uint64_t* outs[1] = {out};
+  return host_query(B->qbuf, B->stream, ins, 1, nq, outs, 1, B->err.as<uint32_t>(),
+                    [&](const uint64_t** din, uint64_t** dout) {
+                      return launch_bv_select(B->bv, t_b, din[0], nq, dout[0], B->stream);
+                    });
+}
+
+int wtg_bv_select_device(wtg_bv* B, int t_b, const uint64_t* d_i, uint64_t nq, uint64_t* d_out, void* stream) {
+  if (!B || (t_b != 0 && t_b != 1)) return fail(WTG_ERR_INVALID, "bad argument");
+  return launch_bv_select(B->bv, t_b, d_i, nq, d_out, (cudaStream_t)stream);
+}
+
+// ------------------------------------------------------------------ helpers
+
+int wtg_remap_alphabet(void* seq, uint64_t n, int elem_bytes, uint64_t* sigma_out) {
+  int rc;
+  if (!sigma_out || (!seq && n)) return fail(WTG_ERR_INVALID, "null argument");
+  if (elem_bytes != 1 && elem_bytes != 2 && elem_bytes != 4 && elem_bytes != 8)
+    return fail(WTG_ERR_INVALID, "elem_bytes must be 1, 2, 4 or 8");
+  if ((rc = check_device())) return rc;
+  cudaStream_t s;
+  WTG_CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  DevBuf d, tmp, scan_tmp, err;
+  rc = d.ensure(n * elem_bytes, s);
+  if (!rc) rc = err.ensure(sizeof(uint32_t), s);
+  if (!rc) {
+    cudaError_t ce = cudaMemsetAsync(err.p, 0, sizeof(uint32_t), s);
+    if (ce == cudaSuccess && n) ce = cudaMemcpyAsync(d.p, seq, n * elem_bytes, cudaMemcpyHostToDevice, s);
+    if (ce != cudaSuccess) rc = cuda_fail(ce, "copy sequence");
+  }
+  if (!rc) rc = remap_alphabet_device(d.p, n, elem_bytes, sigma_out, tmp, scan_tmp, err.as<uint32_t>(), s);
+  if (!rc && n) {
+    cudaError_t ce = cudaMemcpyAsync(seq, d.p, n * elem_bytes, cudaMemcpyDeviceToHost, s);
+    if (ce != cudaSuccess) rc = cuda_fail(ce, "copy sequence back");
+  }
+  if (!rc) rc = sync_and_check(s, err.as<uint32_t>());
+  d.release(s);
+  tmp.release(s);
+  scan_tmp.release(s);
+  err.release(s);
+  cudaStreamSynchronize(s);
+  cudaStreamDestroy(s);
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,232 @@
+// wtg_internal.cuh -- device primitives and internal host interfaces shared by
+// the wtg CUDA sources (GB300 / sm_103a).
+//
+// Data layouts kept bit-exact with the reference (jlabeit/wavelet-suffix-fm-index):
+//   * level bitvector: level l occupies bits [l*n, (l+1)*n) of one array of
+//     64-bit words, LSB first (wavelet/levelWT/WT.C:97,104,136);
+//   * rank_support_v<1> table: interleaved (absolute count, seven 9-bit
+//     cumulative block counts) per 512-bit superblock
+//     (rank/rank_support_v_par.hpp:78-113);
+//   * select_support_mcl<t_b>: m_superblock int_vector<0> of width logn, and
+//     per superblock a 64-entry mini block or a 4096-entry long block
+//     (select/select_support_mcl_par.hpp:483-561), stored flat (see
+//     include/wtg.h).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+#include <string>
+
+#include "../../include/wtg.h"
+
+namespace wtg {
+
+// number of kernel launches issued (reported through wtg_launch_count)
+extern std::atomic<uint64_t> g_launches;
+inline void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+// kernel-class profiling (wtg_profile_enable / wtg_profile_read)
+enum ProfClass { PROF_LEVEL = 0, PROF_LEVEL_LAST, PROF_HIST, PROF_TABLES, PROF_BVPASS, PROF_SELECT, PROF_N };
+bool prof_on();
+void prof_begin(int cls, cudaStream_t s);  // call right before a launch
+void prof_end(int cls, cudaStream_t s);    // call right after it
+
+// ------------------------------------------------------------------ errors
+
+// Device-side error codes written to the per-handle error word.
+enum : uint32_t {
+  DERR_NONE = 0,
+  DERR_LOOKBACK_TIMEOUT = 1,  // a decoupled look-back wait gave up
+  DERR_BAD_SYMBOL = 2,
+  DERR_SELECT_OVERFLOW = 3,  // more args in a superblock than fit its block
+  DERR_BAD_INDEX = 4,        // a computed destination fell outside its buffer
+};
+
+void set_error(const std::string& msg);
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+
+#define WTG_CK(call)                                   \
+  do {                                                 \
+    cudaError_t _e = (call);                           \
+    if (_e != cudaSuccess) return ::wtg::cuda_fail(_e, #call); \
+  } while (0)
+
+// ------------------------------------------------------ device primitives
+
+constexpr uint64_t NONE64 = ~0ull;
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+  uint32_t m;
+  asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// position of the i-th (1-based) set bit of x (bits::sel semantics); i <= popc(x)
+__device__ __forceinline__ uint32_t sel64(uint64_t x, uint32_t i) {
+  uint32_t lo = __popc((uint32_t)x);
+  uint32_t base = 0;
+  uint32_t w = (uint32_t)x;
+  if (i > lo) { i -= lo; w = (uint32_t)(x >> 32); base = 32; }
+  // binary search over the 32-bit half
+  uint32_t c = __popc(w & 0xFFFFu);
+  if (i > c) { i -= c; w >>= 16; base += 16; }
+  c = __popc(w & 0xFFu);
+  if (i > c) { i -= c; w >>= 8; base += 8; }
+  c = __popc(w & 0xFu);
+  if (i > c) { i -= c; w >>= 4; base += 4; }
+  c = __popc(w & 0x3u);
+  if (i > c) { i -= c; w >>= 2; base += 2; }
+  c = w & 1u;
+  if (i > c) { base += 1; }
+  return base;
+}
+
+// sdsl bits::hi (0 for x == 0)
+__host__ __device__ __forceinline__ uint32_t hi64(uint64_t x) {
+#ifdef __CUDA_ARCH__
+  return x ? 63u - __clzll((long long)x) : 0u;
+#else
+  return x ? 63u - (uint32_t)__builtin_clzll(x) : 0u;
+#endif
+}
+
+// entry j of an int_vector<0> of width w stored at words
+__device__ __forceinline__ uint64_t packed_get(const uint64_t* __restrict__ words, uint64_t j, uint32_t w) {
+  uint64_t off = j * (uint64_t)w;
+  uint64_t wi = off >> 6;
+  uint32_t sh = (uint32_t)(off & 63);
+  uint64_t v = words[wi] >> sh;
+  if (sh + w > 64) v |= words[wi + 1] << (64 - sh);
+  return w < 64 ? (v & ((1ull << w) - 1)) : v;
+}
+
+// output word q of an int_vector<0> of width w whose entries are given by f(j)
+// (entries j >= count are zero)
+template <typename F>
+__device__ __forceinline__ uint64_t packed_word(uint64_t q, uint32_t w, uint64_t count, F f) {
+  uint64_t lo = q * 64, hi = lo + 63;
+  uint64_t j0 = lo / w, j1 = hi / w;
+  uint64_t out = 0;
+  uint64_t mask = w < 64 ? ((1ull << w) - 1) : ~0ull;
+  for (uint64_t j = j0; j <= j1 && j < count; ++j) {
+    uint64_t v = f(j) & mask;
+    int64_t sh = (int64_t)(j * w) - (int64_t)lo;
+    if (sh >= 0) out |= v << sh;
+    else out |= v >> (-sh);
+  }
+  return out;
+}
+
+// ------------------------------------------------ decoupled look-back scan
+//
+// Single-pass scan status words (Merrill & Garland, "Single-pass Parallel
+// Prefix Scan with Decoupled Look-back", 2016): each tile publishes its
+// aggregate, then its inclusive prefix.  64-bit word = flag (2 bits) | value.
+// Tiles take their index from an atomic counter, so every predecessor of a
+// tile has already started and the chain always completes; every wait is
+// nevertheless bounded, and on expiry the tile records DERR_LOOKBACK_TIMEOUT
+// and proceeds (the host then reports the build as failed).
+
+constexpr uint64_t LB_FLAG_AGG = 1ull << 62;
+constexpr uint64_t LB_FLAG_INC = 2ull << 62;
+constexpr uint64_t LB_VALUE_MASK = (1ull << 62) - 1;
+constexpr uint32_t LB_SPIN_LIMIT = 1u << 22;  // ~ seconds with the backoff below
+
+__device__ __forceinline__ void lb_publish(uint64_t* status, uint32_t tile, uint64_t flag, uint64_t v) {
+  __threadfence();
+  atomicExch((unsigned long long*)&status[tile], (unsigned long long)(flag | (v & LB_VALUE_MASK)));
+}
+
+__device__ __forceinline__ uint64_t lb_load(const uint64_t* status, uint64_t idx) {
+  return *((volatile const unsigned long long*)&status[idx]);
+}
+
+// Warp-cooperative look-back; call with the whole warp.  Returns the exclusive
+// prefix of `tile` (tile > 0).
+__device__ __forceinline__ uint64_t lb_lookback_warp(uint64_t* status, uint32_t tile, uint32_t* err) {
+  const uint32_t lane = threadIdx.x & 31;
+  uint64_t prefix = 0;
+  int64_t base = (int64_t)tile - 1;
+  while (base >= 0) {
+    int64_t j = base - lane;
+    uint64_t s = 0;
+    if (j >= 0) {
+      uint32_t spins = 0, ns = 32;
+      s = lb_load(status, (uint64_t)j);
+      while ((s >> 62) == 0) {
+        if (++spins > LB_SPIN_LIMIT) {
+          atomicCAS(err, 0u, (uint32_t)DERR_LOOKBACK_TIMEOUT);
+          s = LB_FLAG_INC;  // give up: treat as an inclusive zero
+          break;
+        }
+        __nanosleep(ns);
+        if (ns < 1024) ns <<= 1;
+        s = lb_load(status, (uint64_t)j);
+      }
+    } else {
+      s = LB_FLAG_INC;  // before tile 0: inclusive zero
+    }
+    uint32_t inc_mask = __ballot_sync(0xffffffffu, (s >> 62) == 2);
+    uint64_t v = s & LB_VALUE_MASK;
+    if (inc_mask) {
+      uint32_t first = __ffs(inc_mask) - 1;  // nearest inclusive predecessor
+      if (lane > first) v = 0;
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      prefix += v;
+      break;
+    }
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    prefix += v;
+    base -= 32;
+  }
+  return prefix;
+}
+
+// ------------------------------------------------------- host-side pieces
+
+// Stream-ordered device buffer that keeps its allocation across rebuilds.
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  int ensure(size_t need, cudaStream_t s);
+  void release(cudaStream_t s);
+  template <typename T>
+  T* as() const { return (T*)p; }
+};
+
+int scan_exclusive_u32(const uint32_t* in, uint32_t* out, uint64_t n, DevBuf& scratch, uint32_t* d_err,
+                       cudaStream_t s);
+int scan_exclusive_u64(const uint64_t* in, uint64_t* out, uint64_t n, DevBuf& scratch, uint32_t* d_err,
+                       cudaStream_t s);
+
+// Flat select_support_mcl on the device.
+struct SelectDev {
+  uint64_t arg_cnt = 0, nsb = 0, logn = 0, logn4 = 0, has_long = 0, sb_nwords = 0, pool_nwords = 0;
+  DevBuf ends;      // superblock end positions (upper-bound sized)
+  DevBuf desc;      // per superblock descriptor
+  DevBuf sizes;     // per superblock pool words (scan input)
+  DevBuf sb_words;  // packed m_superblock
+  DevBuf pool;      // packed mini/long blocks
+  DevBuf long_list; // superblock ids of long blocks
+};
+
+// Rank/select support over one bitvector (caller or tree owned words).
+struct BvSupport {
+  uint64_t size = 0;
+  const uint64_t* words = nullptr;  // device
+  uint32_t flags = 0;
+  DevBuf rank;       // rank_support_v table
+  DevBuf samples;    // every 64th arg: select1 from the front, select0 from the back
+  DevBuf info;       // device scalars (see bitvec.cu)
+  DevBuf status;     // look-back status words + tile counter
+  DevBuf scan_tmp;
+  SelectDev sel[2];  // [t_b]
+};
+
+int bv_build(BvSupport& bv, const uint64_t* d_words, uint64_t size, uint32_t flags, uint32_t* d_err,
+             cudaStream_t s);
+void bv_release(BvSupport& bv, cudaStream_t s);
+
+}  // namespace wtg

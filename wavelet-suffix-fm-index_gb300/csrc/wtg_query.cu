@@ -1,0 +1,384 @@
+// wtg_query.cu -- batched queries on the GPU: rank_support_v::rank,
+// select_support_mcl::select, and wt_int's access / rank / inverse_select /
+// select, one thread per query; plus the alphabet remap helper.
+#include <algorithm>
+
+#include "wtg_tree.cuh"
+
+namespace wtg {
+
+// rank_support_v<1>::rank (rank/rank_support_v_par.hpp:131-142)
+__device__ __forceinline__ uint64_t rank1_dev(const uint64_t* __restrict__ tbl, const uint64_t* __restrict__ w,
+                                              uint64_t idx) {
+  const uint64_t* p = tbl + ((idx >> 8) & 0xFFFFFFFFFFFFFFFEull);
+  uint64_t r = p[0] + ((p[1] >> (63 - 9 * ((idx & 0x1FF) >> 6))) & 0x1FF);
+  if (idx & 0x3F) r += __popcll(w[idx >> 6] & ((1ull << (idx & 63)) - 1));
+  return r;
+}
+
+struct SelView {
+  const uint64_t* words;
+  uint64_t nwords;  // data words at `words`
+  const uint64_t* sb_words;
+  const uint64_t* desc;
+  const uint64_t* pool;
+  uint64_t arg_cnt;
+  uint32_t logn;
+  int has_long;
+  int t_b;
+};
+
+// select_support_mcl::select(i), 1 <= i <= arg_cnt
+// (select/select_support_mcl_par.hpp:564-611) on the flat layout
+__device__ __forceinline__ uint64_t select_dev(const SelView& v, uint64_t i) {
+  if (i == 0 || i > v.arg_cnt) return NONE64;
+  i = i - 1;
+  const uint64_t sb = i >> 12, off = i & 0xFFF;
+  const uint64_t d = v.desc[sb];
+  const uint32_t wdt = (uint32_t)(d & 127);
+  const uint64_t* blk = v.pool + (d >> 8);
+  if (v.has_long && ((d >> 7) & 1)) return packed_get(blk, off, wdt);
+  const uint64_t base = packed_get(v.sb_words, sb, v.logn);
+  const uint64_t mini = packed_get(blk, off >> 6, wdt);
+  if ((off & 0x3F) == 0) return base + mini;
+  i = i - (sb << 12) - ((off >> 6) << 6);
+  const uint64_t pos = base + mini + 1;
+  uint64_t word_pos = pos >> 6;
+  const uint32_t word_off = (uint32_t)(pos & 0x3F);
+  if (word_pos >= v.nwords) return NONE64;
+  uint64_t wd = v.words[word_pos];
+  if (!v.t_b) wd = ~wd;
+  const uint64_t first = wd & (~0ull << word_off);
+  uint64_t args = __popcll(first);
+  if (args >= i) return (word_pos << 6) + sel64(first, (uint32_t)i);
+  uint64_t sum = args;
+  word_pos += 1;
+  if (word_pos >= v.nwords) return NONE64;
+  wd = v.words[word_pos];
+  if (!v.t_b) wd = ~wd;
+  args = __popcll(wd);
+  while (sum + args < i) {
+    sum += args;
+    word_pos += 1;
+    if (word_pos >= v.nwords) return NONE64;  // inconsistent tables: never read past the data
+    wd = v.words[word_pos];
+    if (!v.t_b) wd = ~wd;
+    args = __popcll(wd);
+  }
+  return (word_pos << 6) + sel64(wd, (uint32_t)(i - sum));
+}
+
+static SelView sel_view(const BvSupport& bv, int t_b) {
+  const SelectDev& sd = bv.sel[t_b];
+  SelView v;
+  v.words = bv.words;
+  v.nwords = (bv.size + 63) / 64;  // a valid query never reads past the data words
+  v.sb_words = sd.sb_words.as<uint64_t>();
+  v.desc = sd.desc.as<uint64_t>();
+  v.pool = sd.pool.as<uint64_t>();
+  v.arg_cnt = sd.arg_cnt;
+  v.logn = (uint32_t)sd.logn;
+  v.has_long = (int)sd.has_long;
+  v.t_b = t_b;
+  return v;
+}
+
+__device__ __forceinline__ int bit_at(const uint64_t* __restrict__ w, uint64_t p) {
+  return (int)((w[p >> 6] >> (p & 63)) & 1);
+}
+
+// wt_int::operator[] (wt_int/wt_int_par.hpp:519-541)
+__global__ void wt_access_kernel(const uint64_t* __restrict__ tree, const uint64_t* __restrict__ rt, uint64_t n,
+                                 int L, const uint64_t* __restrict__ q, uint64_t nq, uint64_t* __restrict__ out) {
+  uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nq) return;
+  uint64_t i = q[k];
+  if (i >= n) {
+    out[k] = NONE64;
+    return;
+  }
+  uint64_t offset = 0, res = 0, node_size = n;
+  for (int lv = 0; lv < L; ++lv) {
+    res <<= 1;
+    const uint64_t o = rank1_dev(rt, tree, offset);
+    const uint64_t oi = rank1_dev(rt, tree, offset + i) - o;
+    const uint64_t oe = rank1_dev(rt, tree, offset + node_size) - o;
+    if (bit_at(tree, offset + i)) {
+      offset += node_size - oe;
+      node_size = oe;
+      i = oi;
+      res |= 1;
+    } else {
+      node_size = node_size - oe;
+      i = i - oi;
+    }
+    offset += n;
+  }
+  out[k] = res;
+}
+
+// wt_int::rank (wt_int_par.hpp:553-577)
+__global__ void wt_rank_kernel(const uint64_t* __restrict__ tree, const uint64_t* __restrict__ rt, uint64_t n,
+                               int L, const uint64_t* __restrict__ q, const uint64_t* __restrict__ sym, uint64_t nq,
+                               uint64_t* __restrict__ out) {
+  uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nq) return;
+  uint64_t i = q[k];
+  const uint64_t c = sym[k];
+  if (i > n) {
+    out[k] = NONE64;
+    return;
+  }
+  if (L < 64 && (1ull << L) <= c) {
+    out[k] = 0;
+    return;
+  }
+  uint64_t offset = 0, mask = 1ull << (L - 1), node_size = n;
+  for (int lv = 0; lv < L && i; ++lv) {
+    const uint64_t o = rank1_dev(rt, tree, offset);
+    const uint64_t oi = rank1_dev(rt, tree, offset + i) - o;
+    const uint64_t oe = rank1_dev(rt, tree, offset + node_size) - o;
+    if (c & mask) {
+      offset += node_size - oe;
+      node_size = oe;
+      i = oi;
+    } else {
+      node_size = node_size - oe;
+      i = i - oi;
+    }
+    offset += n;
+    mask >>= 1;
+  }
+  out[k] = i;
+}
+
+// wt_int::inverse_select (wt_int_par.hpp:588-611)
+__global__ void wt_inverse_select_kernel(const uint64_t* __restrict__ tree, const uint64_t* __restrict__ rt,
+                                         uint64_t n, int L, const uint64_t* __restrict__ q, uint64_t nq,
+                                         uint64_t* __restrict__ rank_out, uint64_t* __restrict__ sym_out) {
+  uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nq) return;
+  uint64_t i = q[k];
+  if (i >= n) {
+    rank_out[k] = sym_out[k] = NONE64;
+    return;
+  }
+  uint64_t c = 0, node_size = n, offset = 0;
+  for (int lv = 0; lv < L; ++lv) {
+    const uint64_t o = rank1_dev(rt, tree, offset);
+    const uint64_t oi = rank1_dev(rt, tree, offset + i) - o;
+    const uint64_t oe = rank1_dev(rt, tree, offset + node_size) - o;
+    c <<= 1;
+    if (bit_at(tree, offset + i)) {
+      offset += node_size - oe;
+      node_size = oe;
+      i = oi;
+      c |= 1;
+    } else {
+      node_size = node_size - oe;
+      i = i - oi;
+    }
+    offset += n;
+  }
+  rank_out[k] = i;
+  sym_out[k] = c;
+}
+
+// wt_int::select (wt_int_par.hpp:622-660)
+__global__ void wt_select_kernel(const uint64_t* __restrict__ tree, const uint64_t* __restrict__ rt, SelView s1,
+                                 SelView s0, uint64_t n, int L, const uint64_t* __restrict__ q,
+                                 const uint64_t* __restrict__ sym, uint64_t nq, uint64_t* __restrict__ out) {
+  uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nq) return;
+  uint64_t i = q[k];
+  const uint64_t c = sym[k];
+  uint64_t path_off[25], path_rank[25];
+  uint64_t offset = 0, mask = 1ull << (L - 1), node_size = n;
+  path_off[0] = path_rank[0] = 0;
+  if (i == 0 || (L < 64 && (1ull << L) <= c)) {
+    out[k] = NONE64;
+    return;
+  }
+  for (int lv = 0; lv < L && node_size; ++lv) {
+    const uint64_t o = rank1_dev(rt, tree, offset);
+    path_rank[lv] = o;
+    const uint64_t oe = rank1_dev(rt, tree, offset + node_size) - o;
+    if (c & mask) {
+      offset += node_size - oe;
+      node_size = oe;
+    } else {
+      node_size = node_size - oe;
+    }
+    offset += n;
+    path_off[lv + 1] = offset;
+    mask >>= 1;
+  }
+  if (node_size == 0 || node_size < i) {
+    out[k] = NONE64;  // the reference throws std::logic_error here
+    return;
+  }
+  mask = 1;
+  for (int lv = L; lv > 0; --lv) {
+    offset = path_off[lv - 1];
+    const uint64_t o = path_rank[lv - 1];
+    if (c & mask) i = select_dev(s1, o + i) - offset + 1;
+    else i = select_dev(s0, offset - o + i) - offset + 1;
+    mask <<= 1;
+  }
+  out[k] = i - 1;
+}
+
+__global__ void bv_rank_kernel(const uint64_t* __restrict__ words, const uint64_t* __restrict__ rt, uint64_t size,
+                               const uint64_t* __restrict__ q, uint64_t nq, uint64_t* __restrict__ out) {
+  uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nq) return;
+  const uint64_t idx = q[k];
+  out[k] = idx <= size ? rank1_dev(rt, words, idx) : NONE64;
+}
+
+__global__ void bv_select_kernel(SelView v, const uint64_t* __restrict__ q, uint64_t nq, uint64_t* __restrict__ out) {
+  uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nq) return;
+  out[k] = select_dev(v, q[k]);
+}
+
+static unsigned qgrid(uint64_t nq) { return (unsigned)((nq + 255) / 256); }
+
+static int need(const TreeImpl& t, uint32_t f, const char* what) {
+  if ((t.flags & f) != f) return fail(WTG_ERR_INVALID, std::string(what) + " needs a tree built with the supports it uses");
+  return WTG_OK;
+}
+
+int launch_wt_access(const TreeImpl& t, const uint64_t* idx, uint64_t nq, uint64_t* out, cudaStream_t s) {
+  if (int rc = need(t, WTG_RANK, "access")) return rc;
+  if (!nq) return WTG_OK;
+  wt_access_kernel<<<qgrid(nq), 256, 0, s>>>(t.bits.as<uint64_t>(), t.bv.rank.as<uint64_t>(), t.n, t.levels, idx,
+                                            nq, out);
+  count_launch();
+  WTG_CK(cudaGetLastError());
+  return WTG_OK;
+}
+
+int launch_wt_rank(const TreeImpl& t, const uint64_t* idx, const uint64_t* sym, uint64_t nq, uint64_t* out,
+                   cudaStream_t s) {
+  if (int rc = need(t, WTG_RANK, "rank")) return rc;
+  if (!nq) return WTG_OK;
+  wt_rank_kernel<<<qgrid(nq), 256, 0, s>>>(t.bits.as<uint64_t>(), t.bv.rank.as<uint64_t>(), t.n, t.levels, idx,
+                                          sym, nq, out);
+  count_launch();
+  WTG_CK(cudaGetLastError());
+  return WTG_OK;
+}
+
+int launch_wt_inverse_select(const TreeImpl& t, const uint64_t* idx, uint64_t nq, uint64_t* rank_out,
+                             uint64_t* sym_out, cudaStream_t s) {
+  if (int rc = need(t, WTG_RANK, "inverse_select")) return rc;
+  if (!nq) return WTG_OK;
+  wt_inverse_select_kernel<<<qgrid(nq), 256, 0, s>>>(t.bits.as<uint64_t>(), t.bv.rank.as<uint64_t>(), t.n,
+                                                    t.levels, idx, nq, rank_out, sym_out);
+  count_launch();
+  WTG_CK(cudaGetLastError());
+  return WTG_OK;
+}
+
+int launch_wt_select(const TreeImpl& t, const uint64_t* i, const uint64_t* sym, uint64_t nq, uint64_t* out,
+                     cudaStream_t s) {
+  if (int rc = need(t, WTG_ALL, "select")) return rc;
+  if (!nq) return WTG_OK;
+  wt_select_kernel<<<qgrid(nq), 256, 0, s>>>(t.bits.as<uint64_t>(), t.bv.rank.as<uint64_t>(), sel_view(t.bv, 1),
+                                            sel_view(t.bv, 0), t.n, t.levels, i, sym, nq, out);
+  count_launch();
+  WTG_CK(cudaGetLastError());
+  return WTG_OK;
+}
+
+int launch_bv_rank(const BvSupport& bv, const uint64_t* idx, uint64_t nq, uint64_t* out, cudaStream_t s) {
+  if (!(bv.flags & WTG_RANK)) return fail(WTG_ERR_INVALID, "rank needs WTG_RANK");
+  if (!nq) return WTG_OK;
+  bv_rank_kernel<<<qgrid(nq), 256, 0, s>>>(bv.words, bv.rank.as<uint64_t>(), bv.size, idx, nq, out);
+  count_launch();
+  WTG_CK(cudaGetLastError());
+  return WTG_OK;
+}
+
+int launch_bv_select(const BvSupport& bv, int t_b, const uint64_t* i, uint64_t nq, uint64_t* out, cudaStream_t s) {
+  if (!(bv.flags & (t_b ? WTG_SELECT1 : WTG_SELECT0))) return fail(WTG_ERR_INVALID, "select needs its support built");
+  if (!nq) return WTG_OK;
+  bv_select_kernel<<<qgrid(nq), 256, 0, s>>>(sel_view(bv, t_b), i, nq, out);
+  count_launch();
+  WTG_CK(cudaGetLastError());
+  return WTG_OK;
+}
+
+// ---------------------------------------------------------- alphabet remap
+
+template <typename T>
+__global__ void remap_mark_kernel(const T* __restrict__ s, uint64_t n, uint32_t* __restrict__ flag) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    flag[(uint64_t)s[i]] = 1;
+}
+
+template <typename T>
+__global__ void remap_apply_kernel(T* __restrict__ s, uint64_t n, const uint32_t* __restrict__ rank) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    s[i] = (T)rank[(uint64_t)s[i]];
+}
+
+template <typename T>
+__global__ void remap_max_kernel(const T* __restrict__ s, uint64_t n, unsigned long long* out) {
+  uint64_t m = 0;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t x = s[i];
+    m = x > m ? x : m;
+  }
+  atomicMax(out, (unsigned long long)m);
+}
+
+template <typename T>
+static int remap_t(T* d, uint64_t n, uint64_t* sigma, DevBuf& tmp, DevBuf& scan_tmp, uint32_t* d_err,
+                   cudaStream_t s) {
+  int rc;
+  unsigned grid = (unsigned)std::min<uint64_t>((n + 255) / 256, 152 * 8);
+  if (grid == 0) grid = 1;
+  if ((rc = tmp.ensure(sizeof(unsigned long long), s))) return rc;
+  WTG_CK(cudaMemsetAsync(tmp.p, 0, sizeof(unsigned long long), s));
+  remap_max_kernel<T><<<grid, 256, 0, s>>>(d, n, tmp.as<unsigned long long>());
+  count_launch();
+  WTG_CK(cudaGetLastError());
+  unsigned long long mx = 0;
+  WTG_CK(cudaMemcpyAsync(&mx, tmp.p, sizeof(mx), cudaMemcpyDeviceToHost, s));
+  WTG_CK(cudaStreamSynchronize(s));
+  if (mx >= (1ull << 31)) return fail(WTG_ERR_RANGE, "remap: symbol values must be below 2^31");
+  const uint64_t k = mx + 2;  // flags for values 0..max, plus the total
+  if ((rc = tmp.ensure(k * sizeof(uint32_t), s))) return rc;
+  uint32_t* flag = tmp.as<uint32_t>();
+  WTG_CK(cudaMemsetAsync(flag, 0, k * sizeof(uint32_t), s));
+  remap_mark_kernel<T><<<grid, 256, 0, s>>>(d, n, flag);
+  count_launch();
+  WTG_CK(cudaGetLastError());
+  if ((rc = scan_exclusive_u32(flag, flag, k, scan_tmp, d_err, s))) return rc;
+  remap_apply_kernel<T><<<grid, 256, 0, s>>>(d, n, flag);
+  count_launch();
+  WTG_CK(cudaGetLastError());
+  uint32_t sg = 0;
+  WTG_CK(cudaMemcpyAsync(&sg, flag + (k - 1), sizeof(sg), cudaMemcpyDeviceToHost, s));
+  WTG_CK(cudaStreamSynchronize(s));
+  *sigma = sg;
+  return WTG_OK;
+}
+
+int remap_alphabet_device(void* d_seq, uint64_t n, int eb, uint64_t* sigma, DevBuf& tmp, DevBuf& scan_tmp,
+                          uint32_t* d_err, cudaStream_t s) {
+  if (n == 0) {
+    *sigma = 0;
+    return WTG_OK;
+  }
+  switch (eb) {
+    case 1: return remap_t<uint8_t>((uint8_t*)d_seq, n, sigma, tmp, scan_tmp, d_err, s);
+    case 2: return remap_t<uint16_t>((uint16_t*)d_seq, n, sigma, tmp, scan_tmp, d_err, s);
+    case 4: return remap_t<uint32_t>((uint32_t*)d_seq, n, sigma, tmp, scan_tmp, d_err, s);
+    default: return remap_t<uint64_t>((uint64_t*)d_seq, n, sigma, tmp, scan_tmp, d_err, s);
+  }
+}
+
+}  // namespace wtg

@@ -1,0 +1,323 @@
+"""Python binding of libwtg (include/wtg.h): GPU wavelet-tree construction,
+rank_support_v / select_support_mcl supports and wt_int queries.
+
+Mirrors the reference's interface for this path:
+  * WT(s, sigma)                -> (nodes, bits) like WT(symbol*, n, sigma)
+                                   (wavelet/levelWT/WT.h:43)
+  * WaveletTree(seq, max_level) -> sdsl::wt_int<> (wt_int/wt_int_par.hpp:368),
+                                   with access ([]), rank, select,
+                                   inverse_select
+  * BitVectorSupport(words, n)  -> rank_support_v<1> + select_support_mcl<1>/<0>
+                                   over a bit_vector
+Every call runs CUDA kernels through the C ABI; there is no CPU path.  If the
+library cannot be loaded, or no GPU is usable, calls raise WtgError.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libwtg.so")
+
+OK, ERR_INVALID, ERR_OOM, ERR_CUDA, ERR_TIMEOUT, ERR_RANGE = 0, 1, 2, 3, 4, 5
+RANK, SELECT1, SELECT0, ALL = 1, 2, 4, 7
+NONE = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+u64 = ctypes.c_uint64
+vp = ctypes.c_void_p
+i32 = ctypes.c_int
+
+
+class WtgError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"wtg error {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def build():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("wtg_build_lib", os.path.join(HERE, "build_lib.py"))
+    m = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(m)
+    return m.build()
+
+
+_SIGS = {
+    "wtg_last_error": ([], ctypes.c_char_p),
+    "wtg_version": ([], i32),
+    "wtg_launch_count": ([], u64),
+    "wtg_tree_build": ([vp, u64, i32, i32, ctypes.c_uint32, vp], i32),
+    "wtg_tree_build_device": ([vp, u64, i32, i32, ctypes.c_uint32, vp, vp], i32),
+    "wtg_tree_sync": ([vp], i32),
+    "wtg_tree_free": ([vp], i32),
+    "wtg_tree_info": ([vp, vp], i32),
+    "wtg_tree_select_info": ([vp, i32, vp], i32),
+    "wtg_tree_get_bits": ([vp, vp, u64], i32),
+    "wtg_tree_get_nodes": ([vp, i32, u64, vp], i32),
+    "wtg_tree_get_rank": ([vp, vp, u64], i32),
+    "wtg_tree_get_select": ([vp, i32, vp, vp, vp], i32),
+    "wtg_tree_device_ptrs": ([vp, vp], i32),
+    "wtg_query_access": ([vp, vp, u64, vp], i32),
+    "wtg_query_rank": ([vp, vp, vp, u64, vp], i32),
+    "wtg_query_inverse_select": ([vp, vp, u64, vp, vp], i32),
+    "wtg_query_select": ([vp, vp, vp, u64, vp], i32),
+    "wtg_query_access_device": ([vp, vp, u64, vp, vp], i32),
+    "wtg_query_rank_device": ([vp, vp, vp, u64, vp, vp], i32),
+    "wtg_bv_build": ([vp, u64, ctypes.c_uint32, vp], i32),
+    "wtg_bv_build_device": ([vp, u64, ctypes.c_uint32, vp, vp], i32),
+    "wtg_bv_sync": ([vp], i32),
+    "wtg_bv_free": ([vp], i32),
+    "wtg_bv_rank_words": ([vp, vp], i32),
+    "wtg_bv_get_rank": ([vp, vp, u64], i32),
+    "wtg_bv_select_info": ([vp, i32, vp], i32),
+    "wtg_bv_get_select": ([vp, i32, vp, vp, vp], i32),
+    "wtg_bv_rank": ([vp, vp, u64, vp], i32),
+    "wtg_bv_select": ([vp, i32, vp, u64, vp], i32),
+    "wtg_bv_select_device": ([vp, i32, vp, u64, vp, vp], i32),
+    "wtg_remap_alphabet": ([vp, u64, i32, vp], i32),
+    "wtg_profile_enable": ([i32], i32),
+    "wtg_profile_read": ([vp, vp], i32),
+}
+
+
+def lib():
+    """The loaded libwtg (built on first use when missing)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (args, res) in _SIGS.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = res
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None else None
+
+
+def _ck(rc):
+    if rc != OK:
+        msg = lib().wtg_last_error()
+        raise WtgError(rc, msg.decode() if msg else "")
+
+
+def launch_count():
+    return int(lib().wtg_launch_count())
+
+
+PROF_CLASSES = ("level", "level_last", "hist", "tables", "bvpass", "select")
+
+
+def profile_enable(on=True):
+    _ck(lib().wtg_profile_enable(1 if on else 0))
+
+
+def profile_read():
+    """{class: (launches, total device ms)} recorded since the last read."""
+    n = np.zeros(len(PROF_CLASSES), dtype=np.uint64)
+    ms = np.zeros(len(PROF_CLASSES), dtype=np.float64)
+    _ck(lib().wtg_profile_read(_p(n), _p(ms)))
+    return {c: (int(n[i]), float(ms[i])) for i, c in enumerate(PROF_CLASSES)}
+
+
+def levels_for_sigma(sigma):
+    """max(1, log2Up(sigma)) (wavelet/levelWT/WT.C:96)."""
+    a, b = 0, int(sigma) - 1
+    while b > 0:
+        b >>= 1
+        a += 1
+    return max(1, a)
+
+
+def _u64(a):
+    return np.ascontiguousarray(a, dtype=np.uint64)
+
+
+class _SelectTables:
+    """select_support_mcl<t_b> in the flat packed layout (see include/wtg.h)."""
+
+    def __init__(self, info, sb_words, desc, pool):
+        (self.size, self.arg_cnt, self.logn, self.logn4, self.nsb, self.has_long,
+         self.sb_nwords, self.pool_nwords) = [int(x) for x in info]
+        self.sb_words, self.desc, self.pool = sb_words, desc, pool
+
+
+class WaveletTree:
+    """Wavelet tree over n symbols built on the GPU (sdsl::wt_int<> semantics
+    with levels = max_level; the level bits equal levelWT's WT() for
+    levels = max(1, log2Up(sigma)))."""
+
+    def __init__(self, seq=None, levels=0, flags=ALL, _handle=None):
+        self.h = vp()
+        if _handle is not None:
+            self.h = _handle
+        else:
+            seq = np.ascontiguousarray(seq)
+            if seq.dtype.itemsize not in (1, 2, 4, 8) or seq.dtype.kind != "u":
+                raise ValueError("sequence must be an unsigned integer array of 1, 2, 4 or 8 byte symbols")
+            _ck(lib().wtg_tree_build(_p(seq), seq.size, seq.dtype.itemsize, int(levels), flags,
+                                     ctypes.byref(self.h)))
+        info = np.zeros(4, dtype=np.uint64)
+        _ck(lib().wtg_tree_info(self.h, _p(info)))
+        self.n, self.levels, self.bit_words, self.rank_words = [int(x) for x in info]
+        self.flags = flags
+
+    @classmethod
+    def from_device(cls, d_ptr, n, elem_bytes, levels, flags=ALL, stream=0, tree=None):
+        """Build (or rebuild `tree`) from a device pointer on a CUDA stream."""
+        h = tree.h if tree is not None else vp()
+        _ck(lib().wtg_tree_build_device(vp(d_ptr), n, elem_bytes, levels, flags, vp(stream), ctypes.byref(h)))
+        if tree is not None:
+            tree.__init__(_handle=h, flags=flags)
+            return tree
+        return cls(_handle=h, flags=flags)
+
+    def sync(self):
+        _ck(lib().wtg_tree_sync(self.h))
+
+    def free(self):
+        if self.h:
+            lib().wtg_tree_free(self.h)
+            self.h = vp()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    # outputs in the reference layouts
+    def bits(self):
+        out = np.zeros(self.bit_words, dtype=np.uint64)
+        _ck(lib().wtg_tree_get_bits(self.h, _p(out), out.size))
+        return out
+
+    def nodes(self, n_entries, index_bytes=8):
+        out = np.zeros((n_entries, 5), dtype=np.uint32 if index_bytes == 4 else np.uint64)
+        _ck(lib().wtg_tree_get_nodes(self.h, index_bytes, n_entries, _p(out)))
+        return out
+
+    def rank_table(self):
+        out = np.zeros(self.rank_words, dtype=np.uint64)
+        _ck(lib().wtg_tree_get_rank(self.h, _p(out), out.size))
+        return out
+
+    def select_tables(self, t_b):
+        info = np.zeros(8, dtype=np.uint64)
+        _ck(lib().wtg_tree_select_info(self.h, t_b, _p(info)))
+        sb = np.zeros(max(int(info[6]), 1), dtype=np.uint64)
+        desc = np.zeros(max(int(info[4]), 1), dtype=np.uint64)
+        pool = np.zeros(max(int(info[7]), 1), dtype=np.uint64)
+        _ck(lib().wtg_tree_get_select(self.h, t_b, _p(sb), _p(desc), _p(pool)))
+        return _SelectTables(info, sb[: int(info[6])], desc[: int(info[4])], pool[: int(info[7])])
+
+    def device_ptrs(self):
+        out = np.zeros(8, dtype=np.uint64)
+        _ck(lib().wtg_tree_device_ptrs(self.h, _p(out)))
+        return [int(x) for x in out]
+
+    # wt_int queries (batched)
+    def access(self, idx):
+        idx = _u64(idx)
+        out = np.zeros(idx.size, dtype=np.uint64)
+        _ck(lib().wtg_query_access(self.h, _p(idx), idx.size, _p(out)))
+        return out
+
+    def __getitem__(self, i):
+        return int(self.access(np.array([i]))[0])
+
+    def rank(self, idx, sym):
+        idx, sym = _u64(idx), _u64(sym)
+        out = np.zeros(idx.size, dtype=np.uint64)
+        _ck(lib().wtg_query_rank(self.h, _p(idx), _p(sym), idx.size, _p(out)))
+        return out
+
+    def inverse_select(self, idx):
+        idx = _u64(idx)
+        r = np.zeros(idx.size, dtype=np.uint64)
+        c = np.zeros(idx.size, dtype=np.uint64)
+        _ck(lib().wtg_query_inverse_select(self.h, _p(idx), idx.size, _p(r), _p(c)))
+        return r, c
+
+    def select(self, i, sym):
+        i, sym = _u64(i), _u64(sym)
+        out = np.zeros(i.size, dtype=np.uint64)
+        _ck(lib().wtg_query_select(self.h, _p(i), _p(sym), i.size, _p(out)))
+        return out
+
+
+def WT(s, sigma, index_bytes=4):
+    """levelWT's WT(s, n, sigma): returns (nodes [2*sigma, 5], bits) with
+    levels = max(1, log2Up(sigma)) (wavelet/levelWT/WT.C:86-270)."""
+    t = WaveletTree(s, levels=levels_for_sigma(sigma), flags=0)
+    try:
+        return t.nodes(2 * int(sigma), index_bytes), t.bits()
+    finally:
+        t.free()
+
+
+class BitVectorSupport:
+    """rank_support_v<1> and select_support_mcl<1>/<0> over the first
+    size_bits bits of a bit_vector given as uint64 words."""
+
+    def __init__(self, words, size_bits, flags=ALL):
+        self.h = vp()
+        words = _u64(words)
+        self.size = int(size_bits)
+        self.flags = flags
+        _ck(lib().wtg_bv_build(_p(words), self.size, flags, ctypes.byref(self.h)))
+
+    def free(self):
+        if self.h:
+            lib().wtg_bv_free(self.h)
+            self.h = vp()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def rank_table(self):
+        n = ctypes.c_uint64(0)
+        _ck(lib().wtg_bv_rank_words(self.h, ctypes.byref(n)))
+        out = np.zeros(n.value, dtype=np.uint64)
+        _ck(lib().wtg_bv_get_rank(self.h, _p(out), out.size))
+        return out
+
+    def select_tables(self, t_b):
+        info = np.zeros(8, dtype=np.uint64)
+        _ck(lib().wtg_bv_select_info(self.h, t_b, _p(info)))
+        sb = np.zeros(max(int(info[6]), 1), dtype=np.uint64)
+        desc = np.zeros(max(int(info[4]), 1), dtype=np.uint64)
+        pool = np.zeros(max(int(info[7]), 1), dtype=np.uint64)
+        _ck(lib().wtg_bv_get_select(self.h, t_b, _p(sb), _p(desc), _p(pool)))
+        return _SelectTables(info, sb[: int(info[6])], desc[: int(info[4])], pool[: int(info[7])])
+
+    def rank(self, idx):
+        idx = _u64(idx)
+        out = np.zeros(idx.size, dtype=np.uint64)
+        _ck(lib().wtg_bv_rank(self.h, _p(idx), idx.size, _p(out)))
+        return out
+
+    def select(self, i, t_b=1):
+        i = _u64(i)
+        out = np.zeros(i.size, dtype=np.uint64)
+        _ck(lib().wtg_bv_select(self.h, t_b, _p(i), i.size, _p(out)))
+        return out
+
+
+def remap_alphabet(seq):
+    """levelWT/WTTime.C:80-94 on the GPU: returns (remapped copy, sigma)."""
+    s = np.array(seq, copy=True)
+    sigma = ctypes.c_uint64(0)
+    _ck(lib().wtg_remap_alphabet(_p(s), s.size, s.dtype.itemsize, ctypes.byref(sigma)))
+    return s, int(sigma.value)
