@@ -245,68 +245,71 @@ __global__ void select_sb_pack_kernel(int t_b, uint64_t nsb, uint32_t logn, cons
   });
 }
 
-// block per long superblock: all 4096 arg positions, packed
+// Long blocks, step 1: a warp per 64-arg group of each long superblock.  The
+// group's args lie between two consecutive samples (positions of args 64k and
+// 64(k+1)), so every group is extracted independently and all long spans are
+// read once, in parallel (init_longblock_serial, :401-438, restated).
 __global__ void __launch_bounds__(256)
-    select_long_kernel(int t_b, const uint64_t* __restrict__ words, uint64_t size, uint64_t W,
-                       const uint64_t* __restrict__ samples, uint64_t samp_last, const uint64_t* __restrict__ ends,
-                       const unsigned long long* info, const uint64_t* __restrict__ long_list,
-                       const uint64_t* __restrict__ descw, const uint64_t* __restrict__ offs,
-                       uint64_t* __restrict__ pool, uint32_t* err) {
-  __shared__ uint64_t ent[4096];
-  __shared__ uint32_t s_wsum[8];
-  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    select_long_extract_kernel(int t_b, const uint64_t* __restrict__ words, uint64_t size, uint64_t W,
+                               const uint64_t* __restrict__ samples, uint64_t samp_last,
+                               const unsigned long long* info, const uint64_t* __restrict__ long_list,
+                               uint64_t* __restrict__ ent) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint64_t m = info[t_b ? INF_M1 : INF_M0];
-  const uint64_t nsb = (m + 4095) >> 12;
+  const uint64_t last = info[t_b ? INF_LAST1 : INF_LAST0];  // last arg position + 1
   const uint64_t nlong = info[t_b ? INF_NLONG1 : INF_NLONG0];
+  const uint64_t li = gw >> 6, g = gw & 63;
+  if (li >= nlong) return;
+  const uint64_t i = long_list[li];
+  const uint64_t a0 = 4096 * i + 64 * g;
+  if (a0 >= m) return;  // entries past the arg count stay zero
+  auto samp = [&](uint64_t k) { return t_b ? samples[k] : samples[samp_last - k]; };
+  const uint64_t p0 = samp(a0 >> 6);
+  const uint64_t pend = (a0 + 64 < m) ? samp((a0 >> 6) + 1) : last;
   const uint64_t tailmask = (size & 63) ? ((1ull << (size & 63)) - 1) : ~0ull;
+  uint64_t* out = ent + li * 4096 + 64 * g;
+  uint64_t cnt = 0;
+  for (uint64_t wb = p0 >> 6; (wb << 6) < pend && cnt < 64; wb += 32) {
+    const uint64_t wi = wb + lane;
+    uint64_t x = 0;
+    if ((wi << 6) < pend && wi < W) {
+      x = words[wi];
+      if (!t_b) x = ~x;
+      if (wi == W - 1) x &= tailmask;
+      if (wi == (p0 >> 6)) x &= ~0ull << (p0 & 63);
+      if ((wi << 6) + 64 > pend) x &= (1ull << (pend & 63)) - 1;
+    }
+    const uint32_t c = __popcll(x);
+    uint32_t inc = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= (uint32_t)o) inc += t;
+    }
+    uint64_t p = cnt + inc - c;
+    while (x) {
+      if (p < 64) out[p] = (wi << 6) + (__ffsll((long long)x) - 1);
+      ++p;
+      x &= x - 1;
+    }
+    cnt += __shfl_sync(0xffffffffu, inc, 31);
+  }
+}
+
+// Long blocks, step 2: pack each long block's 4096 positions (width hi(end)+1).
+__global__ void __launch_bounds__(256)
+    select_long_pack_kernel(int t_b, const unsigned long long* info, const uint64_t* __restrict__ long_list,
+                            const uint64_t* __restrict__ descw, const uint64_t* __restrict__ offs,
+                            const uint64_t* __restrict__ ent, uint64_t* __restrict__ pool) {
+  const uint64_t nlong = info[t_b ? INF_NLONG1 : INF_NLONG0];
   for (uint64_t li = blockIdx.x; li < nlong; li += gridDim.x) {
     const uint64_t i = long_list[li];
-    const uint64_t start = t_b ? samples[64 * i] : samples[samp_last - 64 * i];
-    const uint64_t end = (i + 1 < nsb) ? ends[i] : (uint64_t)info[t_b ? INF_LAST1 : INF_LAST0] - 1;
     const uint32_t wdt = (uint32_t)(descw[i] & 127);
     const uint64_t off = offs[i];
-    for (uint32_t j = tid; j < 4096; j += 256) ent[j] = 0;
-    __syncthreads();
-    uint64_t count = 0;
-    for (uint64_t wb = start >> 6; wb <= (end >> 6); wb += 256) {
-      const uint64_t wi = wb + tid;
-      uint64_t x = 0;
-      if (wi <= (end >> 6) && wi < W) {
-        x = words[wi];
-        if (!t_b) x = ~x;
-        if (wi == W - 1) x &= tailmask;
-        if (wi == (start >> 6)) x &= ~0ull << (start & 63);
-        if (wi == (end >> 6) && (end & 63) != 63) x &= (1ull << ((end & 63) + 1)) - 1;
-      }
-      uint32_t cx = __popcll(x);
-      uint32_t inc = cx;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
-        if (lane >= (uint32_t)o) inc += t;
-      }
-      if (lane == 31) s_wsum[warp] = inc;
-      __syncthreads();
-      uint32_t before = 0, total = 0;
-#pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        uint32_t t = s_wsum[k];
-        if ((uint32_t)k < warp) before += t;
-        total += t;
-      }
-      uint64_t p = count + before + inc - cx;
-      while (x) {
-        if (p < 4096) ent[p] = (wi << 6) + __ffsll((long long)x) - 1;
-        ++p;
-        x &= x - 1;
-      }
-      count += total;
-      __syncthreads();
-    }
-    if (count > 4096 && tid == 0) atomicCAS(err, 0u, (uint32_t)DERR_SELECT_OVERFLOW);
-    for (uint64_t q = tid; q < 64ull * wdt; q += 256)
-      pool[off + q] = packed_word(q, wdt, 4096, [&](uint64_t j) { return ent[j]; });
-    __syncthreads();
+    const uint64_t* e = ent + li * 4096;
+    for (uint64_t q = threadIdx.x; q < 64ull * wdt; q += blockDim.x)
+      pool[off + q] = packed_word(q, wdt, 4096, [&](uint64_t j) { return e[j]; });
   }
 }
 
@@ -330,6 +333,7 @@ void bv_release(BvSupport& bv, cudaStream_t s) {
     sd.sb_words.release(s);
     sd.pool.release(s);
     sd.long_list.release(s);
+    sd.long_ent.release(s);
   }
 }
 
@@ -434,11 +438,19 @@ int bv_build(BvSupport& bv, const uint64_t* d_words, uint64_t size, uint32_t fla
     WTG_CK(cudaGetLastError());
     const uint64_t nlong = h[t_b ? INF_NLONG1 : INF_NLONG0];
     if (nlong) {
-      unsigned grid = (unsigned)std::min<uint64_t>(nlong, 4 * 152);
+      if ((rc = sd.long_ent.ensure(nlong * 4096 * sizeof(uint64_t), s))) return rc;
+      WTG_CK(cudaMemsetAsync(sd.long_ent.p, 0, nlong * 4096 * sizeof(uint64_t), s));
+      const uint64_t warps = nlong * 64;
       prof_begin(PROF_SELECT, s);
-      select_long_kernel<<<grid, 256, 0, s>>>(t_b, d_words, size, W, samples, samp_n - 1, sd.ends.as<uint64_t>(),
-                                              info, sd.long_list.as<uint64_t>(), descw, offs,
-                                              sd.pool.as<uint64_t>(), d_err);
+      select_long_extract_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(
+          t_b, d_words, size, W, samples, samp_n - 1, info, sd.long_list.as<uint64_t>(), sd.long_ent.as<uint64_t>());
+      prof_end(PROF_SELECT, s);
+      count_launch();
+      WTG_CK(cudaGetLastError());
+      unsigned grid = (unsigned)std::min<uint64_t>(nlong, 8 * 152);
+      prof_begin(PROF_SELECT, s);
+      select_long_pack_kernel<<<grid, 256, 0, s>>>(t_b, info, sd.long_list.as<uint64_t>(), descw, offs,
+                                                   sd.long_ent.as<uint64_t>(), sd.pool.as<uint64_t>());
       prof_end(PROF_SELECT, s);
       count_launch();
       WTG_CK(cudaGetLastError());

@@ -119,6 +119,60 @@ __device__ __forceinline__ uint64_t packed_word(uint64_t q, uint32_t w, uint64_t
   return out;
 }
 
+// ------------------------------------------- bulk copies and mbarriers
+// 1-D bulk copy global -> shared (cp.async.bulk, completion counted on an
+// mbarrier in bytes).  Source and destination 16-byte aligned, size a
+// multiple of 16.  Every wait is bounded.
+
+constexpr uint32_t MBAR_SPIN_LIMIT = 1u << 24;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_fence_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// waits for phase `parity` of bar to complete; false (and err set) on timeout
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t* err) {
+  for (uint32_t k = 0; k < MBAR_SPIN_LIMIT; ++k)
+    if (mbar_try_wait(bar, parity)) return true;
+  atomicCAS(err, 0u, (uint32_t)DERR_LOOKBACK_TIMEOUT);
+  return false;
+}
+
 // ------------------------------------------------ decoupled look-back scan
 //
 // Single-pass scan status words (Merrill & Garland, "Single-pass Parallel
@@ -210,6 +264,7 @@ struct SelectDev {
   DevBuf sb_words;  // packed m_superblock
   DevBuf pool;      // packed mini/long blocks
   DevBuf long_list; // superblock ids of long blocks
+  DevBuf long_ent;  // 4096 unpacked positions per long block
 };
 
 // Rank/select support over one bitvector (caller or tree owned words).
