@@ -38,60 +38,71 @@
 namespace wtg {
 
 constexpr int LV_THREADS = 256;
-constexpr int TOP_BITS = 12;  // bits histogrammed by the pre-pass
+constexpr int TOP_BITS = 2;  // bits histogrammed by the pre-pass (ballot counted)
 
 template <typename T>
 struct LvShape {
-  static constexpr int ROWS = 16384 / (LV_THREADS * (int)sizeof(T));  // rows of 256 symbols per tile
+  static constexpr int ROWS = 16384 / (LV_THREADS * (int)sizeof(T));  // rows of 32 symbols per warp
   static constexpr uint32_t TILE = LV_THREADS * ROWS;                  // symbols per tile (16 KB)
   static constexpr uint32_t BYTES = TILE * sizeof(T);
   static constexpr int NW = ROWS * (LV_THREADS / 32);  // 32-bit words of level bits per tile
+  static constexpr int LOG_TILE = sizeof(T) == 1 ? 14 : sizeof(T) == 2 ? 13 : sizeof(T) == 4 ? 12 : 11;
 };
 
 // ------------------------------------------------------------ pre-pass
-// Histogram of the top K of the L key bits, privatized in shared memory.
+// One read of the input, tile by tile: the zero count of level 0 in every
+// tile (its bit levels-1), and the histogram of the top K <= 2 key bits,
+// both counted with warp ballots.
 
 template <typename T>
-__global__ void __launch_bounds__(256) prehist_kernel(const T* __restrict__ s, uint64_t n, int L, int K,
-                                                      int vec_ok, uint32_t* __restrict__ hist) {
-  extern __shared__ uint32_t sh[];
-  const uint32_t bins = 1u << K;
-  const uint64_t bmask = bins - 1;
-  const int sh_r = L - K;
-  const uint32_t lane = threadIdx.x & 31;
-  for (uint32_t i = threadIdx.x; i < bins; i += blockDim.x) sh[i] = 0;
-  __syncthreads();
-  // whole warps step together so that equal bins of a warp are added once
-  auto add = [&](bool valid, uint32_t key) {
-    const uint32_t k = valid ? key : 0xFFFFFFFFu;
-    const uint32_t grp = __match_any_sync(0xffffffffu, k);
-    if (valid && lane == (uint32_t)(__ffs(grp) - 1)) atomicAdd(&sh[key], (uint32_t)__popc(grp));
-  };
-  const uint64_t wstride = (uint64_t)gridDim.x * blockDim.x;
-  const uint64_t w0 = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u);
-  constexpr int V = 16 / sizeof(T);
-  uint64_t done = 0;
-  if (vec_ok) {
-    const uint64_t nv = n / V;
-    const uint4* s4 = (const uint4*)s;
-    for (uint64_t b = w0; b < nv; b += wstride) {
-      const uint64_t i = b + lane;
-      const bool valid = i < nv;
-      uint4 q = valid ? __ldg(&s4[i]) : make_uint4(0, 0, 0, 0);
-      const T* e = (const T*)&q;
-#pragma unroll
-      for (int k = 0; k < V; ++k) add(valid, (uint32_t)(((uint64_t)e[k] >> sh_r) & bmask));
+__global__ void __launch_bounds__(LV_THREADS) prepass_kernel(const T* __restrict__ s, uint64_t n, int L, int K,
+                                                             uint32_t* __restrict__ tilecnt,
+                                                             uint32_t* __restrict__ hist) {
+  using S = LvShape<T>;
+  __shared__ uint32_t s_wz[LV_THREADS / 32];
+  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint64_t ntiles = (n + S::TILE - 1) / S::TILE;
+  uint32_t h[4] = {0, 0, 0, 0};
+  const int top = L - 1;
+  for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const uint64_t base = tile * S::TILE + (uint64_t)warp * (S::ROWS * 32);
+    uint32_t wz = 0;
+#pragma unroll 4
+    for (int r = 0; r < S::ROWS; ++r) {
+      const uint64_t i = base + r * 32 + lane;
+      const bool valid = i < n;
+      const uint64_t x = valid ? (uint64_t)s[i] : 0ull;
+      const uint32_t b1 = (uint32_t)(x >> top) & 1u;
+      const uint32_t b2 = K > 1 ? (uint32_t)(x >> (top - 1)) & 1u : 0u;
+      const uint32_t vm = __ballot_sync(0xffffffffu, valid);
+      const uint32_t z = __ballot_sync(0xffffffffu, valid && !b1);       // top bits 0x
+      const uint32_t z01 = __ballot_sync(0xffffffffu, valid && !b1 && b2);  // 01
+      const uint32_t o11 = __ballot_sync(0xffffffffu, valid && b1 && b2);   // 11
+      wz += __popc(z);
+      h[0] += __popc(z) - __popc(z01);
+      h[1] += __popc(z01);
+      h[2] += __popc(vm) - __popc(z) - __popc(o11);
+      h[3] += __popc(o11);
     }
-    done = nv * V;
+    if (lane == 0) s_wz[warp] = wz;
+    __syncthreads();
+    if (tid == 0) {
+      uint32_t t = 0;
+      for (int w = 0; w < LV_THREADS / 32; ++w) t += s_wz[w];
+      tilecnt[tile] = t;
+    }
+    __syncthreads();
   }
-  for (uint64_t b = done + w0; b < n; b += wstride) {
-    const uint64_t i = b + lane;
-    const bool valid = i < n;
-    add(valid, valid ? (uint32_t)(((uint64_t)s[i] >> sh_r) & bmask) : 0u);
+  if (lane == 0) {
+    // bins of the top K bits (K = 1: bins 0/1 = top bit 0/1)
+    if (K > 1) {
+      for (int b = 0; b < 4; ++b)
+        if (h[b]) atomicAdd(&hist[b], h[b]);
+    } else {
+      if (h[0] + h[1]) atomicAdd(&hist[0], h[0] + h[1]);
+      if (h[2] + h[3]) atomicAdd(&hist[1], h[2] + h[3]);
+    }
   }
-  __syncthreads();
-  for (uint32_t i = threadIdx.x; i < bins; i += blockDim.x)
-    if (sh[i]) atomicAdd(&hist[i], sh[i]);
 }
 
 template <typename T>
@@ -211,21 +222,27 @@ __device__ __forceinline__ void emit_flush(uint32_t* __restrict__ znext, uint32_
   if (co) atomicAdd(&znext[2 * p + 1], co);
 }
 
-// One level: bits of level `level` for every symbol of the level order in
-// src, and (SCATTER) the stable partition of src into dst, and (EMIT) the
-// zero counts of the level+1 nodes.
-template <typename T, bool SCATTER, bool EMIT>
+// One level over the level-l order in src:
+//   * bits of level `level` (always);
+//   * SCATTER: the stable partition of src into dst (the level-(l+1) order),
+//     with this tile's zeros-before from tilepre (no inter-tile waits);
+//   * EMIT_TILES: for every destination tile of the next level, the number of
+//     its symbols whose next-level bit is 0 (that level's tilepre input);
+//   * EMIT_NODES: for every node of the next level, its left-child size.
+// Tiles are 16 KB; CTAs are persistent (tile = blockIdx.x + k * gridDim.x)
+// and prefetch their next tile with cp.async.bulk into the other buffer.
+// Warp w owns rows [w*ROWS, (w+1)*ROWS) of 32 consecutive symbols.
+template <typename T, bool SCATTER, bool EMIT_NODES, bool EMIT_TILES>
 __global__ void __launch_bounds__(LV_THREADS)
     level_kernel(const T* __restrict__ src, T* __restrict__ dst, uint64_t n, int L, int level,
                  const uint2* __restrict__ base_lvl, uint32_t* __restrict__ bits32, uint64_t bit_off,
-                 uint64_t* status, uint32_t* counter, uint32_t* err, uint32_t* __restrict__ znext, int bulk_ok) {
+                 const uint32_t* __restrict__ tilepre, uint32_t* __restrict__ tilecnt_next,
+                 uint32_t* __restrict__ znext, uint32_t* err, int bulk_ok) {
   using S = LvShape<T>;
   extern __shared__ __align__(128) unsigned char lv_smem[];
   __shared__ __align__(8) uint64_t mbar[2];
-  __shared__ uint32_t s_tile[2];
-  __shared__ uint32_t s_cnt[S::NW];
   __shared__ uint32_t s_bits[S::NW];
-  __shared__ uint32_t s_prefix;
+  __shared__ uint32_t s_wz[LV_THREADS / 32];
   T* const buf0 = (T*)lv_smem;
   T* const buf1 = (T*)(lv_smem + S::BYTES);
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -233,35 +250,29 @@ __global__ void __launch_bounds__(LV_THREADS)
   const uint64_t nfull = bulk_ok ? n / S::TILE : 0;  // tiles fetched with bulk copies
   const int shift = L - 1 - level;
   const uint32_t pmask = level ? (uint32_t)((1ull << level) - 1) : 0u;
+  const uint32_t ltmask = lanemask_lt();
 
   if (tid == 0) {
     mbar_init(&mbar[0], 1);
     mbar_init(&mbar[1], 1);
     mbar_fence_init();
-    const uint32_t t0 = atomicAdd(counter, 1u);
-    s_tile[0] = t0;
-    if (t0 < nfull) {
+    if (blockIdx.x < nfull) {
       mbar_expect_tx(&mbar[0], S::BYTES);
-      bulk_g2s(buf0, src + (uint64_t)t0 * S::TILE, S::BYTES, &mbar[0]);
+      bulk_g2s(buf0, src + (uint64_t)blockIdx.x * S::TILE, S::BYTES, &mbar[0]);
     }
   }
   __syncthreads();
   uint32_t phase0 = 0, phase1 = 0;
   int cur = 0;
-  for (;;) {
-    const uint32_t tile = s_tile[cur];
-    if (tile >= ntiles) break;
-    if (tid == 0) {  // prefetch the next tile into the other buffer
-      const uint32_t nt = atomicAdd(counter, 1u);
-      s_tile[cur ^ 1] = nt;
-      if (nt < nfull) {
-        fence_proxy_async_smem();
-        mbar_expect_tx(&mbar[cur ^ 1], S::BYTES);
-        bulk_g2s(cur ? buf0 : buf1, src + (uint64_t)nt * S::TILE, S::BYTES, &mbar[cur ^ 1]);
-      }
+  for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const uint64_t next = tile + gridDim.x;
+    if (tid == 0 && next < nfull) {  // prefetch into the other buffer
+      fence_proxy_async_smem();
+      mbar_expect_tx(&mbar[cur ^ 1], S::BYTES);
+      bulk_g2s(cur ? buf0 : buf1, src + next * S::TILE, S::BYTES, &mbar[cur ^ 1]);
     }
     T* const tb = cur ? buf1 : buf0;
-    const uint64_t tile_base = (uint64_t)tile * S::TILE;
+    const uint64_t tile_base = tile * S::TILE;
     if (tile < nfull) {
       if (cur) {
         mbar_wait(&mbar[1], phase1, err);
@@ -277,22 +288,22 @@ __global__ void __launch_bounds__(LV_THREADS)
       }
       __syncthreads();
     }
+    const T* const wt = tb + warp * (S::ROWS * 32);
+    const uint64_t wbase = tile_base + (uint64_t)warp * (S::ROWS * 32);
 
-    // 1. level bits and zero counts per (row, warp); next-level zero counts
+    // 1. level bits, this warp's zero count, next-level node zero counts
+    uint32_t wz = 0;
     uint32_t run_p = 0xFFFFFFFFu, c_even = 0, c_odd = 0;
 #pragma unroll 4
     for (int r = 0; r < S::ROWS; ++r) {
-      const uint32_t k = r * LV_THREADS + tid;
-      const bool valid = tile_base + k < n;
-      const uint64_t x = valid ? (uint64_t)tb[k] : 0ull;
+      const bool valid = wbase + r * 32 + lane < n;
+      const uint64_t x = valid ? (uint64_t)wt[r * 32 + lane] : 0ull;
       const bool one = valid && ((x >> shift) & 1);
       const uint32_t ones = __ballot_sync(0xffffffffu, one);
       const uint32_t zeros = __ballot_sync(0xffffffffu, valid && !one);
-      if (lane == 0) {
-        s_bits[r * 8 + warp] = ones;
-        s_cnt[r * 8 + warp] = __popc(zeros);
-      }
-      if (EMIT) {
+      if (lane == 0) s_bits[warp * S::ROWS + r] = ones;
+      wz += __popc(zeros);
+      if (EMIT_NODES) {
         const uint32_t p = level ? ((uint32_t)(x >> (L - level)) & pmask) : 0u;
         const bool zn = valid && !((x >> (shift - 1)) & 1);
         const uint32_t p0 = __shfl_sync(0xffffffffu, p, 0);
@@ -313,7 +324,8 @@ __global__ void __launch_bounds__(LV_THREADS)
         }
       }
     }
-    if (EMIT && lane == 0) emit_flush(znext, run_p, c_even, c_odd);
+    if (EMIT_NODES && lane == 0) emit_flush(znext, run_p, c_even, c_odd);
+    if (lane == 0) s_wz[warp] = wz;
     __syncthreads();
 
     // 2. store the bits: tile word j covers global bits [g + 32 j, g + 32 j + 32)
@@ -335,61 +347,54 @@ __global__ void __launch_bounds__(LV_THREADS)
       }
     }
 
+    // 3. stable partition into the next level's order
     if (SCATTER) {
-      // 3. tile-exclusive zero counts and the tile's prefix (look-back)
-      if (warp == 0) {
-        constexpr int PER = S::NW / 32;
-        uint32_t loc[PER];
-        uint32_t sum = 0;
-#pragma unroll
-        for (int q = 0; q < PER; ++q) {
-          loc[q] = s_cnt[lane * PER + q];
-          sum += loc[q];
-        }
-        uint32_t inc = sum;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
-          if (lane >= (uint32_t)o) inc += t;
-        }
-        uint32_t run = inc - sum;
-#pragma unroll
-        for (int q = 0; q < PER; ++q) {
-          s_cnt[lane * PER + q] = run;
-          run += loc[q];
-        }
-        const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
-        uint64_t prefix = 0;
-        if (tile == 0) {
-          if (lane == 0) lb_publish(status, tile, LB_FLAG_INC, total);
-        } else {
-          if (lane == 0) lb_publish(status, tile, LB_FLAG_AGG, total);
-          prefix = lb_lookback_warp(status, tile, err);
-          if (lane == 0) lb_publish(status, tile, LB_FLAG_INC, prefix + total);
-        }
-        if (lane == 0) s_prefix = (uint32_t)prefix;
-      }
-      __syncthreads();
-
-      // 4. stable partition: scatter into the next level's order
-      const uint32_t zprefix = s_prefix;
-      const uint32_t ltmask = lanemask_lt();
+      uint32_t z = tilepre[tile];
+      for (uint32_t w = 0; w < warp; ++w) z += s_wz[w];
+      uint32_t ka = 0xFFFFFFFFu, ca = 0, kb = 0xFFFFFFFFu, cb = 0;  // destination-tile counts
 #pragma unroll 4
       for (int r = 0; r < S::ROWS; ++r) {
-        const uint32_t k = r * LV_THREADS + tid;
-        const uint64_t i = tile_base + k;
+        const uint64_t i = wbase + r * 32 + lane;
         const bool valid = i < n;
-        const T x = tb[k];
+        const T x = wt[r * 32 + lane];
         const bool one = valid && (((uint64_t)x >> shift) & 1);
         const uint32_t zm = __ballot_sync(0xffffffffu, valid && !one);
+        const uint32_t z_before = z + __popc(zm & ltmask);
+        z += __popc(zm);
+        uint32_t d = 0;
         if (valid) {
-          const uint32_t z_before = zprefix + s_cnt[r * 8 + warp] + __popc(zm & ltmask);
           const uint32_t p = level ? ((uint32_t)((uint64_t)x >> (L - level)) & pmask) : 0u;
           const uint2 b = base_lvl[p];
-          const uint32_t d = one ? b.y + ((uint32_t)i - z_before) : b.x + z_before;
+          d = one ? b.y + ((uint32_t)i - z_before) : b.x + z_before;
           if (d < n) dst[d] = x;
           else atomicCAS(err, 0u, (uint32_t)DERR_BAD_INDEX);
         }
+        if (EMIT_TILES) {
+          const bool pend = valid && d < n && !(((uint64_t)x >> (shift - 1)) & 1);
+          const uint32_t key = d >> S::LOG_TILE;
+          uint32_t rem = __ballot_sync(0xffffffffu, pend);
+          while (rem) {
+            const uint32_t k0 = __shfl_sync(0xffffffffu, key, __ffs(rem) - 1);
+            const uint32_t mk = __ballot_sync(0xffffffffu, pend && key == k0);
+            const uint32_t c = __popc(mk);
+            rem &= ~mk;
+            if (k0 == ka) {
+              ca += c;
+            } else if (k0 == kb) {
+              cb += c;
+            } else {
+              if (lane == 0 && ca) atomicAdd(&tilecnt_next[ka], ca);
+              ka = kb;
+              ca = cb;
+              kb = k0;
+              cb = c;
+            }
+          }
+        }
+      }
+      if (EMIT_TILES && lane == 0) {
+        if (ca) atomicAdd(&tilecnt_next[ka], ca);
+        if (cb) atomicAdd(&tilecnt_next[kb], cb);
       }
     }
     __syncthreads();
@@ -411,27 +416,19 @@ static int sm_count() {
 }
 
 template <typename T>
-static void launch_prehist(const void* s, uint64_t n, int L, int K, uint32_t* hist, cudaStream_t st) {
-  unsigned grid = (unsigned)std::min<uint64_t>((n / (16 / sizeof(T)) + 255) / 256, (uint64_t)sm_count() * 4);
-  if (grid == 0) grid = 1;
-  const int vec_ok = ((uintptr_t)s % 16) == 0;
-  prehist_kernel<T><<<grid, 256, sizeof(uint32_t) << K, st>>>((const T*)s, n, L, K, vec_ok, hist);
-}
-
-template <typename T>
 static void launch_max(const void* s, uint64_t n, unsigned long long* out, cudaStream_t st) {
   unsigned grid = (unsigned)std::min<uint64_t>((n + 255) / 256, (uint64_t)sm_count() * 8);
   if (grid == 0) grid = 1;
   max_kernel<T><<<grid, 256, 0, st>>>((const T*)s, n, out);
 }
 
-template <typename T, bool SC, bool EM>
+template <typename T, bool SC, bool EN, bool ET>
 static int level_grid(uint64_t n) {
   static int per_sm = 0;
   if (!per_sm) {
-    cudaFuncSetAttribute(level_kernel<T, SC, EM>, cudaFuncAttributePreferredSharedMemoryCarveout,
+    cudaFuncSetAttribute(level_kernel<T, SC, EN, ET>, cudaFuncAttributePreferredSharedMemoryCarveout,
                          (int)cudaSharedmemCarveoutMaxShared);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, level_kernel<T, SC, EM>, LV_THREADS,
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, level_kernel<T, SC, EN, ET>, LV_THREADS,
                                                   2 * LvShape<T>::BYTES);
     if (per_sm <= 0) per_sm = 1;
   }
@@ -441,17 +438,29 @@ static int level_grid(uint64_t n) {
 
 template <typename T>
 static void launch_level(const void* src, void* dst, uint64_t n, int L, int level, const uint2* base_lvl,
-                         uint32_t* bits32, uint64_t bit_off, uint64_t* status, uint32_t* counter, uint32_t* err,
-                         uint32_t* znext, bool scatter, bool emit, cudaStream_t st) {
+                         uint32_t* bits32, uint64_t bit_off, const uint32_t* tilepre, uint32_t* tilecnt_next,
+                         uint32_t* znext, uint32_t* err, bool scatter, bool emit_nodes, bool emit_tiles,
+                         cudaStream_t st) {
   const int bulk_ok = ((uintptr_t)src % 16) == 0;
   const size_t shm = 2 * LvShape<T>::BYTES;
-#define WTG_LV(SC, EM)                                                                                       \
-  level_kernel<T, SC, EM><<<level_grid<T, SC, EM>(n), LV_THREADS, shm, st>>>(                               \
-      (const T*)src, (T*)dst, n, L, level, base_lvl, bits32, bit_off, status, counter, err, znext, bulk_ok)
-  if (scatter && emit) WTG_LV(true, true);
-  else if (scatter) WTG_LV(true, false);
-  else WTG_LV(false, false);
+#define WTG_LV(SC, EN, ET)                                                                                \
+  level_kernel<T, SC, EN, ET><<<level_grid<T, SC, EN, ET>(n), LV_THREADS, shm, st>>>(                    \
+      (const T*)src, (T*)dst, n, L, level, base_lvl, bits32, bit_off, tilepre, tilecnt_next, znext, err, \
+      bulk_ok)
+  if (scatter && emit_nodes) WTG_LV(true, true, true);
+  else if (scatter && emit_tiles) WTG_LV(true, false, true);
+  else if (scatter) WTG_LV(true, false, false);
+  else WTG_LV(false, false, false);
 #undef WTG_LV
+}
+
+template <typename T>
+static void launch_prepass(const void* s, uint64_t n, int L, int K, uint32_t* tilecnt, uint32_t* hist,
+                           cudaStream_t st) {
+  const uint64_t tiles = (n + LvShape<T>::TILE - 1) / LvShape<T>::TILE;
+  unsigned grid = (unsigned)std::min<uint64_t>(tiles, (uint64_t)sm_count() * 8);
+  if (grid == 0) grid = 1;
+  prepass_kernel<T><<<grid, LV_THREADS, 0, st>>>((const T*)s, n, L, K, tilecnt, hist);
 }
 
 #define WTG_DISPATCH(eb, fn, ...)                       \
@@ -518,9 +527,17 @@ int tree_build(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int L, uint32
   uint2* base = t.base.as<uint2>();
   WTG_CK(cudaMemsetAsync(S, 0, ((1ull << K) + 1) * sizeof(uint32_t), s));
   WTG_CK(cudaMemsetAsync(Z, 0, 3 * heap * sizeof(uint32_t), s));
+
+  // per-level tile zero counts [L x tiles] and their scan (tilepre)
+  const uint64_t tiles = n ? (n + tile_elems(eb) - 1) / tile_elems(eb) : 0;
+  if ((rc = t.status.ensure(((uint64_t)L + 1) * (tiles + 1) * sizeof(uint32_t), s))) return rc;
+  uint32_t* tilecnt = t.status.as<uint32_t>();
+  uint32_t* tilepre = tilecnt + (uint64_t)L * (tiles + 1);
+  if (n) WTG_CK(cudaMemsetAsync(tilecnt, 0, (uint64_t)L * (tiles + 1) * sizeof(uint32_t), s));
+
   if (n) {
     prof_begin(PROF_HIST, s);
-    WTG_DISPATCH(eb, launch_prehist, d_seq, n, L, K, S, s);
+    WTG_DISPATCH(eb, launch_prepass, d_seq, n, L, K, tilecnt, S, s);
     prof_end(PROF_HIST, s);
     count_launch();
     WTG_CK(cudaGetLastError());
@@ -528,27 +545,22 @@ int tree_build(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int L, uint32
   if ((rc = scan_exclusive_u32(S, S, (1ull << K) + 1, t.scan_tmp, d_err, s))) return rc;
   {
     const uint64_t top = (1ull << K) - 1;
-    unsigned grid = (unsigned)std::min<uint64_t>((top + 255) / 256, 1024);
-    if (grid == 0) grid = 1;
     prof_begin(PROF_TABLES, s);
-    top_tables_kernel<<<grid, 256, 0, s>>>(S, K, C, Z);
+    top_tables_kernel<<<1, 256, 0, s>>>(S, K, C, Z);
     prof_end(PROF_TABLES, s);
     count_launch();
     WTG_CK(cudaGetLastError());
     if ((rc = scan_exclusive_u32(Z, ZS, top + 1, t.scan_tmp, d_err, s))) return rc;
     prof_begin(PROF_TABLES, s);
-    base_kernel<<<grid, 256, 0, s>>>(C, Z, ZS, K, base);
+    base_kernel<<<1, 256, 0, s>>>(C, Z, ZS, K, base);
     prof_end(PROF_TABLES, s);
     count_launch();
     WTG_CK(cudaGetLastError());
   }
 
-  // level passes; levels >= K get their tables from the previous pass
+  // level passes; each scattering pass feeds the next level's tile counts
+  // and (from level K on) its node tables
   if (n) {
-    const uint64_t tiles = (n + tile_elems(eb) - 1) / tile_elems(eb);
-    const uint64_t per_level = tiles + 1;
-    if ((rc = t.status.ensure(per_level * (uint64_t)L * sizeof(uint64_t), s))) return rc;
-    WTG_CK(cudaMemsetAsync(t.status.p, 0, per_level * (uint64_t)L * sizeof(uint64_t), s));
     if (L > 1) {
       if ((rc = t.lvl[0].ensure(n * eb + 16, s))) return rc;
       if ((rc = t.lvl[1].ensure(n * eb + 16, s))) return rc;
@@ -556,13 +568,17 @@ int tree_build(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int L, uint32
     const void* src = d_seq;
     for (int l = 0; l < L; ++l) {
       const bool scatter = l < L - 1;
-      const bool emit = (l + 1 >= K) && (l + 1 <= L - 2);
+      const bool emit_tiles = l + 1 <= L - 2;
+      const bool emit_nodes = emit_tiles && (l + 1 >= K);
       void* dst = scatter ? t.lvl[l & 1].p : nullptr;
-      uint64_t* st = t.status.as<uint64_t>() + per_level * l;
+      if (scatter)
+        if ((rc = scan_exclusive_u32(tilecnt + (uint64_t)l * (tiles + 1), tilepre, tiles, t.scan_tmp, d_err, s)))
+          return rc;
       uint32_t* znext = Z + ((1ull << (l + 1)) - 1);
+      uint32_t* tnext = tilecnt + (uint64_t)(l + 1) * (tiles + 1);
       prof_begin(scatter ? PROF_LEVEL : PROF_LEVEL_LAST, s);
       WTG_DISPATCH(eb, launch_level, src, dst, n, L, l, base + ((1ull << l) - 1), t.bits.as<uint32_t>(),
-                   (uint64_t)l * n, st + 1, (uint32_t*)st, d_err, znext, scatter, emit, s);
+                   (uint64_t)l * n, tilepre, tnext, znext, d_err, scatter, emit_nodes, emit_tiles, s);
       prof_end(scatter ? PROF_LEVEL : PROF_LEVEL_LAST, s);
       count_launch();
       WTG_CK(cudaGetLastError());
