@@ -245,56 +245,53 @@ __global__ void select_sb_pack_kernel(int t_b, uint64_t nsb, uint32_t logn, cons
   });
 }
 
-// Long blocks, step 1: a warp per 64-arg group of each long superblock.  The
-// group's args lie between two consecutive samples (positions of args 64k and
-// 64(k+1)), so every group is extracted independently and all long spans are
-// read once, in parallel (init_longblock_serial, :401-438, restated).
+// Long blocks, step 1: the position of every arg of every long superblock,
+// one thread per entry (init_longblock_serial, :401-438, restated).  Long
+// superblocks are where args are sparse, so instead of scanning their span the
+// k-th arg is located by binary search over the rank table's absolute counts
+// (between the two samples that bracket it), then within its 512-bit
+// superblock by popcounts of at most 8 words.
+__device__ __forceinline__ uint64_t args_before_sb(int t_b, const uint64_t* __restrict__ rank, uint64_t b) {
+  const uint64_t r = rank[2 * b];
+  return t_b ? r : 512 * b - r;
+}
+
 __global__ void __launch_bounds__(256)
-    select_long_extract_kernel(int t_b, const uint64_t* __restrict__ words, uint64_t size, uint64_t W,
-                               const uint64_t* __restrict__ samples, uint64_t samp_last,
-                               const unsigned long long* info, const uint64_t* __restrict__ long_list,
-                               uint64_t* __restrict__ ent) {
-  const uint32_t lane = threadIdx.x & 31;
-  const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    select_long_fill_kernel(int t_b, const uint64_t* __restrict__ words, uint64_t size, uint64_t W,
+                            const uint64_t* __restrict__ rank, const uint64_t* __restrict__ samples,
+                            uint64_t samp_last, const unsigned long long* info,
+                            const uint64_t* __restrict__ long_list, uint64_t* __restrict__ ent, uint32_t* err) {
+  const uint64_t gt = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const uint64_t m = info[t_b ? INF_M1 : INF_M0];
   const uint64_t last = info[t_b ? INF_LAST1 : INF_LAST0];  // last arg position + 1
   const uint64_t nlong = info[t_b ? INF_NLONG1 : INF_NLONG0];
-  const uint64_t li = gw >> 6, g = gw & 63;
+  const uint64_t li = gt >> 12, j = gt & 4095;
   if (li >= nlong) return;
-  const uint64_t i = long_list[li];
-  const uint64_t a0 = 4096 * i + 64 * g;
-  if (a0 >= m) return;  // entries past the arg count stay zero
-  auto samp = [&](uint64_t k) { return t_b ? samples[k] : samples[samp_last - k]; };
-  const uint64_t p0 = samp(a0 >> 6);
-  const uint64_t pend = (a0 + 64 < m) ? samp((a0 >> 6) + 1) : last;
-  const uint64_t tailmask = (size & 63) ? ((1ull << (size & 63)) - 1) : ~0ull;
-  uint64_t* out = ent + li * 4096 + 64 * g;
-  uint64_t cnt = 0;
-  for (uint64_t wb = p0 >> 6; (wb << 6) < pend && cnt < 64; wb += 32) {
-    const uint64_t wi = wb + lane;
-    uint64_t x = 0;
-    if ((wi << 6) < pend && wi < W) {
-      x = words[wi];
-      if (!t_b) x = ~x;
-      if (wi == W - 1) x &= tailmask;
-      if (wi == (p0 >> 6)) x &= ~0ull << (p0 & 63);
-      if ((wi << 6) + 64 > pend) x &= (1ull << (pend & 63)) - 1;
-    }
-    const uint32_t c = __popcll(x);
-    uint32_t inc = c;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
-      if (lane >= (uint32_t)o) inc += t;
-    }
-    uint64_t p = cnt + inc - c;
-    while (x) {
-      if (p < 64) out[p] = (wi << 6) + (__ffsll((long long)x) - 1);
-      ++p;
-      x &= x - 1;
-    }
-    cnt += __shfl_sync(0xffffffffu, inc, 31);
+  const uint64_t k = 4096 * long_list[li] + j;  // 0-based arg index
+  if (k >= m) return;                           // entries past the arg count stay zero
+  auto samp = [&](uint64_t q) { return t_b ? samples[q] : samples[samp_last - q]; };
+  const uint64_t plo = samp(k >> 6);
+  const uint64_t phi = ((k >> 6) + 1) * 64 < m ? samp((k >> 6) + 1) : last - 1;
+  uint64_t lo = plo >> 9, hi = phi >> 9;  // largest b in [lo, hi] with args_before_sb(b) <= k
+  while (lo < hi) {
+    const uint64_t mid = (lo + hi + 1) >> 1;
+    if (args_before_sb(t_b, rank, mid) <= k) lo = mid;
+    else hi = mid - 1;
   }
+  uint64_t rem = k - args_before_sb(t_b, rank, lo);
+  const uint64_t tailmask = (size & 63) ? ((1ull << (size & 63)) - 1) : ~0ull;
+  for (uint64_t wi = 8 * lo; wi < 8 * lo + 8 && wi < W; ++wi) {
+    uint64_t x = words[wi];
+    if (!t_b) x = ~x;
+    if (wi == W - 1) x &= tailmask;
+    const uint32_t c = __popcll(x);
+    if (rem < c) {
+      ent[(li << 12) + j] = (wi << 6) + sel64(x, (uint32_t)rem + 1);
+      return;
+    }
+    rem -= c;
+  }
+  atomicCAS(err, 0u, (uint32_t)DERR_SELECT_OVERFLOW);  // tables inconsistent
 }
 
 // Long blocks, step 2: pack each long block's 4096 positions (width hi(end)+1).
@@ -340,6 +337,9 @@ void bv_release(BvSupport& bv, cudaStream_t s) {
 int bv_build(BvSupport& bv, const uint64_t* d_words, uint64_t size, uint32_t flags, uint32_t* d_err,
              cudaStream_t s) {
   int rc;
+  // select's long blocks are filled through the rank table, so it is built
+  // whenever a select support is
+  if (flags & (WTG_SELECT1 | WTG_SELECT0)) flags |= WTG_RANK;
   bv.size = size;
   bv.words = d_words;
   bv.flags = flags;
@@ -440,10 +440,10 @@ int bv_build(BvSupport& bv, const uint64_t* d_words, uint64_t size, uint32_t fla
     if (nlong) {
       if ((rc = sd.long_ent.ensure(nlong * 4096 * sizeof(uint64_t), s))) return rc;
       WTG_CK(cudaMemsetAsync(sd.long_ent.p, 0, nlong * 4096 * sizeof(uint64_t), s));
-      const uint64_t warps = nlong * 64;
       prof_begin(PROF_SELECT, s);
-      select_long_extract_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(
-          t_b, d_words, size, W, samples, samp_n - 1, info, sd.long_list.as<uint64_t>(), sd.long_ent.as<uint64_t>());
+      select_long_fill_kernel<<<(unsigned)((nlong * 4096 + 255) / 256), 256, 0, s>>>(
+          t_b, d_words, size, W, bv.rank.as<uint64_t>(), samples, samp_n - 1, info, sd.long_list.as<uint64_t>(),
+          sd.long_ent.as<uint64_t>(), d_err);
       prof_end(PROF_SELECT, s);
       count_launch();
       WTG_CK(cudaGetLastError());

@@ -216,18 +216,53 @@ __global__ void node_kernel(const uint32_t* __restrict__ C, const uint32_t* __re
 
 // ------------------------------------------------------------ level pass
 
-__device__ __forceinline__ void emit_flush(uint32_t* __restrict__ znext, uint32_t p, uint32_t ce, uint32_t co) {
-  if (p == 0xFFFFFFFFu) return;
-  if (ce) atomicAdd(&znext[2 * p], ce);
-  if (co) atomicAdd(&znext[2 * p + 1], co);
+// Warp-uniform two-entry counter cache: counts per key are accumulated in
+// registers and added to `target` (one atomic) when a key is evicted.  Keys
+// of a row arrive sorted by node or by destination, so two entries catch
+// almost every repeat.
+struct Slot2 {
+  uint32_t ka = 0xFFFFFFFFu, ca = 0, kb = 0xFFFFFFFFu, cb = 0;
+};
+
+__device__ __forceinline__ void slot2_count(Slot2& s, bool pend, uint32_t key, uint32_t* __restrict__ target,
+                                            uint32_t lane) {
+  uint32_t rem = __ballot_sync(0xffffffffu, pend);
+  while (rem) {
+    const uint32_t k0 = __shfl_sync(0xffffffffu, key, __ffs(rem) - 1);
+    const uint32_t mk = __ballot_sync(0xffffffffu, pend && key == k0);
+    const uint32_t c = __popc(mk);
+    rem &= ~mk;
+    if (k0 == s.ka) {
+      s.ca += c;
+    } else if (k0 == s.kb) {
+      s.cb += c;
+    } else {
+      if (lane == 0 && s.ca) atomicAdd(&target[s.ka], s.ca);
+      s.ka = s.kb;
+      s.ca = s.cb;
+      s.kb = k0;
+      s.cb = c;
+    }
+  }
+}
+
+__device__ __forceinline__ void slot2_flush(Slot2& s, uint32_t* __restrict__ target, uint32_t lane) {
+  if (lane == 0) {
+    if (s.ca) atomicAdd(&target[s.ka], s.ca);
+    if (s.cb) atomicAdd(&target[s.kb], s.cb);
+  }
+  s = Slot2();
 }
 
 // One level over the level-l order in src:
 //   * bits of level `level` (always);
-//   * SCATTER: the stable partition of src into dst (the level-(l+1) order),
-//     with this tile's zeros-before from tilepre (no inter-tile waits);
+//   * SCATTER: the stable partition of src into dst (the level-(l+1) order).
+//     The tile is partitioned locally in shared memory (its zeros, then its
+//     ones, each in order) and every run is then stored contiguously; the
+//     tile's zeros-before come from tilepre, so tiles never wait on each
+//     other;
 //   * EMIT_TILES: for every destination tile of the next level, the number of
-//     its symbols whose next-level bit is 0 (that level's tilepre input);
+//     its symbols whose next-level bit is 0 (the next level's tilepre input);
 //   * EMIT_NODES: for every node of the next level, its left-child size.
 // Tiles are 16 KB; CTAs are persistent (tile = blockIdx.x + k * gridDim.x)
 // and prefetch their next tile with cp.async.bulk into the other buffer.
@@ -245,6 +280,7 @@ __global__ void __launch_bounds__(LV_THREADS)
   __shared__ uint32_t s_wz[LV_THREADS / 32];
   T* const buf0 = (T*)lv_smem;
   T* const buf1 = (T*)(lv_smem + S::BYTES);
+  T* const stage = (T*)(lv_smem + 2 * S::BYTES);
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint64_t ntiles = (n + S::TILE - 1) / S::TILE;
   const uint64_t nfull = bulk_ok ? n / S::TILE : 0;  // tiles fetched with bulk copies
@@ -264,6 +300,8 @@ __global__ void __launch_bounds__(LV_THREADS)
   __syncthreads();
   uint32_t phase0 = 0, phase1 = 0;
   int cur = 0;
+  uint32_t cache_p = 0xFFFFFFFFu;  // warp-uniform node constants cache
+  uint2 cache_b = make_uint2(0, 0);
   for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const uint64_t next = tile + gridDim.x;
     if (tid == 0 && next < nfull) {  // prefetch into the other buffer
@@ -273,6 +311,7 @@ __global__ void __launch_bounds__(LV_THREADS)
     }
     T* const tb = cur ? buf1 : buf0;
     const uint64_t tile_base = tile * S::TILE;
+    const uint32_t nvalid = (uint32_t)min((uint64_t)S::TILE, n - tile_base);
     if (tile < nfull) {
       if (cur) {
         mbar_wait(&mbar[1], phase1, err);
@@ -282,22 +321,19 @@ __global__ void __launch_bounds__(LV_THREADS)
         phase0 ^= 1;
       }
     } else {
-      for (uint32_t k = tid; k < S::TILE; k += LV_THREADS) {
-        const uint64_t i = tile_base + k;
-        tb[k] = i < n ? src[i] : T(0);
-      }
+      for (uint32_t k = tid; k < S::TILE; k += LV_THREADS) tb[k] = k < nvalid ? src[tile_base + k] : T(0);
       __syncthreads();
     }
-    const T* const wt = tb + warp * (S::ROWS * 32);
-    const uint64_t wbase = tile_base + (uint64_t)warp * (S::ROWS * 32);
+    const uint32_t wofs = warp * (S::ROWS * 32);
 
     // 1. level bits, this warp's zero count, next-level node zero counts
     uint32_t wz = 0;
-    uint32_t run_p = 0xFFFFFFFFu, c_even = 0, c_odd = 0;
+    Slot2 nodes;
 #pragma unroll 4
     for (int r = 0; r < S::ROWS; ++r) {
-      const bool valid = wbase + r * 32 + lane < n;
-      const uint64_t x = valid ? (uint64_t)wt[r * 32 + lane] : 0ull;
+      const uint32_t k = wofs + r * 32 + lane;
+      const bool valid = k < nvalid;
+      const uint64_t x = (uint64_t)tb[k];
       const bool one = valid && ((x >> shift) & 1);
       const uint32_t ones = __ballot_sync(0xffffffffu, one);
       const uint32_t zeros = __ballot_sync(0xffffffffu, valid && !one);
@@ -306,25 +342,10 @@ __global__ void __launch_bounds__(LV_THREADS)
       if (EMIT_NODES) {
         const uint32_t p = level ? ((uint32_t)(x >> (L - level)) & pmask) : 0u;
         const bool zn = valid && !((x >> (shift - 1)) & 1);
-        const uint32_t p0 = __shfl_sync(0xffffffffu, p, 0);
-        if (__ballot_sync(0xffffffffu, valid && p != p0) == 0) {
-          const uint32_t ce = __popc(__ballot_sync(0xffffffffu, zn && !one));
-          const uint32_t co = __popc(__ballot_sync(0xffffffffu, zn && one));
-          if (p0 != run_p) {
-            if (lane == 0) emit_flush(znext, run_p, c_even, c_odd);
-            run_p = p0;
-            c_even = c_odd = 0;
-          }
-          c_even += ce;
-          c_odd += co;
-        } else {
-          const uint32_t key = zn ? (2 * p + (one ? 1u : 0u)) : 0xFFFFFFFFu;
-          const uint32_t grp = __match_any_sync(0xffffffffu, key);
-          if (zn && lane == (uint32_t)(__ffs(grp) - 1)) atomicAdd(&znext[key], (uint32_t)__popc(grp));
-        }
+        slot2_count(nodes, zn, 2 * p + (one ? 1u : 0u), znext, lane);
       }
     }
-    if (EMIT_NODES && lane == 0) emit_flush(znext, run_p, c_even, c_odd);
+    if (EMIT_NODES) slot2_flush(nodes, znext, lane);
     if (lane == 0) s_wz[warp] = wz;
     __syncthreads();
 
@@ -333,69 +354,73 @@ __global__ void __launch_bounds__(LV_THREADS)
       const uint64_t g = bit_off + tile_base;
       const uint32_t g0 = (uint32_t)(g & 31);
       const uint64_t G = g >> 5;
-      const uint64_t valid_bits = min((uint64_t)S::TILE, n - tile_base);
       for (int j = tid; j <= S::NW; j += LV_THREADS) {
         if (g0 == 0 && j == S::NW) break;
         const uint32_t curw = j < S::NW ? s_bits[j] : 0u;
         const uint32_t prev = j > 0 ? s_bits[j - 1] : 0u;
         const uint32_t val = g0 ? ((curw << g0) | (prev >> (32 - g0))) : curw;
         const uint64_t wlo = (G + j) * 32;
-        if (wlo >= g + valid_bits) continue;
-        const bool full = (wlo >= g) && (wlo + 32 <= g + valid_bits);
+        if (wlo >= g + nvalid) continue;
+        const bool full = (wlo >= g) && (wlo + 32 <= g + nvalid);
         if (full) bits32[G + j] = val;
         else if (val) atomicOr(&bits32[G + j], val);
       }
     }
 
-    // 3. stable partition into the next level's order
     if (SCATTER) {
-      uint32_t z = tilepre[tile];
-      for (uint32_t w = 0; w < warp; ++w) z += s_wz[w];
-      uint32_t ka = 0xFFFFFFFFu, ca = 0, kb = 0xFFFFFFFFu, cb = 0;  // destination-tile counts
+      // 3. local stable partition: zeros of the tile first, then its ones
+      uint32_t zt = 0, zl = 0;
+#pragma unroll
+      for (uint32_t w = 0; w < LV_THREADS / 32; ++w) {
+        const uint32_t c = s_wz[w];
+        zl += w < warp ? c : 0u;
+        zt += c;
+      }
 #pragma unroll 4
       for (int r = 0; r < S::ROWS; ++r) {
-        const uint64_t i = wbase + r * 32 + lane;
-        const bool valid = i < n;
-        const T x = wt[r * 32 + lane];
+        const uint32_t k = wofs + r * 32 + lane;
+        const bool valid = k < nvalid;
+        const T x = tb[k];
         const bool one = valid && (((uint64_t)x >> shift) & 1);
         const uint32_t zm = __ballot_sync(0xffffffffu, valid && !one);
-        const uint32_t z_before = z + __popc(zm & ltmask);
-        z += __popc(zm);
-        uint32_t d = 0;
-        if (valid) {
-          const uint32_t p = level ? ((uint32_t)((uint64_t)x >> (L - level)) & pmask) : 0u;
-          const uint2 b = base_lvl[p];
-          d = one ? b.y + ((uint32_t)i - z_before) : b.x + z_before;
-          if (d < n) dst[d] = x;
-          else atomicCAS(err, 0u, (uint32_t)DERR_BAD_INDEX);
-        }
-        if (EMIT_TILES) {
-          const bool pend = valid && d < n && !(((uint64_t)x >> (shift - 1)) & 1);
-          const uint32_t key = d >> S::LOG_TILE;
-          uint32_t rem = __ballot_sync(0xffffffffu, pend);
-          while (rem) {
-            const uint32_t k0 = __shfl_sync(0xffffffffu, key, __ffs(rem) - 1);
-            const uint32_t mk = __ballot_sync(0xffffffffu, pend && key == k0);
-            const uint32_t c = __popc(mk);
-            rem &= ~mk;
-            if (k0 == ka) {
-              ca += c;
-            } else if (k0 == kb) {
-              cb += c;
-            } else {
-              if (lane == 0 && ca) atomicAdd(&tilecnt_next[ka], ca);
-              ka = kb;
-              ca = cb;
-              kb = k0;
-              cb = c;
-            }
+        const uint32_t zb = zl + __popc(zm & ltmask);
+        zl += __popc(zm);
+        if (valid) stage[one ? zt + (k - zb) : zb] = x;
+      }
+      __syncthreads();
+
+      // 4. store the runs: slot j < zt is the tile's j-th zero, slot j >= zt
+      //    its (j - zt)-th one; consecutive slots of a node go to consecutive
+      //    destinations
+      const uint32_t zpre = tilepre[tile];
+      const uint32_t opre = (uint32_t)tile_base - zpre;
+      Slot2 tiles;
+      for (uint32_t j0 = warp * 32; j0 < nvalid; j0 += LV_THREADS) {
+        const uint32_t j = j0 + lane;
+        const bool valid = j < nvalid;
+        const T x = stage[valid ? j : j0];
+        const uint32_t p = level ? ((uint32_t)((uint64_t)x >> (L - level)) & pmask) : 0u;
+        const uint32_t p0 = __shfl_sync(0xffffffffu, p, 0);
+        uint2 b;
+        if (__ballot_sync(0xffffffffu, valid && p != p0) == 0) {
+          if (p0 != cache_p) {
+            cache_p = p0;
+            cache_b = base_lvl[p0];
           }
+          b = cache_b;
+        } else {
+          b = base_lvl[p];
+        }
+        const uint32_t d = j >= zt ? b.y + opre + (j - zt) : b.x + zpre + j;
+        const bool ok = valid && d < n;
+        if (ok) dst[d] = x;
+        else if (valid) atomicCAS(err, 0u, (uint32_t)DERR_BAD_INDEX);
+        if (EMIT_TILES) {
+          const bool pend = ok && !(((uint64_t)x >> (shift - 1)) & 1);
+          slot2_count(tiles, pend, d >> S::LOG_TILE, tilecnt_next, lane);
         }
       }
-      if (EMIT_TILES && lane == 0) {
-        if (ca) atomicAdd(&tilecnt_next[ka], ca);
-        if (cb) atomicAdd(&tilecnt_next[kb], cb);
-      }
+      if (EMIT_TILES) slot2_flush(tiles, tilecnt_next, lane);
     }
     __syncthreads();
     cur ^= 1;
@@ -428,8 +453,10 @@ static int level_grid(uint64_t n) {
   if (!per_sm) {
     cudaFuncSetAttribute(level_kernel<T, SC, EN, ET>, cudaFuncAttributePreferredSharedMemoryCarveout,
                          (int)cudaSharedmemCarveoutMaxShared);
+    cudaFuncSetAttribute(level_kernel<T, SC, EN, ET>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(3 * LvShape<T>::BYTES));
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, level_kernel<T, SC, EN, ET>, LV_THREADS,
-                                                  2 * LvShape<T>::BYTES);
+                                                  3 * LvShape<T>::BYTES);
     if (per_sm <= 0) per_sm = 1;
   }
   const uint64_t tiles = (n + LvShape<T>::TILE - 1) / LvShape<T>::TILE;
@@ -442,7 +469,7 @@ static void launch_level(const void* src, void* dst, uint64_t n, int L, int leve
                          uint32_t* znext, uint32_t* err, bool scatter, bool emit_nodes, bool emit_tiles,
                          cudaStream_t st) {
   const int bulk_ok = ((uintptr_t)src % 16) == 0;
-  const size_t shm = 2 * LvShape<T>::BYTES;
+  const size_t shm = 3 * LvShape<T>::BYTES;
 #define WTG_LV(SC, EN, ET)                                                                                \
   level_kernel<T, SC, EN, ET><<<level_grid<T, SC, EN, ET>(n), LV_THREADS, shm, st>>>(                    \
       (const T*)src, (T*)dst, n, L, level, base_lvl, bits32, bit_off, tilepre, tilecnt_next, znext, err, \
