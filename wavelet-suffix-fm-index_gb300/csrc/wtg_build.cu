@@ -40,13 +40,14 @@ namespace wtg {
 constexpr int LV_THREADS = 256;
 constexpr int TOP_BITS = 2;  // bits histogrammed by the pre-pass (ballot counted)
 
+constexpr int CHUNK = 512;      // symbols per warp chunk (16 rows of 32)
+constexpr int LOG_CHUNK = 9;
+constexpr int WROWS = CHUNK / 32;
+
 template <typename T>
 struct LvShape {
-  static constexpr int ROWS = 16384 / (LV_THREADS * (int)sizeof(T));  // rows of 32 symbols per warp
-  static constexpr uint32_t TILE = LV_THREADS * ROWS;                  // symbols per tile (16 KB)
+  static constexpr uint32_t TILE = LV_THREADS / 32 * CHUNK;  // symbols per CTA tile
   static constexpr uint32_t BYTES = TILE * sizeof(T);
-  static constexpr int NW = ROWS * (LV_THREADS / 32);  // 32-bit words of level bits per tile
-  static constexpr int LOG_TILE = sizeof(T) == 1 ? 14 : sizeof(T) == 2 ? 13 : sizeof(T) == 4 ? 12 : 11;
 };
 
 // ------------------------------------------------------------ pre-pass
@@ -59,16 +60,15 @@ __global__ void __launch_bounds__(LV_THREADS) prepass_kernel(const T* __restrict
                                                              uint32_t* __restrict__ tilecnt,
                                                              uint32_t* __restrict__ hist) {
   using S = LvShape<T>;
-  __shared__ uint32_t s_wz[LV_THREADS / 32];
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint64_t ntiles = (n + S::TILE - 1) / S::TILE;
   uint32_t h[4] = {0, 0, 0, 0};
   const int top = L - 1;
   for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const uint64_t base = tile * S::TILE + (uint64_t)warp * (S::ROWS * 32);
+    const uint64_t base = tile * S::TILE + (uint64_t)warp * CHUNK;
     uint32_t wz = 0;
 #pragma unroll 4
-    for (int r = 0; r < S::ROWS; ++r) {
+    for (int r = 0; r < WROWS; ++r) {
       const uint64_t i = base + r * 32 + lane;
       const bool valid = i < n;
       const uint64_t x = valid ? (uint64_t)s[i] : 0ull;
@@ -84,14 +84,7 @@ __global__ void __launch_bounds__(LV_THREADS) prepass_kernel(const T* __restrict
       h[2] += __popc(vm) - __popc(z) - __popc(o11);
       h[3] += __popc(o11);
     }
-    if (lane == 0) s_wz[warp] = wz;
-    __syncthreads();
-    if (tid == 0) {
-      uint32_t t = 0;
-      for (int w = 0; w < LV_THREADS / 32; ++w) t += s_wz[w];
-      tilecnt[tile] = t;
-    }
-    __syncthreads();
+    if (lane == 0 && base < n) tilecnt[base >> LOG_CHUNK] = wz;  // zeros of this 512-symbol chunk
   }
   if (lane == 0) {
     // bins of the top K bits (K = 1: bins 0/1 = top bit 0/1)
@@ -246,6 +239,12 @@ __device__ __forceinline__ void slot2_count(Slot2& s, bool pend, uint32_t key, u
   }
 }
 
+__device__ __forceinline__ void emit_flush(uint32_t* __restrict__ znext, uint32_t p, uint32_t ce, uint32_t co) {
+  if (p == 0xFFFFFFFFu) return;
+  if (ce) atomicAdd(&znext[2 * p], ce);
+  if (co) atomicAdd(&znext[2 * p + 1], co);
+}
+
 __device__ __forceinline__ void slot2_flush(Slot2& s, uint32_t* __restrict__ target, uint32_t lane) {
   if (lane == 0) {
     if (s.ca) atomicAdd(&target[s.ka], s.ca);
@@ -254,37 +253,40 @@ __device__ __forceinline__ void slot2_flush(Slot2& s, uint32_t* __restrict__ tar
   s = Slot2();
 }
 
-// One level over the level-l order in src:
-//   * bits of level `level` (always);
-//   * SCATTER: the stable partition of src into dst (the level-(l+1) order).
-//     The tile is partitioned locally in shared memory (its zeros, then its
-//     ones, each in order) and every run is then stored contiguously; the
-//     tile's zeros-before come from tilepre, so tiles never wait on each
-//     other;
-//   * EMIT_TILES: for every destination tile of the next level, the number of
-//     its symbols whose next-level bit is 0 (the next level's tilepre input);
-//   * EMIT_NODES: for every node of the next level, its left-child size.
-// Tiles are 16 KB; CTAs are persistent (tile = blockIdx.x + k * gridDim.x)
-// and prefetch their next tile with cp.async.bulk into the other buffer.
-// Warp w owns rows [w*ROWS, (w+1)*ROWS) of 32 consecutive symbols.
+// One level over the level-l order in src.  Each warp owns independent
+// 512-symbol chunks; its zeros-before come from chunkpre (the scan of the
+// counts the previous pass emitted), so warps and CTAs never wait on each
+// other.  Per chunk:
+//   * the level's bits: one ballot per 32 symbols, stored as whole words;
+//   * SCATTER: every symbol goes straight to its place in the next level's
+//     order (dst): bit 0 -> C(p) + zeros before it in node p, bit 1 ->
+//     C(p) + zeros(p) + ones before it in node p, through base(p) = (C - Zb,
+//     zeros + Zb) and the level-wide zero rank;
+//   * EMIT_TILES: per 512-symbol chunk of the next level, the number of its
+//     symbols whose next bit is 0 (the next pass's chunkpre input);
+//   * EMIT_NODES: per node of the next level, its left-child size.
+// A chunk inside one node (the common case) uses one base(p) for all rows;
+// its zero run and one run are contiguous in dst and each touches at most two
+// destination chunks, so emission is four ballot counts per row and four
+// atomics per chunk.  Chunks that straddle nodes take a general path.
+// Tiles of 8 chunks arrive by cp.async.bulk into a double buffer; CTAs are
+// persistent (tile = blockIdx.x + k * gridDim.x).
 template <typename T, bool SCATTER, bool EMIT_NODES, bool EMIT_TILES>
 __global__ void __launch_bounds__(LV_THREADS)
     level_kernel(const T* __restrict__ src, T* __restrict__ dst, uint64_t n, int L, int level,
                  const uint2* __restrict__ base_lvl, uint32_t* __restrict__ bits32, uint64_t bit_off,
-                 const uint32_t* __restrict__ tilepre, uint32_t* __restrict__ tilecnt_next,
+                 const uint32_t* __restrict__ chunkpre, uint32_t* __restrict__ chunkcnt_next,
                  uint32_t* __restrict__ znext, uint32_t* err, int bulk_ok) {
   using S = LvShape<T>;
   extern __shared__ __align__(128) unsigned char lv_smem[];
   __shared__ __align__(8) uint64_t mbar[2];
-  __shared__ uint32_t s_bits[S::NW];
-  __shared__ uint32_t s_wz[LV_THREADS / 32];
   T* const buf0 = (T*)lv_smem;
   T* const buf1 = (T*)(lv_smem + S::BYTES);
-  T* const stage = (T*)(lv_smem + 2 * S::BYTES);
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint64_t ntiles = (n + S::TILE - 1) / S::TILE;
   const uint64_t nfull = bulk_ok ? n / S::TILE : 0;  // tiles fetched with bulk copies
   const int shift = L - 1 - level;
+  const int pshift = L - level;
   const uint32_t pmask = level ? (uint32_t)((1ull << level) - 1) : 0u;
   const uint32_t ltmask = lanemask_lt();
 
@@ -300,8 +302,9 @@ __global__ void __launch_bounds__(LV_THREADS)
   __syncthreads();
   uint32_t phase0 = 0, phase1 = 0;
   int cur = 0;
-  uint32_t cache_p = 0xFFFFFFFFu;  // warp-uniform node constants cache
+  uint32_t cache_p = 0xFFFFFFFFu;  // warp-uniform base(p) cache
   uint2 cache_b = make_uint2(0, 0);
+  uint32_t run_p = 0xFFFFFFFFu, run_e = 0, run_o = 0;  // EMIT_NODES run over uniform chunks
   for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const uint64_t next = tile + gridDim.x;
     if (tid == 0 && next < nfull) {  // prefetch into the other buffer
@@ -311,7 +314,6 @@ __global__ void __launch_bounds__(LV_THREADS)
     }
     T* const tb = cur ? buf1 : buf0;
     const uint64_t tile_base = tile * S::TILE;
-    const uint32_t nvalid = (uint32_t)min((uint64_t)S::TILE, n - tile_base);
     if (tile < nfull) {
       if (cur) {
         mbar_wait(&mbar[1], phase1, err);
@@ -321,110 +323,124 @@ __global__ void __launch_bounds__(LV_THREADS)
         phase0 ^= 1;
       }
     } else {
-      for (uint32_t k = tid; k < S::TILE; k += LV_THREADS) tb[k] = k < nvalid ? src[tile_base + k] : T(0);
+      const uint32_t nv = (uint32_t)min((uint64_t)S::TILE, n - tile_base);
+      for (uint32_t k = tid; k < S::TILE; k += LV_THREADS) tb[k] = k < nv ? src[tile_base + k] : T(0);
       __syncthreads();
     }
-    const uint32_t wofs = warp * (S::ROWS * 32);
 
-    // 1. level bits, this warp's zero count, next-level node zero counts
-    uint32_t wz = 0;
-    Slot2 nodes;
-#pragma unroll 4
-    for (int r = 0; r < S::ROWS; ++r) {
-      const uint32_t k = wofs + r * 32 + lane;
-      const bool valid = k < nvalid;
-      const uint64_t x = (uint64_t)tb[k];
-      const bool one = valid && ((x >> shift) & 1);
-      const uint32_t ones = __ballot_sync(0xffffffffu, one);
-      const uint32_t zeros = __ballot_sync(0xffffffffu, valid && !one);
-      if (lane == 0) s_bits[warp * S::ROWS + r] = ones;
-      wz += __popc(zeros);
-      if (EMIT_NODES) {
-        const uint32_t p = level ? ((uint32_t)(x >> (L - level)) & pmask) : 0u;
-        const bool zn = valid && !((x >> (shift - 1)) & 1);
-        slot2_count(nodes, zn, 2 * p + (one ? 1u : 0u), znext, lane);
+    const uint64_t cbase = tile_base + (uint64_t)warp * CHUNK;
+    if (cbase < n) {
+      const uint32_t cvalid = (uint32_t)min((uint64_t)CHUNK, n - cbase);
+      const T* const wt = tb + warp * CHUNK;
+      const uint32_t i0 = (uint32_t)cbase;
+      uint32_t z = SCATTER ? chunkpre[cbase >> LOG_CHUNK] : 0u;  // level-wide zeros before the chunk
+      bool uniform = true;
+      uint32_t p0 = 0;
+      uint2 b = make_uint2(0, 0);
+      if (SCATTER && level) {
+        p0 = (uint32_t)((uint64_t)wt[0] >> pshift) & pmask;
+        const uint32_t pl = (uint32_t)((uint64_t)wt[cvalid - 1] >> pshift) & pmask;
+        uniform = p0 == pl;  // the level order is sorted by node
       }
-    }
-    if (EMIT_NODES) slot2_flush(nodes, znext, lane);
-    if (lane == 0) s_wz[warp] = wz;
-    __syncthreads();
+      if (SCATTER && uniform) {
+        if (p0 != cache_p) {
+          cache_p = p0;
+          cache_b = base_lvl[p0];
+        }
+        b = cache_b;
+      }
+      // uniform chunk: the zero run starts in dst chunk key0, the one run in key1
+      const uint32_t key0 = (b.x + z) >> LOG_CHUNK;
+      const uint32_t key1 = (b.y + (i0 - z)) >> LOG_CHUNK;
+      uint32_t t0 = 0, t1 = 0, a0 = 0, a1 = 0;
+      Slot2 tiles_s, nodes_s;
+      uint32_t myword = 0;
+#pragma unroll
+      for (int r = 0; r < WROWS; ++r) {
+        const uint32_t k = r * 32 + lane;
+        const bool valid = k < cvalid;
+        const T x = wt[k];
+        const bool one = valid && (((uint64_t)x >> shift) & 1);
+        const uint32_t om = __ballot_sync(0xffffffffu, one);
+        if (lane == (uint32_t)r) myword = om;
+        if (SCATTER) {
+          const uint32_t zm = __ballot_sync(0xffffffffu, valid && !one);
+          const uint32_t zb = z + __popc(zm & ltmask);
+          z += __popc(zm);
+          const uint32_t i = i0 + k;
+          uint32_t d;
+          if (uniform) {
+            d = one ? b.y + (i - zb) : b.x + zb;
+          } else {
+            const uint32_t p = (uint32_t)((uint64_t)x >> pshift) & pmask;
+            const uint2 bb = base_lvl[p];
+            d = one ? bb.y + (i - zb) : bb.x + zb;
+          }
+          const bool ok = valid && d < n;
+          if (ok) dst[d] = x;
+          else if (valid) atomicCAS(err, 0u, (uint32_t)DERR_BAD_INDEX);
+          if (EMIT_TILES) {
+            const bool nb0 = ok && !(((uint64_t)x >> (shift - 1)) & 1);
+            if (uniform) {
+              const uint32_t nbm = __ballot_sync(0xffffffffu, nb0);
+              t0 += __popc(zm & nbm);
+              t1 += __popc(om & nbm);
+              const uint32_t key = d >> LOG_CHUNK;
+              a0 += __popc(__ballot_sync(0xffffffffu, nb0 && !one && key == key0));
+              a1 += __popc(__ballot_sync(0xffffffffu, nb0 && one && key == key1));
+            } else {
+              slot2_count(tiles_s, nb0, d >> LOG_CHUNK, chunkcnt_next, lane);
+              if (EMIT_NODES) {
+                const uint32_t p = (uint32_t)((uint64_t)x >> pshift) & pmask;
+                slot2_count(nodes_s, nb0, 2 * p + (one ? 1u : 0u), znext, lane);
+              }
+            }
+          }
+        }
+      }
+      if (EMIT_TILES) {
+        if (uniform) {
+          if (lane == 0) {
+            if (a0) atomicAdd(&chunkcnt_next[key0], a0);
+            if (t0 - a0) atomicAdd(&chunkcnt_next[key0 + 1], t0 - a0);
+            if (a1) atomicAdd(&chunkcnt_next[key1], a1);
+            if (t1 - a1) atomicAdd(&chunkcnt_next[key1 + 1], t1 - a1);
+          }
+          if (EMIT_NODES) {
+            if (p0 != run_p) {
+              if (lane == 0) emit_flush(znext, run_p, run_e, run_o);
+              run_p = p0;
+              run_e = run_o = 0;
+            }
+            run_e += t0;
+            run_o += t1;
+          }
+        } else {
+          slot2_flush(tiles_s, chunkcnt_next, lane);
+          if (EMIT_NODES) slot2_flush(nodes_s, znext, lane);
+        }
+      }
 
-    // 2. store the bits: tile word j covers global bits [g + 32 j, g + 32 j + 32)
-    {
-      const uint64_t g = bit_off + tile_base;
+      // the chunk's bits: word j covers global bits [g + 32 j, g + 32 j + 32)
+      const uint64_t g = bit_off + cbase;
       const uint32_t g0 = (uint32_t)(g & 31);
       const uint64_t G = g >> 5;
-      for (int j = tid; j <= S::NW; j += LV_THREADS) {
-        if (g0 == 0 && j == S::NW) break;
-        const uint32_t curw = j < S::NW ? s_bits[j] : 0u;
-        const uint32_t prev = j > 0 ? s_bits[j - 1] : 0u;
-        const uint32_t val = g0 ? ((curw << g0) | (prev >> (32 - g0))) : curw;
-        const uint64_t wlo = (G + j) * 32;
-        if (wlo >= g + nvalid) continue;
-        const bool full = (wlo >= g) && (wlo + 32 <= g + nvalid);
-        if (full) bits32[G + j] = val;
-        else if (val) atomicOr(&bits32[G + j], val);
-      }
-    }
-
-    if (SCATTER) {
-      // 3. local stable partition: zeros of the tile first, then its ones
-      uint32_t zt = 0, zl = 0;
-#pragma unroll
-      for (uint32_t w = 0; w < LV_THREADS / 32; ++w) {
-        const uint32_t c = s_wz[w];
-        zl += w < warp ? c : 0u;
-        zt += c;
-      }
-#pragma unroll 4
-      for (int r = 0; r < S::ROWS; ++r) {
-        const uint32_t k = wofs + r * 32 + lane;
-        const bool valid = k < nvalid;
-        const T x = tb[k];
-        const bool one = valid && (((uint64_t)x >> shift) & 1);
-        const uint32_t zm = __ballot_sync(0xffffffffu, valid && !one);
-        const uint32_t zb = zl + __popc(zm & ltmask);
-        zl += __popc(zm);
-        if (valid) stage[one ? zt + (k - zb) : zb] = x;
-      }
-      __syncthreads();
-
-      // 4. store the runs: slot j < zt is the tile's j-th zero, slot j >= zt
-      //    its (j - zt)-th one; consecutive slots of a node go to consecutive
-      //    destinations
-      const uint32_t zpre = tilepre[tile];
-      const uint32_t opre = (uint32_t)tile_base - zpre;
-      Slot2 tiles;
-      for (uint32_t j0 = warp * 32; j0 < nvalid; j0 += LV_THREADS) {
-        const uint32_t j = j0 + lane;
-        const bool valid = j < nvalid;
-        const T x = stage[valid ? j : j0];
-        const uint32_t p = level ? ((uint32_t)((uint64_t)x >> (L - level)) & pmask) : 0u;
-        const uint32_t p0 = __shfl_sync(0xffffffffu, p, 0);
-        uint2 b;
-        if (__ballot_sync(0xffffffffu, valid && p != p0) == 0) {
-          if (p0 != cache_p) {
-            cache_p = p0;
-            cache_b = base_lvl[p0];
-          }
-          b = cache_b;
-        } else {
-          b = base_lvl[p];
-        }
-        const uint32_t d = j >= zt ? b.y + opre + (j - zt) : b.x + zpre + j;
-        const bool ok = valid && d < n;
-        if (ok) dst[d] = x;
-        else if (valid) atomicCAS(err, 0u, (uint32_t)DERR_BAD_INDEX);
-        if (EMIT_TILES) {
-          const bool pend = ok && !(((uint64_t)x >> (shift - 1)) & 1);
-          slot2_count(tiles, pend, d >> S::LOG_TILE, tilecnt_next, lane);
+      const uint32_t prev = __shfl_up_sync(0xffffffffu, myword, 1);
+      if (lane <= (uint32_t)WROWS && !(g0 == 0 && lane == (uint32_t)WROWS)) {
+        const uint32_t curw = lane < (uint32_t)WROWS ? myword : 0u;
+        const uint32_t val = g0 ? ((curw << g0) | ((lane ? prev : 0u) >> (32 - g0))) : curw;
+        const uint64_t wlo = (G + lane) * 32;
+        if (wlo < g + cvalid) {
+          const bool full = (wlo >= g) && (wlo + 32 <= g + cvalid);
+          if (full) bits32[G + lane] = val;
+          else if (val) atomicOr(&bits32[G + lane], val);
         }
       }
-      if (EMIT_TILES) slot2_flush(tiles, tilecnt_next, lane);
     }
     __syncthreads();
     cur ^= 1;
   }
+  if (EMIT_NODES && lane == 0) emit_flush(znext, run_p, run_e, run_o);
 }
 
 // ------------------------------------------------------------------ host
@@ -454,9 +470,9 @@ static int level_grid(uint64_t n) {
     cudaFuncSetAttribute(level_kernel<T, SC, EN, ET>, cudaFuncAttributePreferredSharedMemoryCarveout,
                          (int)cudaSharedmemCarveoutMaxShared);
     cudaFuncSetAttribute(level_kernel<T, SC, EN, ET>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)(3 * LvShape<T>::BYTES));
+                         (int)(2 * LvShape<T>::BYTES));
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, level_kernel<T, SC, EN, ET>, LV_THREADS,
-                                                  3 * LvShape<T>::BYTES);
+                                                  2 * LvShape<T>::BYTES);
     if (per_sm <= 0) per_sm = 1;
   }
   const uint64_t tiles = (n + LvShape<T>::TILE - 1) / LvShape<T>::TILE;
@@ -469,7 +485,7 @@ static void launch_level(const void* src, void* dst, uint64_t n, int L, int leve
                          uint32_t* znext, uint32_t* err, bool scatter, bool emit_nodes, bool emit_tiles,
                          cudaStream_t st) {
   const int bulk_ok = ((uintptr_t)src % 16) == 0;
-  const size_t shm = 3 * LvShape<T>::BYTES;
+  const size_t shm = 2 * LvShape<T>::BYTES;
 #define WTG_LV(SC, EN, ET)                                                                                \
   level_kernel<T, SC, EN, ET><<<level_grid<T, SC, EN, ET>(n), LV_THREADS, shm, st>>>(                    \
       (const T*)src, (T*)dst, n, L, level, base_lvl, bits32, bit_off, tilepre, tilecnt_next, znext, err, \
@@ -498,7 +514,7 @@ static void launch_prepass(const void* s, uint64_t n, int L, int K, uint32_t* ti
     default: fn<uint64_t>(__VA_ARGS__); break;          \
   }
 
-static uint64_t tile_elems(int eb) { return 16384 / eb; }
+static uint64_t tile_elems(int) { return CHUNK; }  // counts are kept per 512-symbol chunk
 
 int tree_levels_from_max(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int* levels) {
   cudaStream_t s = t.stream;
