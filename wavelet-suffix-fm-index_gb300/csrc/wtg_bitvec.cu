@@ -26,18 +26,6 @@ namespace wtg {
 constexpr int BV_THREADS = 256;  // one 512-bit superblock per thread
 constexpr int BV_SB_PER_TILE = BV_THREADS;
 
-enum {
-  INF_M1 = 0,   // number of ones
-  INF_M0,       // number of zeros
-  INF_LAST1,    // position of the last one + 1
-  INF_LAST0,    // position of the last zero + 1
-  INF_NLONG1,   // long superblocks of select1
-  INF_NLONG0,
-  INF_POOL1,    // pool words of select1
-  INF_POOL0,
-  INF_N = 16
-};
-
 __device__ __forceinline__ uint64_t warp_max_u64(uint64_t v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -45,17 +33,6 @@ __device__ __forceinline__ uint64_t warp_max_u64(uint64_t v) {
     v = t > v ? t : v;
   }
   return v;
-}
-
-// records the sample / superblock-end positions of args [K, K+c) that sit in
-// word wi (x = the word's arg mask)
-__device__ __forceinline__ void select_marks(uint64_t x, uint32_t c, uint64_t K, uint64_t wi,
-                                             uint64_t* __restrict__ samp, int64_t samp_dir,
-                                             uint64_t* __restrict__ ends) {
-  uint64_t q = (K + 63) & ~63ull;  // next multiple of 64
-  if (q < K + c) samp[samp_dir * (int64_t)(q >> 6)] = (wi << 6) + sel64(x, (uint32_t)(q - K + 1));
-  uint64_t e = K | 4095ull;  // next index with e % 4096 == 4095
-  if (e < K + c) ends[e >> 12] = (wi << 6) + sel64(x, (uint32_t)(e - K + 1));
 }
 
 __global__ void __launch_bounds__(BV_THREADS)
@@ -334,8 +311,19 @@ void bv_release(BvSupport& bv, cudaStream_t s) {
   }
 }
 
-int bv_build(BvSupport& bv, const uint64_t* d_words, uint64_t size, uint32_t flags, uint32_t* d_err,
-             cudaStream_t s) {
+__global__ void fused_totals_kernel(const uint64_t* zeros_total, uint64_t size, uint64_t NB, uint64_t* rank,
+                                    unsigned long long* info) {
+  const uint64_t z = *zeros_total;
+  info[INF_M1] = size - z;
+  info[INF_M0] = z;
+  if (rank) {  // the pair after the last superblock: (total, 0), rank_support_v_par.hpp:95-110
+    rank[2 * NB] = size - z;
+    rank[2 * NB + 1] = 0;
+  }
+}
+
+int bv_prepare(BvSupport& bv, const uint64_t* d_words, uint64_t size, uint32_t& flags, cudaStream_t s,
+               FuseOut* out) {
   int rc;
   // select's long blocks are filled through the rank table, so it is built
   // whenever a select support is
@@ -347,9 +335,6 @@ int bv_build(BvSupport& bv, const uint64_t* d_words, uint64_t size, uint32_t fla
   const uint64_t NB = W >> 3;
   const uint64_t nsb_cap = size / 4096 + 2;
   const uint64_t samp_n = W + 2;
-  const uint32_t logn = logn_of(size);
-  const uint64_t logn4 = (uint64_t)(uint32_t)(logn * logn * logn * logn);  // uint32 as in initData
-
   if ((rc = bv.info.ensure(INF_N * sizeof(uint64_t), s))) return rc;
   WTG_CK(cudaMemsetAsync(bv.info.p, 0, INF_N * sizeof(uint64_t), s));
   if (flags & WTG_RANK)
@@ -364,22 +349,61 @@ int bv_build(BvSupport& bv, const uint64_t* d_words, uint64_t size, uint32_t fla
     if ((rc = sd.sizes.ensure(2 * nsb_cap * sizeof(uint64_t), s))) return rc;  // [sizes | offsets]
     if ((rc = sd.long_list.ensure(nsb_cap * sizeof(uint64_t), s))) return rc;
   }
+  if (out) {
+    out->rank = (flags & WTG_RANK) ? bv.rank.as<uint64_t>() : nullptr;
+    out->samples = bv.samples.as<uint64_t>();
+    out->samp_last = samp_n - 1;
+    out->ends1 = (flags & WTG_SELECT1) ? bv.sel[1].ends.as<uint64_t>() : nullptr;
+    out->ends0 = (flags & WTG_SELECT0) ? bv.sel[0].ends.as<uint64_t>() : nullptr;
+    out->info = bv.info.as<unsigned long long>();
+    out->flags = flags;
+  }
+  return WTG_OK;
+}
+
+int bv_fused_totals(BvSupport& bv, const uint64_t* zeros_total, cudaStream_t s) {
+  const uint64_t NB = ((bv.size + 63) / 64) >> 3;
+  fused_totals_kernel<<<1, 1, 0, s>>>(zeros_total, bv.size, NB, (bv.flags & WTG_RANK) ? bv.rank.as<uint64_t>() : nullptr,
+                                      bv.info.as<unsigned long long>());
+  count_launch();
+  WTG_CK(cudaGetLastError());
+  return WTG_OK;
+}
+
+int bv_pass(BvSupport& bv, uint32_t* d_err, cudaStream_t s) {
+  int rc;
+  const uint64_t size = bv.size;
+  const uint64_t W = (size + 63) / 64;
+  const uint64_t NB = W >> 3;
+  const uint64_t samp_n = W + 2;
   const uint64_t tiles = (NB + 1 + BV_SB_PER_TILE - 1) / BV_SB_PER_TILE;
   if (tiles > 0x7fffffffull) return fail(WTG_ERR_INVALID, "bitvector too large");
   if ((rc = bv.status.ensure((tiles + 1) * sizeof(uint64_t), s))) return rc;
   WTG_CK(cudaMemsetAsync(bv.status.p, 0, (tiles + 1) * sizeof(uint64_t), s));
-
-  unsigned long long* info = bv.info.as<unsigned long long>();
-  uint64_t* samples = bv.samples.as<uint64_t>();
   prof_begin(PROF_BVPASS, s);
   bv_pass_kernel<<<(unsigned)tiles, BV_THREADS, 0, s>>>(
-      d_words, size, W, NB, flags, bv.rank.as<uint64_t>(), samples, samp_n - 1, bv.sel[1].ends.as<uint64_t>(),
-      bv.sel[0].ends.as<uint64_t>(), info, bv.status.as<uint64_t>() + 1, bv.status.as<uint32_t>(), d_err);
+      bv.words, size, W, NB, bv.flags, bv.rank.as<uint64_t>(), bv.samples.as<uint64_t>(), samp_n - 1,
+      bv.sel[1].ends.as<uint64_t>(), bv.sel[0].ends.as<uint64_t>(), bv.info.as<unsigned long long>(),
+      bv.status.as<uint64_t>() + 1, bv.status.as<uint32_t>(), d_err);
   prof_end(PROF_BVPASS, s);
   count_launch();
   WTG_CK(cudaGetLastError());
+  return WTG_OK;
+}
 
+int bv_finish(BvSupport& bv, uint32_t* d_err, cudaStream_t s) {
+  int rc;
+  const uint32_t flags = bv.flags;
   if (!(flags & (WTG_SELECT1 | WTG_SELECT0))) return WTG_OK;
+  const uint64_t size = bv.size;
+  const uint64_t W = (size + 63) / 64;
+  const uint64_t nsb_cap = size / 4096 + 2;
+  const uint64_t samp_n = W + 2;
+  const uint32_t logn = logn_of(size);
+  const uint64_t logn4 = (uint64_t)(uint32_t)(logn * logn * logn * logn);  // uint32 as in initData
+  const uint64_t* d_words = bv.words;
+  unsigned long long* info = bv.info.as<unsigned long long>();
+  uint64_t* samples = bv.samples.as<uint64_t>();
 
   for (int t_b = 0; t_b < 2; ++t_b) {
     if (!(flags & (t_b ? WTG_SELECT1 : WTG_SELECT0))) continue;
@@ -423,9 +447,8 @@ int bv_build(BvSupport& bv, const uint64_t* d_words, uint64_t size, uint32_t fla
     if (sd.nsb == 0) continue;
     uint64_t* descw = sd.desc.as<uint64_t>() + nsb_cap;
     uint64_t* offs = sd.sizes.as<uint64_t>() + nsb_cap;
-    const uint64_t warps = sd.nsb;
     prof_begin(PROF_SELECT, s);
-    select_mini_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(
+    select_mini_kernel<<<(unsigned)((sd.nsb * 32 + 255) / 256), 256, 0, s>>>(
         t_b, sd.nsb, m, samples, samp_n - 1, descw, offs, sd.desc.as<uint64_t>(), sd.pool.as<uint64_t>());
     prof_end(PROF_SELECT, s);
     count_launch();
@@ -457,6 +480,14 @@ int bv_build(BvSupport& bv, const uint64_t* d_words, uint64_t size, uint32_t fla
     }
   }
   return WTG_OK;
+}
+
+int bv_build(BvSupport& bv, const uint64_t* d_words, uint64_t size, uint32_t flags, uint32_t* d_err,
+             cudaStream_t s) {
+  int rc;
+  if ((rc = bv_prepare(bv, d_words, size, flags, s, nullptr))) return rc;
+  if ((rc = bv_pass(bv, d_err, s))) return rc;
+  return bv_finish(bv, d_err, s);
 }
 
 }  // namespace wtg

@@ -31,6 +31,7 @@
 // table (WT.C:110,156-159,234-257) follows from the per-node starts and zero
 // counts alone.
 #include <algorithm>
+#include <type_traits>
 
 #include "wtg_internal.cuh"
 #include "wtg_tree.cuh"
@@ -51,49 +52,69 @@ struct LvShape {
 };
 
 // ------------------------------------------------------------ pre-pass
-// One read of the input, tile by tile: the zero count of level 0 in every
-// tile (its bit levels-1), and the histogram of the top K <= 2 key bits,
-// both counted with warp ballots.
+// One read of the input: the zero count of level 0 (bit levels-1) in every
+// 512-symbol chunk, and the histogram of the top K <= 2 key bits.  A warp per
+// chunk, 16-byte coalesced loads, counts kept in registers.
 
 template <typename T>
 __global__ void __launch_bounds__(LV_THREADS) prepass_kernel(const T* __restrict__ s, uint64_t n, int L, int K,
-                                                             uint32_t* __restrict__ tilecnt,
+                                                             int vec_ok, uint32_t* __restrict__ chunkcnt,
                                                              uint32_t* __restrict__ hist) {
-  using S = LvShape<T>;
-  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const uint64_t ntiles = (n + S::TILE - 1) / S::TILE;
-  uint32_t h[4] = {0, 0, 0, 0};
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  const uint64_t nchunks = (n + CHUNK - 1) / CHUNK;
   const int top = L - 1;
-  for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const uint64_t base = tile * S::TILE + (uint64_t)warp * CHUNK;
-    uint32_t wz = 0;
-#pragma unroll 4
-    for (int r = 0; r < WROWS; ++r) {
-      const uint64_t i = base + r * 32 + lane;
-      const bool valid = i < n;
-      const uint64_t x = valid ? (uint64_t)s[i] : 0ull;
+  const int top2 = K > 1 ? L - 2 : 0;
+  uint32_t c1 = 0, c2 = 0, c12 = 0, cnt = 0;  // top bit set, second bit set, both, symbols
+  constexpr int PER = 16 / sizeof(T);
+  constexpr int NV = CHUNK * sizeof(T) / 16 / 32;  // 16-byte loads per lane and chunk
+  for (uint64_t c = gw; c < nchunks; c += nwarps) {
+    const uint64_t base = c * CHUNK;
+    const uint32_t cv = (uint32_t)min((uint64_t)CHUNK, n - base);
+    uint32_t ones = 0;
+    auto take = [&](uint64_t x) {
       const uint32_t b1 = (uint32_t)(x >> top) & 1u;
-      const uint32_t b2 = K > 1 ? (uint32_t)(x >> (top - 1)) & 1u : 0u;
-      const uint32_t vm = __ballot_sync(0xffffffffu, valid);
-      const uint32_t z = __ballot_sync(0xffffffffu, valid && !b1);       // top bits 0x
-      const uint32_t z01 = __ballot_sync(0xffffffffu, valid && !b1 && b2);  // 01
-      const uint32_t o11 = __ballot_sync(0xffffffffu, valid && b1 && b2);   // 11
-      wz += __popc(z);
-      h[0] += __popc(z) - __popc(z01);
-      h[1] += __popc(z01);
-      h[2] += __popc(vm) - __popc(z) - __popc(o11);
-      h[3] += __popc(o11);
-    }
-    if (lane == 0 && base < n) tilecnt[base >> LOG_CHUNK] = wz;  // zeros of this 512-symbol chunk
-  }
-  if (lane == 0) {
-    // bins of the top K bits (K = 1: bins 0/1 = top bit 0/1)
-    if (K > 1) {
-      for (int b = 0; b < 4; ++b)
-        if (h[b]) atomicAdd(&hist[b], h[b]);
+      const uint32_t b2 = K > 1 ? (uint32_t)(x >> top2) & 1u : 0u;
+      ones += b1;
+      c2 += b2;
+      c12 += b1 & b2;
+    };
+    if (vec_ok && cv == CHUNK) {
+      const uint4* q = (const uint4*)(s + base);
+#pragma unroll
+      for (int j = 0; j < NV; ++j) {
+        uint4 v = __ldg(&q[j * 32 + lane]);
+        const T* e = (const T*)&v;
+#pragma unroll
+        for (int k = 0; k < PER; ++k) take((uint64_t)e[k]);
+      }
+      cnt += CHUNK / 32;
     } else {
-      if (h[0] + h[1]) atomicAdd(&hist[0], h[0] + h[1]);
-      if (h[2] + h[3]) atomicAdd(&hist[1], h[2] + h[3]);
+      for (uint32_t k = lane; k < cv; k += 32) {
+        take((uint64_t)s[base + k]);
+        ++cnt;
+      }
+    }
+    c1 += ones;
+    uint32_t wz = ones;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) wz += __shfl_xor_sync(0xffffffffu, wz, o);
+    if (lane == 0) chunkcnt[c] = cv - wz;  // zeros of level 0 in this chunk
+  }
+  // bins of the top K bits (K = 1: bins 0/1 = top bit 0/1)
+  uint32_t h[4] = {cnt - c1 - c2 + c12, c2 - c12, c1 - c12, c12};
+#pragma unroll
+  for (int b2 = 0; b2 < 4; ++b2)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) h[b2] += __shfl_xor_sync(0xffffffffu, h[b2], o);
+  if (lane == 0) {
+    if (K > 1) {
+      for (int b2 = 0; b2 < 4; ++b2)
+        if (h[b2]) atomicAdd(&hist[b2], h[b2]);
+    } else {
+      if (h[0]) atomicAdd(&hist[0], h[0]);
+      if (h[2]) atomicAdd(&hist[1], h[2]);
     }
   }
 }
@@ -213,6 +234,15 @@ __global__ void node_kernel(const uint32_t* __restrict__ C, const uint32_t* __re
 // registers and added to `target` (one atomic) when a key is evicted.  Keys
 // of a row arrive sorted by node or by destination, so two entries catch
 // almost every repeat.
+__device__ __forceinline__ uint64_t warp_max64(uint64_t v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const uint64_t t = __shfl_xor_sync(0xffffffffu, v, o);
+    v = t > v ? t : v;
+  }
+  return v;
+}
+
 struct Slot2 {
   uint32_t ka = 0xFFFFFFFFu, ca = 0, kb = 0xFFFFFFFFu, cb = 0;
 };
@@ -253,6 +283,49 @@ __device__ __forceinline__ void slot2_flush(Slot2& s, uint32_t* __restrict__ tar
   s = Slot2();
 }
 
+// FUSE: the chunk is one 512-bit rank superblock of the concatenated
+// bitvector (n % 512 == 0).  Lanes 0..7 hold its eight 64-bit words and write
+// the rank pair (rank_support_v_par.hpp:95-113: absolute count before the
+// superblock, seven cumulative 9-bit block counts) and the select samples of
+// their word (every 64th one / zero and the superblock ends).
+__device__ __forceinline__ void fuse_chunk(const FuseOut& f, uint64_t bitpos, uint64_t zeros_before,
+                                           uint32_t myword, uint32_t lane, uint64_t& last1, uint64_t& last0) {
+  const uint64_t ones_before = bitpos - zeros_before;
+  const uint32_t lo = __shfl_sync(0xffffffffu, myword, (2 * lane) & 15);
+  const uint32_t hi = __shfl_sync(0xffffffffu, myword, (2 * lane + 1) & 15);
+  const uint64_t w = (uint64_t)lo | ((uint64_t)hi << 32);
+  const uint32_t c = lane < 8 ? (uint32_t)__popcll(w) : 0u;
+  uint32_t inc = c;
+#pragma unroll
+  for (int o = 1; o < 8; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+    if ((lane & 7) >= (uint32_t)o) inc += t;
+  }
+  const uint32_t pre = inc - c;  // ones in the words before this lane's word
+  if (f.rank) {
+    uint64_t part = (lane >= 1 && lane < 8) ? ((uint64_t)pre << (63 - 9 * lane)) : 0ull;
+#pragma unroll
+    for (int o = 1; o < 8; o <<= 1) part |= __shfl_xor_sync(0xffffffffu, part, o);
+    if (lane == 0) {
+      const uint64_t b = bitpos >> 9;
+      f.rank[2 * b] = ones_before;
+      f.rank[2 * b + 1] = part;
+    }
+  }
+  if (lane < 8) {
+    const uint64_t wi = (bitpos >> 6) + lane;
+    if (f.ends1 && c) {
+      select_marks(w, c, ones_before + pre, wi, f.samples, 1, f.ends1);
+      last1 = max(last1, (wi << 6) + hi64(w) + 1);
+    }
+    if (f.ends0 && c < 64) {
+      const uint64_t zw = ~w;
+      select_marks(zw, 64 - c, zeros_before + 64 * lane - pre, wi, f.samples + f.samp_last, -1, f.ends0);
+      last0 = max(last0, (wi << 6) + hi64(zw) + 1);
+    }
+  }
+}
+
 // One level over the level-l order in src.  Each warp owns independent
 // 512-symbol chunks; its zeros-before come from chunkpre (the scan of the
 // counts the previous pass emitted), so warps and CTAs never wait on each
@@ -271,12 +344,14 @@ __device__ __forceinline__ void slot2_flush(Slot2& s, uint32_t* __restrict__ tar
 // atomics per chunk.  Chunks that straddle nodes take a general path.
 // Tiles of 8 chunks arrive by cp.async.bulk into a double buffer; CTAs are
 // persistent (tile = blockIdx.x + k * gridDim.x).
-template <typename T, bool SCATTER, bool EMIT_NODES, bool EMIT_TILES>
-__global__ void __launch_bounds__(LV_THREADS)
+template <typename T, bool SCATTER, bool EMIT_NODES, bool EMIT_TILES, bool FUSE>
+__global__ void __launch_bounds__(LV_THREADS, 4)
     level_kernel(const T* __restrict__ src, T* __restrict__ dst, uint64_t n, int L, int level,
                  const uint2* __restrict__ base_lvl, uint32_t* __restrict__ bits32, uint64_t bit_off,
-                 const uint32_t* __restrict__ chunkpre, uint32_t* __restrict__ chunkcnt_next,
-                 uint32_t* __restrict__ znext, uint32_t* err, int bulk_ok) {
+                 const uint32_t* __restrict__ chunkpre, const uint32_t* __restrict__ chunkcnt,
+                 uint32_t* __restrict__ chunkcnt_next, uint32_t* __restrict__ znext, uint32_t* err, int bulk_ok,
+                 FuseOut fuse) {
+  constexpr bool NEED_Z = SCATTER || FUSE;
   using S = LvShape<T>;
   extern __shared__ __align__(128) unsigned char lv_smem[];
   __shared__ __align__(8) uint64_t mbar[2];
@@ -289,6 +364,14 @@ __global__ void __launch_bounds__(LV_THREADS)
   const int pshift = L - level;
   const uint32_t pmask = level ? (uint32_t)((1ull << level) - 1) : 0u;
   const uint32_t ltmask = lanemask_lt();
+  uint64_t lvl_zeros = 0, last1 = 0, last0 = 0;  // FUSE: zeros of the levels before this one
+  if (FUSE) {
+    lvl_zeros = fuse.lvl_zb[level];
+    if (blockIdx.x == 0 && tid == 0) {  // zeros through this level, for the next pass
+      const uint64_t nch = (n + CHUNK - 1) / CHUNK;
+      fuse.lvl_zb[level + 1] = lvl_zeros + chunkpre[nch - 1] + chunkcnt[nch - 1];
+    }
+  }
 
   if (tid == 0) {
     mbar_init(&mbar[0], 1);
@@ -333,7 +416,8 @@ __global__ void __launch_bounds__(LV_THREADS)
       const uint32_t cvalid = (uint32_t)min((uint64_t)CHUNK, n - cbase);
       const T* const wt = tb + warp * CHUNK;
       const uint32_t i0 = (uint32_t)cbase;
-      uint32_t z = SCATTER ? chunkpre[cbase >> LOG_CHUNK] : 0u;  // level-wide zeros before the chunk
+      uint32_t z = NEED_Z ? chunkpre[cbase >> LOG_CHUNK] : 0u;  // level-wide zeros before the chunk
+      const uint32_t z_chunk = z;
       bool uniform = true;
       uint32_t p0 = 0;
       uint2 b = make_uint2(0, 0);
@@ -355,49 +439,65 @@ __global__ void __launch_bounds__(LV_THREADS)
       uint32_t t0 = 0, t1 = 0, a0 = 0, a1 = 0;
       Slot2 tiles_s, nodes_s;
       uint32_t myword = 0;
+      // FULL: all 512 symbols valid (every chunk but the last)
+      auto rows = [&](auto full_tag) {
+        constexpr bool FULL = decltype(full_tag)::value;
 #pragma unroll
-      for (int r = 0; r < WROWS; ++r) {
-        const uint32_t k = r * 32 + lane;
-        const bool valid = k < cvalid;
-        const T x = wt[k];
-        const bool one = valid && (((uint64_t)x >> shift) & 1);
-        const uint32_t om = __ballot_sync(0xffffffffu, one);
-        if (lane == (uint32_t)r) myword = om;
-        if (SCATTER) {
-          const uint32_t zm = __ballot_sync(0xffffffffu, valid && !one);
-          const uint32_t zb = z + __popc(zm & ltmask);
-          z += __popc(zm);
-          const uint32_t i = i0 + k;
-          uint32_t d;
-          if (uniform) {
-            d = one ? b.y + (i - zb) : b.x + zb;
-          } else {
-            const uint32_t p = (uint32_t)((uint64_t)x >> pshift) & pmask;
-            const uint2 bb = base_lvl[p];
+        for (int r = 0; r < WROWS; ++r) {
+          const uint32_t k = r * 32 + lane;
+          const bool valid = FULL || k < cvalid;
+          const T x = wt[k];
+          const bool one = valid && (((uint64_t)x >> shift) & 1);
+          const uint32_t om = __ballot_sync(0xffffffffu, one);
+          if (lane == (uint32_t)r) myword = om;
+          if (FUSE && !SCATTER) z += FULL ? 32u - __popc(om) : __popc(__ballot_sync(0xffffffffu, valid && !one));
+          if (SCATTER) {
+            const uint32_t zm = FULL ? ~om : __ballot_sync(0xffffffffu, valid && !one);
+            const uint32_t zb = z + __popc(zm & ltmask);
+            z += __popc(zm);
+            const uint32_t i = i0 + k;
+            uint32_t d;
+            bool row_uniform = uniform;
+            uint2 bb = b;
+            uint32_t p = p0;
+            if (!uniform) {
+              // straddling chunk: most rows still lie in one node
+              p = (uint32_t)((uint64_t)x >> pshift) & pmask;
+              const uint32_t plo = __shfl_sync(0xffffffffu, p, 0);
+              row_uniform = __ballot_sync(0xffffffffu, valid && p != plo) == 0;
+              if (row_uniform) {
+                if (plo != cache_p) {
+                  cache_p = plo;
+                  cache_b = base_lvl[plo];
+                }
+                bb = cache_b;
+              } else {
+                bb = base_lvl[p];
+              }
+            }
             d = one ? bb.y + (i - zb) : bb.x + zb;
-          }
-          const bool ok = valid && d < n;
-          if (ok) dst[d] = x;
-          else if (valid) atomicCAS(err, 0u, (uint32_t)DERR_BAD_INDEX);
-          if (EMIT_TILES) {
-            const bool nb0 = ok && !(((uint64_t)x >> (shift - 1)) & 1);
-            if (uniform) {
-              const uint32_t nbm = __ballot_sync(0xffffffffu, nb0);
-              t0 += __popc(zm & nbm);
-              t1 += __popc(om & nbm);
-              const uint32_t key = d >> LOG_CHUNK;
-              a0 += __popc(__ballot_sync(0xffffffffu, nb0 && !one && key == key0));
-              a1 += __popc(__ballot_sync(0xffffffffu, nb0 && one && key == key1));
-            } else {
-              slot2_count(tiles_s, nb0, d >> LOG_CHUNK, chunkcnt_next, lane);
-              if (EMIT_NODES) {
-                const uint32_t p = (uint32_t)((uint64_t)x >> pshift) & pmask;
-                slot2_count(nodes_s, nb0, 2 * p + (one ? 1u : 0u), znext, lane);
+            const bool ok = valid && d < n;
+            if (ok) dst[d] = x;
+            else if (valid) atomicCAS(err, 0u, (uint32_t)DERR_BAD_INDEX);
+            if (EMIT_TILES) {
+              const bool nb0 = ok && !(((uint64_t)x >> (shift - 1)) & 1);
+              if (uniform) {
+                const uint32_t nbm = __ballot_sync(0xffffffffu, nb0);
+                t0 += __popc(zm & nbm);
+                t1 += __popc(om & nbm);
+                const uint32_t key = d >> LOG_CHUNK;
+                a0 += __popc(__ballot_sync(0xffffffffu, nb0 && !one && key == key0));
+                a1 += __popc(__ballot_sync(0xffffffffu, nb0 && one && key == key1));
+              } else {
+                slot2_count(tiles_s, nb0, d >> LOG_CHUNK, chunkcnt_next, lane);
+                if (EMIT_NODES) slot2_count(nodes_s, nb0, 2 * p + (one ? 1u : 0u), znext, lane);
               }
             }
           }
         }
-      }
+      };
+      if (cvalid == CHUNK) rows(std::true_type());
+      else rows(std::false_type());
       if (EMIT_TILES) {
         if (uniform) {
           if (lane == 0) {
@@ -436,9 +536,18 @@ __global__ void __launch_bounds__(LV_THREADS)
           else if (val) atomicOr(&bits32[G + lane], val);
         }
       }
+      if (FUSE) fuse_chunk(fuse, g, lvl_zeros + z_chunk, myword, lane, last1, last0);
     }
     __syncthreads();
     cur ^= 1;
+  }
+  if (FUSE) {
+    last1 = warp_max64(last1);
+    last0 = warp_max64(last0);
+    if (lane == 0) {
+      if (last1) atomicMax(&fuse.info[INF_LAST1], (unsigned long long)last1);
+      if (last0) atomicMax(&fuse.info[INF_LAST0], (unsigned long long)last0);
+    }
   }
   if (EMIT_NODES && lane == 0) emit_flush(znext, run_p, run_e, run_o);
 }
@@ -463,15 +572,15 @@ static void launch_max(const void* s, uint64_t n, unsigned long long* out, cudaS
   max_kernel<T><<<grid, 256, 0, st>>>((const T*)s, n, out);
 }
 
-template <typename T, bool SC, bool EN, bool ET>
+template <typename T, bool SC, bool EN, bool ET, bool FU>
 static int level_grid(uint64_t n) {
   static int per_sm = 0;
   if (!per_sm) {
-    cudaFuncSetAttribute(level_kernel<T, SC, EN, ET>, cudaFuncAttributePreferredSharedMemoryCarveout,
+    cudaFuncSetAttribute(level_kernel<T, SC, EN, ET, FU>, cudaFuncAttributePreferredSharedMemoryCarveout,
                          (int)cudaSharedmemCarveoutMaxShared);
-    cudaFuncSetAttribute(level_kernel<T, SC, EN, ET>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(level_kernel<T, SC, EN, ET, FU>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)(2 * LvShape<T>::BYTES));
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, level_kernel<T, SC, EN, ET>, LV_THREADS,
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, level_kernel<T, SC, EN, ET, FU>, LV_THREADS,
                                                   2 * LvShape<T>::BYTES);
     if (per_sm <= 0) per_sm = 1;
   }
@@ -479,31 +588,55 @@ static int level_grid(uint64_t n) {
   return (int)std::min<uint64_t>(tiles, (uint64_t)per_sm * sm_count());
 }
 
-template <typename T>
-static void launch_level(const void* src, void* dst, uint64_t n, int L, int level, const uint2* base_lvl,
-                         uint32_t* bits32, uint64_t bit_off, const uint32_t* tilepre, uint32_t* tilecnt_next,
-                         uint32_t* znext, uint32_t* err, bool scatter, bool emit_nodes, bool emit_tiles,
-                         cudaStream_t st) {
-  const int bulk_ok = ((uintptr_t)src % 16) == 0;
+struct LevelArgs {
+  const void* src;
+  void* dst;
+  uint64_t n;
+  int L, level;
+  const uint2* base_lvl;
+  uint32_t* bits32;
+  uint64_t bit_off;
+  const uint32_t* chunkpre;
+  const uint32_t* chunkcnt;
+  uint32_t* chunkcnt_next;
+  uint32_t* znext;
+  uint32_t* err;
+  bool scatter, emit_nodes, emit_tiles, fuse;
+  FuseOut fo;
+};
+
+template <typename T, bool SC, bool EN, bool ET, bool FU>
+static void launch_level_v(const LevelArgs& a, cudaStream_t st) {
+  const int bulk_ok = ((uintptr_t)a.src % 16) == 0;
   const size_t shm = 2 * LvShape<T>::BYTES;
-#define WTG_LV(SC, EN, ET)                                                                                \
-  level_kernel<T, SC, EN, ET><<<level_grid<T, SC, EN, ET>(n), LV_THREADS, shm, st>>>(                    \
-      (const T*)src, (T*)dst, n, L, level, base_lvl, bits32, bit_off, tilepre, tilecnt_next, znext, err, \
-      bulk_ok)
-  if (scatter && emit_nodes) WTG_LV(true, true, true);
-  else if (scatter && emit_tiles) WTG_LV(true, false, true);
-  else if (scatter) WTG_LV(true, false, false);
-  else WTG_LV(false, false, false);
-#undef WTG_LV
+  level_kernel<T, SC, EN, ET, FU><<<level_grid<T, SC, EN, ET, FU>(a.n), LV_THREADS, shm, st>>>(
+      (const T*)a.src, (T*)a.dst, a.n, a.L, a.level, a.base_lvl, a.bits32, a.bit_off, a.chunkpre, a.chunkcnt,
+      a.chunkcnt_next, a.znext, a.err, bulk_ok, a.fo);
+}
+
+template <typename T>
+static void launch_level(const LevelArgs& a, cudaStream_t st) {
+  if (a.fuse) {
+    if (a.scatter && a.emit_nodes) launch_level_v<T, true, true, true, true>(a, st);
+    else if (a.scatter && a.emit_tiles) launch_level_v<T, true, false, true, true>(a, st);
+    else if (a.scatter) launch_level_v<T, true, false, false, true>(a, st);
+    else launch_level_v<T, false, false, false, true>(a, st);
+  } else {
+    if (a.scatter && a.emit_nodes) launch_level_v<T, true, true, true, false>(a, st);
+    else if (a.scatter && a.emit_tiles) launch_level_v<T, true, false, true, false>(a, st);
+    else if (a.scatter) launch_level_v<T, true, false, false, false>(a, st);
+    else launch_level_v<T, false, false, false, false>(a, st);
+  }
 }
 
 template <typename T>
 static void launch_prepass(const void* s, uint64_t n, int L, int K, uint32_t* tilecnt, uint32_t* hist,
                            cudaStream_t st) {
-  const uint64_t tiles = (n + LvShape<T>::TILE - 1) / LvShape<T>::TILE;
-  unsigned grid = (unsigned)std::min<uint64_t>(tiles, (uint64_t)sm_count() * 8);
+  const uint64_t chunks = (n + CHUNK - 1) / CHUNK;
+  unsigned grid = (unsigned)std::min<uint64_t>((chunks + 7) / 8, (uint64_t)sm_count() * 8);
   if (grid == 0) grid = 1;
-  prepass_kernel<T><<<grid, LV_THREADS, 0, st>>>((const T*)s, n, L, K, tilecnt, hist);
+  const int vec_ok = ((uintptr_t)s % 16) == 0;
+  prepass_kernel<T><<<grid, LV_THREADS, 0, st>>>((const T*)s, n, L, K, vec_ok, tilecnt, hist);
 }
 
 #define WTG_DISPATCH(eb, fn, ...)                       \
@@ -601,8 +734,19 @@ int tree_build(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int L, uint32
     WTG_CK(cudaGetLastError());
   }
 
-  // level passes; each scattering pass feeds the next level's tile counts
-  // and (from level K on) its node tables
+  // level passes; each scattering pass feeds the next level's chunk counts
+  // and (from level K on) its node tables.  When n % 512 == 0 every chunk is
+  // one rank superblock and the passes also write the rank table and the
+  // select samples (fused); otherwise a separate pass over the bits does.
+  const bool fuse = flags && n > 0 && (n % CHUNK) == 0;
+  FuseOut fo{};
+  uint32_t bflags = flags;
+  if (fuse) {
+    if ((rc = bv_prepare(t.bv, t.bits.as<uint64_t>(), n * (uint64_t)L, bflags, s, &fo))) return rc;
+    if ((rc = t.scratch.ensure((L + 2) * sizeof(uint64_t), s))) return rc;
+    WTG_CK(cudaMemsetAsync(t.scratch.p, 0, (L + 2) * sizeof(uint64_t), s));
+    fo.lvl_zb = t.scratch.as<uint64_t>();
+  }
   if (n) {
     if (L > 1) {
       if ((rc = t.lvl[0].ensure(n * eb + 16, s))) return rc;
@@ -610,22 +754,33 @@ int tree_build(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int L, uint32
     }
     const void* src = d_seq;
     for (int l = 0; l < L; ++l) {
-      const bool scatter = l < L - 1;
-      const bool emit_tiles = l + 1 <= L - 2;
-      const bool emit_nodes = emit_tiles && (l + 1 >= K);
-      void* dst = scatter ? t.lvl[l & 1].p : nullptr;
-      if (scatter)
-        if ((rc = scan_exclusive_u32(tilecnt + (uint64_t)l * (tiles + 1), tilepre, tiles, t.scan_tmp, d_err, s)))
-          return rc;
-      uint32_t* znext = Z + ((1ull << (l + 1)) - 1);
-      uint32_t* tnext = tilecnt + (uint64_t)(l + 1) * (tiles + 1);
-      prof_begin(scatter ? PROF_LEVEL : PROF_LEVEL_LAST, s);
-      WTG_DISPATCH(eb, launch_level, src, dst, n, L, l, base + ((1ull << l) - 1), t.bits.as<uint32_t>(),
-                   (uint64_t)l * n, tilepre, tnext, znext, d_err, scatter, emit_nodes, emit_tiles, s);
-      prof_end(scatter ? PROF_LEVEL : PROF_LEVEL_LAST, s);
+      LevelArgs a{};
+      a.scatter = l < L - 1;
+      a.emit_tiles = (l + 1 <= L - 2) || (fuse && l + 1 == L - 1);
+      a.emit_nodes = (l + 1 <= L - 2) && (l + 1 >= K);
+      a.fuse = fuse;
+      a.src = src;
+      a.dst = a.scatter ? t.lvl[l & 1].p : nullptr;
+      a.n = n;
+      a.L = L;
+      a.level = l;
+      a.base_lvl = base + ((1ull << l) - 1);
+      a.bits32 = t.bits.as<uint32_t>();
+      a.bit_off = (uint64_t)l * n;
+      a.chunkcnt = tilecnt + (uint64_t)l * (tiles + 1);
+      a.chunkpre = tilepre;
+      a.chunkcnt_next = tilecnt + (uint64_t)(l + 1) * (tiles + 1);
+      a.znext = Z + ((1ull << (l + 1)) - 1);
+      a.err = d_err;
+      a.fo = fo;
+      if (a.scatter || fuse)
+        if ((rc = scan_exclusive_u32(a.chunkcnt, tilepre, tiles, t.scan_tmp, d_err, s))) return rc;
+      prof_begin(a.scatter ? PROF_LEVEL : PROF_LEVEL_LAST, s);
+      WTG_DISPATCH(eb, launch_level, a, s);
+      prof_end(a.scatter ? PROF_LEVEL : PROF_LEVEL_LAST, s);
       count_launch();
       WTG_CK(cudaGetLastError());
-      src = dst;
+      src = a.dst;
       const int m = l + 1;  // next level: derive its tables when the pre-pass did not
       if (m >= K && m <= L - 1) {
         const uint64_t cnt = 1ull << m;
@@ -643,7 +798,10 @@ int tree_build(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int L, uint32
   }
 
   // rank / select over the concatenated bitvector
-  if (flags) {
+  if (fuse) {
+    if ((rc = bv_fused_totals(t.bv, fo.lvl_zb + L, s))) return rc;
+    if ((rc = bv_finish(t.bv, d_err, s))) return rc;
+  } else if (flags) {
     if ((rc = bv_build(t.bv, t.bits.as<uint64_t>(), n * (uint64_t)L, flags, d_err, s))) return rc;
   }
   return WTG_OK;
