@@ -738,7 +738,11 @@ int tree_build(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int L, uint32
   // and (from level K on) its node tables.  When n % 512 == 0 every chunk is
   // one rank superblock and the passes also write the rank table and the
   // select samples (fused); otherwise a separate pass over the bits does.
-  const bool fuse = flags && n > 0 && (n % CHUNK) == 0;
+  // Fusion is kept available but off: measured on GB300, the per-chunk rank
+  // and select work slows every level pass by more than the separate pass
+  // over the bits costs.
+  constexpr bool kFuseRankSelect = false;
+  const bool fuse = kFuseRankSelect && flags && n > 0 && (n % CHUNK) == 0;
   FuseOut fo{};
   uint32_t bflags = flags;
   if (fuse) {
