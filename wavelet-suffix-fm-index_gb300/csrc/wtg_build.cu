@@ -283,271 +283,239 @@ __device__ __forceinline__ void slot2_flush(Slot2& s, uint32_t* __restrict__ tar
   s = Slot2();
 }
 
-// FUSE: the chunk is one 512-bit rank superblock of the concatenated
-// bitvector (n % 512 == 0).  Lanes 0..7 hold its eight 64-bit words and write
-// the rank pair (rank_support_v_par.hpp:95-113: absolute count before the
-// superblock, seven cumulative 9-bit block counts) and the select samples of
-// their word (every 64th one / zero and the superblock ends).
-__device__ __forceinline__ void fuse_chunk(const FuseOut& f, uint64_t bitpos, uint64_t zeros_before,
-                                           uint32_t myword, uint32_t lane, uint64_t& last1, uint64_t& last0) {
-  const uint64_t ones_before = bitpos - zeros_before;
-  const uint32_t lo = __shfl_sync(0xffffffffu, myword, (2 * lane) & 15);
-  const uint32_t hi = __shfl_sync(0xffffffffu, myword, (2 * lane + 1) & 15);
-  const uint64_t w = (uint64_t)lo | ((uint64_t)hi << 32);
-  const uint32_t c = lane < 8 ? (uint32_t)__popcll(w) : 0u;
-  uint32_t inc = c;
-#pragma unroll
-  for (int o = 1; o < 8; o <<= 1) {
-    const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
-    if ((lane & 7) >= (uint32_t)o) inc += t;
-  }
-  const uint32_t pre = inc - c;  // ones in the words before this lane's word
-  if (f.rank) {
-    uint64_t part = (lane >= 1 && lane < 8) ? ((uint64_t)pre << (63 - 9 * lane)) : 0ull;
-#pragma unroll
-    for (int o = 1; o < 8; o <<= 1) part |= __shfl_xor_sync(0xffffffffu, part, o);
-    if (lane == 0) {
-      const uint64_t b = bitpos >> 9;
-      f.rank[2 * b] = ones_before;
-      f.rank[2 * b + 1] = part;
-    }
-  }
-  if (lane < 8) {
-    const uint64_t wi = (bitpos >> 6) + lane;
-    if (f.ends1 && c) {
-      select_marks(w, c, ones_before + pre, wi, f.samples, 1, f.ends1);
-      last1 = max(last1, (wi << 6) + hi64(w) + 1);
-    }
-    if (f.ends0 && c < 64) {
-      const uint64_t zw = ~w;
-      select_marks(zw, 64 - c, zeros_before + 64 * lane - pre, wi, f.samples + f.samp_last, -1, f.ends0);
-      last0 = max(last0, (wi << 6) + hi64(zw) + 1);
-    }
-  }
+// 32-bit shifts for symbols of up to 4 bytes, 64-bit otherwise
+template <typename T>
+__device__ __forceinline__ uint32_t bit_of(T x, int s) {
+  if constexpr (sizeof(T) <= 4) return ((uint32_t)x >> s) & 1u;
+  else return (uint32_t)((uint64_t)x >> s) & 1u;
+}
+template <typename T>
+__device__ __forceinline__ uint32_t prefix_of(T x, int s, uint32_t mask) {
+  if constexpr (sizeof(T) <= 4) return (s >= 32 ? 0u : ((uint32_t)x >> s)) & mask;
+  else return (uint32_t)((uint64_t)x >> s) & mask;
 }
 
-// One level over the level-l order in src.  Each warp owns independent
-// 512-symbol chunks; its zeros-before come from chunkpre (the scan of the
-// counts the previous pass emitted), so warps and CTAs never wait on each
-// other.  Per chunk:
+// One level over the level-l order in src.  Every warp runs its own
+// pipeline over 512-symbol chunks (chunk = global warp id + k * warps): it
+// prefetches its next chunk with cp.async.bulk into the other half of its
+// private double buffer and waits on its own mbarrier, so warps never
+// synchronise with each other.  The chunk's zeros-before come from chunkpre
+// (the scan of the counts the previous pass emitted).  Per chunk:
 //   * the level's bits: one ballot per 32 symbols, stored as whole words;
 //   * SCATTER: every symbol goes straight to its place in the next level's
-//     order (dst): bit 0 -> C(p) + zeros before it in node p, bit 1 ->
-//     C(p) + zeros(p) + ones before it in node p, through base(p) = (C - Zb,
-//     zeros + Zb) and the level-wide zero rank;
+//     order: bit 0 -> C(p) + zeros before it in node p, bit 1 ->
+//     C(p) + zeros(p) + ones before it in node p, through base(p) =
+//     (C - Zb, zeros + Zb) and the level-wide zero rank;
 //   * EMIT_TILES: per 512-symbol chunk of the next level, the number of its
 //     symbols whose next bit is 0 (the next pass's chunkpre input);
 //   * EMIT_NODES: per node of the next level, its left-child size.
-// A chunk inside one node (the common case) uses one base(p) for all rows;
-// its zero run and one run are contiguous in dst and each touches at most two
-// destination chunks, so emission is four ballot counts per row and four
-// atomics per chunk.  Chunks that straddle nodes take a general path.
-// Tiles of 8 chunks arrive by cp.async.bulk into a double buffer; CTAs are
-// persistent (tile = blockIdx.x + k * gridDim.x).
-template <typename T, bool SCATTER, bool EMIT_NODES, bool EMIT_TILES, bool FUSE>
+// A full chunk inside one node (the common case) takes a lean unrolled path:
+// one base(p), its zero run and one run contiguous in dst, each touching at
+// most two destination chunks, so emission is per-lane counting and four
+// atomics per chunk.  Other chunks take a compact general path.
+template <typename T, bool SCATTER, bool EMIT_NODES, bool EMIT_TILES>
 __global__ void __launch_bounds__(LV_THREADS, 4)
     level_kernel(const T* __restrict__ src, T* __restrict__ dst, uint64_t n, int L, int level,
                  const uint2* __restrict__ base_lvl, uint32_t* __restrict__ bits32, uint64_t bit_off,
-                 const uint32_t* __restrict__ chunkpre, const uint32_t* __restrict__ chunkcnt,
-                 uint32_t* __restrict__ chunkcnt_next, uint32_t* __restrict__ znext, uint32_t* err, int bulk_ok,
-                 FuseOut fuse) {
-  constexpr bool NEED_Z = SCATTER || FUSE;
-  using S = LvShape<T>;
+                 const uint32_t* __restrict__ chunkpre, uint32_t* __restrict__ chunkcnt_next,
+                 uint32_t* __restrict__ znext, uint32_t* err, int bulk_ok) {
+  constexpr uint32_t CBYTES = CHUNK * sizeof(T);
   extern __shared__ __align__(128) unsigned char lv_smem[];
-  __shared__ __align__(8) uint64_t mbar[2];
-  T* const buf0 = (T*)lv_smem;
-  T* const buf1 = (T*)(lv_smem + S::BYTES);
-  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const uint64_t ntiles = (n + S::TILE - 1) / S::TILE;
-  const uint64_t nfull = bulk_ok ? n / S::TILE : 0;  // tiles fetched with bulk copies
+  __shared__ __align__(8) uint64_t mbar[LV_THREADS / 32][2];
+  __shared__ uint32_t s_words[LV_THREADS / 32][WROWS];
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T* const wbuf0 = (T*)(lv_smem + (2 * warp) * CBYTES);
+  T* const wbuf1 = (T*)(lv_smem + (2 * warp + 1) * CBYTES);
+  uint64_t* const bar0 = &mbar[warp][0];
+  uint64_t* const bar1 = &mbar[warp][1];
+  uint32_t* const myw = s_words[warp];
+  const uint64_t nchunks = (n + CHUNK - 1) / CHUNK;
+  const uint64_t nfull = bulk_ok ? n / CHUNK : 0;  // chunks fetched with bulk copies
+  const uint64_t stride = (uint64_t)gridDim.x * (LV_THREADS / 32);
+  const uint64_t c0 = (uint64_t)blockIdx.x * (LV_THREADS / 32) + warp;
   const int shift = L - 1 - level;
   const int pshift = L - level;
   const uint32_t pmask = level ? (uint32_t)((1ull << level) - 1) : 0u;
   const uint32_t ltmask = lanemask_lt();
-  uint64_t lvl_zeros = 0, last1 = 0, last0 = 0;  // FUSE: zeros of the levels before this one
-  if (FUSE) {
-    lvl_zeros = fuse.lvl_zb[level];
-    if (blockIdx.x == 0 && tid == 0) {  // zeros through this level, for the next pass
-      const uint64_t nch = (n + CHUNK - 1) / CHUNK;
-      fuse.lvl_zb[level + 1] = lvl_zeros + chunkpre[nch - 1] + chunkcnt[nch - 1];
-    }
-  }
+  const uint32_t n32 = (uint32_t)n;  // n < 2^32
 
-  if (tid == 0) {
-    mbar_init(&mbar[0], 1);
-    mbar_init(&mbar[1], 1);
+  if (lane == 0) {
+    mbar_init(bar0, 1);
+    mbar_init(bar1, 1);
     mbar_fence_init();
-    if (blockIdx.x < nfull) {
-      mbar_expect_tx(&mbar[0], S::BYTES);
-      bulk_g2s(buf0, src + (uint64_t)blockIdx.x * S::TILE, S::BYTES, &mbar[0]);
+    if (c0 < nfull) {
+      mbar_expect_tx(bar0, CBYTES);
+      bulk_g2s(wbuf0, src + c0 * CHUNK, CBYTES, bar0);
     }
   }
-  __syncthreads();
+  __syncwarp();
   uint32_t phase0 = 0, phase1 = 0;
   int cur = 0;
-  uint32_t cache_p = 0xFFFFFFFFu;  // warp-uniform base(p) cache
+  uint32_t cache_p = 0xFFFFFFFFu;  // base(p) cache
   uint2 cache_b = make_uint2(0, 0);
   uint32_t run_p = 0xFFFFFFFFu, run_e = 0, run_o = 0;  // EMIT_NODES run over uniform chunks
-  for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const uint64_t next = tile + gridDim.x;
-    if (tid == 0 && next < nfull) {  // prefetch into the other buffer
+  for (uint64_t c = c0; c < nchunks; c += stride) {
+    const uint64_t nx = c + stride;
+    if (lane == 0 && nx < nfull) {  // prefetch into the other buffer
       fence_proxy_async_smem();
-      mbar_expect_tx(&mbar[cur ^ 1], S::BYTES);
-      bulk_g2s(cur ? buf0 : buf1, src + next * S::TILE, S::BYTES, &mbar[cur ^ 1]);
+      uint64_t* nb = cur ? bar0 : bar1;
+      mbar_expect_tx(nb, CBYTES);
+      bulk_g2s(cur ? wbuf0 : wbuf1, src + nx * CHUNK, CBYTES, nb);
     }
-    T* const tb = cur ? buf1 : buf0;
-    const uint64_t tile_base = tile * S::TILE;
-    if (tile < nfull) {
+    T* const wt = cur ? wbuf1 : wbuf0;
+    const uint64_t cbase = c * CHUNK;
+    const uint32_t cvalid = (uint32_t)min((uint64_t)CHUNK, n - cbase);
+    if (c < nfull) {
       if (cur) {
-        mbar_wait(&mbar[1], phase1, err);
+        mbar_wait(bar1, phase1, err);
         phase1 ^= 1;
       } else {
-        mbar_wait(&mbar[0], phase0, err);
+        mbar_wait(bar0, phase0, err);
         phase0 ^= 1;
       }
     } else {
-      const uint32_t nv = (uint32_t)min((uint64_t)S::TILE, n - tile_base);
-      for (uint32_t k = tid; k < S::TILE; k += LV_THREADS) tb[k] = k < nv ? src[tile_base + k] : T(0);
-      __syncthreads();
+      for (uint32_t k = lane; k < CHUNK; k += 32) wt[k] = k < cvalid ? src[cbase + k] : T(0);
+      __syncwarp();
     }
 
-    const uint64_t cbase = tile_base + (uint64_t)warp * CHUNK;
-    if (cbase < n) {
-      const uint32_t cvalid = (uint32_t)min((uint64_t)CHUNK, n - cbase);
-      const T* const wt = tb + warp * CHUNK;
-      const uint32_t i0 = (uint32_t)cbase;
-      uint32_t z = NEED_Z ? chunkpre[cbase >> LOG_CHUNK] : 0u;  // level-wide zeros before the chunk
-      const uint32_t z_chunk = z;
-      bool uniform = true;
-      uint32_t p0 = 0;
-      uint2 b = make_uint2(0, 0);
-      if (SCATTER && level) {
-        p0 = (uint32_t)((uint64_t)wt[0] >> pshift) & pmask;
-        const uint32_t pl = (uint32_t)((uint64_t)wt[cvalid - 1] >> pshift) & pmask;
-        uniform = p0 == pl;  // the level order is sorted by node
+    const uint32_t i0 = (uint32_t)cbase;
+    uint32_t z = SCATTER ? chunkpre[c] : 0u;  // level-wide zeros before the chunk
+    uint32_t p0 = 0;
+    bool uniform = true;
+    if (SCATTER && level) {
+      p0 = prefix_of(wt[0], pshift, pmask);
+      uniform = p0 == prefix_of(wt[cvalid - 1], pshift, pmask);  // the level order is sorted by node
+    }
+
+    if (!SCATTER) {
+      // last level: bits only
+#pragma unroll 4
+      for (int r = 0; r < WROWS; ++r) {
+        const uint32_t k = r * 32 + lane;
+        const uint32_t om = __ballot_sync(0xffffffffu, k < cvalid && bit_of(wt[k], shift));
+        if (lane == 0) myw[r] = om;
       }
-      if (SCATTER && uniform) {
-        if (p0 != cache_p) {
-          cache_p = p0;
-          cache_b = base_lvl[p0];
-        }
-        b = cache_b;
+    } else if (uniform && cvalid == CHUNK) {
+      // ---- fast path: full chunk inside one node
+      if (p0 != cache_p) {
+        cache_p = p0;
+        cache_b = base_lvl[p0];
       }
-      // uniform chunk: the zero run starts in dst chunk key0, the one run in key1
-      const uint32_t key0 = (b.x + z) >> LOG_CHUNK;
-      const uint32_t key1 = (b.y + (i0 - z)) >> LOG_CHUNK;
-      uint32_t t0 = 0, t1 = 0, a0 = 0, a1 = 0;
-      Slot2 tiles_s, nodes_s;
-      uint32_t myword = 0;
-      // FULL: all 512 symbols valid (every chunk but the last)
-      auto rows = [&](auto full_tag) {
-        constexpr bool FULL = decltype(full_tag)::value;
+      const uint2 b = cache_b;
+      const uint32_t ob0 = i0 - z;                      // ones before the chunk
+      const uint32_t zlim = ((b.x + z + CHUNK) & ~(uint32_t)(CHUNK - 1)) - b.x;   // zero rank where dst crosses
+      const uint32_t olim = ((b.y + ob0 + CHUNK) & ~(uint32_t)(CHUNK - 1)) - b.y; // one rank where dst crosses
+      uint32_t t0 = 0, t1 = 0, a0 = 0, a1 = 0;  // per-lane emission counters
 #pragma unroll
-        for (int r = 0; r < WROWS; ++r) {
-          const uint32_t k = r * 32 + lane;
-          const bool valid = FULL || k < cvalid;
-          const T x = wt[k];
-          const bool one = valid && (((uint64_t)x >> shift) & 1);
-          const uint32_t om = __ballot_sync(0xffffffffu, one);
-          if (lane == (uint32_t)r) myword = om;
-          if (FUSE && !SCATTER) z += FULL ? 32u - __popc(om) : __popc(__ballot_sync(0xffffffffu, valid && !one));
-          if (SCATTER) {
-            const uint32_t zm = FULL ? ~om : __ballot_sync(0xffffffffu, valid && !one);
-            const uint32_t zb = z + __popc(zm & ltmask);
-            z += __popc(zm);
-            const uint32_t i = i0 + k;
-            uint32_t d;
-            bool row_uniform = uniform;
-            uint2 bb = b;
-            uint32_t p = p0;
-            if (!uniform) {
-              // straddling chunk: most rows still lie in one node
-              p = (uint32_t)((uint64_t)x >> pshift) & pmask;
-              const uint32_t plo = __shfl_sync(0xffffffffu, p, 0);
-              row_uniform = __ballot_sync(0xffffffffu, valid && p != plo) == 0;
-              if (row_uniform) {
-                if (plo != cache_p) {
-                  cache_p = plo;
-                  cache_b = base_lvl[plo];
-                }
-                bb = cache_b;
-              } else {
-                bb = base_lvl[p];
-              }
-            }
-            d = one ? bb.y + (i - zb) : bb.x + zb;
-            const bool ok = valid && d < n;
-            if (ok) dst[d] = x;
-            else if (valid) atomicCAS(err, 0u, (uint32_t)DERR_BAD_INDEX);
-            if (EMIT_TILES) {
-              const bool nb0 = ok && !(((uint64_t)x >> (shift - 1)) & 1);
-              if (uniform) {
-                const uint32_t nbm = __ballot_sync(0xffffffffu, nb0);
-                t0 += __popc(zm & nbm);
-                t1 += __popc(om & nbm);
-                const uint32_t key = d >> LOG_CHUNK;
-                a0 += __popc(__ballot_sync(0xffffffffu, nb0 && !one && key == key0));
-                a1 += __popc(__ballot_sync(0xffffffffu, nb0 && one && key == key1));
-              } else {
-                slot2_count(tiles_s, nb0, d >> LOG_CHUNK, chunkcnt_next, lane);
-                if (EMIT_NODES) slot2_count(nodes_s, nb0, 2 * p + (one ? 1u : 0u), znext, lane);
-              }
-            }
+      for (int r = 0; r < WROWS; ++r) {
+        const uint32_t k = r * 32 + lane;
+        const T x = wt[k];
+        const uint32_t one = bit_of(x, shift);
+        const uint32_t om = __ballot_sync(0xffffffffu, one);
+        if (lane == 0) myw[r] = om;
+        const uint32_t zb = z + __popc(~om & ltmask);  // zeros before x (level-wide)
+        z += 32u - __popc(om);
+        const uint32_t ob = i0 + k - zb;                // ones before x (level-wide)
+        const uint32_t d = one ? b.y + ob : b.x + zb;
+        if (d < n32) dst[d] = x;
+        else atomicCAS(err, 0u, (uint32_t)DERR_BAD_INDEX);
+        if (EMIT_TILES) {
+          const uint32_t nz = bit_of(x, shift - 1) ^ 1u;  // next-level bit is 0
+          if (one) {
+            t1 += nz;
+            a1 += nz & (ob < olim);
+          } else {
+            t0 += nz;
+            a0 += nz & (zb < zlim);
           }
         }
-      };
-      if (cvalid == CHUNK) rows(std::true_type());
-      else rows(std::false_type());
+      }
       if (EMIT_TILES) {
-        if (uniform) {
-          if (lane == 0) {
-            if (a0) atomicAdd(&chunkcnt_next[key0], a0);
-            if (t0 - a0) atomicAdd(&chunkcnt_next[key0 + 1], t0 - a0);
-            if (a1) atomicAdd(&chunkcnt_next[key1], a1);
-            if (t1 - a1) atomicAdd(&chunkcnt_next[key1 + 1], t1 - a1);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          t0 += __shfl_xor_sync(0xffffffffu, t0, o);
+          t1 += __shfl_xor_sync(0xffffffffu, t1, o);
+          a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+          a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+        }
+        const uint32_t zs = i0 - ob0;  // zeros before the chunk
+        const uint32_t k0 = (b.x + zs) >> LOG_CHUNK, k1 = (b.y + ob0) >> LOG_CHUNK;
+        if (lane == 0) {
+          if (a0) atomicAdd(&chunkcnt_next[k0], a0);
+          if (t0 - a0) atomicAdd(&chunkcnt_next[k0 + 1], t0 - a0);
+          if (a1) atomicAdd(&chunkcnt_next[k1], a1);
+          if (t1 - a1) atomicAdd(&chunkcnt_next[k1 + 1], t1 - a1);
+        }
+        if (EMIT_NODES) {
+          if (p0 != run_p) {
+            if (lane == 0) emit_flush(znext, run_p, run_e, run_o);
+            run_p = p0;
+            run_e = run_o = 0;
           }
-          if (EMIT_NODES) {
-            if (p0 != run_p) {
-              if (lane == 0) emit_flush(znext, run_p, run_e, run_o);
-              run_p = p0;
-              run_e = run_o = 0;
-            }
-            run_e += t0;
-            run_o += t1;
+          run_e += t0;
+          run_o += t1;
+        }
+      }
+    } else {
+      // ---- general path: a node boundary inside the chunk, or its last chunk
+      Slot2 tiles_s, nodes_s;
+#pragma unroll 1
+      for (int r = 0; r < WROWS; ++r) {
+        const uint32_t k = r * 32 + lane;
+        const bool valid = k < cvalid;
+        const T x = wt[k];
+        const bool one = valid && bit_of(x, shift);
+        const uint32_t om = __ballot_sync(0xffffffffu, one);
+        const uint32_t zm = __ballot_sync(0xffffffffu, valid && !one);
+        if (lane == 0) myw[r] = om;
+        const uint32_t zb = z + __popc(zm & ltmask);
+        z += __popc(zm);
+        const uint32_t p = prefix_of(x, pshift, pmask);
+        const uint32_t plo = __shfl_sync(0xffffffffu, p, 0);
+        uint2 bb;
+        if (__ballot_sync(0xffffffffu, valid && p != plo) == 0) {
+          if (plo != cache_p) {
+            cache_p = plo;
+            cache_b = base_lvl[plo];
           }
+          bb = cache_b;
         } else {
-          slot2_flush(tiles_s, chunkcnt_next, lane);
-          if (EMIT_NODES) slot2_flush(nodes_s, znext, lane);
+          bb = base_lvl[p];
+        }
+        const uint32_t d = one ? bb.y + (i0 + k - zb) : bb.x + zb;
+        const bool ok = valid && d < n32;
+        if (ok) dst[d] = x;
+        else if (valid) atomicCAS(err, 0u, (uint32_t)DERR_BAD_INDEX);
+        if (EMIT_TILES) {
+          const bool nb0 = ok && !bit_of(x, shift - 1);
+          slot2_count(tiles_s, nb0, d >> LOG_CHUNK, chunkcnt_next, lane);
+          if (EMIT_NODES) slot2_count(nodes_s, nb0, 2 * p + (one ? 1u : 0u), znext, lane);
         }
       }
+      if (EMIT_TILES) {
+        slot2_flush(tiles_s, chunkcnt_next, lane);
+        if (EMIT_NODES) slot2_flush(nodes_s, znext, lane);
+      }
+    }
+    __syncwarp();
 
-      // the chunk's bits: word j covers global bits [g + 32 j, g + 32 j + 32)
-      const uint64_t g = bit_off + cbase;
-      const uint32_t g0 = (uint32_t)(g & 31);
-      const uint64_t G = g >> 5;
-      const uint32_t prev = __shfl_up_sync(0xffffffffu, myword, 1);
-      if (lane <= (uint32_t)WROWS && !(g0 == 0 && lane == (uint32_t)WROWS)) {
-        const uint32_t curw = lane < (uint32_t)WROWS ? myword : 0u;
-        const uint32_t val = g0 ? ((curw << g0) | ((lane ? prev : 0u) >> (32 - g0))) : curw;
-        const uint64_t wlo = (G + lane) * 32;
-        if (wlo < g + cvalid) {
-          const bool full = (wlo >= g) && (wlo + 32 <= g + cvalid);
-          if (full) bits32[G + lane] = val;
-          else if (val) atomicOr(&bits32[G + lane], val);
-        }
+    // the chunk's bits: word j covers global bits [g + 32 j, g + 32 j + 32)
+    const uint64_t g = bit_off + cbase;
+    const uint32_t g0 = (uint32_t)(g & 31);
+    const uint64_t G = g >> 5;
+    if (lane <= (uint32_t)WROWS && !(g0 == 0 && lane == (uint32_t)WROWS)) {
+      const uint32_t curw = lane < (uint32_t)WROWS ? myw[lane] : 0u;
+      const uint32_t prev = lane ? myw[lane - 1] : 0u;
+      const uint32_t val = g0 ? ((curw << g0) | (prev >> (32 - g0))) : curw;
+      const uint64_t wlo = (G + lane) * 32;
+      if (wlo < g + cvalid) {
+        const bool full = (wlo >= g) && (wlo + 32 <= g + cvalid);
+        if (full) bits32[G + lane] = val;
+        else if (val) atomicOr(&bits32[G + lane], val);
       }
-      if (FUSE) fuse_chunk(fuse, g, lvl_zeros + z_chunk, myword, lane, last1, last0);
     }
-    __syncthreads();
+    __syncwarp();
     cur ^= 1;
-  }
-  if (FUSE) {
-    last1 = warp_max64(last1);
-    last0 = warp_max64(last0);
-    if (lane == 0) {
-      if (last1) atomicMax(&fuse.info[INF_LAST1], (unsigned long long)last1);
-      if (last0) atomicMax(&fuse.info[INF_LAST0], (unsigned long long)last0);
-    }
   }
   if (EMIT_NODES && lane == 0) emit_flush(znext, run_p, run_e, run_o);
 }
@@ -572,15 +540,15 @@ static void launch_max(const void* s, uint64_t n, unsigned long long* out, cudaS
   max_kernel<T><<<grid, 256, 0, st>>>((const T*)s, n, out);
 }
 
-template <typename T, bool SC, bool EN, bool ET, bool FU>
+template <typename T, bool SC, bool EN, bool ET>
 static int level_grid(uint64_t n) {
   static int per_sm = 0;
   if (!per_sm) {
-    cudaFuncSetAttribute(level_kernel<T, SC, EN, ET, FU>, cudaFuncAttributePreferredSharedMemoryCarveout,
+    cudaFuncSetAttribute(level_kernel<T, SC, EN, ET>, cudaFuncAttributePreferredSharedMemoryCarveout,
                          (int)cudaSharedmemCarveoutMaxShared);
-    cudaFuncSetAttribute(level_kernel<T, SC, EN, ET, FU>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(level_kernel<T, SC, EN, ET>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)(2 * LvShape<T>::BYTES));
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, level_kernel<T, SC, EN, ET, FU>, LV_THREADS,
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, level_kernel<T, SC, EN, ET>, LV_THREADS,
                                                   2 * LvShape<T>::BYTES);
     if (per_sm <= 0) per_sm = 1;
   }
@@ -597,36 +565,27 @@ struct LevelArgs {
   uint32_t* bits32;
   uint64_t bit_off;
   const uint32_t* chunkpre;
-  const uint32_t* chunkcnt;
   uint32_t* chunkcnt_next;
   uint32_t* znext;
   uint32_t* err;
-  bool scatter, emit_nodes, emit_tiles, fuse;
-  FuseOut fo;
+  bool scatter, emit_nodes, emit_tiles;
 };
 
-template <typename T, bool SC, bool EN, bool ET, bool FU>
+template <typename T, bool SC, bool EN, bool ET>
 static void launch_level_v(const LevelArgs& a, cudaStream_t st) {
   const int bulk_ok = ((uintptr_t)a.src % 16) == 0;
   const size_t shm = 2 * LvShape<T>::BYTES;
-  level_kernel<T, SC, EN, ET, FU><<<level_grid<T, SC, EN, ET, FU>(a.n), LV_THREADS, shm, st>>>(
-      (const T*)a.src, (T*)a.dst, a.n, a.L, a.level, a.base_lvl, a.bits32, a.bit_off, a.chunkpre, a.chunkcnt,
-      a.chunkcnt_next, a.znext, a.err, bulk_ok, a.fo);
+  level_kernel<T, SC, EN, ET><<<level_grid<T, SC, EN, ET>(a.n), LV_THREADS, shm, st>>>(
+      (const T*)a.src, (T*)a.dst, a.n, a.L, a.level, a.base_lvl, a.bits32, a.bit_off, a.chunkpre,
+      a.chunkcnt_next, a.znext, a.err, bulk_ok);
 }
 
 template <typename T>
 static void launch_level(const LevelArgs& a, cudaStream_t st) {
-  if (a.fuse) {
-    if (a.scatter && a.emit_nodes) launch_level_v<T, true, true, true, true>(a, st);
-    else if (a.scatter && a.emit_tiles) launch_level_v<T, true, false, true, true>(a, st);
-    else if (a.scatter) launch_level_v<T, true, false, false, true>(a, st);
-    else launch_level_v<T, false, false, false, true>(a, st);
-  } else {
-    if (a.scatter && a.emit_nodes) launch_level_v<T, true, true, true, false>(a, st);
-    else if (a.scatter && a.emit_tiles) launch_level_v<T, true, false, true, false>(a, st);
-    else if (a.scatter) launch_level_v<T, true, false, false, false>(a, st);
-    else launch_level_v<T, false, false, false, false>(a, st);
-  }
+  if (a.scatter && a.emit_nodes) launch_level_v<T, true, true, true>(a, st);
+  else if (a.scatter && a.emit_tiles) launch_level_v<T, true, false, true>(a, st);
+  else if (a.scatter) launch_level_v<T, true, false, false>(a, st);
+  else launch_level_v<T, false, false, false>(a, st);
 }
 
 template <typename T>
@@ -735,22 +694,7 @@ int tree_build(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int L, uint32
   }
 
   // level passes; each scattering pass feeds the next level's chunk counts
-  // and (from level K on) its node tables.  When n % 512 == 0 every chunk is
-  // one rank superblock and the passes also write the rank table and the
-  // select samples (fused); otherwise a separate pass over the bits does.
-  // Fusion is kept available but off: measured on GB300, the per-chunk rank
-  // and select work slows every level pass by more than the separate pass
-  // over the bits costs.
-  constexpr bool kFuseRankSelect = false;
-  const bool fuse = kFuseRankSelect && flags && n > 0 && (n % CHUNK) == 0;
-  FuseOut fo{};
-  uint32_t bflags = flags;
-  if (fuse) {
-    if ((rc = bv_prepare(t.bv, t.bits.as<uint64_t>(), n * (uint64_t)L, bflags, s, &fo))) return rc;
-    if ((rc = t.scratch.ensure((L + 2) * sizeof(uint64_t), s))) return rc;
-    WTG_CK(cudaMemsetAsync(t.scratch.p, 0, (L + 2) * sizeof(uint64_t), s));
-    fo.lvl_zb = t.scratch.as<uint64_t>();
-  }
+  // and (from level K on) its node tables
   if (n) {
     if (L > 1) {
       if ((rc = t.lvl[0].ensure(n * eb + 16, s))) return rc;
@@ -760,9 +704,8 @@ int tree_build(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int L, uint32
     for (int l = 0; l < L; ++l) {
       LevelArgs a{};
       a.scatter = l < L - 1;
-      a.emit_tiles = (l + 1 <= L - 2) || (fuse && l + 1 == L - 1);
-      a.emit_nodes = (l + 1 <= L - 2) && (l + 1 >= K);
-      a.fuse = fuse;
+      a.emit_tiles = l + 1 <= L - 2;
+      a.emit_nodes = a.emit_tiles && (l + 1 >= K);
       a.src = src;
       a.dst = a.scatter ? t.lvl[l & 1].p : nullptr;
       a.n = n;
@@ -771,14 +714,13 @@ int tree_build(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int L, uint32
       a.base_lvl = base + ((1ull << l) - 1);
       a.bits32 = t.bits.as<uint32_t>();
       a.bit_off = (uint64_t)l * n;
-      a.chunkcnt = tilecnt + (uint64_t)l * (tiles + 1);
       a.chunkpre = tilepre;
       a.chunkcnt_next = tilecnt + (uint64_t)(l + 1) * (tiles + 1);
       a.znext = Z + ((1ull << (l + 1)) - 1);
       a.err = d_err;
-      a.fo = fo;
-      if (a.scatter || fuse)
-        if ((rc = scan_exclusive_u32(a.chunkcnt, tilepre, tiles, t.scan_tmp, d_err, s))) return rc;
+      if (a.scatter)
+        if ((rc = scan_exclusive_u32(tilecnt + (uint64_t)l * (tiles + 1), tilepre, tiles, t.scan_tmp, d_err, s)))
+          return rc;
       prof_begin(a.scatter ? PROF_LEVEL : PROF_LEVEL_LAST, s);
       WTG_DISPATCH(eb, launch_level, a, s);
       prof_end(a.scatter ? PROF_LEVEL : PROF_LEVEL_LAST, s);
@@ -802,10 +744,7 @@ int tree_build(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int L, uint32
   }
 
   // rank / select over the concatenated bitvector
-  if (fuse) {
-    if ((rc = bv_fused_totals(t.bv, fo.lvl_zb + L, s))) return rc;
-    if ((rc = bv_finish(t.bv, d_err, s))) return rc;
-  } else if (flags) {
+  if (flags) {
     if ((rc = bv_build(t.bv, t.bits.as<uint64_t>(), n * (uint64_t)L, flags, d_err, s))) return rc;
   }
   return WTG_OK;
