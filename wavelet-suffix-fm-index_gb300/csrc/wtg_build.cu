@@ -39,6 +39,7 @@
 namespace wtg {
 
 constexpr int LV_THREADS = 256;
+constexpr int LV_STAGES = 3;  // chunk buffers per warp (prefetch depth + 1)
 constexpr int TOP_BITS = 2;  // bits histogrammed by the pre-pass (ballot counted)
 
 constexpr int CHUNK = 512;      // symbols per warp chunk (16 rows of 32)
@@ -48,7 +49,8 @@ constexpr int WROWS = CHUNK / 32;
 template <typename T>
 struct LvShape {
   static constexpr uint32_t TILE = LV_THREADS / 32 * CHUNK;  // symbols per CTA tile
-  static constexpr uint32_t BYTES = TILE * sizeof(T);
+  static constexpr uint32_t BYTES = TILE * sizeof(T);  // one chunk per warp
+  static constexpr uint32_t SMEM = LV_STAGES * BYTES;   // the warps' rings
 };
 
 // ------------------------------------------------------------ pre-pass
@@ -321,13 +323,11 @@ __global__ void __launch_bounds__(LV_THREADS, 4)
                  uint32_t* __restrict__ znext, uint32_t* err, int bulk_ok) {
   constexpr uint32_t CBYTES = CHUNK * sizeof(T);
   extern __shared__ __align__(128) unsigned char lv_smem[];
-  __shared__ __align__(8) uint64_t mbar[LV_THREADS / 32][2];
+  __shared__ __align__(8) uint64_t mbar[LV_THREADS / 32][LV_STAGES];
   __shared__ uint32_t s_words[LV_THREADS / 32][WROWS];
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  T* const wbuf0 = (T*)(lv_smem + (2 * warp) * CBYTES);
-  T* const wbuf1 = (T*)(lv_smem + (2 * warp + 1) * CBYTES);
-  uint64_t* const bar0 = &mbar[warp][0];
-  uint64_t* const bar1 = &mbar[warp][1];
+  T* const wring = (T*)(lv_smem + warp * LV_STAGES * CBYTES);  // this warp's LV_STAGES chunk buffers
+  uint64_t* const bars = mbar[warp];
   uint32_t* const myw = s_words[warp];
   const uint64_t nchunks = (n + CHUNK - 1) / CHUNK;
   const uint64_t nfull = bulk_ok ? n / CHUNK : 0;  // chunks fetched with bulk copies
@@ -339,40 +339,42 @@ __global__ void __launch_bounds__(LV_THREADS, 4)
   const uint32_t ltmask = lanemask_lt();
   const uint32_t n32 = (uint32_t)n;  // n < 2^32
 
+  // ring of LV_STAGES buffers: chunk number j (0, 1, ... of this warp) uses
+  // slot j % LV_STAGES; LV_STAGES - 1 chunks are in flight ahead of the one
+  // being processed
   if (lane == 0) {
-    mbar_init(bar0, 1);
-    mbar_init(bar1, 1);
+#pragma unroll
+    for (int q = 0; q < LV_STAGES; ++q) mbar_init(&bars[q], 1);
     mbar_fence_init();
-    if (c0 < nfull) {
-      mbar_expect_tx(bar0, CBYTES);
-      bulk_g2s(wbuf0, src + c0 * CHUNK, CBYTES, bar0);
+#pragma unroll
+    for (int q = 0; q < LV_STAGES - 1; ++q) {
+      const uint64_t cq = c0 + (uint64_t)q * stride;
+      if (cq < nfull) {
+        mbar_expect_tx(&bars[q], CBYTES);
+        bulk_g2s(wring + q * CHUNK, src + cq * CHUNK, CBYTES, &bars[q]);
+      }
     }
   }
   __syncwarp();
-  uint32_t phase0 = 0, phase1 = 0;
-  int cur = 0;
+  uint32_t phases = 0;  // bit q: parity of slot q's next completion
+  int slot = 0;
   uint32_t cache_p = 0xFFFFFFFFu;  // base(p) cache
   uint2 cache_b = make_uint2(0, 0);
   uint32_t run_p = 0xFFFFFFFFu, run_e = 0, run_o = 0;  // EMIT_NODES run over uniform chunks
   for (uint64_t c = c0; c < nchunks; c += stride) {
-    const uint64_t nx = c + stride;
-    if (lane == 0 && nx < nfull) {  // prefetch into the other buffer
+    const uint64_t nx = c + (uint64_t)(LV_STAGES - 1) * stride;
+    const int nslot = slot == 0 ? LV_STAGES - 1 : slot - 1;  // (slot + STAGES - 1) % STAGES
+    if (lane == 0 && nx < nfull) {  // refill the slot freed by the previous chunk
       fence_proxy_async_smem();
-      uint64_t* nb = cur ? bar0 : bar1;
-      mbar_expect_tx(nb, CBYTES);
-      bulk_g2s(cur ? wbuf0 : wbuf1, src + nx * CHUNK, CBYTES, nb);
+      mbar_expect_tx(&bars[nslot], CBYTES);
+      bulk_g2s(wring + nslot * CHUNK, src + nx * CHUNK, CBYTES, &bars[nslot]);
     }
-    T* const wt = cur ? wbuf1 : wbuf0;
+    T* const wt = wring + slot * CHUNK;
     const uint64_t cbase = c * CHUNK;
     const uint32_t cvalid = (uint32_t)min((uint64_t)CHUNK, n - cbase);
     if (c < nfull) {
-      if (cur) {
-        mbar_wait(bar1, phase1, err);
-        phase1 ^= 1;
-      } else {
-        mbar_wait(bar0, phase0, err);
-        phase0 ^= 1;
-      }
+      mbar_wait(&bars[slot], (phases >> slot) & 1u, err);
+      phases ^= 1u << slot;
     } else {
       for (uint32_t k = lane; k < CHUNK; k += 32) wt[k] = k < cvalid ? src[cbase + k] : T(0);
       __syncwarp();
@@ -421,13 +423,11 @@ __global__ void __launch_bounds__(LV_THREADS, 4)
         else atomicCAS(err, 0u, (uint32_t)DERR_BAD_INDEX);
         if (EMIT_TILES) {
           const uint32_t nz = bit_of(x, shift - 1) ^ 1u;  // next-level bit is 0
-          if (one) {
-            t1 += nz;
-            a1 += nz & (ob < olim);
-          } else {
-            t0 += nz;
-            a0 += nz & (zb < zlim);
-          }
+          const uint32_t nzo = nz & one, nzz = nz & (one ^ 1u);
+          t1 += nzo;
+          t0 += nzz;
+          a1 += nzo & (uint32_t)(ob < olim);
+          a0 += nzz & (uint32_t)(zb < zlim);
         }
       }
       if (EMIT_TILES) {
@@ -515,7 +515,7 @@ __global__ void __launch_bounds__(LV_THREADS, 4)
       }
     }
     __syncwarp();
-    cur ^= 1;
+    slot = slot + 1 == LV_STAGES ? 0 : slot + 1;
   }
   if (EMIT_NODES && lane == 0) emit_flush(znext, run_p, run_e, run_o);
 }
@@ -547,9 +547,9 @@ static int level_grid(uint64_t n) {
     cudaFuncSetAttribute(level_kernel<T, SC, EN, ET>, cudaFuncAttributePreferredSharedMemoryCarveout,
                          (int)cudaSharedmemCarveoutMaxShared);
     cudaFuncSetAttribute(level_kernel<T, SC, EN, ET>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)(2 * LvShape<T>::BYTES));
+                         (int)LvShape<T>::SMEM);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, level_kernel<T, SC, EN, ET>, LV_THREADS,
-                                                  2 * LvShape<T>::BYTES);
+                                                  LvShape<T>::SMEM);
     if (per_sm <= 0) per_sm = 1;
   }
   const uint64_t tiles = (n + LvShape<T>::TILE - 1) / LvShape<T>::TILE;
@@ -574,7 +574,7 @@ struct LevelArgs {
 template <typename T, bool SC, bool EN, bool ET>
 static void launch_level_v(const LevelArgs& a, cudaStream_t st) {
   const int bulk_ok = ((uintptr_t)a.src % 16) == 0;
-  const size_t shm = 2 * LvShape<T>::BYTES;
+  const size_t shm = LvShape<T>::SMEM;
   level_kernel<T, SC, EN, ET><<<level_grid<T, SC, EN, ET>(a.n), LV_THREADS, shm, st>>>(
       (const T*)a.src, (T*)a.dst, a.n, a.L, a.level, a.base_lvl, a.bits32, a.bit_off, a.chunkpre,
       a.chunkcnt_next, a.znext, a.err, bulk_ok);
