@@ -24,7 +24,6 @@
 namespace wtg {
 
 constexpr int BV_THREADS = 256;  // one 512-bit superblock per thread
-constexpr int BV_SB_PER_TILE = BV_THREADS;
 
 __device__ __forceinline__ uint64_t warp_max_u64(uint64_t v) {
 #pragma unroll
@@ -35,53 +34,84 @@ __device__ __forceinline__ uint64_t warp_max_u64(uint64_t v) {
   return v;
 }
 
+// records, among args [K, K+c) in word wi (x = its arg mask): every 64th
+// arg's position (low 32 bits) in samp[samp_dir * (arg / 64)], the start of
+// every superblock (arg 4096q) and its end (arg 4096q + 4095)
+__device__ __forceinline__ void select_marks32(uint64_t x, uint32_t c, uint64_t K, uint64_t wi,
+                                               uint32_t* __restrict__ samp, int64_t samp_dir,
+                                               uint64_t* __restrict__ starts, uint64_t* __restrict__ ends) {
+  const uint64_t q = (K + 63) & ~63ull;  // next multiple of 64
+  if (q < K + c) {
+    const uint64_t pos = (wi << 6) + sel64(x, (uint32_t)(q - K + 1));
+    samp[samp_dir * (int64_t)(q >> 6)] = (uint32_t)pos;
+    if ((q & 4095) == 0) starts[q >> 12] = pos;
+  }
+  const uint64_t e = K | 4095ull;  // next index with e % 4096 == 4095
+  if (e < K + c) ends[e >> 12] = (wi << 6) + sel64(x, (uint32_t)(e - K + 1));
+}
+
+// One pass over the bitvector: lane per 64-bit word, 8 lanes per 512-bit
+// superblock, a tile of 256 superblocks per CTA (coalesced 2 KB rows), one
+// decoupled look-back scan of the tile one-counts.
+constexpr int BVT_ITER = 8;                        // rows of 256 words per tile
+constexpr int BVT_SB = BVT_ITER * BV_THREADS / 8;  // superblocks per tile
+
 __global__ void __launch_bounds__(BV_THREADS)
     bv_pass_kernel(const uint64_t* __restrict__ words, uint64_t size, uint64_t W, uint64_t NB, uint32_t flags,
-                   uint64_t* __restrict__ rank, uint64_t* __restrict__ samples, uint64_t samp_last,
-                   uint64_t* __restrict__ ends1, uint64_t* __restrict__ ends0, unsigned long long* info,
-                   uint64_t* status, uint32_t* counter, uint32_t* err) {
+                   uint64_t* __restrict__ rank, uint32_t* __restrict__ samples, uint64_t samp_last,
+                   uint64_t* __restrict__ starts1, uint64_t* __restrict__ starts0, uint64_t* __restrict__ ends1,
+                   uint64_t* __restrict__ ends0, unsigned long long* info, uint64_t* status, uint32_t* counter,
+                   uint32_t* err) {
   __shared__ uint32_t s_tile;
-  __shared__ uint64_t s_wsum[BV_THREADS / 32];
+  __shared__ uint32_t s_sb[BVT_SB];
   __shared__ uint64_t s_prefix;
   if (threadIdx.x == 0) s_tile = atomicAdd(counter, 1u);
   __syncthreads();
   const uint32_t tile = s_tile;
-  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint64_t b = (uint64_t)tile * BV_SB_PER_TILE + threadIdx.x;
+  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, g8 = lane & 7;
+  const uint64_t wbase = (uint64_t)tile * (BVT_ITER * BV_THREADS);
   const uint64_t tailmask = (size & 63) ? ((1ull << (size & 63)) - 1) : ~0ull;
-
-  uint64_t w[8];
-  uint32_t c[8];
-  uint32_t tot = 0;
+  uint64_t w[BVT_ITER];
+  uint32_t c[BVT_ITER], inc[BVT_ITER];
 #pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    uint64_t wi = 8 * b + k;
-    uint64_t x = (b <= NB && wi < W) ? __ldg(&words[wi]) : 0ull;
+  for (int j = 0; j < BVT_ITER; ++j) {
+    const uint64_t wi = wbase + j * BV_THREADS + tid;
+    uint64_t x = wi < W ? __ldg(&words[wi]) : 0ull;
     if (wi == W - 1) x &= tailmask;
-    w[k] = x;
-    c[k] = __popcll(x);
-    tot += c[k];
-  }
-
-  // block exclusive scan of the superblock one-counts
-  uint64_t incl = tot;
+    w[j] = x;
+    c[j] = __popcll(x);
+    uint32_t v = c[j];
 #pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    uint64_t t = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= (uint32_t)o) incl += t;
+    for (int o = 1; o < 8; o <<= 1) {  // inclusive scan within the superblock's 8 lanes
+      const uint32_t t = __shfl_up_sync(0xffffffffu, v, o);
+      if (g8 >= (uint32_t)o) v += t;
+    }
+    inc[j] = v;
+    if (g8 == 7) s_sb[j * (BV_THREADS / 8) + warp * 4 + (lane >> 3)] = v;
   }
-  if (lane == 31) s_wsum[warp] = incl;
   __syncthreads();
   if (warp == 0) {
-    uint64_t v = lane < BV_THREADS / 32 ? s_wsum[lane] : 0;
-    uint64_t vinc = v;
+    constexpr int PER = BVT_SB / 32;
+    uint32_t loc[PER];
+    uint32_t sum = 0;
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      loc[q] = s_sb[lane * PER + q];
+      sum += loc[q];
+    }
+    uint32_t incw = sum;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      uint64_t t = __shfl_up_sync(0xffffffffu, vinc, o);
-      if (lane >= (uint32_t)o) vinc += t;
+      const uint32_t t = __shfl_up_sync(0xffffffffu, incw, o);
+      if (lane >= (uint32_t)o) incw += t;
     }
-    if (lane < BV_THREADS / 32) s_wsum[lane] = vinc - v;
-    uint64_t total = __shfl_sync(0xffffffffu, vinc, BV_THREADS / 32 - 1);
+    uint32_t run = incw - sum;
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      s_sb[lane * PER + q] = run;
+      run += loc[q];
+    }
+    const uint64_t total = __shfl_sync(0xffffffffu, incw, 31);
     uint64_t prefix = 0;
     if (tile == 0) {
       if (lane == 0) lb_publish(status, tile, LB_FLAG_INC, total);
@@ -93,55 +123,46 @@ __global__ void __launch_bounds__(BV_THREADS)
     if (lane == 0) s_prefix = prefix;
   }
   __syncthreads();
-  const uint64_t ones_before = s_prefix + s_wsum[warp] + incl - tot;
-
-  if (b <= NB) {
-    if (flags & WTG_RANK) {
-      // fields 1..7 hold the count before block k of the superblock; in the
-      // final superblock only fields 1..max(r,1) are written (r = its words)
-      const uint64_t r = W - 8 * NB;
-      const uint32_t kmax = (b < NB) ? 7u : (r > 1 ? (uint32_t)r : 1u);
-      uint64_t second = 0;
-      uint64_t cum = 0;
-#pragma unroll
-      for (int k = 1; k < 8; ++k) {
-        cum += c[k - 1];
-        if ((uint32_t)k <= kmax) second |= cum << (63 - 9 * k);
-      }
-      rank[2 * b] = ones_before;
-      rank[2 * b + 1] = second;
-    }
-    if (b == NB) {
-      info[INF_M1] = ones_before + tot;
-      info[INF_M0] = size - (ones_before + tot);
-    }
-  }
-
+  const uint64_t tprefix = s_prefix;
+  const uint64_t r_last = W - 8 * NB;  // words of the final superblock
   uint64_t last1 = 0, last0 = 0;
-  if (flags & WTG_SELECT1) {
-    uint64_t K = ones_before;
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      if (c[k]) {
-        uint64_t wi = 8 * b + k;
-        select_marks(w[k], c[k], K, wi, samples, 1, ends1);
-        last1 = (wi << 6) + hi64(w[k]) + 1;
-        K += c[k];
+  for (int j = 0; j < BVT_ITER; ++j) {
+    const uint32_t sbl = j * (BV_THREADS / 8) + warp * 4 + (lane >> 3);
+    const uint64_t b = (uint64_t)tile * BVT_SB + sbl;  // superblock
+    const uint64_t wi = wbase + j * BV_THREADS + tid;
+    const uint64_t sb_before = tprefix + s_sb[sbl];    // ones before the superblock
+    const uint32_t excl = inc[j] - c[j];               // ones before the word in its superblock
+    const uint32_t sbt = __shfl_sync(0xffffffffu, inc[j], (lane & ~7u) + 7);  // ones in the superblock
+    if (flags & WTG_RANK) {
+      // field k (1..7) = count before block k; the final superblock writes
+      // only fields 1..max(r,1), r = its words (rank_support_v_par.hpp:99-108)
+      const uint32_t kmax = (b < NB) ? 7u : (r_last > 1 ? (uint32_t)r_last : 1u);
+      uint64_t part = (g8 >= 1 && g8 <= kmax) ? ((uint64_t)excl << (63 - 9 * g8)) : 0ull;
+#pragma unroll
+      for (int o = 1; o < 8; o <<= 1) part |= __shfl_xor_sync(0xffffffffu, part, o);
+      if (g8 == 0 && b <= NB) {
+        rank[2 * b] = sb_before;
+        rank[2 * b + 1] = part;
       }
     }
-  }
-  if (flags & WTG_SELECT0) {
-    uint64_t K = 8 * b * 64 - ones_before;  // zeros before the superblock
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      uint64_t wi = 8 * b + k;
-      uint64_t z = 0;
-      if (b <= NB && wi < W) z = (wi == W - 1) ? (~w[k] & tailmask) : ~w[k];
-      uint32_t cz = __popcll(z);
-      if (cz) {
-        select_marks(z, cz, K, wi, samples + samp_last, -1, ends0);
-        last0 = (wi << 6) + hi64(z) + 1;
-        K += cz;
+    if (b == NB && g8 == 0) {
+      info[INF_M1] = sb_before + sbt;
+      info[INF_M0] = size - (sb_before + sbt);
+    }
+    if (wi < W) {
+      const uint64_t K1 = sb_before + excl;  // ones before this word
+      if ((flags & WTG_SELECT1) && c[j]) {
+        select_marks32(w[j], c[j], K1, wi, samples, 1, starts1, ends1);
+        last1 = max(last1, (wi << 6) + hi64(w[j]) + 1);
+      }
+      if (flags & WTG_SELECT0) {
+        const uint64_t z = (wi == W - 1) ? (~w[j] & tailmask) : ~w[j];
+        const uint32_t cz = __popcll(z);
+        if (cz) {
+          select_marks32(z, cz, (wi << 6) - K1, wi, samples + samp_last, -1, starts0, ends0);
+          last0 = max(last0, (wi << 6) + hi64(z) + 1);
+        }
       }
     }
   }
@@ -154,7 +175,7 @@ __global__ void __launch_bounds__(BV_THREADS)
 }
 
 // per superblock: long/mini choice, width and pool words
-__global__ void select_desc_kernel(int t_b, const uint64_t* __restrict__ samples, uint64_t samp_last,
+__global__ void select_desc_kernel(int t_b, const uint64_t* __restrict__ starts,
                                    const uint64_t* __restrict__ ends, unsigned long long* info, uint64_t logn4,
                                    uint64_t nsb_cap, uint64_t* __restrict__ descw, uint64_t* __restrict__ sizes,
                                    uint64_t* __restrict__ long_list) {
@@ -166,7 +187,7 @@ __global__ void select_desc_kernel(int t_b, const uint64_t* __restrict__ samples
     sizes[i] = 0;
     return;
   }
-  const uint64_t start = t_b ? samples[64 * i] : samples[samp_last - 64 * i];
+  const uint64_t start = starts[i];
   const uint64_t end = (i + 1 < nsb) ? ends[i] : (uint64_t)info[t_b ? INF_LAST1 : INF_LAST0] - 1;
   const uint64_t span = end - start;
   const uint64_t lng = span > logn4;
@@ -188,7 +209,7 @@ __global__ void select_pool_total_kernel(int t_b, unsigned long long* info, cons
 
 // warp per superblock: final descriptors, and the 64-entry mini blocks
 __global__ void __launch_bounds__(256)
-    select_mini_kernel(int t_b, uint64_t nsb, uint64_t m, const uint64_t* __restrict__ samples, uint64_t samp_last,
+    select_mini_kernel(int t_b, uint64_t nsb, uint64_t m, const uint32_t* __restrict__ samples, uint64_t samp_last,
                        const uint64_t* __restrict__ descw, const uint64_t* __restrict__ offs,
                        uint64_t* __restrict__ desc, uint64_t* __restrict__ pool) {
   __shared__ uint64_t ent[256 / 32][64];
@@ -201,25 +222,25 @@ __global__ void __launch_bounds__(256)
   if ((d >> 7) & 1) return;  // long block
   const uint32_t wdt = (uint32_t)(d & 127);
   auto samp = [&](uint64_t k) { return t_b ? samples[k] : samples[samp_last - k]; };
-  const uint64_t start = samp(64 * i);
+  // positions are kept mod 2^32; a mini block spans at most log^4 n < 2^32
+  // bits, so the offsets are exact
+  const uint32_t start = samp(64 * i);
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
     uint32_t j = lane + 32 * h;
     uint64_t k = 4096 * i + 64 * (uint64_t)j;
-    ent[warp][j] = (k < m) ? samp(64 * i + j) - start : 0;
+    ent[warp][j] = (k < m) ? (uint64_t)(uint32_t)(samp(64 * i + j) - start) : 0;
   }
   __syncwarp();
   if (lane < wdt) pool[off + lane] = packed_word(lane, wdt, 64, [&](uint64_t j) { return ent[warp][j]; });
 }
 
 // m_superblock: entry i = position of arg 4096*i, width logn
-__global__ void select_sb_pack_kernel(int t_b, uint64_t nsb, uint32_t logn, const uint64_t* __restrict__ samples,
-                                      uint64_t samp_last, uint64_t nwords, uint64_t* __restrict__ sb_words) {
+__global__ void select_sb_pack_kernel(uint64_t nsb, uint32_t logn, const uint64_t* __restrict__ starts,
+                                      uint64_t nwords, uint64_t* __restrict__ sb_words) {
   uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= nwords) return;
-  sb_words[q] = packed_word(q, logn, nsb, [&](uint64_t i) {
-    return t_b ? samples[64 * i] : samples[samp_last - 64 * i];
-  });
+  sb_words[q] = packed_word(q, logn, nsb, [&](uint64_t i) { return starts[i]; });
 }
 
 // Long blocks, step 1: the position of every arg of every long superblock,
@@ -235,8 +256,8 @@ __device__ __forceinline__ uint64_t args_before_sb(int t_b, const uint64_t* __re
 
 __global__ void __launch_bounds__(256)
     select_long_fill_kernel(int t_b, const uint64_t* __restrict__ words, uint64_t size, uint64_t W,
-                            const uint64_t* __restrict__ rank, const uint64_t* __restrict__ samples,
-                            uint64_t samp_last, const unsigned long long* info,
+                            const uint64_t* __restrict__ rank, const uint64_t* __restrict__ starts,
+                            const uint64_t* __restrict__ ends, const unsigned long long* info,
                             const uint64_t* __restrict__ long_list, uint64_t* __restrict__ ent, uint32_t* err) {
   const uint64_t gt = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const uint64_t m = info[t_b ? INF_M1 : INF_M0];
@@ -244,11 +265,12 @@ __global__ void __launch_bounds__(256)
   const uint64_t nlong = info[t_b ? INF_NLONG1 : INF_NLONG0];
   const uint64_t li = gt >> 12, j = gt & 4095;
   if (li >= nlong) return;
-  const uint64_t k = 4096 * long_list[li] + j;  // 0-based arg index
-  if (k >= m) return;                           // entries past the arg count stay zero
-  auto samp = [&](uint64_t q) { return t_b ? samples[q] : samples[samp_last - q]; };
-  const uint64_t plo = samp(k >> 6);
-  const uint64_t phi = ((k >> 6) + 1) * 64 < m ? samp((k >> 6) + 1) : last - 1;
+  const uint64_t i = long_list[li];
+  const uint64_t k = 4096 * i + j;  // 0-based arg index
+  if (k >= m) return;               // entries past the arg count stay zero
+  const uint64_t nsb = (m + 4095) >> 12;
+  const uint64_t plo = starts[i];
+  const uint64_t phi = i + 1 < nsb ? ends[i] : last - 1;
   uint64_t lo = plo >> 9, hi = phi >> 9;  // largest b in [lo, hi] with args_before_sb(b) <= k
   while (lo < hi) {
     const uint64_t mid = (lo + hi + 1) >> 1;
@@ -308,22 +330,11 @@ void bv_release(BvSupport& bv, cudaStream_t s) {
     sd.pool.release(s);
     sd.long_list.release(s);
     sd.long_ent.release(s);
+    sd.starts.release(s);
   }
 }
 
-__global__ void fused_totals_kernel(const uint64_t* zeros_total, uint64_t size, uint64_t NB, uint64_t* rank,
-                                    unsigned long long* info) {
-  const uint64_t z = *zeros_total;
-  info[INF_M1] = size - z;
-  info[INF_M0] = z;
-  if (rank) {  // the pair after the last superblock: (total, 0), rank_support_v_par.hpp:95-110
-    rank[2 * NB] = size - z;
-    rank[2 * NB + 1] = 0;
-  }
-}
-
-int bv_prepare(BvSupport& bv, const uint64_t* d_words, uint64_t size, uint32_t& flags, cudaStream_t s,
-               FuseOut* out) {
+int bv_prepare(BvSupport& bv, const uint64_t* d_words, uint64_t size, uint32_t& flags, cudaStream_t s) {
   int rc;
   // select's long blocks are filled through the rank table, so it is built
   // whenever a select support is
@@ -340,33 +351,16 @@ int bv_prepare(BvSupport& bv, const uint64_t* d_words, uint64_t size, uint32_t& 
   if (flags & WTG_RANK)
     if ((rc = bv.rank.ensure(2 * (NB + 1) * sizeof(uint64_t), s))) return rc;
   if (flags & (WTG_SELECT1 | WTG_SELECT0))
-    if ((rc = bv.samples.ensure(samp_n * sizeof(uint64_t), s))) return rc;
+    if ((rc = bv.samples.ensure(samp_n * sizeof(uint32_t), s))) return rc;
   for (int t_b = 0; t_b < 2; ++t_b) {
     if (!(flags & (t_b ? WTG_SELECT1 : WTG_SELECT0))) continue;
     SelectDev& sd = bv.sel[t_b];
     if ((rc = sd.ends.ensure(nsb_cap * sizeof(uint64_t), s))) return rc;
+    if ((rc = sd.starts.ensure(nsb_cap * sizeof(uint64_t), s))) return rc;
     if ((rc = sd.desc.ensure(2 * nsb_cap * sizeof(uint64_t), s))) return rc;   // [final | working]
     if ((rc = sd.sizes.ensure(2 * nsb_cap * sizeof(uint64_t), s))) return rc;  // [sizes | offsets]
     if ((rc = sd.long_list.ensure(nsb_cap * sizeof(uint64_t), s))) return rc;
   }
-  if (out) {
-    out->rank = (flags & WTG_RANK) ? bv.rank.as<uint64_t>() : nullptr;
-    out->samples = bv.samples.as<uint64_t>();
-    out->samp_last = samp_n - 1;
-    out->ends1 = (flags & WTG_SELECT1) ? bv.sel[1].ends.as<uint64_t>() : nullptr;
-    out->ends0 = (flags & WTG_SELECT0) ? bv.sel[0].ends.as<uint64_t>() : nullptr;
-    out->info = bv.info.as<unsigned long long>();
-    out->flags = flags;
-  }
-  return WTG_OK;
-}
-
-int bv_fused_totals(BvSupport& bv, const uint64_t* zeros_total, cudaStream_t s) {
-  const uint64_t NB = ((bv.size + 63) / 64) >> 3;
-  fused_totals_kernel<<<1, 1, 0, s>>>(zeros_total, bv.size, NB, (bv.flags & WTG_RANK) ? bv.rank.as<uint64_t>() : nullptr,
-                                      bv.info.as<unsigned long long>());
-  count_launch();
-  WTG_CK(cudaGetLastError());
   return WTG_OK;
 }
 
@@ -376,15 +370,16 @@ int bv_pass(BvSupport& bv, uint32_t* d_err, cudaStream_t s) {
   const uint64_t W = (size + 63) / 64;
   const uint64_t NB = W >> 3;
   const uint64_t samp_n = W + 2;
-  const uint64_t tiles = (NB + 1 + BV_SB_PER_TILE - 1) / BV_SB_PER_TILE;
+  const uint64_t tiles = (NB + 1 + BVT_SB - 1) / BVT_SB;
   if (tiles > 0x7fffffffull) return fail(WTG_ERR_INVALID, "bitvector too large");
   if ((rc = bv.status.ensure((tiles + 1) * sizeof(uint64_t), s))) return rc;
   WTG_CK(cudaMemsetAsync(bv.status.p, 0, (tiles + 1) * sizeof(uint64_t), s));
   prof_begin(PROF_BVPASS, s);
   bv_pass_kernel<<<(unsigned)tiles, BV_THREADS, 0, s>>>(
-      bv.words, size, W, NB, bv.flags, bv.rank.as<uint64_t>(), bv.samples.as<uint64_t>(), samp_n - 1,
-      bv.sel[1].ends.as<uint64_t>(), bv.sel[0].ends.as<uint64_t>(), bv.info.as<unsigned long long>(),
-      bv.status.as<uint64_t>() + 1, bv.status.as<uint32_t>(), d_err);
+      bv.words, size, W, NB, bv.flags, bv.rank.as<uint64_t>(), bv.samples.as<uint32_t>(), samp_n - 1,
+      bv.sel[1].starts.as<uint64_t>(), bv.sel[0].starts.as<uint64_t>(), bv.sel[1].ends.as<uint64_t>(),
+      bv.sel[0].ends.as<uint64_t>(), bv.info.as<unsigned long long>(), bv.status.as<uint64_t>() + 1,
+      bv.status.as<uint32_t>(), d_err);
   prof_end(PROF_BVPASS, s);
   count_launch();
   WTG_CK(cudaGetLastError());
@@ -403,7 +398,7 @@ int bv_finish(BvSupport& bv, uint32_t* d_err, cudaStream_t s) {
   const uint64_t logn4 = (uint64_t)(uint32_t)(logn * logn * logn * logn);  // uint32 as in initData
   const uint64_t* d_words = bv.words;
   unsigned long long* info = bv.info.as<unsigned long long>();
-  uint64_t* samples = bv.samples.as<uint64_t>();
+  uint32_t* samples = bv.samples.as<uint32_t>();
 
   for (int t_b = 0; t_b < 2; ++t_b) {
     if (!(flags & (t_b ? WTG_SELECT1 : WTG_SELECT0))) continue;
@@ -413,7 +408,7 @@ int bv_finish(BvSupport& bv, uint32_t* d_err, cudaStream_t s) {
     uint64_t* offs = sizes + nsb_cap;
     prof_begin(PROF_SELECT, s);
     select_desc_kernel<<<(unsigned)((nsb_cap + 255) / 256), 256, 0, s>>>(
-        t_b, samples, samp_n - 1, sd.ends.as<uint64_t>(), info, logn4, nsb_cap, descw, sizes,
+        t_b, sd.starts.as<uint64_t>(), sd.ends.as<uint64_t>(), info, logn4, nsb_cap, descw, sizes,
         sd.long_list.as<uint64_t>());
     prof_end(PROF_SELECT, s);
     count_launch();
@@ -455,7 +450,7 @@ int bv_finish(BvSupport& bv, uint32_t* d_err, cudaStream_t s) {
     WTG_CK(cudaGetLastError());
     prof_begin(PROF_SELECT, s);
     select_sb_pack_kernel<<<(unsigned)((sd.sb_nwords + 255) / 256), 256, 0, s>>>(
-        t_b, sd.nsb, logn, samples, samp_n - 1, sd.sb_nwords, sd.sb_words.as<uint64_t>());
+        sd.nsb, logn, sd.starts.as<uint64_t>(), sd.sb_nwords, sd.sb_words.as<uint64_t>());
     prof_end(PROF_SELECT, s);
     count_launch();
     WTG_CK(cudaGetLastError());
@@ -465,8 +460,8 @@ int bv_finish(BvSupport& bv, uint32_t* d_err, cudaStream_t s) {
       WTG_CK(cudaMemsetAsync(sd.long_ent.p, 0, nlong * 4096 * sizeof(uint64_t), s));
       prof_begin(PROF_SELECT, s);
       select_long_fill_kernel<<<(unsigned)((nlong * 4096 + 255) / 256), 256, 0, s>>>(
-          t_b, d_words, size, W, bv.rank.as<uint64_t>(), samples, samp_n - 1, info, sd.long_list.as<uint64_t>(),
-          sd.long_ent.as<uint64_t>(), d_err);
+          t_b, d_words, size, W, bv.rank.as<uint64_t>(), sd.starts.as<uint64_t>(), sd.ends.as<uint64_t>(), info,
+          sd.long_list.as<uint64_t>(), sd.long_ent.as<uint64_t>(), d_err);
       prof_end(PROF_SELECT, s);
       count_launch();
       WTG_CK(cudaGetLastError());
@@ -485,7 +480,7 @@ int bv_finish(BvSupport& bv, uint32_t* d_err, cudaStream_t s) {
 int bv_build(BvSupport& bv, const uint64_t* d_words, uint64_t size, uint32_t flags, uint32_t* d_err,
              cudaStream_t s) {
   int rc;
-  if ((rc = bv_prepare(bv, d_words, size, flags, s, nullptr))) return rc;
+  if ((rc = bv_prepare(bv, d_words, size, flags, s))) return rc;
   if ((rc = bv_pass(bv, d_err, s))) return rc;
   return bv_finish(bv, d_err, s);
 }

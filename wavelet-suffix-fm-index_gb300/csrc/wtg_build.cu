@@ -39,7 +39,10 @@
 namespace wtg {
 
 constexpr int LV_THREADS = 256;
-constexpr int LV_STAGES = 3;  // chunk buffers per warp (prefetch depth + 1)
+// chunk buffers per warp (prefetch depth + 1): the bits-only last level is
+// latency bound and takes a deeper ring
+template <bool SCATTER>
+constexpr int lv_stages() { return SCATTER ? 2 : 3; }
 constexpr int TOP_BITS = 2;  // bits histogrammed by the pre-pass (ballot counted)
 
 constexpr int CHUNK = 512;      // symbols per warp chunk (16 rows of 32)
@@ -50,7 +53,8 @@ template <typename T>
 struct LvShape {
   static constexpr uint32_t TILE = LV_THREADS / 32 * CHUNK;  // symbols per CTA tile
   static constexpr uint32_t BYTES = TILE * sizeof(T);  // one chunk per warp
-  static constexpr uint32_t SMEM = LV_STAGES * BYTES;   // the warps' rings
+  template <bool SCATTER>
+  static constexpr uint32_t smem() { return lv_stages<SCATTER>() * BYTES; }  // the warps' rings
 };
 
 // ------------------------------------------------------------ pre-pass
@@ -322,6 +326,7 @@ __global__ void __launch_bounds__(LV_THREADS, 4)
                  const uint32_t* __restrict__ chunkpre, uint32_t* __restrict__ chunkcnt_next,
                  uint32_t* __restrict__ znext, uint32_t* err, int bulk_ok) {
   constexpr uint32_t CBYTES = CHUNK * sizeof(T);
+  constexpr int LV_STAGES = lv_stages<SCATTER>();
   extern __shared__ __align__(128) unsigned char lv_smem[];
   __shared__ __align__(8) uint64_t mbar[LV_THREADS / 32][LV_STAGES];
   __shared__ uint32_t s_words[LV_THREADS / 32][WROWS];
@@ -547,9 +552,9 @@ static int level_grid(uint64_t n) {
     cudaFuncSetAttribute(level_kernel<T, SC, EN, ET>, cudaFuncAttributePreferredSharedMemoryCarveout,
                          (int)cudaSharedmemCarveoutMaxShared);
     cudaFuncSetAttribute(level_kernel<T, SC, EN, ET>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)LvShape<T>::SMEM);
+                         (int)LvShape<T>::template smem<SC>());
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, level_kernel<T, SC, EN, ET>, LV_THREADS,
-                                                  LvShape<T>::SMEM);
+                                                  LvShape<T>::template smem<SC>());
     if (per_sm <= 0) per_sm = 1;
   }
   const uint64_t tiles = (n + LvShape<T>::TILE - 1) / LvShape<T>::TILE;
@@ -574,7 +579,7 @@ struct LevelArgs {
 template <typename T, bool SC, bool EN, bool ET>
 static void launch_level_v(const LevelArgs& a, cudaStream_t st) {
   const int bulk_ok = ((uintptr_t)a.src % 16) == 0;
-  const size_t shm = LvShape<T>::SMEM;
+  const size_t shm = LvShape<T>::template smem<SC>();
   level_kernel<T, SC, EN, ET><<<level_grid<T, SC, EN, ET>(a.n), LV_THREADS, shm, st>>>(
       (const T*)a.src, (T*)a.dst, a.n, a.L, a.level, a.base_lvl, a.bits32, a.bit_off, a.chunkpre,
       a.chunkcnt_next, a.znext, a.err, bulk_ok);

@@ -238,7 +238,7 @@ __device__ __forceinline__ uint64_t lb_lookback_warp(uint64_t* status, uint32_t 
   return prefix;
 }
 
-// ------------------------------------------------ select sample marking
+// ------------------------------------------------ bitvector support build
 // Device scalars shared by the bitvector-support build steps.
 enum {
   INF_M1 = 0,   // number of ones
@@ -250,30 +250,6 @@ enum {
   INF_POOL1,    // pool words of select1
   INF_POOL0,
   INF_N = 16
-};
-
-// records the sample (every 64th arg) and superblock-end (arg 4096q+4095)
-// positions among args [K, K+c) that sit in word wi (x = the word's arg mask);
-// samples are indexed samp[samp_dir * (arg / 64)]
-__device__ __forceinline__ void select_marks(uint64_t x, uint32_t c, uint64_t K, uint64_t wi,
-                                             uint64_t* __restrict__ samp, int64_t samp_dir,
-                                             uint64_t* __restrict__ ends) {
-  const uint64_t q = (K + 63) & ~63ull;  // next multiple of 64
-  if (q < K + c) samp[samp_dir * (int64_t)(q >> 6)] = (wi << 6) + sel64(x, (uint32_t)(q - K + 1));
-  const uint64_t e = K | 4095ull;  // next index with e % 4096 == 4095
-  if (e < K + c) ends[e >> 12] = (wi << 6) + sel64(x, (uint32_t)(e - K + 1));
-}
-
-// Outputs a level pass writes when rank/select construction is fused into it.
-struct FuseOut {
-  uint64_t* rank;      // rank_support_v table (null: not built)
-  uint64_t* samples;   // every 64th arg: select1 from the front, select0 back from samp_last
-  uint64_t samp_last;
-  uint64_t* ends1;     // superblock end positions (null: support not built)
-  uint64_t* ends0;
-  unsigned long long* info;
-  uint64_t* lvl_zb;    // zeros of the levels before level l, [L + 1]
-  uint32_t flags;
 };
 
 // ------------------------------------------------------- host-side pieces
@@ -297,6 +273,7 @@ int scan_exclusive_u64(const uint64_t* in, uint64_t* out, uint64_t n, DevBuf& sc
 struct SelectDev {
   uint64_t arg_cnt = 0, nsb = 0, logn = 0, logn4 = 0, has_long = 0, sb_nwords = 0, pool_nwords = 0;
   DevBuf ends;      // superblock end positions (upper-bound sized)
+  DevBuf starts;    // superblock start positions (upper-bound sized)
   DevBuf desc;      // per superblock descriptor
   DevBuf sizes;     // per superblock pool words (scan input)
   DevBuf sb_words;  // packed m_superblock
@@ -311,7 +288,7 @@ struct BvSupport {
   const uint64_t* words = nullptr;  // device
   uint32_t flags = 0;
   DevBuf rank;       // rank_support_v table
-  DevBuf samples;    // every 64th arg: select1 from the front, select0 from the back
+  DevBuf samples;    // every 64th arg, low 32 bits: select1 from the front, select0 from the back
   DevBuf info;       // device scalars (see bitvec.cu)
   DevBuf status;     // look-back status words + tile counter
   DevBuf scan_tmp;
@@ -320,14 +297,11 @@ struct BvSupport {
 
 int bv_build(BvSupport& bv, const uint64_t* d_words, uint64_t size, uint32_t flags, uint32_t* d_err,
              cudaStream_t s);
-// the same in three steps, for builds that produce the pass's outputs
-// themselves (FuseOut): allocate and clear, run the pass, finish the select
-int bv_prepare(BvSupport& bv, const uint64_t* d_words, uint64_t size, uint32_t& flags, cudaStream_t s,
-               FuseOut* out);
+// the same in three steps: allocate and clear, the pass over the bits, and
+// the select structures' finishing kernels
+int bv_prepare(BvSupport& bv, const uint64_t* d_words, uint64_t size, uint32_t& flags, cudaStream_t s);
 int bv_pass(BvSupport& bv, uint32_t* d_err, cudaStream_t s);
 int bv_finish(BvSupport& bv, uint32_t* d_err, cudaStream_t s);
-// totals of a fused build: args and the final rank pair from the zero count
-int bv_fused_totals(BvSupport& bv, const uint64_t* zeros_total, cudaStream_t s);
 void bv_release(BvSupport& bv, cudaStream_t s);
 
 }  // namespace wtg
