@@ -174,6 +174,127 @@ __global__ void __launch_bounds__(BV_THREADS)
   }
 }
 
+// Rank table and select samples of a wavelet tree's concatenated bitvector
+// when n % 512 == 0: superblock b is chunk c of level l (b = l * n/512 + c),
+// and the zeros before it are the zeros of the levels before l (lvl_zb) plus
+// the chunk's prefix within its level (the level passes' chunk counts,
+// scanned) -- no scan over the bits.  Lane per 64-bit word, 8 lanes per
+// superblock, grid-stride over groups of 4 superblocks.
+__global__ void __launch_bounds__(256)
+    rs_levels_kernel(const uint64_t* __restrict__ words, uint64_t W, uint64_t chunks_per_level,
+                     const uint32_t* __restrict__ chunkpre, uint64_t prestride, const uint64_t* __restrict__ lvl_zb,
+                     uint32_t flags, uint64_t* __restrict__ rank, uint32_t* __restrict__ samples, uint64_t samp_last,
+                     uint64_t* __restrict__ starts1, uint64_t* __restrict__ starts0, uint64_t* __restrict__ ends1,
+                     uint64_t* __restrict__ ends0, unsigned long long* info) {
+  const uint32_t lane = threadIdx.x & 31, g8 = lane & 7;
+  const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  const uint64_t ngroups = (W + 31) / 32;
+  uint64_t last1 = 0, last0 = 0;
+  for (uint64_t grp = gw; grp < ngroups; grp += nwarps) {
+    const uint64_t wi = grp * 32 + lane;
+    const bool valid = wi < W;
+    const uint64_t x = valid ? __ldg(&words[wi]) : 0ull;
+    const uint32_t c = __popcll(x);
+    uint32_t inc = c;
+#pragma unroll
+    for (int o = 1; o < 8; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+      if (g8 >= (uint32_t)o) inc += t;
+    }
+    const uint32_t excl = inc - c;
+    const uint64_t b = wi >> 3;
+    const uint64_t l = b / chunks_per_level, ci = b - l * chunks_per_level;
+    const uint64_t zb = valid ? lvl_zb[l] + chunkpre[l * prestride + ci] : 0ull;  // zeros before the superblock
+    const uint64_t sb_before = 512 * b - zb;                                          // ones before it
+    if (flags & WTG_RANK) {
+      uint64_t part = g8 >= 1 ? ((uint64_t)excl << (63 - 9 * g8)) : 0ull;
+#pragma unroll
+      for (int o = 1; o < 8; o <<= 1) part |= __shfl_xor_sync(0xffffffffu, part, o);
+      if (g8 == 0 && valid) {
+        rank[2 * b] = sb_before;
+        rank[2 * b + 1] = part;
+      }
+    }
+    if (valid) {
+      const uint64_t K1 = sb_before + excl;
+      if ((flags & WTG_SELECT1) && c) {
+        select_marks32(x, c, K1, wi, samples, 1, starts1, ends1);
+        last1 = max(last1, (wi << 6) + hi64(x) + 1);
+      }
+      if ((flags & WTG_SELECT0) && c < 64) {
+        const uint64_t z = ~x;
+        select_marks32(z, 64 - c, (wi << 6) - K1, wi, samples + samp_last, -1, starts0, ends0);
+        last0 = max(last0, (wi << 6) + hi64(z) + 1);
+      }
+    }
+  }
+  last1 = warp_max_u64(last1);
+  last0 = warp_max_u64(last0);
+  if (lane == 0) {
+    if (last1) atomicMax(&info[INF_LAST1], (unsigned long long)last1);
+    if (last0) atomicMax(&info[INF_LAST0], (unsigned long long)last0);
+  }
+}
+
+// arg counts and the rank pair after the last superblock, (total, 0)
+// (rank_support_v_par.hpp:95-110 with capacity % 512 == 0)
+__global__ void rs_levels_totals_kernel(const uint64_t* lvl_zb, int L, uint64_t size, uint64_t NB, uint64_t* rank,
+                                        unsigned long long* info) {
+  const uint64_t z = lvl_zb[L];
+  info[INF_M1] = size - z;
+  info[INF_M0] = z;
+  if (rank) {
+    rank[2 * NB] = size - z;
+    rank[2 * NB + 1] = 0;
+  }
+}
+
+// zeros before every level: lvl_zb[l + 1] = lvl_zb[l] + zeros of level l
+__global__ void level_zeros_kernel(const uint32_t* __restrict__ chunkcnt, const uint32_t* __restrict__ chunkpre,
+                                   uint64_t stride, uint64_t nchunks, int L, uint64_t* __restrict__ lvl_zb) {
+  uint64_t acc = 0;
+  lvl_zb[0] = 0;
+  for (int l = 0; l < L; ++l) {
+    acc += (uint64_t)chunkpre[l * stride + nchunks - 1] + chunkcnt[l * stride + nchunks - 1];
+    lvl_zb[l + 1] = acc;
+  }
+}
+
+int bv_from_levels(BvSupport& bv, const uint64_t* d_words, uint64_t n, int L, const uint32_t* chunkcnt,
+                   const uint32_t* chunkpre, uint64_t stride, uint64_t nchunks, uint64_t* lvl_zb, uint32_t flags,
+                   uint32_t* d_err, cudaStream_t s) {
+  int rc;
+  const uint64_t size = n * (uint64_t)L;
+  if ((rc = bv_prepare(bv, d_words, size, flags, s))) return rc;
+  const uint64_t W = size / 64, NB = W >> 3, samp_n = W + 2;
+  level_zeros_kernel<<<1, 1, 0, s>>>(chunkcnt, chunkpre, stride, nchunks, L, lvl_zb);
+  count_launch();
+  WTG_CK(cudaGetLastError());
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  const uint64_t groups = (W + 31) / 32;
+  const unsigned grid = (unsigned)std::min<uint64_t>((groups + 7) / 8, (uint64_t)sms * 8);
+  prof_begin(PROF_BVPASS, s);
+  rs_levels_kernel<<<grid ? grid : 1, 256, 0, s>>>(
+      d_words, W, n / 512, chunkpre, stride, lvl_zb, flags, bv.rank.as<uint64_t>(), bv.samples.as<uint32_t>(),
+      samp_n - 1, bv.sel[1].starts.as<uint64_t>(), bv.sel[0].starts.as<uint64_t>(), bv.sel[1].ends.as<uint64_t>(),
+      bv.sel[0].ends.as<uint64_t>(), bv.info.as<unsigned long long>());
+  prof_end(PROF_BVPASS, s);
+  count_launch();
+  WTG_CK(cudaGetLastError());
+  rs_levels_totals_kernel<<<1, 1, 0, s>>>(lvl_zb, L, size, NB, (flags & WTG_RANK) ? bv.rank.as<uint64_t>() : nullptr,
+                                         bv.info.as<unsigned long long>());
+  count_launch();
+  WTG_CK(cudaGetLastError());
+  return bv_finish(bv, d_err, s);
+}
+
 // per superblock: long/mini choice, width and pool words
 __global__ void select_desc_kernel(int t_b, const uint64_t* __restrict__ starts,
                                    const uint64_t* __restrict__ ends, unsigned long long* info, uint64_t logn4,

@@ -324,7 +324,7 @@ __global__ void __launch_bounds__(LV_THREADS, 4)
     level_kernel(const T* __restrict__ src, T* __restrict__ dst, uint64_t n, int L, int level,
                  const uint2* __restrict__ base_lvl, uint32_t* __restrict__ bits32, uint64_t bit_off,
                  const uint32_t* __restrict__ chunkpre, uint32_t* __restrict__ chunkcnt_next,
-                 uint32_t* __restrict__ znext, uint32_t* err, int bulk_ok) {
+                 uint32_t* __restrict__ znext, uint32_t* err, int bulk_ok, uint32_t* __restrict__ chunkcnt_self) {
   constexpr uint32_t CBYTES = CHUNK * sizeof(T);
   constexpr int LV_STAGES = lv_stages<SCATTER>();
   extern __shared__ __align__(128) unsigned char lv_smem[];
@@ -395,13 +395,17 @@ __global__ void __launch_bounds__(LV_THREADS, 4)
     }
 
     if (!SCATTER) {
-      // last level: bits only
+      // last level: bits only (and, when asked, the chunk's zero count)
+      uint32_t zc = 0;
 #pragma unroll 4
       for (int r = 0; r < WROWS; ++r) {
         const uint32_t k = r * 32 + lane;
-        const uint32_t om = __ballot_sync(0xffffffffu, k < cvalid && bit_of(wt[k], shift));
+        const bool valid = k < cvalid;
+        const uint32_t om = __ballot_sync(0xffffffffu, valid && bit_of(wt[k], shift));
         if (lane == 0) myw[r] = om;
+        zc += __popc(__ballot_sync(0xffffffffu, valid) & ~om);
       }
+      if (chunkcnt_self && lane == 0) chunkcnt_self[c] = zc;
     } else if (uniform && cvalid == CHUNK) {
       // ---- fast path: full chunk inside one node
       if (p0 != cache_p) {
@@ -573,6 +577,7 @@ struct LevelArgs {
   uint32_t* chunkcnt_next;
   uint32_t* znext;
   uint32_t* err;
+  uint32_t* chunkcnt_self;
   bool scatter, emit_nodes, emit_tiles;
 };
 
@@ -582,7 +587,7 @@ static void launch_level_v(const LevelArgs& a, cudaStream_t st) {
   const size_t shm = LvShape<T>::template smem<SC>();
   level_kernel<T, SC, EN, ET><<<level_grid<T, SC, EN, ET>(a.n), LV_THREADS, shm, st>>>(
       (const T*)a.src, (T*)a.dst, a.n, a.L, a.level, a.base_lvl, a.bits32, a.bit_off, a.chunkpre,
-      a.chunkcnt_next, a.znext, a.err, bulk_ok);
+      a.chunkcnt_next, a.znext, a.err, bulk_ok, a.chunkcnt_self);
 }
 
 template <typename T>
@@ -670,9 +675,11 @@ int tree_build(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int L, uint32
 
   // per-level tile zero counts [L x tiles] and their scan (tilepre)
   const uint64_t tiles = n ? (n + tile_elems(eb) - 1) / tile_elems(eb) : 0;
-  if ((rc = t.status.ensure(((uint64_t)L + 1) * (tiles + 1) * sizeof(uint32_t), s))) return rc;
+  // [L + 1][tiles + 1] counts, then [L][tiles + 1] prefixes (kept per level:
+  // the rank/select pass reads them all)
+  if ((rc = t.status.ensure((2 * (uint64_t)L + 1) * (tiles + 1) * sizeof(uint32_t), s))) return rc;
   uint32_t* tilecnt = t.status.as<uint32_t>();
-  uint32_t* tilepre = tilecnt + (uint64_t)L * (tiles + 1);
+  uint32_t* tilepre_all = tilecnt + ((uint64_t)L + 1) * (tiles + 1);
   if (n) WTG_CK(cudaMemsetAsync(tilecnt, 0, (uint64_t)L * (tiles + 1) * sizeof(uint32_t), s));
 
   if (n) {
@@ -699,7 +706,9 @@ int tree_build(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int L, uint32
   }
 
   // level passes; each scattering pass feeds the next level's chunk counts
-  // and (from level K on) its node tables
+  // and (from level K on) its node tables.  With n % 512 == 0 the chunk
+  // counts of every level also give the rank/select pass its prefixes.
+  const bool rs_from_levels = flags && n > 0 && (n % CHUNK) == 0;
   if (n) {
     if (L > 1) {
       if ((rc = t.lvl[0].ensure(n * eb + 16, s))) return rc;
@@ -719,8 +728,10 @@ int tree_build(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int L, uint32
       a.base_lvl = base + ((1ull << l) - 1);
       a.bits32 = t.bits.as<uint32_t>();
       a.bit_off = (uint64_t)l * n;
+      uint32_t* tilepre = tilepre_all + (uint64_t)l * (tiles + 1);
       a.chunkpre = tilepre;
       a.chunkcnt_next = tilecnt + (uint64_t)(l + 1) * (tiles + 1);
+      a.chunkcnt_self = (!a.scatter && rs_from_levels) ? tilecnt + (uint64_t)l * (tiles + 1) : nullptr;
       a.znext = Z + ((1ull << (l + 1)) - 1);
       a.err = d_err;
       if (a.scatter)
@@ -749,7 +760,15 @@ int tree_build(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int L, uint32
   }
 
   // rank / select over the concatenated bitvector
-  if (flags) {
+  if (rs_from_levels) {
+    uint32_t* last_cnt = tilecnt + (uint64_t)(L - 1) * (tiles + 1);
+    uint32_t* last_pre = tilepre_all + (uint64_t)(L - 1) * (tiles + 1);
+    if ((rc = scan_exclusive_u32(last_cnt, last_pre, tiles, t.scan_tmp, d_err, s))) return rc;
+    if ((rc = t.scratch.ensure(((uint64_t)L + 1) * sizeof(uint64_t), s))) return rc;
+    if ((rc = bv_from_levels(t.bv, t.bits.as<uint64_t>(), n, L, tilecnt, tilepre_all, tiles + 1, tiles,
+                             t.scratch.as<uint64_t>(), flags, d_err, s)))
+      return rc;
+  } else if (flags) {
     if ((rc = bv_build(t.bv, t.bits.as<uint64_t>(), n * (uint64_t)L, flags, d_err, s))) return rc;
   }
   return WTG_OK;

@@ -302,6 +302,12 @@ int bv_build(BvSupport& bv, const uint64_t* d_words, uint64_t size, uint32_t fla
 int bv_prepare(BvSupport& bv, const uint64_t* d_words, uint64_t size, uint32_t& flags, cudaStream_t s);
 int bv_pass(BvSupport& bv, uint32_t* d_err, cudaStream_t s);
 int bv_finish(BvSupport& bv, uint32_t* d_err, cudaStream_t s);
+// for a wavelet tree's bits with n % 512 == 0: the same structures from the
+// level passes' per-chunk zero counts (chunkcnt) and their scans (chunkpre),
+// both [L][stride]; lvl_zb receives L + 1 words
+int bv_from_levels(BvSupport& bv, const uint64_t* d_words, uint64_t n, int L, const uint32_t* chunkcnt,
+                   const uint32_t* chunkpre, uint64_t stride, uint64_t nchunks, uint64_t* lvl_zb, uint32_t flags,
+                   uint32_t* d_err, cudaStream_t s);
 void bv_release(BvSupport& bv, cudaStream_t s);
 
 }  // namespace wtg
