@@ -34,20 +34,44 @@ __device__ __forceinline__ uint64_t warp_max_u64(uint64_t v) {
   return v;
 }
 
-// records, among args [K, K+c) in word wi (x = its arg mask): every 64th
-// arg's position (low 32 bits) in samp[samp_dir * (arg / 64)], the start of
-// every superblock (arg 4096q) and its end (arg 4096q + 4095)
-__device__ __forceinline__ void select_marks32(uint64_t x, uint32_t c, uint64_t K, uint64_t wi,
-                                               uint32_t* __restrict__ samp, int64_t samp_dir,
-                                               uint64_t* __restrict__ starts, uint64_t* __restrict__ ends) {
-  const uint64_t q = (K + 63) & ~63ull;  // next multiple of 64
-  if (q < K + c) {
-    const uint64_t pos = (wi << 6) + sel64(x, (uint32_t)(q - K + 1));
-    samp[samp_dir * (int64_t)(q >> 6)] = (uint32_t)pos;
-    if ((q & 4095) == 0) starts[q >> 12] = pos;
+// Select marks of one 64-bit word wi, given K1 = ones before it: for
+// select1 (x) and select0 (~x) the position of every 64th arg (low 32 bits,
+// samp[dir * (arg / 64)]), every superblock start (arg 4096q) and end (arg
+// 4096q + 4095).  The next multiple of 64 is (-K) & 63 args into the word
+// (for zeros, K0 = 64 wi - K1, so K1 & 63); one branch-free select per
+// support and word, stores predicated.  zmask clears bits past the end.
+__device__ __forceinline__ void word_marks(uint64_t x, uint32_t c, uint64_t K1, uint64_t wi, uint64_t zmask,
+                                           bool sel1, bool sel0, uint32_t* __restrict__ samples, uint64_t samp_last,
+                                           uint64_t* __restrict__ starts1, uint64_t* __restrict__ starts0,
+                                           uint64_t* __restrict__ ends1, uint64_t* __restrict__ ends0,
+                                           uint64_t& last1, uint64_t& last0) {
+  if (sel1 && c) {
+    const uint32_t d = (uint32_t)(0u - (uint32_t)K1) & 63u;
+    const uint64_t pos = (wi << 6) + sel64_0(x, d & 63u);
+    if (d < c) {
+      const uint64_t k = K1 + d;
+      samples[k >> 6] = (uint32_t)pos;
+      if ((k & 4095) == 0) starts1[k >> 12] = pos;
+    }
+    const uint32_t e = 4095u - ((uint32_t)K1 & 4095u);
+    if (e < c) ends1[(K1 + e) >> 12] = (wi << 6) + sel64_0(x, e);
+    last1 = max(last1, (wi << 6) + hi64(x) + 1);
   }
-  const uint64_t e = K | 4095ull;  // next index with e % 4096 == 4095
-  if (e < K + c) ends[e >> 12] = (wi << 6) + sel64(x, (uint32_t)(e - K + 1));
+  const uint64_t z = ~x & zmask;
+  const uint32_t cz = __popcll(z);
+  if (sel0 && cz) {
+    const uint64_t K0 = (wi << 6) - K1;
+    const uint32_t d = (uint32_t)K1 & 63u;  // == (-K0) & 63
+    const uint64_t pos = (wi << 6) + sel64_0(z, d);
+    if (d < cz) {
+      const uint64_t k = K0 + d;
+      samples[samp_last - (k >> 6)] = (uint32_t)pos;
+      if ((k & 4095) == 0) starts0[k >> 12] = pos;
+    }
+    const uint32_t e = 4095u - ((uint32_t)K0 & 4095u);
+    if (e < cz) ends0[(K0 + e) >> 12] = (wi << 6) + sel64_0(z, e);
+    last0 = max(last0, (wi << 6) + hi64(z) + 1);
+  }
 }
 
 // One pass over the bitvector: lane per 64-bit word, 8 lanes per 512-bit
@@ -150,21 +174,9 @@ __global__ void __launch_bounds__(BV_THREADS)
       info[INF_M1] = sb_before + sbt;
       info[INF_M0] = size - (sb_before + sbt);
     }
-    if (wi < W) {
-      const uint64_t K1 = sb_before + excl;  // ones before this word
-      if ((flags & WTG_SELECT1) && c[j]) {
-        select_marks32(w[j], c[j], K1, wi, samples, 1, starts1, ends1);
-        last1 = max(last1, (wi << 6) + hi64(w[j]) + 1);
-      }
-      if (flags & WTG_SELECT0) {
-        const uint64_t z = (wi == W - 1) ? (~w[j] & tailmask) : ~w[j];
-        const uint32_t cz = __popcll(z);
-        if (cz) {
-          select_marks32(z, cz, (wi << 6) - K1, wi, samples + samp_last, -1, starts0, ends0);
-          last0 = max(last0, (wi << 6) + hi64(z) + 1);
-        }
-      }
-    }
+    if (wi < W)
+      word_marks(w[j], c[j], sb_before + excl, wi, wi == W - 1 ? tailmask : ~0ull, flags & WTG_SELECT1,
+                 flags & WTG_SELECT0, samples, samp_last, starts1, starts0, ends1, ends0, last1, last0);
   }
   last1 = warp_max_u64(last1);
   last0 = warp_max_u64(last0);
@@ -216,18 +228,9 @@ __global__ void __launch_bounds__(256)
         rank[2 * b + 1] = part;
       }
     }
-    if (valid) {
-      const uint64_t K1 = sb_before + excl;
-      if ((flags & WTG_SELECT1) && c) {
-        select_marks32(x, c, K1, wi, samples, 1, starts1, ends1);
-        last1 = max(last1, (wi << 6) + hi64(x) + 1);
-      }
-      if ((flags & WTG_SELECT0) && c < 64) {
-        const uint64_t z = ~x;
-        select_marks32(z, 64 - c, (wi << 6) - K1, wi, samples + samp_last, -1, starts0, ends0);
-        last0 = max(last0, (wi << 6) + hi64(z) + 1);
-      }
-    }
+    if (valid)
+      word_marks(x, c, sb_before + excl, wi, ~0ull, flags & WTG_SELECT1, flags & WTG_SELECT0, samples, samp_last,
+                 starts1, starts0, ends1, ends0, last1, last0);
   }
   last1 = warp_max_u64(last1);
   last0 = warp_max_u64(last0);

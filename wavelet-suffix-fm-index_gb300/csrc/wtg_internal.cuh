@@ -63,25 +63,30 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
   return m;
 }
 
-// position of the i-th (1-based) set bit of x (bits::sel semantics); i <= popc(x)
-__device__ __forceinline__ uint32_t sel64(uint64_t x, uint32_t i) {
-  uint32_t lo = __popc((uint32_t)x);
-  uint32_t base = 0;
-  uint32_t w = (uint32_t)x;
-  if (i > lo) { i -= lo; w = (uint32_t)(x >> 32); base = 32; }
-  // binary search over the 32-bit half
+// position of the r-th (0-based) set bit of x, r < popc(x); branch-free
+// halving search over popcounts
+__device__ __forceinline__ uint32_t sel64_0(uint64_t x, uint32_t r) {
+  const uint32_t lo = (uint32_t)x, hi = (uint32_t)(x >> 32);
+  const uint32_t cl = __popc(lo);
+  uint32_t up = r >= cl;
+  uint32_t w = up ? hi : lo;
+  r -= up ? cl : 0u;
+  uint32_t pos = up << 5;
   uint32_t c = __popc(w & 0xFFFFu);
-  if (i > c) { i -= c; w >>= 16; base += 16; }
+  up = r >= c; w = up ? w >> 16 : w; r -= up ? c : 0u; pos += up << 4;
   c = __popc(w & 0xFFu);
-  if (i > c) { i -= c; w >>= 8; base += 8; }
+  up = r >= c; w = up ? w >> 8 : w; r -= up ? c : 0u; pos += up << 3;
   c = __popc(w & 0xFu);
-  if (i > c) { i -= c; w >>= 4; base += 4; }
+  up = r >= c; w = up ? w >> 4 : w; r -= up ? c : 0u; pos += up << 2;
   c = __popc(w & 0x3u);
-  if (i > c) { i -= c; w >>= 2; base += 2; }
+  up = r >= c; w = up ? w >> 2 : w; r -= up ? c : 0u; pos += up << 1;
   c = w & 1u;
-  if (i > c) { base += 1; }
-  return base;
+  pos += (r >= c) ? 1u : 0u;
+  return pos;
 }
+
+// position of the i-th (1-based) set bit of x (bits::sel semantics); i <= popc(x)
+__device__ __forceinline__ uint32_t sel64(uint64_t x, uint32_t i) { return sel64_0(x, i - 1); }
 
 // sdsl bits::hi (0 for x == 0)
 __host__ __device__ __forceinline__ uint32_t hi64(uint64_t x) {
