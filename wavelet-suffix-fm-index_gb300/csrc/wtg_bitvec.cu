@@ -193,7 +193,7 @@ __global__ void __launch_bounds__(BV_THREADS)
 // scanned) -- no scan over the bits.  Lane per 64-bit word, 8 lanes per
 // superblock, grid-stride over groups of 4 superblocks.
 __global__ void __launch_bounds__(256)
-    rs_levels_kernel(const uint64_t* __restrict__ words, uint64_t W, uint64_t chunks_per_level,
+    rs_levels_kernel(const uint64_t* __restrict__ words, int L, uint64_t chunks_per_level,
                      const uint32_t* __restrict__ chunkpre, uint64_t prestride, const uint64_t* __restrict__ lvl_zb,
                      uint32_t flags, uint64_t* __restrict__ rank, uint32_t* __restrict__ samples, uint64_t samp_last,
                      uint64_t* __restrict__ starts1, uint64_t* __restrict__ starts0, uint64_t* __restrict__ ends1,
@@ -201,36 +201,42 @@ __global__ void __launch_bounds__(256)
   const uint32_t lane = threadIdx.x & 31, g8 = lane & 7;
   const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-  const uint64_t ngroups = (W + 31) / 32;
+  const uint64_t lw = chunks_per_level * 8;  // words per level
+  const uint64_t ngroups = (lw + 31) / 32;   // groups of 32 words (4 superblocks) per level
   uint64_t last1 = 0, last0 = 0;
-  for (uint64_t grp = gw; grp < ngroups; grp += nwarps) {
-    const uint64_t wi = grp * 32 + lane;
-    const bool valid = wi < W;
-    const uint64_t x = valid ? __ldg(&words[wi]) : 0ull;
-    const uint32_t c = __popcll(x);
-    uint32_t inc = c;
+  for (int l = 0; l < L; ++l) {
+    const uint64_t zl = lvl_zb[l];
+    const uint32_t* __restrict__ pre = chunkpre + (uint64_t)l * prestride;
+    const uint64_t w0 = (uint64_t)l * lw;
+    for (uint64_t grp = gw; grp < ngroups; grp += nwarps) {
+      const uint64_t lwi = grp * 32 + lane;  // word within the level
+      const bool valid = lwi < lw;
+      const uint64_t wi = w0 + lwi;
+      const uint64_t x = valid ? __ldg(&words[wi]) : 0ull;
+      const uint32_t c = __popcll(x);
+      uint32_t inc = c;
 #pragma unroll
-    for (int o = 1; o < 8; o <<= 1) {
-      const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
-      if (g8 >= (uint32_t)o) inc += t;
-    }
-    const uint32_t excl = inc - c;
-    const uint64_t b = wi >> 3;
-    const uint64_t l = b / chunks_per_level, ci = b - l * chunks_per_level;
-    const uint64_t zb = valid ? lvl_zb[l] + chunkpre[l * prestride + ci] : 0ull;  // zeros before the superblock
-    const uint64_t sb_before = 512 * b - zb;                                          // ones before it
-    if (flags & WTG_RANK) {
-      uint64_t part = g8 >= 1 ? ((uint64_t)excl << (63 - 9 * g8)) : 0ull;
-#pragma unroll
-      for (int o = 1; o < 8; o <<= 1) part |= __shfl_xor_sync(0xffffffffu, part, o);
-      if (g8 == 0 && valid) {
-        rank[2 * b] = sb_before;
-        rank[2 * b + 1] = part;
+      for (int o = 1; o < 8; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (g8 >= (uint32_t)o) inc += t;
       }
+      const uint32_t excl = inc - c;
+      const uint64_t ci = lwi >> 3;  // chunk (superblock) within the level
+      const uint64_t b = wi >> 3;
+      const uint64_t sb_before = 512 * b - (valid ? zl + pre[ci] : 0ull);  // ones before the superblock
+      if (flags & WTG_RANK) {
+        uint64_t part = g8 >= 1 ? ((uint64_t)excl << (63 - 9 * g8)) : 0ull;
+#pragma unroll
+        for (int o = 1; o < 8; o <<= 1) part |= __shfl_xor_sync(0xffffffffu, part, o);
+        if (g8 == 0 && valid) {
+          rank[2 * b] = sb_before;
+          rank[2 * b + 1] = part;
+        }
+      }
+      if (valid)
+        word_marks(x, c, sb_before + excl, wi, ~0ull, flags & WTG_SELECT1, flags & WTG_SELECT0, samples, samp_last,
+                   starts1, starts0, ends1, ends0, last1, last0);
     }
-    if (valid)
-      word_marks(x, c, sb_before + excl, wi, ~0ull, flags & WTG_SELECT1, flags & WTG_SELECT0, samples, samp_last,
-                 starts1, starts0, ends1, ends0, last1, last0);
   }
   last1 = warp_max_u64(last1);
   last0 = warp_max_u64(last0);
@@ -285,7 +291,7 @@ int bv_from_levels(BvSupport& bv, const uint64_t* d_words, uint64_t n, int L, co
   const unsigned grid = (unsigned)std::min<uint64_t>((groups + 7) / 8, (uint64_t)sms * 8);
   prof_begin(PROF_BVPASS, s);
   rs_levels_kernel<<<grid ? grid : 1, 256, 0, s>>>(
-      d_words, W, n / 512, chunkpre, stride, lvl_zb, flags, bv.rank.as<uint64_t>(), bv.samples.as<uint32_t>(),
+      d_words, L, n / 512, chunkpre, stride, lvl_zb, flags, bv.rank.as<uint64_t>(), bv.samples.as<uint32_t>(),
       samp_n - 1, bv.sel[1].starts.as<uint64_t>(), bv.sel[0].starts.as<uint64_t>(), bv.sel[1].ends.as<uint64_t>(),
       bv.sel[0].ends.as<uint64_t>(), bv.info.as<unsigned long long>());
   prof_end(PROF_BVPASS, s);

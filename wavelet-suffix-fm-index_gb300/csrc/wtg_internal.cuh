@@ -108,18 +108,27 @@ __device__ __forceinline__ uint64_t packed_get(const uint64_t* __restrict__ word
 }
 
 // output word q of an int_vector<0> of width w whose entries are given by f(j)
-// (entries j >= count are zero)
+// (entries j >= count are zero); 32-bit offsets while the bit position fits
 template <typename F>
 __device__ __forceinline__ uint64_t packed_word(uint64_t q, uint32_t w, uint64_t count, F f) {
-  uint64_t lo = q * 64, hi = lo + 63;
-  uint64_t j0 = lo / w, j1 = hi / w;
+  const uint64_t mask = w < 64 ? ((1ull << w) - 1) : ~0ull;
   uint64_t out = 0;
-  uint64_t mask = w < 64 ? ((1ull << w) - 1) : ~0ull;
+  if (q < (1ull << 25)) {  // q*64 + 63 < 2^31
+    const uint32_t lo = (uint32_t)q * 64, hi = lo + 63;
+    const uint32_t j0 = lo / w, j1 = hi / w;
+    for (uint32_t j = j0; j <= j1 && j < count; ++j) {
+      const uint64_t v = f((uint64_t)j) & mask;
+      const int32_t sh = (int32_t)(j * w) - (int32_t)lo;
+      out |= sh >= 0 ? (v << sh) : (v >> (-sh));
+    }
+    return out;
+  }
+  const uint64_t lo = q * 64, hi = lo + 63;
+  const uint64_t j0 = lo / w, j1 = hi / w;
   for (uint64_t j = j0; j <= j1 && j < count; ++j) {
-    uint64_t v = f(j) & mask;
-    int64_t sh = (int64_t)(j * w) - (int64_t)lo;
-    if (sh >= 0) out |= v << sh;
-    else out |= v >> (-sh);
+    const uint64_t v = f(j) & mask;
+    const int64_t sh = (int64_t)(j * w) - (int64_t)lo;
+    out |= sh >= 0 ? (v << sh) : (v >> (-sh));
   }
   return out;
 }
