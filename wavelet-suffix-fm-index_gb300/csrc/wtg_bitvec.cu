@@ -192,6 +192,8 @@ __global__ void __launch_bounds__(BV_THREADS)
 // the chunk's prefix within its level (the level passes' chunk counts,
 // scanned) -- no scan over the bits.  Lane per 64-bit word, 8 lanes per
 // superblock, grid-stride over groups of 4 superblocks.
+constexpr int RS_U = 4;  // 32-word groups per warp step
+
 __global__ void __launch_bounds__(256)
     rs_levels_kernel(const uint64_t* __restrict__ words, int L, uint64_t chunks_per_level,
                      const uint32_t* __restrict__ chunkpre, uint64_t prestride, const uint64_t* __restrict__ lvl_zb,
@@ -208,34 +210,46 @@ __global__ void __launch_bounds__(256)
     const uint64_t zl = lvl_zb[l];
     const uint32_t* __restrict__ pre = chunkpre + (uint64_t)l * prestride;
     const uint64_t w0 = (uint64_t)l * lw;
-    for (uint64_t grp = gw; grp < ngroups; grp += nwarps) {
-      const uint64_t lwi = grp * 32 + lane;  // word within the level
-      const bool valid = lwi < lw;
-      const uint64_t wi = w0 + lwi;
-      const uint64_t x = valid ? __ldg(&words[wi]) : 0ull;
-      const uint32_t c = __popcll(x);
-      uint32_t inc = c;
+    // a warp takes RS_U consecutive groups per step, all loads issued first
+    for (uint64_t grp = gw * RS_U; grp < ngroups; grp += nwarps * RS_U) {
+      uint64_t xs[RS_U];
+      uint32_t pres[RS_U];
 #pragma unroll
-      for (int o = 1; o < 8; o <<= 1) {
-        const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
-        if (g8 >= (uint32_t)o) inc += t;
+      for (int u = 0; u < RS_U; ++u) {
+        const uint64_t lwi = (grp + u) * 32 + lane;
+        const bool valid = lwi < lw;
+        xs[u] = valid ? __ldg(&words[w0 + lwi]) : 0ull;
+        pres[u] = valid ? __ldg(&pre[lwi >> 3]) : 0u;
       }
-      const uint32_t excl = inc - c;
-      const uint64_t ci = lwi >> 3;  // chunk (superblock) within the level
-      const uint64_t b = wi >> 3;
-      const uint64_t sb_before = 512 * b - (valid ? zl + pre[ci] : 0ull);  // ones before the superblock
-      if (flags & WTG_RANK) {
-        uint64_t part = g8 >= 1 ? ((uint64_t)excl << (63 - 9 * g8)) : 0ull;
 #pragma unroll
-        for (int o = 1; o < 8; o <<= 1) part |= __shfl_xor_sync(0xffffffffu, part, o);
-        if (g8 == 0 && valid) {
-          rank[2 * b] = sb_before;
-          rank[2 * b + 1] = part;
+      for (int u = 0; u < RS_U; ++u) {
+        const uint64_t lwi = (grp + u) * 32 + lane;  // word within the level
+        const bool valid = lwi < lw;
+        const uint64_t wi = w0 + lwi;
+        const uint64_t x = xs[u];
+        const uint32_t c = __popcll(x);
+        uint32_t inc = c;
+#pragma unroll
+        for (int o = 1; o < 8; o <<= 1) {
+          const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+          if (g8 >= (uint32_t)o) inc += t;
         }
+        const uint32_t excl = inc - c;
+        const uint64_t b = wi >> 3;
+        const uint64_t sb_before = 512 * b - (zl + pres[u]);  // ones before the superblock
+        if (flags & WTG_RANK) {
+          uint64_t part = g8 >= 1 ? ((uint64_t)excl << (63 - 9 * g8)) : 0ull;
+#pragma unroll
+          for (int o = 1; o < 8; o <<= 1) part |= __shfl_xor_sync(0xffffffffu, part, o);
+          if (g8 == 0 && valid) {
+            rank[2 * b] = sb_before;
+            rank[2 * b + 1] = part;
+          }
+        }
+        if (valid)
+          word_marks(x, c, sb_before + excl, wi, ~0ull, flags & WTG_SELECT1, flags & WTG_SELECT0, samples,
+                     samp_last, starts1, starts0, ends1, ends0, last1, last0);
       }
-      if (valid)
-        word_marks(x, c, sb_before + excl, wi, ~0ull, flags & WTG_SELECT1, flags & WTG_SELECT0, samples, samp_last,
-                   starts1, starts0, ends1, ends0, last1, last0);
     }
   }
   last1 = warp_max_u64(last1);
@@ -288,7 +302,7 @@ int bv_from_levels(BvSupport& bv, const uint64_t* d_words, uint64_t n, int L, co
     if (sms <= 0) sms = 1;
   }
   const uint64_t groups = (W + 31) / 32;
-  const unsigned grid = (unsigned)std::min<uint64_t>((groups + 7) / 8, (uint64_t)sms * 8);
+  const unsigned grid = (unsigned)std::min<uint64_t>((groups + 8 * RS_U - 1) / (8 * RS_U), (uint64_t)sms * 8);
   prof_begin(PROF_BVPASS, s);
   rs_levels_kernel<<<grid ? grid : 1, 256, 0, s>>>(
       d_words, L, n / 512, chunkpre, stride, lvl_zb, flags, bv.rank.as<uint64_t>(), bv.samples.as<uint32_t>(),
