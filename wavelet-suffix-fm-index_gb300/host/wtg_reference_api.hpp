@@ -1,0 +1,234 @@
+// wtg_reference_api.hpp -- the reference's C++ interface for the
+// wavelet-tree path, backed by libwtg (include/wtg.h).
+//
+// Header-only.  Include it instead of compiling wavelet/levelWT/WT.C (or
+// ddWT/recWT/serialWT) and instead of the rank/select/wt_int "_par" headers;
+// link with -lwtg.  Names, argument meaning and ownership follow the
+// reference:
+//   * WT(symbol* s, uintT n, uintT sigma) -> pair<WTnode*, long*>
+//     (wavelet/levelWT/WT.h:30-43): outputs are malloc'ed, freed by the caller
+//     with free() (levelWT/WTTime.C:99,135); `symbol`, `uintT` and the WTnode
+//     field width follow the same -DINT / -DLONG knobs (parallel.h:71-81).
+//   * wtg::wt_int (sdsl::wt_int<>, wt_int/wt_int_par.hpp:368-660): operator[],
+//     rank, inverse_select, select, size, sigma-free; std::logic_error where
+//     the reference throws one (wt_int_par.hpp:377,645).
+//   * wtg::rank_support_v / wtg::select_support_mcl<t_b>
+//     (rank/rank_support_v_par.hpp:69-142, select/select_support_mcl_par.hpp:
+//     120-129,564-611) over a bit vector given as 64-bit words.
+// Every call runs on the current CUDA device; failures other than the
+// reference's own exceptions raise std::runtime_error with wtg_last_error().
+#pragma once
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/wtg.h"
+
+#ifndef WTG_NO_REFERENCE_TYPES
+#if defined(LONG)
+typedef unsigned long uintT;
+#else
+typedef unsigned int uintT;
+#endif
+#ifdef INT
+typedef uintT symbol;
+#else
+typedef unsigned char symbol;
+#endif
+typedef uintT intOffset;
+struct WTnode {
+  intOffset bitmapPtr;
+  uintT length;
+  uintT parent, leftChild, rightChild;
+};
+#endif
+
+namespace wtg {
+
+inline void check(int rc) {
+  if (rc != WTG_OK) throw std::runtime_error(std::string("wtg: ") + wtg_last_error());
+}
+
+// max(1, log2Up(sigma)) (wavelet/levelWT/WT.C:96)
+inline int levels_for_sigma(uint64_t sigma) {
+  int a = 0;
+  for (uint64_t b = sigma - 1; b > 0; b >>= 1) ++a;
+  return a < 1 ? 1 : a;
+}
+
+// Owning handle of a GPU-built tree.
+class tree {
+ public:
+  tree() = default;
+  tree(const void* seq, uint64_t n, int elem_bytes, int levels, uint32_t flags) {
+    check(wtg_tree_build(seq, n, elem_bytes, levels, flags, &t_));
+    check(wtg_tree_info(t_, info_));
+  }
+  tree(const tree&) = delete;
+  tree& operator=(const tree&) = delete;
+  tree(tree&& o) noexcept : t_(o.t_) {
+    std::memcpy(info_, o.info_, sizeof(info_));
+    o.t_ = nullptr;
+  }
+  tree& operator=(tree&& o) noexcept {
+    if (this != &o) {
+      wtg_tree_free(t_);
+      t_ = o.t_;
+      std::memcpy(info_, o.info_, sizeof(info_));
+      o.t_ = nullptr;
+    }
+    return *this;
+  }
+  ~tree() { wtg_tree_free(t_); }
+  wtg_tree* get() const { return t_; }
+  uint64_t n() const { return info_[0]; }
+  int levels() const { return (int)info_[1]; }
+  uint64_t bit_words() const { return info_[2]; }
+  uint64_t rank_words() const { return info_[3]; }
+
+ private:
+  wtg_tree* t_ = nullptr;
+  uint64_t info_[4] = {0, 0, 0, 0};
+};
+
+// sdsl::wt_int<> (wt_int/wt_int_par.hpp): level bits, rank_support_v and
+// select_support_mcl<1>/<0> over them, built on the GPU.
+class wt_int {
+ public:
+  typedef uint64_t size_type;
+  typedef uint64_t value_type;
+  wt_int() = default;
+  // wt_int(buf, size, max_level) (wt_int_par.hpp:368-406); max_level 0 derives
+  // hi(max(1, max symbol)) + 1
+  template <typename T>
+  wt_int(const std::vector<T>& buf, size_type size, uint32_t max_level = 0) {
+    if (buf.size() < size)
+      throw std::logic_error("n=" + std::to_string(buf.size()) + " < " + std::to_string(size) + "=m_size");
+    if (size) t_ = tree(buf.data(), size, (int)sizeof(T), (int)max_level, WTG_ALL);
+  }
+  size_type size() const { return t_.n(); }
+  bool empty() const { return size() == 0; }
+  uint32_t max_level() const { return (uint32_t)t_.levels(); }
+
+  value_type operator[](size_type i) const {
+    uint64_t out = 0;
+    check(wtg_query_access(t_.get(), &i, 1, &out));
+    return out;
+  }
+  size_type rank(size_type i, value_type c) const {
+    uint64_t out = 0;
+    check(wtg_query_rank(t_.get(), &i, &c, 1, &out));
+    return out;
+  }
+  std::pair<size_type, value_type> inverse_select(size_type i) const {
+    uint64_t r = 0, c = 0;
+    check(wtg_query_inverse_select(t_.get(), &i, 1, &r, &c));
+    return std::make_pair(r, c);
+  }
+  size_type select(size_type i, value_type c) const {
+    uint64_t out = 0;
+    check(wtg_query_select(t_.get(), &i, &c, 1, &out));
+    if (out == ~0ull)
+      throw std::logic_error("select(" + std::to_string(i) + "," + std::to_string(c) +
+                             "): c does not occur i times in the WT");
+    return out;
+  }
+  // batched forms (one kernel launch for many queries)
+  void access(const uint64_t* idx, uint64_t nq, uint64_t* out) const {
+    check(wtg_query_access(t_.get(), idx, nq, out));
+  }
+  void rank(const uint64_t* idx, const uint64_t* sym, uint64_t nq, uint64_t* out) const {
+    check(wtg_query_rank(t_.get(), idx, sym, nq, out));
+  }
+  // the concatenated level bitvector (wt_int::tree, wt_int_par.hpp:80,290)
+  std::vector<uint64_t> tree_words() const {
+    std::vector<uint64_t> w(t_.bit_words());
+    check(wtg_tree_get_bits(t_.get(), w.data(), w.size()));
+    return w;
+  }
+
+ private:
+  tree t_;
+};
+
+// rank_support_v<1> over a bit vector (rank/rank_support_v_par.hpp:69-142).
+class rank_support_v {
+ public:
+  rank_support_v(const uint64_t* words, uint64_t size_bits) {
+    check(wtg_bv_build(words, size_bits, WTG_RANK, &b_));
+  }
+  rank_support_v(const rank_support_v&) = delete;
+  rank_support_v& operator=(const rank_support_v&) = delete;
+  ~rank_support_v() { wtg_bv_free(b_); }
+  uint64_t rank(uint64_t idx) const {
+    uint64_t out = 0;
+    check(wtg_bv_rank(b_, &idx, 1, &out));
+    return out;
+  }
+  uint64_t operator()(uint64_t idx) const { return rank(idx); }
+  // m_basic_block in the reference layout
+  std::vector<uint64_t> basic_block() const {
+    uint64_t nw = 0;
+    check(wtg_bv_rank_words(b_, &nw));
+    std::vector<uint64_t> t(nw);
+    check(wtg_bv_get_rank(b_, t.data(), nw));
+    return t;
+  }
+
+ private:
+  wtg_bv* b_ = nullptr;
+};
+
+// select_support_mcl<t_b> over a bit vector (select/select_support_mcl_par.hpp).
+template <uint8_t t_b = 1>
+class select_support_mcl {
+ public:
+  select_support_mcl(const uint64_t* words, uint64_t size_bits) {
+    check(wtg_bv_build(words, size_bits, t_b ? WTG_SELECT1 : WTG_SELECT0, &b_));
+  }
+  select_support_mcl(const select_support_mcl&) = delete;
+  select_support_mcl& operator=(const select_support_mcl&) = delete;
+  ~select_support_mcl() { wtg_bv_free(b_); }
+  // select(i), 1 <= i <= number of args (select_support_mcl_par.hpp:564-611)
+  uint64_t select(uint64_t i) const {
+    uint64_t out = 0;
+    check(wtg_bv_select(b_, t_b, &i, 1, &out));
+    return out;
+  }
+  uint64_t operator()(uint64_t i) const { return select(i); }
+  uint64_t arg_cnt() const {
+    uint64_t info[8];
+    check(wtg_bv_select_info(b_, t_b, info));
+    return info[1];
+  }
+
+ private:
+  wtg_bv* b_ = nullptr;
+};
+
+}  // namespace wtg
+
+#ifndef WTG_NO_REFERENCE_TYPES
+// levelWT's WT() (wavelet/levelWT/WT.h:43, WT.C:86-270): the level-concatenated
+// bitvector of ceil(n*levels/64) words and 2*sigma WTnode records, both
+// malloc'ed; the caller frees them with free().
+inline std::pair<WTnode*, long*> WT(symbol* s, uintT n, uintT sigma) {
+  const int levels = wtg::levels_for_sigma(sigma);
+  wtg::tree t(s, n, (int)sizeof(symbol), levels, 0);
+  const uint64_t nw = t.bit_words();
+  long* wt = (long*)std::malloc(sizeof(long) * (nw ? nw : 1));
+  WTnode* nodes = (WTnode*)std::malloc(sizeof(WTnode) * 2 * (size_t)sigma);
+  if (!wt || !nodes) {
+    std::free(wt);
+    std::free(nodes);
+    throw std::bad_alloc();
+  }
+  wtg::check(wtg_tree_get_bits(t.get(), (uint64_t*)wt, nw));
+  wtg::check(wtg_tree_get_nodes(t.get(), (int)sizeof(uintT), 2 * (uint64_t)sigma, nodes));
+  return std::make_pair(nodes, wt);
+}
+#endif
