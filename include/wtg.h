@@ -146,6 +146,21 @@ int wtg_bv_select(wtg_bv* b, int t_b, const uint64_t* i, uint64_t nq, uint64_t* 
 int wtg_bv_select_device(wtg_bv* b, int t_b, const uint64_t* d_i, uint64_t nq, uint64_t* d_out,
                          void* stream);
 
+/* Allocation-free rank table build.  No counterpart in the reference: an
+ * addition for callers that cannot allocate device memory -- code that runs
+ * inside a memory budget owned by another framework, or in a phase where a
+ * cudaMalloc would synchronise the device or is forbidden by the pool in use.
+ * Builds the same rank_support_v<1> table as wtg_bv_build (WTG_RANK) from
+ * d_words (size_bits bits, device memory) into d_rank (((capacity>>9)+1)*2
+ * words, device memory), on `stream`, and waits for it.  It calls no
+ * cudaMalloc/cudaFree: its scratch is one fixed device array inside the
+ * library (about 1 MB, held on every GPU that loads the library until exit),
+ * which limits size_bits to 2^34; larger inputs return WTG_ERR_RANGE.  The
+ * first call on a device looks up that array's device address (make it
+ * before any stream capture).  All calls share the array, so calls that
+ * overlap on the GPU (other threads or streams) race. */
+int wtg_rank_build_noalloc(const uint64_t* d_words, uint64_t size_bits, uint64_t* d_rank, void* stream);
+
 /* ------------------------------------------------------------ profiling
  * When enabled, every build records a CUDA event pair around each kernel it
  * launches, on the launching stream.  wtg_profile_read waits for those events

@@ -18,6 +18,7 @@
 // re-reading their span (init_longblock_serial :401-438) and m_superblock
 // (:546-549).
 #include <algorithm>
+#include <mutex>
 
 #include "wtg_internal.cuh"
 
@@ -629,4 +630,73 @@ int bv_build(BvSupport& bv, const uint64_t* d_words, uint64_t size, uint32_t fla
   return bv_finish(bv, d_err, s);
 }
 
+// ------------------------------------------------ allocation-free rank build
+//
+// For callers that must not allocate device memory themselves or through
+// this library: code running where the allocator is off limits (inside a
+// memory budget owned by another framework, during a phase where cudaMalloc
+// would synchronise the device, or on a pool that forbids new allocations).
+// The rank pass needs scratch for its look-back status words, its tile
+// counter and a few device scalars; here they live in one file-scope device
+// array of fixed size, so the call allocates nothing.  Every GPU that loads
+// the library holds this array until the process exits.
+constexpr uint64_t NOALLOC_MAX_BITS = 1ull << 34;  // 16 Gbit (2 GiB of bits)
+constexpr uint64_t NOALLOC_TILES = ((NOALLOC_MAX_BITS >> 9) + 1 + BVT_SB - 1) / BVT_SB;
+constexpr uint64_t NOALLOC_WORDS = 1 + NOALLOC_TILES + INF_N + 1;  // counter, status, info, error
+static __device__ __align__(256) uint64_t g_noalloc_scratch[NOALLOC_WORDS];
+
+static uint64_t* noalloc_scratch_ptr(int dev, int* rc) {
+  static std::mutex mu;
+  static uint64_t* ptrs[64] = {nullptr};
+  if (dev < 0 || dev >= 64) {
+    *rc = fail(WTG_ERR_CUDA, "device ordinal out of range");
+    return nullptr;
+  }
+  std::lock_guard<std::mutex> lk(mu);
+  if (!ptrs[dev]) {  // set-up, once per device, with that device current
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) {
+      *rc = cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+      return nullptr;
+    }
+    ptrs[dev] = (uint64_t*)p;
+  }
+  *rc = WTG_OK;
+  return ptrs[dev];
+}
+
 }  // namespace wtg
+
+extern "C" int wtg_rank_build_noalloc(const uint64_t* d_words, uint64_t size_bits, uint64_t* d_rank,
+                                      void* stream) {
+  using namespace wtg;
+  if ((!d_words && size_bits) || !d_rank) return fail(WTG_ERR_INVALID, "null argument");
+  if (size_bits > NOALLOC_MAX_BITS)
+    return fail(WTG_ERR_RANGE, "wtg_rank_build_noalloc: size_bits exceeds its fixed scratch (at most 2^34 bits)");
+  int dev = 0;
+  WTG_CK(cudaGetDevice(&dev));
+  int rc;
+  uint64_t* scratch = noalloc_scratch_ptr(dev, &rc);
+  if (!scratch) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  const uint64_t W = (size_bits + 63) / 64, NB = W >> 3;
+  const uint64_t tiles = (NB + 1 + BVT_SB - 1) / BVT_SB;
+  uint32_t* counter = (uint32_t*)scratch;
+  uint64_t* status = scratch + 1;
+  unsigned long long* info = (unsigned long long*)(scratch + 1 + NOALLOC_TILES);
+  uint32_t* err = (uint32_t*)(scratch + 1 + NOALLOC_TILES + INF_N);
+  // the array keeps the previous call's contents: clear what must start at 0
+  WTG_CK(cudaMemsetAsync(scratch, 0, (1 + tiles) * sizeof(uint64_t), s));
+  WTG_CK(cudaMemsetAsync(info, 0, (INF_N + 1) * sizeof(uint64_t), s));
+  bv_pass_kernel<<<(unsigned)tiles, BV_THREADS, 0, s>>>(d_words, size_bits, W, NB, WTG_RANK, d_rank, nullptr, 0,
+                                                       nullptr, nullptr, nullptr, nullptr, info, status, counter, err);
+  count_launch();
+  WTG_CK(cudaGetLastError());
+  WTG_CK(cudaStreamSynchronize(s));
+  uint32_t e = 0;
+  WTG_CK(cudaMemcpy(&e, err, sizeof(e), cudaMemcpyDeviceToHost));
+  if (e) return fail(WTG_ERR_TIMEOUT, "a device-side wait of the rank pass timed out; the table is invalid");
+  return WTG_OK;
+}
+

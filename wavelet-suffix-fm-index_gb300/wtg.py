@@ -79,6 +79,7 @@ _SIGS = {
     "wtg_bv_select": ([vp, i32, vp, u64, vp], i32),
     "wtg_bv_select_device": ([vp, i32, vp, u64, vp, vp], i32),
     "wtg_remap_alphabet": ([vp, u64, i32, vp], i32),
+    "wtg_rank_build_noalloc": ([vp, u64, vp, vp], i32),
     "wtg_profile_enable": ([i32], i32),
     "wtg_profile_read": ([vp, vp], i32),
 }
@@ -313,6 +314,20 @@ class BitVectorSupport:
         out = np.zeros(i.size, dtype=np.uint64)
         _ck(lib().wtg_bv_select(self.h, t_b, _p(i), i.size, _p(out)))
         return out
+
+
+def rank_build_noalloc(d_words_ptr, size_bits, d_rank_ptr, stream=0):
+    """rank_support_v<1> table of a device bitvector into a device buffer,
+    without any device allocation (include/wtg.h: wtg_rank_build_noalloc)."""
+    _ck(lib().wtg_rank_build_noalloc(vp(d_words_ptr), int(size_bits), vp(d_rank_ptr), vp(stream)))
+
+
+def rank_words(size_bits):
+    """Words of a rank_support_v<1> table over size_bits bits."""
+    if size_bits == 0:
+        return 2
+    cap = (size_bits + 63) // 64 * 64
+    return ((cap >> 9) + 1) << 1
 
 
 def remap_alphabet(seq):
