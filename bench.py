@@ -49,6 +49,13 @@ def algorithmic_bytes(n, L, w, sel_words=0):
     return (L * n * w + (L - 1) * n * w + bits + (bits + 16 * ((nb >> 9) + 1)) + 2 * bits + 8 * sel_words)
 
 
+# DRAM bytes (read + write) per symbol of one uint32 partitioning level pass,
+# from ncu's dram__bytes_read.sum + dram__bytes_write.sum over levels 9-11 of
+# an n=2^26 build (494.5 MB per launch); traffic grows linearly with n, so a
+# full launch's traffic is this figure times n.
+LEVEL_DRAM_BYTES_PER_SYMBOL_U32 = 494.5e6 / 2 ** 26
+
+
 def level_launch_bytes(n, w):
     """Algorithmic bytes of one partitioning level pass: read n symbols,
     write n symbols, write n bits."""
@@ -232,9 +239,10 @@ def run_wtg(args, rank, world, local_rank):
     lv_n, lv_ms = prof["level"]
     lv_avg = lv_ms / max(lv_n, 1)
     lv_bytes = level_launch_bytes(n, 4)
+    traffic = args.traffic if args.traffic is not None else LEVEL_DRAM_BYTES_PER_SYMBOL_U32 * n
     roofline = {
         "bound": "hbm", "kernel": "level_kernel<uint32,partition>", "achieved": lv_bytes / (lv_avg / 1e3) / 1e9,
-        "peak": peak, "unit": "GB/s", "peak_kind": peak_kind, "traffic": args.traffic,
+        "peak": peak, "unit": "GB/s", "peak_kind": peak_kind, "traffic": traffic,
         "launch_ms": lv_avg, "launches": lv_n, "bytes_per_launch": lv_bytes,
     }
     roofline["frac"] = roofline["achieved"] / peak
@@ -340,7 +348,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--traffic", type=float, default=None,
-                    help="DRAM bytes per level launch from an ncu capture, reported as roofline.traffic")
+                    help="DRAM bytes per level launch from an ncu capture, reported as roofline.traffic "
+                         "(default: the n=2^26 capture scaled to n)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
