@@ -172,6 +172,83 @@ def run_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
+def select_queries(torch, m_levels, nq, gen, dev):
+    """nq uniform-random (level, k) select queries: the level uniform over the
+    levels holding at least one arg, k uniform in [1, args of the level]."""
+    valid = [l for l, m in enumerate(m_levels) if m > 0]
+    vl = torch.tensor(valid, device=dev, dtype=torch.int64)
+    mt = torch.tensor([m_levels[l] for l in valid], device=dev, dtype=torch.float64)
+    idx = torch.randint(0, len(valid), (nq,), device=dev, generator=gen)
+    k = torch.floor(torch.rand(nq, device=dev, dtype=torch.float64, generator=gen) * mt[idx]).to(torch.int64) + 1
+    k = torch.minimum(k, mt[idx].to(torch.int64))
+    return vl[idx].contiguous(), k.contiguous()
+
+
+def measure_select(torch, wtg, tree, n, L, dev, stream, log2_q, reps=5):
+    """Learned select against plain select_support_mcl on the tree's levels:
+    2^log2_q select1 and 2^log2_q select0 queries per pass, answers compared
+    in full."""
+    sp = stream.cuda_stream
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+    b0, b1 = ev(), ev()
+    b0.record(stream)
+    ls = wtg.LearnedSelect(tree, segments=1024, samples=1024, max_window=1 << 16)
+    b1.record(stream)
+    torch.cuda.synchronize()
+    build_ms = b0.elapsed_time(b1)
+    info = ls.info()
+    nq = 1 << log2_q
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(SEED + 7)
+    qs = {}
+    for t_b in (1, 0):
+        m_levels = [ls.level_model(t_b, l)[0]["m"] for l in range(L)]
+        qs[t_b] = select_queries(torch, m_levels, nq, gen, dev)
+    outs = {(arm, t_b): torch.empty(nq, device=dev, dtype=torch.int64) for arm in ("plain", "learned")
+            for t_b in (1, 0)}
+
+    def run(arm):
+        for t_b in (1, 0):
+            lv, k = qs[t_b]
+            o = outs[(arm, t_b)]
+            if arm == "plain":
+                tree.level_select_device(t_b, lv.data_ptr(), k.data_ptr(), nq, o.data_ptr(), sp)
+            else:
+                ls.select_device(t_b, lv.data_ptr(), k.data_ptr(), nq, o.data_ptr(), sp)
+
+    res = {}
+    for arm in ("plain", "learned"):
+        for _ in range(3):
+            run(arm)
+        torch.cuda.synchronize()
+        e0, e1 = ev(), ev()
+        e0.record(stream)
+        for _ in range(reps):
+            run(arm)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        res[arm] = e0.elapsed_time(e1) / reps
+    exact = all(torch.equal(outs[("plain", t_b)], outs[("learned", t_b)]) for t_b in (1, 0))
+    none = sum(int((outs[("plain", t_b)] == -1).sum().item()) for t_b in (1, 0))
+    bits = n * L
+    sel_tables = [tree.select_tables(t_b) for t_b in (0, 1)]
+    mcl_words = sum(s.sb_nwords + s.nsb + s.pool_nwords for s in sel_tables)
+    out = {
+        "queries_per_pass": 2 * nq, "query_mix": f"2^{log2_q} select1 + 2^{log2_q} select0, uniform level and k",
+        "plain_mqs": 2 * nq / (res["plain"] / 1e3) / 1e6, "learned_mqs": 2 * nq / (res["learned"] / 1e3) / 1e6,
+        "plain_ms": res["plain"], "learned_ms": res["learned"],
+        "speedup": res["plain"] / res["learned"], "exact": bool(exact and none == 0),
+        "model": "piecewise-linear, 1024 segments per level and polarity, 1024 fitted pairs per segment",
+        "space_bits_per_bit": 8 * info["model_bytes"] / bits,
+        "mcl_space_bits_per_bit": 64 * mcl_words / bits,
+        "fallback_segments": info["fallback_segments"], "segments": info["segments"],
+        "max_window": info["max_window"], "mean_window": info["window_sum"] / max(1, info["segments"] - info["fallback_segments"]),
+        "misses": info["misses"], "build_ms": build_ms,
+    }
+    ls.free()
+    return out
+
+
 def run_wtg(args, rank, world, local_rank):
     import torch
     import wtg
@@ -247,6 +324,10 @@ def run_wtg(args, rank, world, local_rank):
     }
     roofline["frac"] = roofline["achieved"] / peak
     kernel_share = {k: {"launches": v[0], "ms": v[1]} for k, v in prof.items()}
+
+    select = None
+    if not args.no_select:
+        select = measure_select(torch, wtg, tree, n, L, dev, stream, args.select_log2)
 
     # ---- e2e: host API with pinned host buffers, outputs copied back
     e2e = None
@@ -326,6 +407,7 @@ def run_wtg(args, rank, world, local_rank):
         "hbm_frac": value / peak,
         "roofline": roofline,
         "kernel_time": kernel_share,
+        "select": select,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "clocks": clocks.summary(),
@@ -347,6 +429,9 @@ def main():
     ap.add_argument("--cpu-log2", type=int, default=27)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-select", action="store_true")
+    ap.add_argument("--select-log2", type=int, default=26,
+                    help="log2 of the select1 (and of the select0) queries per pass")
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per level launch from an ncu capture, reported as roofline.traffic "
                          "(default: the n=2^26 capture scaled to n)")

@@ -52,6 +52,7 @@ extern "C" {
 
 typedef struct wtg_tree wtg_tree; /* wavelet tree + supports, owns device memory */
 typedef struct wtg_bv wtg_bv;     /* rank/select supports over a caller bitvector */
+typedef struct wtg_lsel wtg_lsel; /* learned select index over a tree's levels */
 
 const char* wtg_last_error(void);
 int wtg_version(void);
@@ -160,6 +161,48 @@ int wtg_bv_select_device(wtg_bv* b, int t_b, const uint64_t* d_i, uint64_t nq, u
  * before any stream capture).  All calls share the array, so calls that
  * overlap on the GPU (other threads or streams) race. */
 int wtg_rank_build_noalloc(const uint64_t* d_words, uint64_t size_bits, uint64_t* d_rank, void* stream);
+
+/* ------------------------------------------ per-level and learned select
+ * A query is a pair (level, k): the position, inside level `level` of the
+ * tree, of that level's k-th one (t_b = 1) or zero (t_b = 0), k >= 1;
+ * UINT64_MAX where the level holds fewer than k.  Levels are the n-bit
+ * slices of the concatenated bitvector.
+ *
+ * wtg_tree_level_select is the plain route: select_support_mcl<t_b> on the
+ * concatenated bitvector after adding the args before the level, which is
+ * wt_int's per-level select step (wt_int/wt_int_par.hpp:651-656) with the
+ * whole level as the node.  Needs WTG_ALL. */
+int wtg_tree_level_select(wtg_tree* t, int t_b, const uint64_t* level, const uint64_t* k, uint64_t nq,
+                          uint64_t* out);
+int wtg_tree_level_select_device(wtg_tree* t, int t_b, const uint64_t* d_level, const uint64_t* d_k, uint64_t nq,
+                                 uint64_t* d_out, void* stream);
+
+/* Learned select index beside select_support_mcl.  No counterpart in the
+ * reference.  Per level and polarity, the args are cut into at most
+ * `segments` segments of 2^g args; each gets a line fitted on the GPU by
+ * least squares to `samples` (k, select(k)) pairs taken from the plain
+ * select, and an error window that holds for every k of the segment.  A
+ * query predicts the position and searches the window exactly through the
+ * rank_support_v superblocks; segments whose window exceeds max_window
+ * positions are answered by the plain select.  Answers equal
+ * wtg_tree_level_select's.  The index reads the tree's bitvector, rank and
+ * select tables: it is valid until the tree is rebuilt or freed (queries
+ * after a rebuild return WTG_ERR_INVALID).  Needs a tree built with WTG_ALL.
+ * Builds on the tree's stream and waits for it. */
+int wtg_lsel_build(wtg_tree* t, uint32_t segments, uint32_t samples, uint32_t max_window, wtg_lsel** out);
+int wtg_lsel_free(wtg_lsel* m);
+/* info[8]: segments (both polarities), model bytes, segments answered by the
+ * plain select, largest window of the others, sum of their windows, searches
+ * that fell back since the build (0 unless the tables are inconsistent),
+ * segments and samples parameters */
+int wtg_lsel_info(wtg_lsel* m, uint64_t info[8]);
+/* one level's model: lvl_info = {args before the level, args in it, g,
+ * segments}; rec (may be NULL) receives 4 u32 per segment: base, slope
+ * (16.16 fixed), dlo, dhi (int32) */
+int wtg_lsel_get_level(wtg_lsel* m, int t_b, int level, uint64_t lvl_info[4], uint32_t* rec, uint64_t nseg);
+int wtg_lsel_query(wtg_lsel* m, int t_b, const uint64_t* level, const uint64_t* k, uint64_t nq, uint64_t* out);
+int wtg_lsel_query_device(wtg_lsel* m, int t_b, const uint64_t* d_level, const uint64_t* d_k, uint64_t nq,
+                          uint64_t* d_out, void* stream);
 
 /* ------------------------------------------------------------ profiling
  * When enabled, every build records a CUDA event pair around each kernel it

@@ -644,6 +644,8 @@ int tree_build(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int L, uint32
   t.elem_bytes = eb;
   t.flags = flags;
   t.bit_words = (n * (uint64_t)L + 63) / 64;
+  t.lvl_args_ok = false;
+  ++t.gen;
   const int K = std::min(L, TOP_BITS);
   const uint64_t heap = 1ull << L;  // heap ids 0 .. 2^L - 2, plus one pad entry
 
@@ -788,6 +790,7 @@ int tree_nodes(TreeImpl& t, int ib, uint64_t n_entries, void* d_out) {
 
 void tree_release(TreeImpl& t) {
   cudaStream_t s = t.stream;
+  lsel_detach_all(t);
   t.seq.release(s);
   t.lvl[0].release(s);
   t.lvl[1].release(s);
@@ -798,6 +801,8 @@ void tree_release(TreeImpl& t) {
   t.status.release(s);
   t.scan_tmp.release(s);
   t.err.release(s);
+  t.lvl_args.release(s);
+  t.lvl_args_ok = false;
   t.scratch.release(s);
   t.nodes.release(s);
   bv_release(t.bv, s);

@@ -10,6 +10,11 @@ struct wtg_tree {
   wtg::TreeImpl t;
 };
 
+struct wtg_lsel {
+  wtg::LselImpl* m = nullptr;
+  wtg::DevBuf qbuf;
+};
+
 struct wtg_bv {
   wtg::BvSupport bv;
   wtg::DevBuf words;  // device copy for host-input builds
@@ -450,6 +455,89 @@ int wtg_bv_select(wtg_bv* B, int t_b, const uint64_t* i, uint64_t nq, uint64_t* 
 int wtg_bv_select_device(wtg_bv* B, int t_b, const uint64_t* d_i, uint64_t nq, uint64_t* d_out, void* stream) {
   if (!B || (t_b != 0 && t_b != 1)) return fail(WTG_ERR_INVALID, "bad argument");
   return launch_bv_select(B->bv, t_b, d_i, nq, d_out, (cudaStream_t)stream);
+}
+
+// ------------------------------------------------ per-level and learned select
+
+int wtg_tree_level_select(wtg_tree* T, int t_b, const uint64_t* level, const uint64_t* k, uint64_t nq,
+                          uint64_t* out) {
+  if (!T || (t_b != 0 && t_b != 1) || (nq && (!level || !k || !out))) return fail(WTG_ERR_INVALID, "bad argument");
+  TreeImpl& t = T->t;
+  const uint64_t* ins[2] = {level, k};
+  uint64_t* outs[1] = {out};
+  return host_query(t.qbuf, t.stream, ins, 2, nq, outs, 1, t.err.as<uint32_t>(),
+                    [&](const uint64_t** din, uint64_t** dout) {
+                      return launch_level_select(t, t_b, din[0], din[1], nq, dout[0], t.stream);
+                    });
+}
+
+int wtg_tree_level_select_device(wtg_tree* T, int t_b, const uint64_t* d_level, const uint64_t* d_k, uint64_t nq,
+                                 uint64_t* d_out, void* stream) {
+  if (!T || (t_b != 0 && t_b != 1)) return fail(WTG_ERR_INVALID, "bad argument");
+  return launch_level_select(T->t, t_b, d_level, d_k, nq, d_out, (cudaStream_t)stream);
+}
+
+int wtg_lsel_build(wtg_tree* T, uint32_t segments, uint32_t samples, uint32_t max_window, wtg_lsel** out) {
+  int rc;
+  if (!T || !out) return fail(WTG_ERR_INVALID, "null argument");
+  wtg_lsel* M = *out;
+  bool fresh = false;
+  if (!M) {
+    M = new (std::nothrow) wtg_lsel();
+    if (M) M->m = lsel_new();
+    if (!M || !M->m) {
+      delete M;
+      return fail(WTG_ERR_OOM, "host allocation failed");
+    }
+    fresh = true;
+  }
+  rc = lsel_build(*M->m, T->t, segments, samples, max_window, T->t.stream);
+  if (rc == WTG_OK) rc = sync_and_check(T->t.stream, T->t.err.as<uint32_t>());
+  if (rc != WTG_OK) {
+    if (fresh) wtg_lsel_free(M);
+    return rc;
+  }
+  *out = M;
+  return WTG_OK;
+}
+
+int wtg_lsel_free(wtg_lsel* M) {
+  if (!M) return WTG_OK;
+  lsel_delete(M->m);  // waits for the device
+  M->qbuf.release(nullptr);
+  cudaDeviceSynchronize();
+  delete M;
+  return WTG_OK;
+}
+
+int wtg_lsel_info(wtg_lsel* M, uint64_t info[8]) {
+  if (!M || !info) return fail(WTG_ERR_INVALID, "null argument");
+  TreeImpl* t = lsel_tree(*M->m);
+  return lsel_info(*M->m, info, t ? t->stream : nullptr);
+}
+
+int wtg_lsel_get_level(wtg_lsel* M, int t_b, int level, uint64_t lvl_info[4], uint32_t* rec, uint64_t nseg) {
+  if (!M || !lvl_info) return fail(WTG_ERR_INVALID, "null argument");
+  TreeImpl* t = lsel_tree(*M->m);
+  return lsel_get_level(*M->m, t_b, level, lvl_info, rec, nseg, t ? t->stream : nullptr);
+}
+
+int wtg_lsel_query(wtg_lsel* M, int t_b, const uint64_t* level, const uint64_t* k, uint64_t nq, uint64_t* out) {
+  if (!M || (t_b != 0 && t_b != 1) || (nq && (!level || !k || !out))) return fail(WTG_ERR_INVALID, "bad argument");
+  TreeImpl* t = lsel_tree(*M->m);
+  if (!t) return fail(WTG_ERR_INVALID, "the index's tree was freed");
+  const uint64_t* ins[2] = {level, k};
+  uint64_t* outs[1] = {out};
+  return host_query(M->qbuf, t->stream, ins, 2, nq, outs, 1, t->err.as<uint32_t>(),
+                    [&](const uint64_t** din, uint64_t** dout) {
+                      return launch_lsel_query(*M->m, t_b, din[0], din[1], nq, dout[0], t->stream);
+                    });
+}
+
+int wtg_lsel_query_device(wtg_lsel* M, int t_b, const uint64_t* d_level, const uint64_t* d_k, uint64_t nq,
+                          uint64_t* d_out, void* stream) {
+  if (!M || (t_b != 0 && t_b != 1)) return fail(WTG_ERR_INVALID, "bad argument");
+  return launch_lsel_query(*M->m, t_b, d_level, d_k, nq, d_out, (cudaStream_t)stream);
 }
 
 // ------------------------------------------------------------------ helpers

@@ -3,85 +3,10 @@
 // select, one thread per query; plus the alphabet remap helper.
 #include <algorithm>
 
+#include "wtg_select.cuh"
 #include "wtg_tree.cuh"
 
 namespace wtg {
-
-// rank_support_v<1>::rank (rank/rank_support_v_par.hpp:131-142)
-__device__ __forceinline__ uint64_t rank1_dev(const uint64_t* __restrict__ tbl, const uint64_t* __restrict__ w,
-                                              uint64_t idx) {
-  const uint64_t* p = tbl + ((idx >> 8) & 0xFFFFFFFFFFFFFFFEull);
-  uint64_t r = p[0] + ((p[1] >> (63 - 9 * ((idx & 0x1FF) >> 6))) & 0x1FF);
-  if (idx & 0x3F) r += __popcll(w[idx >> 6] & ((1ull << (idx & 63)) - 1));
-  return r;
-}
-
-struct SelView {
-  const uint64_t* words;
-  uint64_t nwords;  // data words at `words`
-  const uint64_t* sb_words;
-  const uint64_t* desc;
-  const uint64_t* pool;
-  uint64_t arg_cnt;
-  uint32_t logn;
-  int has_long;
-  int t_b;
-};
-
-// select_support_mcl::select(i), 1 <= i <= arg_cnt
-// (select/select_support_mcl_par.hpp:564-611) on the flat layout
-__device__ __forceinline__ uint64_t select_dev(const SelView& v, uint64_t i) {
-  if (i == 0 || i > v.arg_cnt) return NONE64;
-  i = i - 1;
-  const uint64_t sb = i >> 12, off = i & 0xFFF;
-  const uint64_t d = v.desc[sb];
-  const uint32_t wdt = (uint32_t)(d & 127);
-  const uint64_t* blk = v.pool + (d >> 8);
-  if (v.has_long && ((d >> 7) & 1)) return packed_get(blk, off, wdt);
-  const uint64_t base = packed_get(v.sb_words, sb, v.logn);
-  const uint64_t mini = packed_get(blk, off >> 6, wdt);
-  if ((off & 0x3F) == 0) return base + mini;
-  i = i - (sb << 12) - ((off >> 6) << 6);
-  const uint64_t pos = base + mini + 1;
-  uint64_t word_pos = pos >> 6;
-  const uint32_t word_off = (uint32_t)(pos & 0x3F);
-  if (word_pos >= v.nwords) return NONE64;
-  uint64_t wd = v.words[word_pos];
-  if (!v.t_b) wd = ~wd;
-  const uint64_t first = wd & (~0ull << word_off);
-  uint64_t args = __popcll(first);
-  if (args >= i) return (word_pos << 6) + sel64(first, (uint32_t)i);
-  uint64_t sum = args;
-  word_pos += 1;
-  if (word_pos >= v.nwords) return NONE64;
-  wd = v.words[word_pos];
-  if (!v.t_b) wd = ~wd;
-  args = __popcll(wd);
-  while (sum + args < i) {
-    sum += args;
-    word_pos += 1;
-    if (word_pos >= v.nwords) return NONE64;  // inconsistent tables: never read past the data
-    wd = v.words[word_pos];
-    if (!v.t_b) wd = ~wd;
-    args = __popcll(wd);
-  }
-  return (word_pos << 6) + sel64(wd, (uint32_t)(i - sum));
-}
-
-static SelView sel_view(const BvSupport& bv, int t_b) {
-  const SelectDev& sd = bv.sel[t_b];
-  SelView v;
-  v.words = bv.words;
-  v.nwords = (bv.size + 63) / 64;  // a valid query never reads past the data words
-  v.sb_words = sd.sb_words.as<uint64_t>();
-  v.desc = sd.desc.as<uint64_t>();
-  v.pool = sd.pool.as<uint64_t>();
-  v.arg_cnt = sd.arg_cnt;
-  v.logn = (uint32_t)sd.logn;
-  v.has_long = (int)sd.has_long;
-  v.t_b = t_b;
-  return v;
-}
 
 __device__ __forceinline__ int bit_at(const uint64_t* __restrict__ w, uint64_t p) {
   return (int)((w[p >> 6] >> (p & 63)) & 1);

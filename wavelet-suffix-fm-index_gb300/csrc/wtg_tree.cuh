@@ -1,8 +1,12 @@
 // wtg_tree.cuh -- device-side state of one wavelet tree (internal).
 #pragma once
+#include <vector>
+
 #include "wtg_internal.cuh"
 
 namespace wtg {
+
+struct LselImpl;
 
 // Device memory layout of one tree (all stream-ordered, reused across rebuilds):
 //   seq        the input copied from the host (host-input builds only)
@@ -13,6 +17,8 @@ namespace wtg {
 //   base       per heap node (C - Zb, zeros + Zb) (2^L x uint2)
 //   status     per level: tile counter + look-back status words
 //   bv         rank/select supports over `bits`
+//   lvl_args   ones before each level start, L + 1 words (filled on first use
+//              after a build by tree_level_args)
 struct TreeImpl {
   uint64_t n = 0;
   int levels = 0;
@@ -23,6 +29,10 @@ struct TreeImpl {
   bool own_stream = false;
   DevBuf seq, lvl[2], bits, hist, zeros, base, status, scan_tmp, err, scratch, nodes, qbuf;
   BvSupport bv;
+  DevBuf lvl_args;
+  bool lvl_args_ok = false;
+  uint64_t gen = 0;  // builds so far (indexes built on the tree record it)
+  std::vector<LselImpl*> deps;  // learned select indexes reading this tree
 };
 
 int tree_levels_from_max(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int* levels);
@@ -41,6 +51,30 @@ int launch_wt_select(const TreeImpl& t, const uint64_t* i, const uint64_t* sym, 
 int launch_bv_rank(const BvSupport& bv, const uint64_t* idx, uint64_t nq, uint64_t* out, cudaStream_t s);
 int launch_bv_select(const BvSupport& bv, int t_b, const uint64_t* i, uint64_t nq, uint64_t* out,
                      cudaStream_t s);
+
+// per-level select on the tree's concatenated bitvector -- wt_int's select
+// step (m_tree_select1/0(args before the node + i) - node offset,
+// wt_int_par.hpp:651-656) with the whole level as the node: for each query
+// (level, k) the position, inside the level, of the level's k-th one
+// (t_b = 1) or zero (t_b = 0); UINT64_MAX when the level has fewer than k
+int tree_level_args(TreeImpl& t, cudaStream_t s);
+int launch_level_select(TreeImpl& t, int t_b, const uint64_t* level, const uint64_t* k, uint64_t nq,
+                        uint64_t* out, cudaStream_t s);
+
+// learned select index over the level bitvectors (wtg_lsel.cu).  An index
+// registers with its tree; freeing the tree detaches its indexes (their
+// queries then fail) and freeing an index unregisters it.
+LselImpl* lsel_new();
+void lsel_detach_all(TreeImpl& t);
+TreeImpl* lsel_tree(const LselImpl& m);  // NULL once the tree was freed
+void lsel_delete(LselImpl* m);
+int lsel_build(LselImpl& m, TreeImpl& t, uint32_t segments, uint32_t samples, uint32_t max_window,
+               cudaStream_t s);
+int lsel_info(const LselImpl& m, uint64_t info[8], cudaStream_t s);
+int lsel_get_level(const LselImpl& m, int t_b, int level, uint64_t lvl_info[4], uint32_t* rec, uint64_t nseg,
+                   cudaStream_t s);
+int launch_lsel_query(LselImpl& m, int t_b, const uint64_t* level, const uint64_t* k, uint64_t nq,
+                      uint64_t* out, cudaStream_t s);
 
 // alphabet remap (levelWT/WTTime.C:80-94) on a device sequence, in place
 int remap_alphabet_device(void* d_seq, uint64_t n, int eb, uint64_t* sigma, DevBuf& tmp, DevBuf& scan_tmp,

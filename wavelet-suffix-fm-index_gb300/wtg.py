@@ -78,6 +78,14 @@ _SIGS = {
     "wtg_bv_rank": ([vp, vp, u64, vp], i32),
     "wtg_bv_select": ([vp, i32, vp, u64, vp], i32),
     "wtg_bv_select_device": ([vp, i32, vp, u64, vp, vp], i32),
+    "wtg_tree_level_select": ([vp, i32, vp, vp, u64, vp], i32),
+    "wtg_tree_level_select_device": ([vp, i32, vp, vp, u64, vp, vp], i32),
+    "wtg_lsel_build": ([vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, vp], i32),
+    "wtg_lsel_free": ([vp], i32),
+    "wtg_lsel_info": ([vp, vp], i32),
+    "wtg_lsel_get_level": ([vp, i32, i32, vp, vp, u64], i32),
+    "wtg_lsel_query": ([vp, i32, vp, vp, u64, vp], i32),
+    "wtg_lsel_query_device": ([vp, i32, vp, vp, u64, vp, vp], i32),
     "wtg_remap_alphabet": ([vp, u64, i32, vp], i32),
     "wtg_rank_build_noalloc": ([vp, u64, vp, vp], i32),
     "wtg_profile_enable": ([i32], i32),
@@ -254,6 +262,17 @@ class WaveletTree:
         _ck(lib().wtg_query_select(self.h, _p(i), _p(sym), i.size, _p(out)))
         return out
 
+    def level_select(self, level, k, t_b=1):
+        """Position inside level `level` of its k-th one (t_b=1) or zero
+        (t_b=0) through select_support_mcl (wt_int_par.hpp:651-656)."""
+        level, k = _u64(level), _u64(k)
+        out = np.zeros(k.size, dtype=np.uint64)
+        _ck(lib().wtg_tree_level_select(self.h, t_b, _p(level), _p(k), k.size, _p(out)))
+        return out
+
+    def level_select_device(self, t_b, d_level, d_k, nq, d_out, stream=0):
+        _ck(lib().wtg_tree_level_select_device(self.h, t_b, vp(d_level), vp(d_k), nq, vp(d_out), vp(stream)))
+
 
 def WT(s, sigma, index_bytes=4):
     """levelWT's WT(s, n, sigma): returns (nodes [2*sigma, 5], bits) with
@@ -314,6 +333,54 @@ class BitVectorSupport:
         out = np.zeros(i.size, dtype=np.uint64)
         _ck(lib().wtg_bv_select(self.h, t_b, _p(i), i.size, _p(out)))
         return out
+
+
+class LearnedSelect:
+    """Learned select index over a tree's level bitvectors (include/wtg.h:
+    wtg_lsel_build): per level and polarity, at most `segments` least-squares
+    lines with exact error windows; answers equal WaveletTree.level_select."""
+
+    def __init__(self, tree, segments=1024, samples=1024, max_window=1 << 16):
+        self.h = vp()
+        self.tree = tree  # the index reads the tree's device buffers
+        _ck(lib().wtg_lsel_build(tree.h, segments, samples, max_window, ctypes.byref(self.h)))
+
+    def free(self):
+        if self.h:
+            lib().wtg_lsel_free(self.h)
+            self.h = vp()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def info(self):
+        a = np.zeros(8, dtype=np.uint64)
+        _ck(lib().wtg_lsel_info(self.h, _p(a)))
+        keys = ("segments", "model_bytes", "fallback_segments", "max_window", "window_sum", "misses",
+                "segments_param", "samples_param")
+        return {k: int(v) for k, v in zip(keys, a)}
+
+    def level_model(self, t_b, level):
+        """({A, m, g, nseg}, records [nseg, 4] as (base, slope, dlo, dhi))."""
+        li = np.zeros(4, dtype=np.uint64)
+        _ck(lib().wtg_lsel_get_level(self.h, t_b, level, _p(li), None, 0))
+        nseg = int(li[3])
+        rec = np.zeros((max(nseg, 1), 4), dtype=np.uint32)
+        _ck(lib().wtg_lsel_get_level(self.h, t_b, level, _p(li), _p(rec), nseg))
+        meta = dict(zip(("A", "m", "g", "nseg"), (int(x) for x in li)))
+        return meta, rec[:nseg]
+
+    def select(self, level, k, t_b=1):
+        level, k = _u64(level), _u64(k)
+        out = np.zeros(k.size, dtype=np.uint64)
+        _ck(lib().wtg_lsel_query(self.h, t_b, _p(level), _p(k), k.size, _p(out)))
+        return out
+
+    def select_device(self, t_b, d_level, d_k, nq, d_out, stream=0):
+        _ck(lib().wtg_lsel_query_device(self.h, t_b, vp(d_level), vp(d_k), nq, vp(d_out), vp(stream)))
 
 
 def rank_build_noalloc(d_words_ptr, size_bits, d_rank_ptr, stream=0):
