@@ -184,69 +184,86 @@ def select_queries(torch, m_levels, nq, gen, dev):
     return vl[idx].contiguous(), k.contiguous()
 
 
+LSEL_CONFIGS = (1024, 65536)  # segments per level and polarity: the named model, and a larger one
+
+
 def measure_select(torch, wtg, tree, n, L, dev, stream, log2_q, reps=5):
     """Learned select against plain select_support_mcl on the tree's levels:
-    2^log2_q select1 and 2^log2_q select0 queries per pass, answers compared
-    in full."""
+    2^log2_q select1 and 2^log2_q select0 queries per pass (uniform level,
+    uniform k), every learned answer compared with the plain one.  The first
+    learned model is the named one (1024 segments); the second trades model
+    space for narrower windows."""
     sp = stream.cuda_stream
     ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
-    b0, b1 = ev(), ev()
-    b0.record(stream)
-    ls = wtg.LearnedSelect(tree, segments=1024, samples=1024, max_window=1 << 16)
-    b1.record(stream)
-    torch.cuda.synchronize()
-    build_ms = b0.elapsed_time(b1)
-    info = ls.info()
     nq = 1 << log2_q
     gen = torch.Generator(device=dev)
     gen.manual_seed(SEED + 7)
-    qs = {}
-    for t_b in (1, 0):
-        m_levels = [ls.level_model(t_b, l)[0]["m"] for l in range(L)]
-        qs[t_b] = select_queries(torch, m_levels, nq, gen, dev)
-    outs = {(arm, t_b): torch.empty(nq, device=dev, dtype=torch.int64) for arm in ("plain", "learned")
-            for t_b in (1, 0)}
+    qs, outs = {}, {}
+    bits = n * L
 
-    def run(arm):
-        for t_b in (1, 0):
-            lv, k = qs[t_b]
-            o = outs[(arm, t_b)]
-            if arm == "plain":
-                tree.level_select_device(t_b, lv.data_ptr(), k.data_ptr(), nq, o.data_ptr(), sp)
-            else:
-                ls.select_device(t_b, lv.data_ptr(), k.data_ptr(), nq, o.data_ptr(), sp)
-
-    res = {}
-    for arm in ("plain", "learned"):
+    def timed(fn):
         for _ in range(3):
-            run(arm)
+            fn()
         torch.cuda.synchronize()
         e0, e1 = ev(), ev()
         e0.record(stream)
         for _ in range(reps):
-            run(arm)
+            fn()
         e1.record(stream)
         torch.cuda.synchronize()
-        res[arm] = e0.elapsed_time(e1) / reps
-    exact = all(torch.equal(outs[("plain", t_b)], outs[("learned", t_b)]) for t_b in (1, 0))
-    none = sum(int((outs[("plain", t_b)] == -1).sum().item()) for t_b in (1, 0))
-    bits = n * L
+        return e0.elapsed_time(e1) / reps
+
+    learned = []
+    plain_ms = None
+    exact = True
+    for segs in LSEL_CONFIGS:
+        b0, b1 = ev(), ev()
+        b0.record(stream)
+        ls = wtg.LearnedSelect(tree, segments=segs, samples=1024, max_window=1 << 16)
+        b1.record(stream)
+        torch.cuda.synchronize()
+        info = ls.info()
+        if not qs:
+            for t_b in (1, 0):
+                m_levels = [ls.level_model(t_b, l)[0]["m"] for l in range(L)]
+                qs[t_b] = select_queries(torch, m_levels, nq, gen, dev)
+                outs[t_b] = torch.empty(nq, device=dev, dtype=torch.int64)
+                outs[("l", t_b)] = torch.empty(nq, device=dev, dtype=torch.int64)
+
+            def run_plain():
+                for t_b in (1, 0):
+                    lv, k = qs[t_b]
+                    tree.level_select_device(t_b, lv.data_ptr(), k.data_ptr(), nq, outs[t_b].data_ptr(), sp)
+            plain_ms = timed(run_plain)
+
+        def run_learned():
+            for t_b in (1, 0):
+                lv, k = qs[t_b]
+                ls.select_device(t_b, lv.data_ptr(), k.data_ptr(), nq, outs[("l", t_b)].data_ptr(), sp)
+        ms = timed(run_learned)
+        ok = all(torch.equal(outs[t_b], outs[("l", t_b)]) for t_b in (1, 0))
+        ok = ok and all(int((outs[t_b] == -1).sum().item()) == 0 for t_b in (1, 0))
+        exact = exact and ok
+        learned.append({
+            "segments_per_level": segs, "mqs": 2 * nq / (ms / 1e3) / 1e6, "ms": ms, "speedup": plain_ms / ms,
+            "exact": bool(ok), "space_bits_per_bit": 8 * info["model_bytes"] / bits,
+            "model_bytes": info["model_bytes"], "segments": info["segments"],
+            "fallback_segments": info["fallback_segments"], "max_window": info["max_window"],
+            "mean_window": info["window_sum"] / max(1, info["segments"] - info["fallback_segments"]),
+            "misses": info["misses"], "build_ms": b0.elapsed_time(b1),
+        })
+        ls.free()
     sel_tables = [tree.select_tables(t_b) for t_b in (0, 1)]
     mcl_words = sum(s.sb_nwords + s.nsb + s.pool_nwords for s in sel_tables)
-    out = {
+    return {
         "queries_per_pass": 2 * nq, "query_mix": f"2^{log2_q} select1 + 2^{log2_q} select0, uniform level and k",
-        "plain_mqs": 2 * nq / (res["plain"] / 1e3) / 1e6, "learned_mqs": 2 * nq / (res["learned"] / 1e3) / 1e6,
-        "plain_ms": res["plain"], "learned_ms": res["learned"],
-        "speedup": res["plain"] / res["learned"], "exact": bool(exact and none == 0),
-        "model": "piecewise-linear, 1024 segments per level and polarity, 1024 fitted pairs per segment",
-        "space_bits_per_bit": 8 * info["model_bytes"] / bits,
+        "plain_mqs": 2 * nq / (plain_ms / 1e3) / 1e6, "plain_ms": plain_ms,
+        "learned_mqs": learned[0]["mqs"], "speedup": learned[0]["speedup"], "exact": bool(exact),
+        "model": "piecewise-linear per level and polarity, least squares on 1024 pairs per segment, "
+                 "exact error windows searched through rank_support_v",
         "mcl_space_bits_per_bit": 64 * mcl_words / bits,
-        "fallback_segments": info["fallback_segments"], "segments": info["segments"],
-        "max_window": info["max_window"], "mean_window": info["window_sum"] / max(1, info["segments"] - info["fallback_segments"]),
-        "misses": info["misses"], "build_ms": build_ms,
+        "learned": learned,
     }
-    ls.free()
-    return out
 
 
 def run_wtg(args, rank, world, local_rank):

@@ -46,14 +46,15 @@ struct LselImpl {
   uint64_t n = 0;
   uint64_t nseg[2] = {0, 0};
   std::vector<LselLevel> lv_host[2];
-  DevBuf lv[2], rec[2], stats;
+  SelView plain_host[2];
+  DevBuf lv[2], rec[2], plain[2], stats;  // plain: the SelView of the fallback
 };
 
 namespace {
 
 constexpr int LSEL_FRAC = 16;
 constexpr int LSEL_MAX_PROBES = 40;
-constexpr int LSEL_INTERP_PROBES = 2;
+constexpr int LSEL_INTERP_PROBES = 5;
 constexpr long long LSEL_SAT = 1ll << 30;
 // stats words per polarity: fallback segments, max window, window sum, misses
 constexpr int LSEL_ST = 4;
@@ -271,18 +272,22 @@ struct LselView {
   uint32_t max_window;
   const LselLevel* lv;
   const uint4* rec;
-  SelView plain;
+  const SelView* plain;  // device copy
   unsigned long long* misses;
 };
 
-template <int T_B>
-__device__ __forceinline__ uint64_t lsel_plain(const LselView& v, uint64_t K, uint64_t off) {
-  const uint64_t p = select_dev(v.plain, K);
+// the plain select_support_mcl answer; kept out of line so that its
+// registers do not count against the learned search's occupancy
+__device__ __noinline__ uint64_t lsel_plain(const SelView* v, uint64_t K, uint64_t off) {
+  const uint64_t p = select_dev(*v, K);
   return p == NONE64 ? NONE64 : p - off;
 }
 
+// Learned search for query (l, k).  Returns the answer, or sets *fallback
+// when the plain select must answer (window above max_window, or a search
+// that did not close).
 template <int T_B>
-__device__ __forceinline__ uint64_t lsel_one(const LselView& v, uint64_t l, uint64_t k) {
+__device__ __forceinline__ uint64_t lsel_search(const LselView& v, uint64_t l, uint64_t k, bool* fallback) {
   if (l >= (uint64_t)v.L) return NONE64;
   const LselLevel d = v.lv[l];
   if (k == 0 || k > d.m) return NONE64;
@@ -291,62 +296,63 @@ __device__ __forceinline__ uint64_t lsel_one(const LselView& v, uint64_t l, uint
   const uint64_t j = (k - 1) >> d.g;
   const uint4 r = __ldg(v.rec + d.rec_off + j);
   const long long dlo = (int)r.z, dhi = (int)r.w;
-  if (dhi < dlo || dhi - dlo > (long long)v.max_window) return lsel_plain<T_B>(v, K, off);
+  if (dhi < dlo || dhi - dlo > (long long)v.max_window) {
+    *fallback = true;
+    return 0;
+  }
   const long long pred = (long long)lsel_pred(r.x, r.y, (k - 1) - (j << d.g));
   const long long lo = max(pred + dlo, 0ll), hi = min(pred + dhi, (long long)v.n - 1);
-  if (lo > hi) {
-    atomicAdd(v.misses, 1ull);
-    return lsel_plain<T_B>(v, K, off);
-  }
-  uint64_t s_lo = (off + (uint64_t)lo) >> 9, s_hi = (off + (uint64_t)hi) >> 9;
-  uint64_t s = (off + (uint64_t)min(max(pred, lo), hi)) >> 9;
+  // superblock indices fit 32 bits: n * L < 2^32 * 24 bits
+  uint32_t s_lo = (uint32_t)((off + (uint64_t)lo) >> 9), s_hi = (uint32_t)((off + (uint64_t)hi) >> 9);
+  uint32_t s = (uint32_t)((off + (uint64_t)min(max(pred, lo), hi)) >> 9);
   const uint64_t slope = r.y;
-  for (int probe = 0; probe < LSEL_MAX_PROBES; ++probe) {
-    const ulonglong2 e = __ldg(reinterpret_cast<const ulonglong2*>(v.tbl) + s);
-    const uint64_t R = T_B ? e.x : (s << 9) - e.x;
+  const uint32_t last_word = (uint32_t)(v.nwords - 1);
+  const ulonglong2* __restrict__ tbl2 = reinterpret_cast<const ulonglong2*>(v.tbl);
+  for (int probe = 0; s_lo <= s_hi && probe < LSEL_MAX_PROBES; ++probe) {
+    const ulonglong2 e = __ldg(tbl2 + s);
+    const uint64_t R = T_B ? e.x : ((uint64_t)s << 9) - e.x;
     if (R >= K) {  // the answer lies before superblock s
       if (s == s_lo) break;
       s_hi = s - 1;
       if (probe < LSEL_INTERP_PROBES) {
         const uint64_t back = 1 + ((umin64(R - K + 1, (uint64_t)1 << 31) * slope) >> (LSEL_FRAC + 9));
-        s -= min(back, s - s_lo);
+        s -= (uint32_t)umin64(back, s - s_lo);
       } else {
         s = (s_lo + s_hi) >> 1;
       }
       continue;
     }
-    const uint64_t need = K - R;
+    const uint32_t need = (uint32_t)umin64(K - R, 0xFFFFFFFFu);
     // counts of the words before word q (q = 1..7) hold only for data words;
     // the last superblock's fields past its data are zero
-    const uint64_t qmax = umin64(7, v.nwords - 1 - (s << 3));
-    uint32_t jw = 0;
-    uint64_t cb = 0;
+    const uint32_t qmax = min(7u, last_word - (s << 3));
+    uint32_t jw = 0, cb = 0;
 #pragma unroll
     for (int q = 1; q < 8; ++q) {
-      const uint64_t c1 = (e.y >> (63 - 9 * q)) & 0x1FF;
-      const uint64_t c = T_B ? c1 : (uint64_t)(64 * q) - c1;
-      if ((uint64_t)q <= qmax && c < need) {
+      const uint32_t c1 = (uint32_t)(e.y >> (63 - 9 * q)) & 0x1FFu;
+      const uint32_t c = T_B ? c1 : (uint32_t)(64 * q) - c1;
+      if ((uint32_t)q <= qmax && c < need) {
         jw = (uint32_t)q;
         cb = c;
       }
     }
-    const uint64_t wi = (s << 3) + jw;
-    if (wi >= v.nwords) break;
+    const uint32_t wi = (s << 3) + jw;
     uint64_t word = __ldg(v.words + wi);
     if (!T_B) word = ~word;
-    const uint64_t cnt = (uint64_t)__popcll(word);
-    if (cb + cnt >= need) return (wi << 6) + sel64(word, (uint32_t)(need - cb)) - off;
+    const uint32_t cnt = (uint32_t)__popcll(word);
+    if (cb + cnt >= need) return ((uint64_t)wi << 6) + sel64(word, need - cb) - off;
     if (s == s_hi) break;  // the answer lies after superblock s
     s_lo = s + 1;
     if (probe < LSEL_INTERP_PROBES) {
-      const uint64_t fwd = (umin64(need - cb - cnt, (uint64_t)1 << 31) * slope) >> (LSEL_FRAC + 9);
-      s = s + 1 + min(fwd, s_hi - s - 1);
+      const uint64_t fwd = ((uint64_t)(need - cb - cnt) * slope) >> (LSEL_FRAC + 9);
+      s = s + 1 + (uint32_t)umin64(fwd, s_hi - s - 1);
     } else {
       s = (s_lo + s_hi) >> 1;
     }
   }
   atomicAdd(v.misses, 1ull);
-  return lsel_plain<T_B>(v, K, off);
+  *fallback = true;
+  return 0;
 }
 
 template <int T_B>
@@ -355,7 +361,14 @@ __global__ void __launch_bounds__(256) lsel_query_kernel(LselView v, const uint6
                                                          uint64_t* __restrict__ out) {
   const uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= nq) return;
-  out[q] = lsel_one<T_B>(v, lev[q], kq[q]);
+  const uint64_t l = lev[q], k = kq[q];
+  bool fallback = false;
+  uint64_t res = lsel_search<T_B>(v, l, k, &fallback);
+  if (fallback) {
+    const LselLevel d = v.lv[l];
+    res = lsel_plain(v.plain, d.A + k, l * v.n);
+  }
+  out[q] = res;
 }
 
 unsigned grid_of(uint64_t items, unsigned per_block, unsigned cap) {
@@ -429,6 +442,7 @@ void lsel_delete(LselImpl* m) {
   for (int t = 0; t < 2; ++t) {
     m->lv[t].release(nullptr);
     m->rec[t].release(nullptr);
+    m->plain[t].release(nullptr);
   }
   m->stats.release(nullptr);
   cudaDeviceSynchronize();
@@ -479,6 +493,11 @@ int lsel_build(LselImpl& m, TreeImpl& t, uint32_t segments, uint32_t samples, ui
     if ((rc = m.lv[tb].ensure(std::max(1, L) * sizeof(LselLevel), s))) return rc;
     if ((rc = m.rec[tb].ensure(std::max<uint64_t>(1, off) * sizeof(uint4), s))) return rc;
     WTG_CK(cudaMemcpyAsync(m.lv[tb].p, lv.data(), L * sizeof(LselLevel), cudaMemcpyHostToDevice, s));
+  }
+  for (int tb = 0; tb < 2; ++tb) {
+    m.plain_host[tb] = sel_view(t.bv, tb);
+    if ((rc = m.plain[tb].ensure(sizeof(SelView), s))) return rc;
+    WTG_CK(cudaMemcpyAsync(m.plain[tb].p, &m.plain_host[tb], sizeof(SelView), cudaMemcpyHostToDevice, s));
   }
   if ((rc = m.stats.ensure(2 * LSEL_ST * sizeof(uint64_t), s))) return rc;
   WTG_CK(cudaMemsetAsync(m.stats.p, 0, 2 * LSEL_ST * sizeof(uint64_t), s));
@@ -556,12 +575,13 @@ int launch_lsel_query(LselImpl& m, int t_b, const uint64_t* level, const uint64_
   v.words = t.bits.as<uint64_t>();
   v.tbl = t.bv.rank.as<uint64_t>();
   v.nwords = t.bit_words;
+
   v.n = t.n;
   v.L = t.levels;
   v.max_window = m.max_window;
   v.lv = m.lv[t_b].as<LselLevel>();
   v.rec = m.rec[t_b].as<uint4>();
-  v.plain = sel_view(t.bv, t_b);
+  v.plain = m.plain[t_b].as<SelView>();
   v.misses = m.stats.as<unsigned long long>() + t_b * LSEL_ST + 3;
   const unsigned grid = (unsigned)((nq + 255) / 256);
   count_launch();
