@@ -184,6 +184,40 @@ def select_queries(torch, m_levels, nq, gen, dev):
     return vl[idx].contiguous(), k.contiguous()
 
 
+def measure_queries(torch, tree, seq, n, dev, stream, log2_q, reps=5):
+    """wt_int access and rank(i, c) throughput: 2^log2_q uniform random
+    positions; for rank, i uniform in [0, n] and c drawn from the input."""
+    sp = stream.cuda_stream
+    nq = 1 << log2_q
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(SEED + 11)
+    idx = torch.randint(0, n, (nq,), device=dev, generator=gen, dtype=torch.int64)
+    ri = torch.randint(0, n + 1, (nq,), device=dev, generator=gen, dtype=torch.int64)
+    rc = seq[torch.randint(0, n, (nq,), device=dev, generator=gen, dtype=torch.int64)].to(torch.int64)
+    out = torch.empty(nq, device=dev, dtype=torch.int64)
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+    res = {}
+    for name, fn in (("access", lambda: tree.access_device(idx.data_ptr(), nq, out.data_ptr(), sp)),
+                     ("rank", lambda: tree.rank_device(ri.data_ptr(), rc.data_ptr(), nq, out.data_ptr(), sp))):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = ev(), ev()
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        res[name] = {"mqs": nq / (ms / 1e3) / 1e6, "ms": ms}
+    # access must give back the input
+    tree.access_device(idx.data_ptr(), nq, out.data_ptr(), sp)
+    torch.cuda.synchronize()
+    res["access_exact"] = bool(torch.equal(out, seq[idx].to(torch.int64)))
+    res["queries"] = nq
+    return res
+
+
 LSEL_CONFIGS = (1024, 65536)  # segments per level and polarity: the named model, and a larger one
 
 
@@ -342,9 +376,10 @@ def run_wtg(args, rank, world, local_rank):
     roofline["frac"] = roofline["achieved"] / peak
     kernel_share = {k: {"launches": v[0], "ms": v[1]} for k, v in prof.items()}
 
-    select = None
+    select = queries = None
     if not args.no_select:
         select = measure_select(torch, wtg, tree, n, L, dev, stream, args.select_log2)
+        queries = measure_queries(torch, tree, seq, n, dev, stream, args.select_log2)
 
     # ---- e2e: host API with pinned host buffers, outputs copied back
     e2e = None
@@ -425,6 +460,7 @@ def run_wtg(args, rank, world, local_rank):
         "roofline": roofline,
         "kernel_time": kernel_share,
         "select": select,
+        "queries": queries,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "clocks": clocks.summary(),

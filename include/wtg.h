@@ -162,6 +162,20 @@ int wtg_bv_select_device(wtg_bv* b, int t_b, const uint64_t* d_i, uint64_t nq, u
  * overlap on the GPU (other threads or streams) race. */
 int wtg_rank_build_noalloc(const uint64_t* d_words, uint64_t size_bits, uint64_t* d_rank, void* stream);
 
+/* ------------------------------------------------------------ FM-index count
+ * Backward search over a tree built (with WTG_RANK) on the BWT of a text,
+ * its symbols coded 0..sigma-1: the reference's FM-index is the wavelet tree
+ * of s[SA[i]-1] (s[n-1] where SA[i] == 0) with SA from divsufsort
+ * (fm-index/par/WT.C:33-46); the reference stops at construction, and this
+ * adds the count query.  C[c] = number of BWT symbols below c (sigma
+ * entries).  Pattern p is pat[off[p] .. off[p+1]) (byte codes); out[p] is
+ * the size of its suffix-array range, i.e. its number of occurrences.  A
+ * code >= sigma gives 0, an empty pattern gives n.  sigma <= 256. */
+int wtg_fm_count(wtg_tree* t, const uint64_t* C, uint64_t sigma, const uint8_t* pat, const uint64_t* off,
+                 uint64_t npat, uint64_t* out);
+int wtg_fm_count_device(wtg_tree* t, const uint64_t* d_C, uint64_t sigma, const uint8_t* d_pat,
+                        const uint64_t* d_off, uint64_t npat, uint64_t* d_out, void* stream);
+
 /* ------------------------------------------ per-level and learned select
  * A query is a pair (level, k): the position, inside level `level` of the
  * tree, of that level's k-th one (t_b = 1) or zero (t_b = 0), k >= 1;

@@ -74,6 +74,10 @@ def lib():
         L.or_wt_access_batch.argtypes = [vp, vp, u64, ctypes.c_int, vp, u64, vp]
         L.or_wt_rank_batch.argtypes = [vp, vp, u64, ctypes.c_int, vp, vp, u64, vp]
         L.or_num_threads.restype = ctypes.c_int
+        L.or_suffix_array_u8.argtypes = [vp, ctypes.c_int64, vp]
+        L.or_suffix_array_u8.restype = ctypes.c_int
+        L.or_bwt_u8.argtypes = [vp, vp, ctypes.c_int64, vp]
+        L.or_fm_count.argtypes = [vp, vp, u64, ctypes.c_int, vp, u64, vp, vp, u64, vp]
         _lib = L
     return _lib
 
@@ -199,6 +203,48 @@ def wt_select(tree, rtbl, sel1, sel0, n, levels, i, c):
 # ---------------------------------------------------------------- reference
 
 _ref_libs = {}
+
+
+def suffix_array(s):
+    """Suffix array of a byte string (no sentinel), int64."""
+    s = np.ascontiguousarray(s, dtype=np.uint8)
+    sa = np.zeros(s.size, dtype=np.int64)
+    if lib().or_suffix_array_u8(_p(s), s.size, _p(sa)) != 0:
+        raise MemoryError("oracle suffix array")
+    return sa
+
+
+def bwt(s, sa):
+    """fm-index/par/WT.C:38-41: s[sa[i]-1], or s[n-1] where sa[i] == 0."""
+    s = np.ascontiguousarray(s, dtype=np.uint8)
+    sa = np.ascontiguousarray(sa, dtype=np.int64)
+    out = np.zeros(s.size, dtype=np.uint8)
+    lib().or_bwt_u8(_p(s), _p(sa), s.size, _p(out))
+    return out
+
+
+def fm_count(tree, rtbl, n, levels, C, pat, off):
+    """Backward-search counts of the patterns pat[off[p]:off[p+1]] (codes);
+    C[c] = codes below c, one entry per code."""
+    C = np.ascontiguousarray(C, dtype=np.uint64)
+    pat = np.ascontiguousarray(pat, dtype=np.uint8)
+    off = np.ascontiguousarray(off, dtype=np.uint64)
+    out = np.zeros(off.size - 1, dtype=np.uint64)
+    lib().or_fm_count(_p(tree), _p(rtbl), n, levels, _p(C), C.size, _p(pat) if pat.size else None,
+                      _p(off), out.size, _p(out))
+    return out
+
+
+def ref_divsufsort(s):
+    """The reference's vendored divsufsort (suffixArray/divsufsort), int32 SA."""
+    L = ctypes.CDLL(os.path.join(REF_DIR, "libref_divsufsort.so"))
+    L.divsufsort.argtypes = [vp, vp, ctypes.c_int32]
+    L.divsufsort.restype = ctypes.c_int32
+    s = np.ascontiguousarray(s, dtype=np.uint8)
+    sa = np.zeros(max(s.size, 1), dtype=np.int32)
+    if L.divsufsort(_p(s), _p(sa), s.size) != 0:
+        raise RuntimeError("divsufsort failed")
+    return sa[: s.size]
 
 
 def ref_available(variant="levelwt_u8"):

@@ -586,3 +586,70 @@ void or_wt_rank_batch(const uint64_t* tree, const uint64_t* rt, uint64_t n, int 
 #pragma omp parallel for schedule(static)
   for (int64_t k = 0; k < (int64_t)nq; k++) out[k] = or_wt_rank(tree, rt, n, L, idx[k], sym[k]);
 }
+
+/* ------------------------------------------------------------ FM-index core */
+
+int or_suffix_array_u8(const uint8_t* s, int64_t n, int64_t* sa) {
+  if (n <= 0) return 0;
+  int64_t m = n > 256 ? n : 256;
+  int64_t* x = (int64_t*)malloc(sizeof(int64_t) * n);
+  int64_t* y = (int64_t*)malloc(sizeof(int64_t) * n);
+  int64_t* c = (int64_t*)malloc(sizeof(int64_t) * (m + 1));
+  if (!x || !y || !c) {
+    free(x); free(y); free(c);
+    return -1;
+  }
+  int64_t classes = 256;
+  memset(c, 0, sizeof(int64_t) * (m + 1));
+  for (int64_t i = 0; i < n; i++) c[x[i] = s[i]]++;
+  for (int64_t i = 1; i < classes; i++) c[i] += c[i - 1];
+  for (int64_t i = n - 1; i >= 0; i--) sa[--c[x[i]]] = i;
+  for (int64_t k = 1; k < n; k <<= 1) {
+    /* order by the second key: suffixes without one first, then by sa */
+    int64_t p = 0;
+    for (int64_t i = n - k; i < n; i++) y[p++] = i;
+    for (int64_t i = 0; i < n; i++)
+      if (sa[i] >= k) y[p++] = sa[i] - k;
+    /* stable counting sort by the first key */
+    memset(c, 0, sizeof(int64_t) * (classes + 1));
+    for (int64_t i = 0; i < n; i++) c[x[y[i]]]++;
+    for (int64_t i = 1; i < classes; i++) c[i] += c[i - 1];
+    for (int64_t i = n - 1; i >= 0; i--) sa[--c[x[y[i]]]] = y[i];
+    /* new classes of the first 2k bytes */
+    int64_t* t = x; x = y; y = t;
+    p = 1;
+    x[sa[0]] = 0;
+    for (int64_t i = 1; i < n; i++) {
+      const int64_t a = sa[i - 1], b = sa[i];
+      const int64_t a2 = a + k < n ? y[a + k] : -1, b2 = b + k < n ? y[b + k] : -1;
+      x[b] = (y[a] == y[b] && a2 == b2) ? p - 1 : p++;
+    }
+    if (p >= n) break;
+    classes = p;
+  }
+  free(x); free(y); free(c);
+  return 0;
+}
+
+void or_bwt_u8(const uint8_t* s, const int64_t* sa, int64_t n, uint8_t* bwt) {
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; i++) bwt[i] = s[sa[i] ? sa[i] - 1 : n - 1];
+}
+
+void or_fm_count(const uint64_t* tree, const uint64_t* rt, uint64_t n, int L, const uint64_t* C,
+                 uint64_t sigma, const uint8_t* pat, const uint64_t* off, uint64_t npat, uint64_t* out) {
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int64_t p = 0; p < (int64_t)npat; p++) {
+    uint64_t sp = 0, ep = n;
+    for (uint64_t i = off[p + 1]; i > off[p] && sp < ep; i--) {
+      const uint64_t c = pat[i - 1];
+      if (c >= sigma) {
+        ep = sp;
+        break;
+      }
+      sp = C[c] + or_wt_rank(tree, rt, n, L, sp, c);
+      ep = C[c] + or_wt_rank(tree, rt, n, L, ep, c);
+    }
+    out[p] = ep > sp ? ep - sp : 0;
+  }
+}

@@ -96,6 +96,22 @@ void or_wt_rank_batch(const uint64_t* tree, const uint64_t* rank_tbl, uint64_t n
 void or_select_batch(const or_select* h, const uint64_t* data, const uint64_t* q, uint64_t nq,
                      uint64_t* out);
 
+/* FM-index core (fm-index/par/WT.C:33-46): suffix array, BWT, and counting
+ * by backward search over the wavelet tree of the BWT. */
+/* Suffix array of the n bytes at s: all suffixes, no sentinel, a proper
+ * prefix before its extensions -- the array divsufsort returns
+ * (fm-index/par/WT.C:35-36).  Prefix doubling; returns 0, or -1 when out of
+ * memory. */
+int or_suffix_array_u8(const uint8_t* s, int64_t n, int64_t* sa);
+/* bwt[i] = s[sa[i] - 1], or s[n - 1] where sa[i] == 0 (fm-index/par/WT.C:38-41) */
+void or_bwt_u8(const uint8_t* s, const int64_t* sa, int64_t n, uint8_t* bwt);
+/* Backward search: for pattern p (codes pat[off[p] .. off[p+1])), the size
+ * of its suffix-array range, from [0, n) narrowed right to left by
+ * sp = C[c] + rank(sp, c), ep = C[c] + rank(ep, c) with wt_int's rank over
+ * the tree of the BWT codes; C[c] = number of codes below c. */
+void or_fm_count(const uint64_t* tree, const uint64_t* rank_tbl, uint64_t n, int levels, const uint64_t* C,
+                 uint64_t sigma, const uint8_t* pat, const uint64_t* off, uint64_t npat, uint64_t* out);
+
 /* Number of OpenMP threads the oracle uses (1 without OpenMP). */
 int or_num_threads(void);
 

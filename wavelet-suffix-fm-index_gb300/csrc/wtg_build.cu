@@ -803,6 +803,7 @@ void tree_release(TreeImpl& t) {
   t.err.release(s);
   t.lvl_args.release(s);
   t.lvl_args_ok = false;
+  t.fm_paths.release(s);
   t.scratch.release(s);
   t.nodes.release(s);
   bv_release(t.bv, s);

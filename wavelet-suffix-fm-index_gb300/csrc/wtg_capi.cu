@@ -457,6 +457,41 @@ int wtg_bv_select_device(wtg_bv* B, int t_b, const uint64_t* d_i, uint64_t nq, u
   return launch_bv_select(B->bv, t_b, d_i, nq, d_out, (cudaStream_t)stream);
 }
 
+// ------------------------------------------------------------ FM-index count
+
+int wtg_fm_count(wtg_tree* T, const uint64_t* C, uint64_t sigma, const uint8_t* pat, const uint64_t* off,
+                 uint64_t npat, uint64_t* out) {
+  int rc;
+  if (!T || !C || (npat && (!off || !out))) return fail(WTG_ERR_INVALID, "null argument");
+  if (npat == 0) return WTG_OK;
+  const uint64_t total = off[npat];
+  if (total && !pat) return fail(WTG_ERR_INVALID, "null patterns");
+  for (uint64_t p = 0; p < npat; ++p)
+    if (off[p] > off[p + 1]) return fail(WTG_ERR_INVALID, "pattern offsets must not decrease");
+  if (sigma == 0 || sigma > 256) return fail(WTG_ERR_INVALID, "sigma must be 1..256");
+  TreeImpl& t = T->t;
+  cudaStream_t s = t.stream;
+  const uint64_t words = sigma + (npat + 1) + npat + (total + 7) / 8;
+  if ((rc = t.qbuf.ensure(words * sizeof(uint64_t), s))) return rc;
+  uint64_t* d = t.qbuf.as<uint64_t>();
+  uint64_t* dC = d;
+  uint64_t* dOff = dC + sigma;
+  uint64_t* dOut = dOff + npat + 1;
+  uint8_t* dPat = (uint8_t*)(dOut + npat);
+  WTG_CK(cudaMemcpyAsync(dC, C, sigma * 8, cudaMemcpyHostToDevice, s));
+  WTG_CK(cudaMemcpyAsync(dOff, off, (npat + 1) * 8, cudaMemcpyHostToDevice, s));
+  if (total) WTG_CK(cudaMemcpyAsync(dPat, pat, total, cudaMemcpyHostToDevice, s));
+  if ((rc = launch_fm_count(t, dC, sigma, dPat, dOff, npat, dOut, s))) return rc;
+  WTG_CK(cudaMemcpyAsync(out, dOut, npat * 8, cudaMemcpyDeviceToHost, s));
+  return sync_and_check(s, t.err.as<uint32_t>());
+}
+
+int wtg_fm_count_device(wtg_tree* T, const uint64_t* d_C, uint64_t sigma, const uint8_t* d_pat,
+                        const uint64_t* d_off, uint64_t npat, uint64_t* d_out, void* stream) {
+  if (!T) return fail(WTG_ERR_INVALID, "null tree");
+  return launch_fm_count(T->t, d_C, sigma, d_pat, d_off, npat, d_out, (cudaStream_t)stream);
+}
+
 // ------------------------------------------------ per-level and learned select
 
 int wtg_tree_level_select(wtg_tree* T, int t_b, const uint64_t* level, const uint64_t* k, uint64_t nq,

@@ -31,6 +31,7 @@ struct TreeImpl {
   BvSupport bv;
   DevBuf lvl_args;
   bool lvl_args_ok = false;
+  DevBuf fm_paths;  // per-symbol node paths for FM-index counting
   uint64_t gen = 0;  // builds so far (indexes built on the tree record it)
   std::vector<LselImpl*> deps;  // learned select indexes reading this tree
 };
@@ -75,6 +76,11 @@ int lsel_get_level(const LselImpl& m, int t_b, int level, uint64_t lvl_info[4], 
                    cudaStream_t s);
 int launch_lsel_query(LselImpl& m, int t_b, const uint64_t* level, const uint64_t* k, uint64_t nq,
                       uint64_t* out, cudaStream_t s);
+
+// FM-index counting by backward search over a tree built on a BWT
+// (wtg_fm.cu); C, pat, off and out are device arrays
+int launch_fm_count(TreeImpl& t, const uint64_t* C, uint64_t sigma, const uint8_t* pat, const uint64_t* off,
+                    uint64_t npat, uint64_t* out, cudaStream_t s);
 
 // alphabet remap (levelWT/WTTime.C:80-94) on a device sequence, in place
 int remap_alphabet_device(void* d_seq, uint64_t n, int eb, uint64_t* sigma, DevBuf& tmp, DevBuf& scan_tmp,

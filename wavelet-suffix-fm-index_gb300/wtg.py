@@ -86,6 +86,8 @@ _SIGS = {
     "wtg_lsel_get_level": ([vp, i32, i32, vp, vp, u64], i32),
     "wtg_lsel_query": ([vp, i32, vp, vp, u64, vp], i32),
     "wtg_lsel_query_device": ([vp, i32, vp, vp, u64, vp, vp], i32),
+    "wtg_fm_count": ([vp, vp, u64, vp, vp, u64, vp], i32),
+    "wtg_fm_count_device": ([vp, vp, u64, vp, vp, u64, vp, vp], i32),
     "wtg_remap_alphabet": ([vp, u64, i32, vp], i32),
     "wtg_rank_build_noalloc": ([vp, u64, vp, vp], i32),
     "wtg_profile_enable": ([i32], i32),
@@ -262,6 +264,12 @@ class WaveletTree:
         _ck(lib().wtg_query_select(self.h, _p(i), _p(sym), i.size, _p(out)))
         return out
 
+    def access_device(self, d_idx, nq, d_out, stream=0):
+        _ck(lib().wtg_query_access_device(self.h, vp(d_idx), nq, vp(d_out), vp(stream)))
+
+    def rank_device(self, d_idx, d_sym, nq, d_out, stream=0):
+        _ck(lib().wtg_query_rank_device(self.h, vp(d_idx), vp(d_sym), nq, vp(d_out), vp(stream)))
+
     def level_select(self, level, k, t_b=1):
         """Position inside level `level` of its k-th one (t_b=1) or zero
         (t_b=0) through select_support_mcl (wt_int_par.hpp:651-656)."""
@@ -381,6 +389,39 @@ class LearnedSelect:
 
     def select_device(self, t_b, d_level, d_k, nq, d_out, stream=0):
         _ck(lib().wtg_lsel_query_device(self.h, t_b, vp(d_level), vp(d_k), nq, vp(d_out), vp(stream)))
+
+
+class FMIndex:
+    """FM-index core over a BWT (fm-index/par/WT.C:33-46: the wavelet tree of
+    s[SA[i]-1]): a GPU wavelet tree over the BWT's symbol codes
+    (0..sigma-1), the C array, and backward-search counting on the GPU."""
+
+    def __init__(self, bwt_codes, sigma):
+        bwt_codes = np.ascontiguousarray(bwt_codes, dtype=np.uint8)
+        self.n, self.sigma = bwt_codes.size, int(sigma)
+        self.tree = WaveletTree(bwt_codes, levels=levels_for_sigma(self.sigma), flags=ALL)
+        occ = self.tree.rank(np.full(self.sigma, self.n), np.arange(self.sigma))
+        self.C = np.concatenate([[0], np.cumsum(occ)[:-1]]).astype(np.uint64)
+
+    @staticmethod
+    def pack(patterns):
+        """Concatenated codes and offsets of a list of code arrays."""
+        off = np.zeros(len(patterns) + 1, dtype=np.uint64)
+        off[1:] = np.cumsum([len(p) for p in patterns])
+        pat = np.concatenate([np.asarray(p, dtype=np.uint8) for p in patterns]) if patterns else np.zeros(0, np.uint8)
+        return pat, off
+
+    def count(self, pat, off):
+        pat = np.ascontiguousarray(pat, dtype=np.uint8)
+        off = np.ascontiguousarray(off, dtype=np.uint64)
+        out = np.zeros(off.size - 1, dtype=np.uint64)
+        _ck(lib().wtg_fm_count(self.tree.h, _p(self.C), self.sigma, _p(pat) if pat.size else None, _p(off),
+                               out.size, _p(out)))
+        return out
+
+    def count_device(self, d_C, d_pat, d_off, npat, d_out, stream=0):
+        _ck(lib().wtg_fm_count_device(self.tree.h, vp(d_C), self.sigma, vp(d_pat), vp(d_off), npat, vp(d_out),
+                                      vp(stream)))
 
 
 def rank_build_noalloc(d_words_ptr, size_bits, d_rank_ptr, stream=0):
