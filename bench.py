@@ -218,6 +218,75 @@ def measure_queries(torch, tree, seq, n, dev, stream, log2_q, reps=5):
     return res
 
 
+def measure_batch(torch, wtg, stream, ntexts, reps=5):
+    """Batched build of ntexts DNA-like texts (lengths floor(2^U[10,20]),
+    i.i.d. uniform over 4 symbols, 2 levels, rank + select1 + select0): one
+    persistent launch replayed from a CUDA graph, against the same texts
+    built one by one through the single-sequence device API."""
+    import ctypes
+    rng = np.random.default_rng(SEED + 13)
+    lengths = np.floor(2.0 ** rng.uniform(10, 20, ntexts)).astype(np.uint64)
+    total = int(lengths.sum())
+    texts = rng.integers(0, 4, total, dtype=np.uint8)
+    stream = torch.cuda.Stream()  # the batch runs and is timed on its own stream
+    b = wtg.Batch(lengths, 2, wtg.ALL, stream.cuda_stream)
+    b.load(texts)
+    del texts
+    t0 = time.perf_counter()
+    b.run()  # first run: autotune + graph capture
+    b.sync()
+    first_s = time.perf_counter() - t0
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+    for _ in range(3):
+        b.run()
+    b.sync()
+    e0, e1 = ev(), ev()
+    e0.record(stream)
+    for _ in range(reps):
+        b.run()
+    e1.record(stream)
+    b.sync()
+    ms = e0.elapsed_time(e1) / reps
+    step_bytes = sum(algorithmic_bytes(int(n), 2, 1) for n in lengths)
+    threads, ipt, tune_ms = b.tuning()
+    # the same texts, one single-sequence build each
+    d_in, _ = b.input_device()
+    offs = np.concatenate([[0], np.cumsum(lengths)]).astype(np.uint64)
+    L_ = wtg.lib()
+    h = ctypes.c_void_p()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    wtg._ck(L_.wtg_tree_build_device(ctypes.c_void_p(d_in), int(lengths[0]), 1, 2, wtg.ALL, sp, ctypes.byref(h)))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for t in range(ntexts):
+        wtg._ck(L_.wtg_tree_build_device(ctypes.c_void_p(d_in + int(offs[t])), int(lengths[t]), 1, 2, wtg.ALL, sp,
+                                         ctypes.byref(h)))
+    wtg._ck(L_.wtg_tree_sync(h))
+    plain_s = time.perf_counter() - t0
+    L_.wtg_tree_free(h)
+    # spot check: the batch's outputs for a few texts equal the single builds
+    exact = True
+    for t in rng.choice(ntexts, 4, replace=False):
+        t = int(t)
+        ref = wtg.WaveletTree.from_device(d_in + int(offs[t]), int(lengths[t]), 1, 2, wtg.ALL, stream.cuda_stream)
+        ref.sync()
+        exact = exact and np.array_equal(b.bits(t), ref.bits()) and \
+            np.array_equal(b.rank_table(t), ref.rank_table()) and \
+            np.array_equal(b.select_tables(t, 0).pool, ref.select_tables(0).pool)
+        ref.free()
+    b.free()
+    return {
+        "workload": f"{ntexts} texts, lengths floor(2^U[10,20]), uniform over 4 symbols, 2 levels, "
+                    "rank + select1 + select0 per text",
+        "texts": ntexts, "symbols": total, "algorithmic_bytes": step_bytes,
+        "ms": ms, "gbs": step_bytes / (ms / 1e3) / 1e9, "first_run_s": first_s,
+        "launch_shape": {"threads": threads, "symbols_per_thread": ipt,
+                         "candidates_ms": [round(float(x), 3) for x in tune_ms]},
+        "per_text_plain_ms": plain_s * 1e3, "per_text_plain_gbs": step_bytes / plain_s / 1e9,
+        "speedup_vs_per_text": plain_s * 1e3 / ms, "exact_spot_check": bool(exact),
+    }
+
+
 LSEL_CONFIGS = (1024, 65536)  # segments per level and polarity: the named model, and a larger one
 
 
@@ -376,10 +445,12 @@ def run_wtg(args, rank, world, local_rank):
     roofline["frac"] = roofline["achieved"] / peak
     kernel_share = {k: {"launches": v[0], "ms": v[1]} for k, v in prof.items()}
 
-    select = queries = None
+    select = queries = batch = None
     if not args.no_select:
         select = measure_select(torch, wtg, tree, n, L, dev, stream, args.select_log2)
         queries = measure_queries(torch, tree, seq, n, dev, stream, args.select_log2)
+    if args.batch_texts:
+        batch = measure_batch(torch, wtg, stream, args.batch_texts)
 
     # ---- e2e: host API with pinned host buffers, outputs copied back
     e2e = None
@@ -461,6 +532,7 @@ def run_wtg(args, rank, world, local_rank):
         "kernel_time": kernel_share,
         "select": select,
         "queries": queries,
+        "batch": batch,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "clocks": clocks.summary(),
@@ -483,6 +555,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-select", action="store_true")
+    ap.add_argument("--batch-texts", type=int, default=4096,
+                    help="texts of the batched-build comparison (0: skip it)")
     ap.add_argument("--select-log2", type=int, default=26,
                     help="log2 of the select1 (and of the select0) queries per pass")
     ap.add_argument("--traffic", type=float, default=None,

@@ -53,6 +53,7 @@ extern "C" {
 typedef struct wtg_tree wtg_tree; /* wavelet tree + supports, owns device memory */
 typedef struct wtg_bv wtg_bv;     /* rank/select supports over a caller bitvector */
 typedef struct wtg_lsel wtg_lsel; /* learned select index over a tree's levels */
+typedef struct wtg_batch wtg_batch; /* batched builds of many short texts */
 
 const char* wtg_last_error(void);
 int wtg_version(void);
@@ -161,6 +162,47 @@ int wtg_bv_select_device(wtg_bv* b, int t_b, const uint64_t* d_i, uint64_t nq, u
  * before any stream capture).  All calls share the array, so calls that
  * overlap on the GPU (other threads or streams) race. */
 int wtg_rank_build_noalloc(const uint64_t* d_words, uint64_t size_bits, uint64_t* d_rank, void* stream);
+
+/* ------------------------------------------------------------ batched builds
+ * Many independent texts, each with its own wavelet tree, rank_support_v<1>
+ * and select_support_mcl<1>/<0> -- what a loop of WT() calls
+ * (wavelet/levelWT/WT.h:43) or of wt_int constructions
+ * (wt_int/wt_int_par.hpp:368-406) plus init_support would give, one text per
+ * call -- built in one persistent launch that pulls texts from a device
+ * queue, replayed from a CUDA graph after the first run.
+ *   lengths : symbols of each text (ntexts entries); texts are u8 symbols
+ *             read through their low `levels` bits, concatenated in order
+ *   levels  : 1..4
+ *   flags   : WTG_RANK | WTG_SELECT1 | WTG_SELECT0 (select implies rank)
+ *   stream  : the stream the batch runs on (NULL: the batch makes its own)
+ * The plan allocates every output region (sizes follow from the lengths).
+ * The first wtg_batch_run times each launch shape (threads per CTA x symbols
+ * per thread) on the loaded input, keeps the fastest and captures the build
+ * in a CUDA graph; later runs replay the graph.  Per-text outputs have the
+ * single-sequence layouts (wtg_tree_get_bits / _get_rank / _get_select of a
+ * tree built with the same levels). */
+int wtg_batch_plan(const uint64_t* lengths, uint64_t ntexts, int levels, uint32_t flags, void* stream,
+                   wtg_batch** out);
+/* device address and size of the input buffer (the concatenated texts) */
+int wtg_batch_input(wtg_batch* b, void** d_input, uint64_t* nbytes);
+/* copy the concatenated texts from host memory into the input buffer */
+int wtg_batch_load(wtg_batch* b, const void* texts);
+int wtg_batch_run(wtg_batch* b);
+/* fix the launch shape instead of timing the candidates on the first run:
+ * threads per CTA 256, 512 or 1024; symbols per thread per chunk 4, 8 or 16 */
+int wtg_batch_set_shape(wtg_batch* b, int threads, int items_per_thread);
+int wtg_batch_sync(wtg_batch* b);
+int wtg_batch_free(wtg_batch* b);
+/* after wtg_batch_sync.  text info: n, levels, bit words, rank words, ones,
+ * zeros, and the chosen threads per CTA and symbols per thread */
+int wtg_batch_text_info(wtg_batch* b, uint64_t t, uint64_t info[8]);
+/* select info[8] of text t, as wtg_tree_select_info */
+int wtg_batch_select_info(wtg_batch* b, uint64_t t, int t_b, uint64_t info[8]);
+int wtg_batch_get_bits(wtg_batch* b, uint64_t t, uint64_t* dst, uint64_t nwords);
+int wtg_batch_get_rank(wtg_batch* b, uint64_t t, uint64_t* dst, uint64_t nwords);
+int wtg_batch_get_select(wtg_batch* b, uint64_t t, int t_b, uint64_t* sb_words, uint64_t* desc, uint64_t* pool);
+/* the launch shape the first run chose, and the time of each candidate (ms) */
+int wtg_batch_tuning(wtg_batch* b, int* threads, int* items_per_thread, float ms[8]);
 
 /* ------------------------------------------------------------ FM-index count
  * Backward search over a tree built (with WTG_RANK) on the BWT of a text,

@@ -1,0 +1,118 @@
+"""Batched builds: every text's level bits, rank_support_v table and
+select_support_mcl tables equal those of a single-sequence build of the same
+text (itself bit-exact against the reference and the oracle), for 1..4
+levels, empty and ragged texts, sparse texts with long select blocks, and
+repeated runs replayed from the CUDA graph."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _texts(rng, count, L, max_log2=15):
+    lens = [0, 1, 2, 63, 64, 65, 511, 512, 513, 4095, 4096, 4097, 8192]
+    lens += [int(x) for x in np.floor(2 ** rng.uniform(0, max_log2, count - len(lens)))]
+    texts = [rng.integers(0, 1 << L, n).astype(np.uint8) for n in lens]
+    # values past 2^L are read through their low bits
+    texts.append(rng.integers(0, 256, 3000).astype(np.uint8))
+    return texts
+
+
+def _compare(wtg, b, texts, L):
+    for t, s in enumerate(texts):
+        ref = wtg.WaveletTree(np.asarray(s, dtype=np.uint8), levels=L, flags=wtg.ALL)
+        assert np.array_equal(b.bits(t), ref.bits()), t
+        assert np.array_equal(b.rank_table(t), ref.rank_table()), t
+        for t_b in (0, 1):
+            g, r = b.select_tables(t, t_b), ref.select_tables(t_b)
+            assert (g.size, g.arg_cnt, g.logn, g.logn4, g.nsb, g.has_long, g.sb_nwords, g.pool_nwords) == \
+                   (r.size, r.arg_cnt, r.logn, r.logn4, r.nsb, r.has_long, r.sb_nwords, r.pool_nwords), (t, t_b)
+            assert np.array_equal(g.sb_words, r.sb_words), (t, t_b)
+            assert np.array_equal(g.desc, r.desc), (t, t_b)
+            assert np.array_equal(g.pool, r.pool), (t, t_b)
+        ref.free()
+
+
+@pytest.mark.parametrize("L", [1, 2, 3, 4])
+def test_batch_matches_single_builds(wtg, L):
+    rng = np.random.default_rng(100 + L)
+    texts = _texts(rng, 120, L)
+    b = wtg.Batch.from_texts(texts, L)
+    b.run()
+    b.sync()
+    _compare(wtg, b, texts, L)
+    threads, ipt, ms = b.tuning()
+    assert threads in (256, 512, 1024) and ipt in (4, 8, 16) and (ms > 0).sum() >= 1
+
+
+def test_sparse_texts_take_long_blocks(wtg):
+    rng = np.random.default_rng(7)
+    n = 1 << 20
+    sparse = np.zeros(n, dtype=np.uint8)
+    sparse[rng.choice(n, 900, replace=False)] = 3
+    dense = rng.integers(0, 4, 50000).astype(np.uint8)
+    texts = [sparse, dense, sparse[: n // 2].copy()]
+    b = wtg.Batch.from_texts(texts, 2)
+    b.run()
+    b.sync()
+    assert b.select_tables(0, 1).has_long == 1
+    _compare(wtg, b, texts, 2)
+
+
+def test_graph_replay_is_deterministic(wtg):
+    rng = np.random.default_rng(3)
+    texts = _texts(rng, 60, 2)
+    b = wtg.Batch.from_texts(texts, 2)
+    b.run()
+    b.sync()
+    first = [(b.bits(t), b.rank_table(t), b.select_tables(t, 0).pool) for t in range(len(texts))]
+    for _ in range(3):
+        b.run()
+    b.sync()
+    for t, (bits, rank, pool) in enumerate(first):
+        assert np.array_equal(b.bits(t), bits) and np.array_equal(b.rank_table(t), rank)
+        assert np.array_equal(b.select_tables(t, 0).pool, pool)
+
+
+def test_bits_only_batch(wtg):
+    rng = np.random.default_rng(4)
+    texts = _texts(rng, 40, 3)
+    b = wtg.Batch.from_texts(texts, 3, flags=0)
+    b.run()
+    b.sync()
+    for t, s in enumerate(texts):
+        assert np.array_equal(b.bits(t), wtg.WaveletTree(s, levels=3, flags=0).bits())
+    with pytest.raises(wtg.WtgError):
+        b.rank_table(0)
+
+
+def test_many_texts_per_cta(wtg):
+    # more texts than resident CTAs: every CTA builds several texts in turn
+    rng = np.random.default_rng(11)
+    lens = np.floor(2 ** rng.uniform(8, 14, 1500)).astype(int)
+    texts = [rng.integers(0, 4, n).astype(np.uint8) for n in lens]
+    b = wtg.Batch.from_texts(texts, 2)
+    for _ in range(2):
+        b.run()
+    b.sync()
+    pick = rng.choice(len(texts), 150, replace=False)
+    for t in pick:
+        t = int(t)
+        ref = wtg.WaveletTree(texts[t], levels=2, flags=wtg.ALL)
+        assert np.array_equal(b.bits(t), ref.bits()), t
+        assert np.array_equal(b.rank_table(t), ref.rank_table()), t
+        for t_b in (0, 1):
+            g, r = b.select_tables(t, t_b), ref.select_tables(t_b)
+            assert np.array_equal(g.desc, r.desc) and np.array_equal(g.pool, r.pool), (t, t_b)
+            assert np.array_equal(g.sb_words, r.sb_words), (t, t_b)
+
+
+@pytest.mark.parametrize("L", [2, 3])
+def test_large_texts(wtg, L):
+    rng = np.random.default_rng(21 + L)
+    lens = [1 << 16, (1 << 17) + 5, 300001, (1 << 20) - 1, 777777, 1 << 15]
+    texts = [rng.integers(0, 1 << L, n).astype(np.uint8) for n in lens]
+    b = wtg.Batch.from_texts(texts, L)
+    b.run()
+    b.sync()
+    _compare(wtg, b, texts, L)

@@ -10,6 +10,10 @@ struct wtg_tree {
   wtg::TreeImpl t;
 };
 
+struct wtg_batch {
+  wtg::BatchImpl* b = nullptr;
+};
+
 struct wtg_lsel {
   wtg::LselImpl* m = nullptr;
   wtg::DevBuf qbuf;
@@ -573,6 +577,118 @@ int wtg_lsel_query_device(wtg_lsel* M, int t_b, const uint64_t* d_level, const u
                           uint64_t* d_out, void* stream) {
   if (!M || (t_b != 0 && t_b != 1)) return fail(WTG_ERR_INVALID, "bad argument");
   return launch_lsel_query(*M->m, t_b, d_level, d_k, nq, d_out, (cudaStream_t)stream);
+}
+
+// ------------------------------------------------------------ batched builds
+
+int wtg_batch_plan(const uint64_t* lengths, uint64_t ntexts, int levels, uint32_t flags, void* stream,
+                   wtg_batch** out) {
+  int rc;
+  if (!out || (ntexts && !lengths)) return fail(WTG_ERR_INVALID, "null argument");
+  if ((rc = check_device())) return rc;
+  wtg_batch* B = new (std::nothrow) wtg_batch();
+  if (B) B->b = batch_new();
+  if (!B || !B->b) {
+    delete B;
+    return fail(WTG_ERR_OOM, "host allocation failed");
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  bool own = false;
+  if (!s) {
+    cudaError_t ce = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    if (ce != cudaSuccess) {
+      batch_delete(B->b);
+      delete B;
+      return cuda_fail(ce, "stream create");
+    }
+    own = true;
+  }
+  rc = batch_plan(*B->b, lengths, ntexts, levels, flags, s, own);
+  if (rc != WTG_OK) {
+    batch_delete(B->b);
+    delete B;
+    return rc;
+  }
+  *out = B;
+  return WTG_OK;
+}
+
+int wtg_batch_input(wtg_batch* B, void** d_input, uint64_t* nbytes) {
+  if (!B || !d_input || !nbytes) return fail(WTG_ERR_INVALID, "null argument");
+  *d_input = batch_input(*B->b);
+  *nbytes = batch_total_symbols(*B->b);
+  return WTG_OK;
+}
+
+int wtg_batch_load(wtg_batch* B, const void* texts) {
+  if (!B) return fail(WTG_ERR_INVALID, "null batch");
+  const uint64_t nb = batch_total_symbols(*B->b);
+  if (nb && !texts) return fail(WTG_ERR_INVALID, "null texts");
+  if (nb) WTG_CK(cudaMemcpyAsync(batch_input(*B->b), texts, nb, cudaMemcpyHostToDevice, batch_stream(*B->b)));
+  return WTG_OK;
+}
+
+int wtg_batch_set_shape(wtg_batch* B, int threads, int items_per_thread) {
+  if (!B) return fail(WTG_ERR_INVALID, "null batch");
+  return batch_set_shape(*B->b, threads, items_per_thread);
+}
+
+int wtg_batch_run(wtg_batch* B) {
+  if (!B) return fail(WTG_ERR_INVALID, "null batch");
+  return batch_run(*B->b);
+}
+
+int wtg_batch_sync(wtg_batch* B) {
+  int rc;
+  if (!B) return fail(WTG_ERR_INVALID, "null batch");
+  uint32_t e = 0;
+  if ((rc = batch_sync(*B->b, &e))) return rc;
+  if (e == DERR_SELECT_OVERFLOW) return fail(WTG_ERR_CUDA, "a select pool exceeded its bound (inconsistent tables)");
+  if (e) return fail(WTG_ERR_CUDA, "device reported error code " + std::to_string(e));
+  return WTG_OK;
+}
+
+int wtg_batch_free(wtg_batch* B) {
+  if (!B) return WTG_OK;
+  batch_delete(B->b);
+  delete B;
+  return WTG_OK;
+}
+
+int wtg_batch_text_info(wtg_batch* B, uint64_t t, uint64_t info[8]) {
+  if (!B || !info) return fail(WTG_ERR_INVALID, "null argument");
+  return batch_text_info(*B->b, t, info);
+}
+
+int wtg_batch_select_info(wtg_batch* B, uint64_t t, int t_b, uint64_t info[8]) {
+  if (!B || !info || (t_b != 0 && t_b != 1)) return fail(WTG_ERR_INVALID, "bad argument");
+  return batch_select_info(*B->b, t, t_b, info);
+}
+
+int wtg_batch_get_bits(wtg_batch* B, uint64_t t, uint64_t* dst, uint64_t nwords) {
+  if (!B || (nwords && !dst)) return fail(WTG_ERR_INVALID, "null argument");
+  return batch_get(*B->b, t, 0, 0, dst, nwords);
+}
+
+int wtg_batch_get_rank(wtg_batch* B, uint64_t t, uint64_t* dst, uint64_t nwords) {
+  if (!B || (nwords && !dst)) return fail(WTG_ERR_INVALID, "null argument");
+  return batch_get(*B->b, t, 1, 0, dst, nwords);
+}
+
+int wtg_batch_get_select(wtg_batch* B, uint64_t t, int t_b, uint64_t* sb_words, uint64_t* desc, uint64_t* pool) {
+  int rc;
+  if (!B || (t_b != 0 && t_b != 1)) return fail(WTG_ERR_INVALID, "bad argument");
+  uint64_t si[8];
+  if ((rc = batch_select_info(*B->b, t, t_b, si))) return rc;
+  if ((si[6] && !sb_words) || (si[4] && !desc) || (si[7] && !pool)) return fail(WTG_ERR_INVALID, "null argument");
+  if ((rc = batch_get(*B->b, t, 2, t_b, sb_words, si[6]))) return rc;
+  if ((rc = batch_get(*B->b, t, 3, t_b, desc, si[4]))) return rc;
+  return batch_get(*B->b, t, 4, t_b, pool, si[7]);
+}
+
+int wtg_batch_tuning(wtg_batch* B, int* threads, int* items_per_thread, float ms[8]) {
+  if (!B || !threads || !items_per_thread || !ms) return fail(WTG_ERR_INVALID, "null argument");
+  return batch_tuning(*B->b, threads, items_per_thread, ms, 8);
 }
 
 // ------------------------------------------------------------------ helpers

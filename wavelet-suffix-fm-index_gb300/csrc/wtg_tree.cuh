@@ -82,6 +82,24 @@ int launch_lsel_query(LselImpl& m, int t_b, const uint64_t* level, const uint64_
 int launch_fm_count(TreeImpl& t, const uint64_t* C, uint64_t sigma, const uint8_t* pat, const uint64_t* off,
                     uint64_t npat, uint64_t* out, cudaStream_t s);
 
+// batched builds of many short texts (wtg_batch.cu)
+struct BatchImpl;
+BatchImpl* batch_new();
+void batch_delete(BatchImpl* b);
+int batch_plan(BatchImpl& b, const uint64_t* lengths, uint64_t T, int L, uint32_t flags, cudaStream_t s,
+               bool own_stream);
+int batch_run(BatchImpl& b);
+int batch_set_shape(BatchImpl& b, int threads, int ipt);
+int batch_sync(BatchImpl& b, uint32_t* err_out);
+int batch_text_info(const BatchImpl& b, uint64_t t, uint64_t info[8]);
+int batch_select_info(const BatchImpl& b, uint64_t t, int t_b, uint64_t info[8]);
+// what: 0 bits, 1 rank, 2 m_superblock words, 3 descriptors, 4 pool
+int batch_get(const BatchImpl& b, uint64_t t, int what, int t_b, void* dst, uint64_t nwords);
+void* batch_input(BatchImpl& b);
+cudaStream_t batch_stream(const BatchImpl& b);
+uint64_t batch_total_symbols(const BatchImpl& b);
+int batch_tuning(const BatchImpl& b, int* threads, int* ipt, float* ms, int nms);
+
 // alphabet remap (levelWT/WTTime.C:80-94) on a device sequence, in place
 int remap_alphabet_device(void* d_seq, uint64_t n, int eb, uint64_t* sigma, DevBuf& tmp, DevBuf& scan_tmp,
                           uint32_t* d_err, cudaStream_t s);

@@ -88,6 +88,19 @@ _SIGS = {
     "wtg_lsel_query_device": ([vp, i32, vp, vp, u64, vp, vp], i32),
     "wtg_fm_count": ([vp, vp, u64, vp, vp, u64, vp], i32),
     "wtg_fm_count_device": ([vp, vp, u64, vp, vp, u64, vp, vp], i32),
+    "wtg_batch_plan": ([vp, u64, i32, ctypes.c_uint32, vp, vp], i32),
+    "wtg_batch_input": ([vp, vp, vp], i32),
+    "wtg_batch_load": ([vp, vp], i32),
+    "wtg_batch_run": ([vp], i32),
+    "wtg_batch_set_shape": ([vp, i32, i32], i32),
+    "wtg_batch_sync": ([vp], i32),
+    "wtg_batch_free": ([vp], i32),
+    "wtg_batch_text_info": ([vp, u64, vp], i32),
+    "wtg_batch_select_info": ([vp, u64, i32, vp], i32),
+    "wtg_batch_get_bits": ([vp, u64, vp, u64], i32),
+    "wtg_batch_get_rank": ([vp, u64, vp, u64], i32),
+    "wtg_batch_get_select": ([vp, u64, i32, vp, vp, vp], i32),
+    "wtg_batch_tuning": ([vp, vp, vp, vp], i32),
     "wtg_remap_alphabet": ([vp, u64, i32, vp], i32),
     "wtg_rank_build_noalloc": ([vp, u64, vp, vp], i32),
     "wtg_profile_enable": ([i32], i32),
@@ -422,6 +435,85 @@ class FMIndex:
     def count_device(self, d_C, d_pat, d_off, npat, d_out, stream=0):
         _ck(lib().wtg_fm_count_device(self.tree.h, vp(d_C), self.sigma, vp(d_pat), vp(d_off), npat, vp(d_out),
                                       vp(stream)))
+
+
+class Batch:
+    """Many independent texts (u8 symbols, 1..4 levels), each with its own
+    wavelet tree, rank_support_v and select_support_mcl, built in one
+    persistent launch (include/wtg.h: wtg_batch_plan)."""
+
+    def __init__(self, lengths, levels, flags=ALL, stream=0):
+        self.h = vp()
+        self.lengths = _u64(lengths)
+        self.levels = int(levels)
+        _ck(lib().wtg_batch_plan(_p(self.lengths), self.lengths.size, self.levels, flags, vp(stream),
+                                 ctypes.byref(self.h)))
+
+    @classmethod
+    def from_texts(cls, texts, levels, flags=ALL):
+        b = cls([len(t) for t in texts], levels, flags)
+        b.load(np.concatenate([np.asarray(t, dtype=np.uint8) for t in texts]) if texts else np.zeros(0, np.uint8))
+        return b
+
+    def input_device(self):
+        p, nb = vp(), ctypes.c_uint64(0)
+        _ck(lib().wtg_batch_input(self.h, ctypes.byref(p), ctypes.byref(nb)))
+        return p.value or 0, nb.value
+
+    def load(self, concat):
+        concat = np.ascontiguousarray(concat, dtype=np.uint8)
+        _ck(lib().wtg_batch_load(self.h, _p(concat)))
+
+    def run(self):
+        _ck(lib().wtg_batch_run(self.h))
+
+    def set_shape(self, threads, items_per_thread):
+        _ck(lib().wtg_batch_set_shape(self.h, threads, items_per_thread))
+
+    def sync(self):
+        _ck(lib().wtg_batch_sync(self.h))
+
+    def free(self):
+        if self.h:
+            lib().wtg_batch_free(self.h)
+            self.h = vp()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def text_info(self, t):
+        a = np.zeros(8, dtype=np.uint64)
+        _ck(lib().wtg_batch_text_info(self.h, t, _p(a)))
+        return dict(zip(("n", "levels", "bit_words", "rank_words", "ones", "zeros", "threads", "ipt"),
+                        (int(x) for x in a)))
+
+    def bits(self, t):
+        out = np.zeros(self.text_info(t)["bit_words"], dtype=np.uint64)
+        _ck(lib().wtg_batch_get_bits(self.h, t, _p(out), out.size))
+        return out
+
+    def rank_table(self, t):
+        out = np.zeros(self.text_info(t)["rank_words"], dtype=np.uint64)
+        _ck(lib().wtg_batch_get_rank(self.h, t, _p(out), out.size))
+        return out
+
+    def select_tables(self, t, t_b):
+        info = np.zeros(8, dtype=np.uint64)
+        _ck(lib().wtg_batch_select_info(self.h, t, t_b, _p(info)))
+        sb = np.zeros(max(int(info[6]), 1), dtype=np.uint64)
+        desc = np.zeros(max(int(info[4]), 1), dtype=np.uint64)
+        pool = np.zeros(max(int(info[7]), 1), dtype=np.uint64)
+        _ck(lib().wtg_batch_get_select(self.h, t, t_b, _p(sb), _p(desc), _p(pool)))
+        return _SelectTables(info, sb[: int(info[6])], desc[: int(info[4])], pool[: int(info[7])])
+
+    def tuning(self):
+        th, ipt = ctypes.c_int(0), ctypes.c_int(0)
+        ms = np.zeros(8, dtype=np.float32)
+        _ck(lib().wtg_batch_tuning(self.h, ctypes.byref(th), ctypes.byref(ipt), _p(ms)))
+        return th.value, ipt.value, ms
 
 
 def rank_build_noalloc(d_words_ptr, size_bits, d_rank_ptr, stream=0):
