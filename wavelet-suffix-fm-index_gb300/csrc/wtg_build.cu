@@ -645,6 +645,7 @@ int tree_build(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int L, uint32
   t.flags = flags;
   t.bit_words = (n * (uint64_t)L + 63) / 64;
   t.lvl_args_ok = false;
+  t.node_tab_ok = false;
   ++t.gen;
   const int K = std::min(L, TOP_BITS);
   const uint64_t heap = 1ull << L;  // heap ids 0 .. 2^L - 2, plus one pad entry
@@ -804,6 +805,8 @@ void tree_release(TreeImpl& t) {
   t.lvl_args.release(s);
   t.lvl_args_ok = false;
   t.fm_paths.release(s);
+  t.node_tab.release(s);
+  t.node_tab_ok = false;
   t.scratch.release(s);
   t.nodes.release(s);
   bv_release(t.bv, s);

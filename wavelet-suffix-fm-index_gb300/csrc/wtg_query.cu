@@ -12,41 +12,83 @@ __device__ __forceinline__ int bit_at(const uint64_t* __restrict__ w, uint64_t p
   return (int)((w[p >> 6] >> (p & 63)) & 1);
 }
 
-// wt_int::operator[] (wt_int/wt_int_par.hpp:519-541)
-__global__ void wt_access_kernel(const uint64_t* __restrict__ tree, const uint64_t* __restrict__ rt, uint64_t n,
-                                 int L, const uint64_t* __restrict__ q, uint64_t nq, uint64_t* __restrict__ out) {
-  uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+// Node table: for every heap node h of levels 0..L-1 (root 0, children
+// 2h+1 / 2h+2), x = global bit offset of the node's start and y = ones before
+// it.  These are the `offset` and `o = m_tree_rank(offset)` that wt_int's
+// queries recompute at every level (wt_int_par.hpp:527-536, 561-572,
+// 596-606); with them tabulated, a query level costs one rank probe and one
+// bit word, fetched together with the next level's node entry.
+__global__ void node_table_kernel(const uint64_t* __restrict__ tree, const uint64_t* __restrict__ rt,
+                                  const uint32_t* __restrict__ C, uint64_t n, uint64_t nodes,
+                                  ulonglong2* __restrict__ tab) {
+  const uint64_t h = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (h >= nodes) return;
+  const uint64_t l = 63 - __clzll((long long)(h + 1));
+  const uint64_t off = l * n + C[h];
+  tab[h] = make_ulonglong2(off, rank1_dev(rt, tree, off));
+}
+
+// rank1(pos) with the word holding pos already loaded
+__device__ __forceinline__ uint64_t rank1_with_word(const uint64_t* __restrict__ rt, uint64_t pos, uint64_t word) {
+  const ulonglong2 e = __ldg(reinterpret_cast<const ulonglong2*>(rt) + (pos >> 9));
+  uint64_t r = e.x + ((e.y >> (63 - 9 * ((pos & 0x1FF) >> 6))) & 0x1FF);
+  if (pos & 63) r += __popcll(word & ((1ull << (pos & 63)) - 1));
+  return r;
+}
+
+// wt_int::operator[] (wt_int/wt_int_par.hpp:519-541) and inverse_select
+// (:588-611): descend by the bit at i; the symbol is the path, the rank the
+// final position
+template <bool INV>
+__global__ void wt_descend_kernel(const uint64_t* __restrict__ tree, const uint64_t* __restrict__ rt,
+                                  const ulonglong2* __restrict__ tab, uint64_t n, int L,
+                                  const uint64_t* __restrict__ q, uint64_t nq, uint64_t* __restrict__ out,
+                                  uint64_t* __restrict__ sym_out) {
+  const uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= nq) return;
   uint64_t i = q[k];
   if (i >= n) {
     out[k] = NONE64;
+    if (INV) sym_out[k] = NONE64;
     return;
   }
-  uint64_t offset = 0, res = 0, node_size = n;
+  uint64_t h = 0, c = 0;
+  ulonglong2 nd = __ldg(tab);
   for (int lv = 0; lv < L; ++lv) {
-    res <<= 1;
-    const uint64_t o = rank1_dev(rt, tree, offset);
-    const uint64_t oi = rank1_dev(rt, tree, offset + i) - o;
-    const uint64_t oe = rank1_dev(rt, tree, offset + node_size) - o;
-    if (bit_at(tree, offset + i)) {
-      offset += node_size - oe;
-      node_size = oe;
-      i = oi;
-      res |= 1;
-    } else {
-      node_size = node_size - oe;
-      i = i - oi;
+    const uint64_t pos = nd.x + i;
+    ulonglong2 c0 = nd, c1 = nd;
+    if (lv + 1 < L) {
+      c0 = __ldg(tab + 2 * h + 1);
+      c1 = __ldg(tab + 2 * h + 2);
     }
-    offset += n;
+    const uint64_t word = __ldg(tree + (pos >> 6));
+    const uint64_t r = rank1_with_word(rt, pos, word) - nd.y;
+    const uint64_t bit = (word >> (pos & 63)) & 1;
+    c = (c << 1) | bit;
+    if (bit) {
+      i = r;
+      h = 2 * h + 2;
+      nd = c1;
+    } else {
+      i -= r;
+      h = 2 * h + 1;
+      nd = c0;
+    }
   }
-  out[k] = res;
+  if (INV) {
+    out[k] = i;
+    sym_out[k] = c;
+  } else {
+    out[k] = c;
+  }
 }
 
-// wt_int::rank (wt_int_par.hpp:553-577)
-__global__ void wt_rank_kernel(const uint64_t* __restrict__ tree, const uint64_t* __restrict__ rt, uint64_t n,
-                               int L, const uint64_t* __restrict__ q, const uint64_t* __restrict__ sym, uint64_t nq,
+// wt_int::rank (wt_int_par.hpp:553-577): descend along c's path
+__global__ void wt_rank_kernel(const uint64_t* __restrict__ tree, const uint64_t* __restrict__ rt,
+                               const ulonglong2* __restrict__ tab, uint64_t n, int L,
+                               const uint64_t* __restrict__ q, const uint64_t* __restrict__ sym, uint64_t nq,
                                uint64_t* __restrict__ out) {
-  uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= nq) return;
   uint64_t i = q[k];
   const uint64_t c = sym[k];
@@ -58,55 +100,21 @@ __global__ void wt_rank_kernel(const uint64_t* __restrict__ tree, const uint64_t
     out[k] = 0;
     return;
   }
-  uint64_t offset = 0, mask = 1ull << (L - 1), node_size = n;
+  uint64_t h = 0;
+  ulonglong2 nd = __ldg(tab);
   for (int lv = 0; lv < L && i; ++lv) {
-    const uint64_t o = rank1_dev(rt, tree, offset);
-    const uint64_t oi = rank1_dev(rt, tree, offset + i) - o;
-    const uint64_t oe = rank1_dev(rt, tree, offset + node_size) - o;
-    if (c & mask) {
-      offset += node_size - oe;
-      node_size = oe;
-      i = oi;
-    } else {
-      node_size = node_size - oe;
-      i = i - oi;
-    }
-    offset += n;
-    mask >>= 1;
+    const uint64_t bit = (c >> (L - 1 - lv)) & 1;
+    const uint64_t child = 2 * h + 1 + bit;
+    ulonglong2 next = nd;
+    if (lv + 1 < L) next = __ldg(tab + child);
+    const uint64_t pos = nd.x + i;
+    const uint64_t word = __ldg(tree + (pos >> 6));
+    const uint64_t r = rank1_with_word(rt, pos, word) - nd.y;
+    i = bit ? r : i - r;
+    h = child;
+    nd = next;
   }
   out[k] = i;
-}
-
-// wt_int::inverse_select (wt_int_par.hpp:588-611)
-__global__ void wt_inverse_select_kernel(const uint64_t* __restrict__ tree, const uint64_t* __restrict__ rt,
-                                         uint64_t n, int L, const uint64_t* __restrict__ q, uint64_t nq,
-                                         uint64_t* __restrict__ rank_out, uint64_t* __restrict__ sym_out) {
-  uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= nq) return;
-  uint64_t i = q[k];
-  if (i >= n) {
-    rank_out[k] = sym_out[k] = NONE64;
-    return;
-  }
-  uint64_t c = 0, node_size = n, offset = 0;
-  for (int lv = 0; lv < L; ++lv) {
-    const uint64_t o = rank1_dev(rt, tree, offset);
-    const uint64_t oi = rank1_dev(rt, tree, offset + i) - o;
-    const uint64_t oe = rank1_dev(rt, tree, offset + node_size) - o;
-    c <<= 1;
-    if (bit_at(tree, offset + i)) {
-      offset += node_size - oe;
-      node_size = oe;
-      i = oi;
-      c |= 1;
-    } else {
-      node_size = node_size - oe;
-      i = i - oi;
-    }
-    offset += n;
-  }
-  rank_out[k] = i;
-  sym_out[k] = c;
 }
 
 // wt_int::select (wt_int_par.hpp:622-660)
@@ -174,33 +182,56 @@ static int need(const TreeImpl& t, uint32_t f, const char* what) {
   return WTG_OK;
 }
 
-int launch_wt_access(const TreeImpl& t, const uint64_t* idx, uint64_t nq, uint64_t* out, cudaStream_t s) {
-  if (int rc = need(t, WTG_RANK, "access")) return rc;
+int tree_node_table(TreeImpl& t, cudaStream_t s) {
+  int rc;
+  if (t.node_tab_ok) return WTG_OK;
+  const uint64_t nodes = (1ull << t.levels) - 1;
+  if ((rc = t.node_tab.ensure(nodes * sizeof(ulonglong2), s))) return rc;
+  const uint64_t heap = 1ull << t.levels;
+  node_table_kernel<<<(unsigned)((nodes + 255) / 256), 256, 0, s>>>(
+      t.bits.as<uint64_t>(), t.bv.rank.as<uint64_t>(), t.zeros.as<uint32_t>() + 2 * heap, t.n, nodes,
+      t.node_tab.as<ulonglong2>());
+  count_launch();
+  WTG_CK(cudaGetLastError());
+  t.node_tab_ok = true;
+  return WTG_OK;
+}
+
+int launch_wt_access(TreeImpl& t, const uint64_t* idx, uint64_t nq, uint64_t* out, cudaStream_t s) {
+  int rc;
+  if ((rc = need(t, WTG_RANK, "access"))) return rc;
   if (!nq) return WTG_OK;
-  wt_access_kernel<<<qgrid(nq), 256, 0, s>>>(t.bits.as<uint64_t>(), t.bv.rank.as<uint64_t>(), t.n, t.levels, idx,
-                                            nq, out);
+  if ((rc = tree_node_table(t, s))) return rc;
+  wt_descend_kernel<false><<<qgrid(nq), 256, 0, s>>>(t.bits.as<uint64_t>(), t.bv.rank.as<uint64_t>(),
+                                                    t.node_tab.as<ulonglong2>(), t.n, t.levels, idx, nq, out,
+                                                    nullptr);
   count_launch();
   WTG_CK(cudaGetLastError());
   return WTG_OK;
 }
 
-int launch_wt_rank(const TreeImpl& t, const uint64_t* idx, const uint64_t* sym, uint64_t nq, uint64_t* out,
+int launch_wt_rank(TreeImpl& t, const uint64_t* idx, const uint64_t* sym, uint64_t nq, uint64_t* out,
                    cudaStream_t s) {
-  if (int rc = need(t, WTG_RANK, "rank")) return rc;
+  int rc;
+  if ((rc = need(t, WTG_RANK, "rank"))) return rc;
   if (!nq) return WTG_OK;
-  wt_rank_kernel<<<qgrid(nq), 256, 0, s>>>(t.bits.as<uint64_t>(), t.bv.rank.as<uint64_t>(), t.n, t.levels, idx,
-                                          sym, nq, out);
+  if ((rc = tree_node_table(t, s))) return rc;
+  wt_rank_kernel<<<qgrid(nq), 256, 0, s>>>(t.bits.as<uint64_t>(), t.bv.rank.as<uint64_t>(),
+                                           t.node_tab.as<ulonglong2>(), t.n, t.levels, idx, sym, nq, out);
   count_launch();
   WTG_CK(cudaGetLastError());
   return WTG_OK;
 }
 
-int launch_wt_inverse_select(const TreeImpl& t, const uint64_t* idx, uint64_t nq, uint64_t* rank_out,
+int launch_wt_inverse_select(TreeImpl& t, const uint64_t* idx, uint64_t nq, uint64_t* rank_out,
                              uint64_t* sym_out, cudaStream_t s) {
-  if (int rc = need(t, WTG_RANK, "inverse_select")) return rc;
+  int rc;
+  if ((rc = need(t, WTG_RANK, "inverse_select"))) return rc;
   if (!nq) return WTG_OK;
-  wt_inverse_select_kernel<<<qgrid(nq), 256, 0, s>>>(t.bits.as<uint64_t>(), t.bv.rank.as<uint64_t>(), t.n,
-                                                    t.levels, idx, nq, rank_out, sym_out);
+  if ((rc = tree_node_table(t, s))) return rc;
+  wt_descend_kernel<true><<<qgrid(nq), 256, 0, s>>>(t.bits.as<uint64_t>(), t.bv.rank.as<uint64_t>(),
+                                                   t.node_tab.as<ulonglong2>(), t.n, t.levels, idx, nq, rank_out,
+                                                   sym_out);
   count_launch();
   WTG_CK(cudaGetLastError());
   return WTG_OK;

@@ -32,6 +32,8 @@ struct TreeImpl {
   DevBuf lvl_args;
   bool lvl_args_ok = false;
   DevBuf fm_paths;  // per-symbol node paths for FM-index counting
+  DevBuf node_tab;  // per heap node: bit offset of its start, ones before it
+  bool node_tab_ok = false;
   uint64_t gen = 0;  // builds so far (indexes built on the tree record it)
   std::vector<LselImpl*> deps;  // learned select indexes reading this tree
 };
@@ -41,11 +43,14 @@ int tree_build(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int L, uint32
 int tree_nodes(TreeImpl& t, int ib, uint64_t n_entries, void* d_out);
 void tree_release(TreeImpl& t);
 
-// query launchers (wtg_query.cu); all arrays are device arrays
-int launch_wt_access(const TreeImpl& t, const uint64_t* idx, uint64_t nq, uint64_t* out, cudaStream_t s);
-int launch_wt_rank(const TreeImpl& t, const uint64_t* idx, const uint64_t* sym, uint64_t nq, uint64_t* out,
+// query launchers (wtg_query.cu); all arrays are device arrays.  The node
+// table the access / rank / inverse_select kernels read is filled on first
+// use after a build (tree_node_table).
+int tree_node_table(TreeImpl& t, cudaStream_t s);
+int launch_wt_access(TreeImpl& t, const uint64_t* idx, uint64_t nq, uint64_t* out, cudaStream_t s);
+int launch_wt_rank(TreeImpl& t, const uint64_t* idx, const uint64_t* sym, uint64_t nq, uint64_t* out,
                    cudaStream_t s);
-int launch_wt_inverse_select(const TreeImpl& t, const uint64_t* idx, uint64_t nq, uint64_t* rank_out,
+int launch_wt_inverse_select(TreeImpl& t, const uint64_t* idx, uint64_t nq, uint64_t* rank_out,
                              uint64_t* sym_out, cudaStream_t s);
 int launch_wt_select(const TreeImpl& t, const uint64_t* i, const uint64_t* sym, uint64_t nq, uint64_t* out,
                      cudaStream_t s);
