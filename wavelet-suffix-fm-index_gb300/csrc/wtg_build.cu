@@ -330,10 +330,12 @@ __global__ void __launch_bounds__(LV_THREADS, 4)
   extern __shared__ __align__(128) unsigned char lv_smem[];
   __shared__ __align__(8) uint64_t mbar[LV_THREADS / 32][LV_STAGES];
   __shared__ uint32_t s_words[LV_THREADS / 32][WROWS];
+  __shared__ uint32_t s_nz[LV_THREADS / 32][EMIT_TILES ? WROWS : 1];  // rows' next-level zero masks
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   T* const wring = (T*)(lv_smem + warp * LV_STAGES * CBYTES);  // this warp's LV_STAGES chunk buffers
   uint64_t* const bars = mbar[warp];
   uint32_t* const myw = s_words[warp];
+  uint32_t* const mynz = s_nz[warp];
   const uint64_t nchunks = (n + CHUNK - 1) / CHUNK;
   const uint64_t nfull = bulk_ok ? n / CHUNK : 0;  // chunks fetched with bulk copies
   const uint64_t stride = (uint64_t)gridDim.x * (LV_THREADS / 32);
@@ -414,9 +416,7 @@ __global__ void __launch_bounds__(LV_THREADS, 4)
       }
       const uint2 b = cache_b;
       const uint32_t ob0 = i0 - z;                      // ones before the chunk
-      const uint32_t zlim = ((b.x + z + CHUNK) & ~(uint32_t)(CHUNK - 1)) - b.x;   // zero rank where dst crosses
-      const uint32_t olim = ((b.y + ob0 + CHUNK) & ~(uint32_t)(CHUNK - 1)) - b.y; // one rank where dst crosses
-      uint32_t t0 = 0, t1 = 0, a0 = 0, a1 = 0;  // per-lane emission counters
+      const uint32_t zs = z;                            // zeros before the chunk
 #pragma unroll
       for (int r = 0; r < WROWS; ++r) {
         const uint32_t k = r * 32 + lane;
@@ -431,23 +431,43 @@ __global__ void __launch_bounds__(LV_THREADS, 4)
         if (d < n32) dst[d] = x;
         else atomicCAS(err, 0u, (uint32_t)DERR_BAD_INDEX);
         if (EMIT_TILES) {
-          const uint32_t nz = bit_of(x, shift - 1) ^ 1u;  // next-level bit is 0
-          const uint32_t nzo = nz & one, nzz = nz & (one ^ 1u);
-          t1 += nzo;
-          t0 += nzz;
-          a1 += nzo & (uint32_t)(ob < olim);
-          a0 += nzz & (uint32_t)(zb < zlim);
+          const uint32_t nzm = __ballot_sync(0xffffffffu, !bit_of(x, shift - 1));  // next-level bit is 0
+          if (lane == 0) mynz[r] = nzm;
         }
       }
       if (EMIT_TILES) {
+        // Per 512-symbol chunk of the next level, its symbols whose next bit
+        // is 0: the chunk's zero run lands at b.x + [zs, ...) and its one run
+        // at b.y + [ob0, ...), each crossing at most one destination chunk
+        // boundary (zero rank zlim, one rank olim).  Lane r < WROWS counts
+        // row r from the rows' masks; one warp reduction per value.
+        const uint32_t zlim = ((b.x + zs + CHUNK) & ~(uint32_t)(CHUNK - 1)) - b.x;
+        const uint32_t olim = ((b.y + ob0 + CHUNK) & ~(uint32_t)(CHUNK - 1)) - b.y;
+        __syncwarp();
+        const bool row = lane < (uint32_t)WROWS;
+        const uint32_t omr = row ? myw[lane] : 0u, nzm = row ? mynz[lane] : 0u;
+        const uint32_t zmr = row ? ~omr : 0u;
+        const uint32_t zc = __popc(zmr), oc = __popc(omr);
+        uint32_t zpre = zc;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          t0 += __shfl_xor_sync(0xffffffffu, t0, o);
-          t1 += __shfl_xor_sync(0xffffffffu, t1, o);
-          a0 += __shfl_xor_sync(0xffffffffu, a0, o);
-          a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t q = __shfl_up_sync(0xffffffffu, zpre, o);
+          if (lane >= (uint32_t)o) zpre += q;
         }
-        const uint32_t zs = i0 - ob0;  // zeros before the chunk
+        zpre -= zc;                                 // zeros of the chunk before row `lane`
+        const uint32_t zrow = zs + zpre;            // level-wide zero rank of the row's first zero
+        const uint32_t orow = ob0 + 32u * lane - zpre;  // and one rank of its first one
+        const uint32_t nzz = nzm & zmr, nzo = nzm & omr;
+        uint32_t t0 = __popc(nzz), t1 = __popc(nzo);
+        uint32_t a0 = zlim >= zrow + zc ? t0 : 0u, a1 = olim >= orow + oc ? t1 : 0u;
+        if (zlim > zrow && zlim < zrow + zc)
+          a0 = __popc(nzz & ((1u << sel64_0((uint64_t)zmr, zlim - zrow)) - 1u));
+        if (olim > orow && olim < orow + oc)
+          a1 = __popc(nzo & ((1u << sel64_0((uint64_t)omr, olim - orow)) - 1u));
+        t0 = __reduce_add_sync(0xffffffffu, t0);
+        t1 = __reduce_add_sync(0xffffffffu, t1);
+        a0 = __reduce_add_sync(0xffffffffu, a0);
+        a1 = __reduce_add_sync(0xffffffffu, a1);
         const uint32_t k0 = (b.x + zs) >> LOG_CHUNK, k1 = (b.y + ob0) >> LOG_CHUNK;
         if (lane == 0) {
           if (a0) atomicAdd(&chunkcnt_next[k0], a0);
