@@ -7,8 +7,9 @@ rank_support_v<1>, select_support_mcl<1> and select_support_mcl<0> over the
 concatenated 20 x 2^30-bit level bitvector.
 
   value : algorithmic GB/s of the whole build with the input resident in HBM
-  e2e   : the same through the host API (wtg_tree_build from pinned host
-          memory, plus the copy of bits, rank and select tables back)
+  e2e   : the same through the host API from pinned host memory:
+          wtg_tree_build_out (input copied in, bits and rank table copied
+          back while the build runs) plus the select tables' getters
 The algorithmic bytes of one build are
   L*n*w (level reads) + (L-1)*n*w (next-level writes) + L*n/8 (bits)
   + [L*n/8 + 16*((L*n>>9)+1)] (rank: read bits, write table)
@@ -479,9 +480,10 @@ def run_wtg(args, rank, world, local_rank):
         vp = ctypes.c_void_p
 
         def e2e_step():
-            wtg._ck(L_.wtg_tree_build(vp(host_in.data_ptr()), n, 4, L, wtg.ALL, ctypes.byref(h)))
-            wtg._ck(L_.wtg_tree_get_bits(h, vp(outs["bits"].data_ptr()), t_e.bit_words))
-            wtg._ck(L_.wtg_tree_get_rank(h, vp(outs["rank"].data_ptr()), t_e.rank_words))
+            # bits and rank table come back while the build runs; then the
+            # select tables (their sizes are known only after the build)
+            wtg._ck(L_.wtg_tree_build_out(vp(host_in.data_ptr()), n, 4, L, wtg.ALL, vp(outs["bits"].data_ptr()),
+                                          vp(outs["rank"].data_ptr()), ctypes.byref(h)))
             for tb in (1, 0):
                 wtg._ck(L_.wtg_tree_get_select(h, tb, vp(outs[f"sb{tb}"].data_ptr()),
                                                vp(outs[f"desc{tb}"].data_ptr()), vp(outs[f"pool{tb}"].data_ptr())))

@@ -80,6 +80,17 @@ int wtg_tree_build(const void* seq, uint64_t n, int elem_bytes, int levels, uint
 /* When *out is non-NULL on entry, wtg_tree_build rebuilds that handle in place
  * (reusing its device buffers) instead of creating a new one. */
 
+/* Same as wtg_tree_build, and copies the level bitvector (bit words) and the
+ * rank table (rank words, see wtg_tree_info) to host memory while the build
+ * runs: the bits of each level leave as soon as its pass is done and the
+ * rank table beside the select finishing kernels.  Either destination may be
+ * NULL; levels must be given (not 0).  With page-locked destinations the
+ * copies overlap the kernels; pageable ones work but wait for each copy.
+ * Returns once the build and the copies are complete.  No counterpart in the
+ * reference: WT()'s output arrays (wavelet/levelWT/WT.h:43) filled in place. */
+int wtg_tree_build_out(const void* seq, uint64_t n, int elem_bytes, int levels, uint32_t flags, uint64_t* bits_dst,
+                       uint64_t* rank_dst, wtg_tree** out);
+
 /* Same, from device memory, enqueued on `stream` (a cudaStream_t, NULL for
  * the legacy default stream).  When *out is non-NULL the handle is rebuilt in
  * place, reusing its device buffers.  Returns once the work is enqueued and

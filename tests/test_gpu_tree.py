@@ -189,3 +189,24 @@ def test_large_properties(wtg):
             assert sym[int(pos[0])] == c and sym[int(pos[1])] == c
             assert np.count_nonzero(sym[: int(pos[0])] == c) == 0
             assert t.rank(np.array([n], dtype=np.uint64), np.array([c], dtype=np.uint64))[0] == k
+
+
+@pytest.mark.parametrize("kind,n", [("exp20", 100003), ("exp20", 1 << 20), ("five3", 4097), ("zipf8", 1 << 18),
+                                    ("bin1", 65)])
+def test_build_out_copies_equal_getters(wtg, kind, n):
+    import torch
+    sym, L = _gen(kind, n, seed=3 * n)
+    ref = wtg.WaveletTree(sym, levels=L, flags=wtg.ALL)
+    for pinned in (False, True):
+        if pinned:
+            bits_t = torch.zeros(ref.bit_words, dtype=torch.int64).pin_memory()
+            rank_t = torch.zeros(ref.rank_words, dtype=torch.int64).pin_memory()
+            bits, rank = bits_t.numpy().view(np.uint64), rank_t.numpy().view(np.uint64)
+        else:
+            bits = np.zeros(ref.bit_words, dtype=np.uint64)
+            rank = np.zeros(ref.rank_words, dtype=np.uint64)
+        t = wtg.WaveletTree.build_out(sym, L, wtg.ALL, bits.ctypes.data, rank.ctypes.data)
+        assert np.array_equal(bits, ref.bits())
+        assert np.array_equal(rank, ref.rank_table())
+        assert np.array_equal(t.select_tables(1).pool, ref.select_tables(1).pool)
+        t.free()

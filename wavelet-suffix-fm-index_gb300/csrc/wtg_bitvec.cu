@@ -277,6 +277,7 @@ int bv_from_levels(BvSupport& bv, const uint64_t* d_words, uint64_t n, int L, co
                                          bv.info.as<unsigned long long>());
   count_launch();
   WTG_CK(cudaGetLastError());
+  if (bv.rank_done) WTG_CK(cudaEventRecord(bv.rank_done, s));
   return bv_finish(bv, d_err, s);
 }
 
@@ -588,6 +589,7 @@ int bv_build(BvSupport& bv, const uint64_t* d_words, uint64_t size, uint32_t fla
   int rc;
   if ((rc = bv_prepare(bv, d_words, size, flags, s))) return rc;
   if ((rc = bv_pass(bv, d_err, s))) return rc;
+  if (bv.rank_done) WTG_CK(cudaEventRecord(bv.rank_done, s));
   return bv_finish(bv, d_err, s);
 }
 

@@ -766,6 +766,18 @@ int tree_build(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int L, uint32
       count_launch();
       WTG_CK(cudaGetLastError());
       src = a.dst;
+      if (t.host_bits) {
+        // words holding only bits of levels <= l are final now; the word
+        // shared with level l + 1 goes with the next level
+        const uint64_t w_lo = ((uint64_t)l * n) >> 6;
+        const uint64_t w_hi = (l == L - 1) ? t.bit_words : (((uint64_t)l + 1) * n) >> 6;
+        if (w_hi > w_lo) {
+          WTG_CK(cudaEventRecord(t.copy_ev, s));
+          WTG_CK(cudaStreamWaitEvent(t.copy_stream, t.copy_ev, 0));
+          WTG_CK(cudaMemcpyAsync(t.host_bits + w_lo, t.bits.as<uint64_t>() + w_lo, (w_hi - w_lo) * 8,
+                                 cudaMemcpyDeviceToHost, t.copy_stream));
+        }
+      }
       const int m = l + 1;  // next level: derive its tables when the pre-pass did not
       if (m >= K && m <= L - 1) {
         const uint64_t cnt = 1ull << m;
@@ -783,6 +795,7 @@ int tree_build(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int L, uint32
   }
 
   // rank / select over the concatenated bitvector
+  t.bv.rank_done = (t.host_rank && (flags & WTG_RANK)) ? t.rank_ev : nullptr;
   if (rs_from_levels) {
     uint32_t* last_cnt = tilecnt + (uint64_t)(L - 1) * (tiles + 1);
     uint32_t* last_pre = tilepre_all + (uint64_t)(L - 1) * (tiles + 1);
@@ -793,6 +806,16 @@ int tree_build(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int L, uint32
       return rc;
   } else if (flags) {
     if ((rc = bv_build(t.bv, t.bits.as<uint64_t>(), n * (uint64_t)L, flags, d_err, s))) return rc;
+  }
+  if (t.bv.rank_done) {
+    // the rank table was complete before the select finishing kernels
+    // started; its copy runs beside them
+    const uint64_t size = n * (uint64_t)L;
+    const uint64_t cap = (size + 63) / 64 * 64;
+    const uint64_t rank_words = size ? ((cap >> 9) + 1) * 2 : 2;
+    WTG_CK(cudaStreamWaitEvent(t.copy_stream, t.bv.rank_done, 0));
+    WTG_CK(cudaMemcpyAsync(t.host_rank, t.bv.rank.p, rank_words * 8, cudaMemcpyDeviceToHost, t.copy_stream));
+    t.bv.rank_done = nullptr;
   }
   return WTG_OK;
 }
@@ -811,6 +834,14 @@ int tree_nodes(TreeImpl& t, int ib, uint64_t n_entries, void* d_out) {
 
 void tree_release(TreeImpl& t) {
   cudaStream_t s = t.stream;
+  if (t.copy_stream) {
+    cudaStreamSynchronize(t.copy_stream);
+    cudaStreamDestroy(t.copy_stream);
+    t.copy_stream = nullptr;
+  }
+  if (t.copy_ev) cudaEventDestroy(t.copy_ev);
+  if (t.rank_ev) cudaEventDestroy(t.rank_ev);
+  t.copy_ev = t.rank_ev = nullptr;
   lsel_detach_all(t);
   t.seq.release(s);
   t.lvl[0].release(s);

@@ -162,6 +162,57 @@ int wtg_tree_build(const void* seq, uint64_t n, int elem_bytes, int levels, uint
   return WTG_OK;
 }
 
+int wtg_tree_build_out(const void* seq, uint64_t n, int elem_bytes, int levels, uint32_t flags, uint64_t* bits_dst,
+                       uint64_t* rank_dst, wtg_tree** out) {
+  int rc;
+  if (!out || (!seq && n)) return fail(WTG_ERR_INVALID, "null argument");
+  if ((rc = check_seq_args(n, elem_bytes, levels, flags))) return rc;
+  if (levels == 0 && (bits_dst || rank_dst))
+    return fail(WTG_ERR_INVALID, "give the levels explicitly when outputs are copied during the build");
+  if (rank_dst && !(flags & WTG_RANK)) return fail(WTG_ERR_INVALID, "rank_dst needs WTG_RANK");
+  if ((rc = check_device())) return rc;
+  wtg_tree* T = *out;
+  const bool fresh = (T == nullptr);
+  if (fresh) {
+    T = new (std::nothrow) wtg_tree();
+    if (!T) return fail(WTG_ERR_OOM, "host allocation failed");
+  }
+  TreeImpl& t = T->t;
+  cudaError_t e = cudaSuccess;
+  if (!t.own_stream) {
+    e = cudaStreamCreateWithFlags(&t.stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) t.own_stream = true;
+  }
+  if (e == cudaSuccess && !t.copy_stream) e = cudaStreamCreateWithFlags(&t.copy_stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess && !t.copy_ev) e = cudaEventCreateWithFlags(&t.copy_ev, cudaEventDisableTiming);
+  if (e == cudaSuccess && !t.rank_ev) e = cudaEventCreateWithFlags(&t.rank_ev, cudaEventDisableTiming);
+  if (e != cudaSuccess) {
+    if (fresh) wtg_tree_free(T);
+    return cuda_fail(e, "stream/event create");
+  }
+  if ((rc = t.seq.ensure(n * elem_bytes, t.stream)) == WTG_OK) {
+    cudaError_t ce = cudaSuccess;
+    if (n) ce = cudaMemcpyAsync(t.seq.p, seq, n * elem_bytes, cudaMemcpyHostToDevice, t.stream);
+    if (ce != cudaSuccess) rc = cuda_fail(ce, "cudaMemcpyAsync(seq)");
+  }
+  t.host_bits = bits_dst;
+  t.host_rank = rank_dst;
+  if (rc == WTG_OK) rc = build_tree_common(T, t.seq.p, n, elem_bytes, levels, flags);
+  t.host_bits = nullptr;
+  t.host_rank = nullptr;
+  if (rc == WTG_OK) rc = sync_and_check(t.stream, t.err.as<uint32_t>());
+  if (rc == WTG_OK) {
+    const cudaError_t ce = cudaStreamSynchronize(t.copy_stream);
+    if (ce != cudaSuccess) rc = cuda_fail(ce, "copies of the outputs");
+  }
+  if (rc != WTG_OK) {
+    if (fresh) wtg_tree_free(T);
+    return rc;
+  }
+  *out = T;
+  return WTG_OK;
+}
+
 int wtg_tree_build_device(const void* d_seq, uint64_t n, int elem_bytes, int levels, uint32_t flags, void* stream,
                           wtg_tree** out) {
   int rc;

@@ -307,6 +307,7 @@ struct BvSupport {
   DevBuf status;     // look-back status words + tile counter
   DevBuf scan_tmp;
   SelectDev sel[2];  // [t_b]
+  cudaEvent_t rank_done = nullptr;  // when set, recorded once the rank table is complete
 };
 
 int bv_build(BvSupport& bv, const uint64_t* d_words, uint64_t size, uint32_t flags, uint32_t* d_err,

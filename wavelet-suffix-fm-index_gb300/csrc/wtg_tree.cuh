@@ -35,6 +35,12 @@ struct TreeImpl {
   DevBuf node_tab;  // per heap node: bit offset of its start, ones before it
   bool node_tab_ok = false;
   uint64_t gen = 0;  // builds so far (indexes built on the tree record it)
+  // host destinations filled while the build runs (wtg_tree_build_out): the
+  // bits of each level are copied on copy_stream as soon as its pass is done
+  uint64_t* host_bits = nullptr;
+  uint64_t* host_rank = nullptr;
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t copy_ev = nullptr, rank_ev = nullptr;
   std::vector<LselImpl*> deps;  // learned select indexes reading this tree
 };
 

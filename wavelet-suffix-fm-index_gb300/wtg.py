@@ -52,6 +52,7 @@ _SIGS = {
     "wtg_launch_count": ([], u64),
     "wtg_tree_build": ([vp, u64, i32, i32, ctypes.c_uint32, vp], i32),
     "wtg_tree_build_device": ([vp, u64, i32, i32, ctypes.c_uint32, vp, vp], i32),
+    "wtg_tree_build_out": ([vp, u64, i32, i32, ctypes.c_uint32, vp, vp, vp], i32),
     "wtg_tree_sync": ([vp], i32),
     "wtg_tree_free": ([vp], i32),
     "wtg_tree_info": ([vp, vp], i32),
@@ -193,6 +194,20 @@ class WaveletTree:
         _ck(lib().wtg_tree_info(self.h, _p(info)))
         self.n, self.levels, self.bit_words, self.rank_words = [int(x) for x in info]
         self.flags = flags
+
+    @classmethod
+    def build_out(cls, seq, levels, flags, bits_ptr, rank_ptr, tree=None):
+        """Build from host memory and copy the bits (and the rank table) to
+        the host buffers at bits_ptr / rank_ptr while the build runs
+        (wtg_tree_build_out); returns the tree for the remaining outputs."""
+        seq = np.ascontiguousarray(seq)
+        h = tree.h if tree is not None else vp()
+        _ck(lib().wtg_tree_build_out(_p(seq), seq.size, seq.dtype.itemsize, int(levels), flags, vp(bits_ptr),
+                                     vp(rank_ptr), ctypes.byref(h)))
+        if tree is not None:
+            tree.__init__(_handle=h, flags=flags)
+            return tree
+        return cls(_handle=h, flags=flags)
 
     @classmethod
     def from_device(cls, d_ptr, n, elem_bytes, levels, flags=ALL, stream=0, tree=None):
