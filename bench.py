@@ -63,6 +63,22 @@ def level_launch_bytes(n, w):
     return 2 * n * w + n / 8
 
 
+def slowest_rank(dist, torch, seconds, device):
+    """The job's time: the maximum of one value over all ranks (identity
+    without a process group)."""
+    if not dist:
+        return seconds
+    t = torch.tensor([seconds], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(world, steps, step_bytes, seconds):
+    """Whole-job GB/s: every rank builds its own sequence of step_bytes per
+    step (replicas), all finishing within `seconds` (the slowest rank)."""
+    return world * steps * step_bytes / seconds / 1e9
+
+
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -426,12 +442,8 @@ def run_wtg(args, rank, world, local_rank):
     launches = wtg.launch_count() - launches0
     wtg.profile_enable(False)
     prof = wtg.profile_read()
-    ms = start.elapsed_time(end)
-    if dist:
-        t = torch.tensor([ms], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * args.steps * step_bytes / (ms / 1e3) / 1e9
+    ms = slowest_rank(dist, torch, start.elapsed_time(end), dev)
+    value = job_throughput(world, args.steps, step_bytes, ms / 1e3)
 
     peak, peak_kind = measured_peaks()
     lv_n, lv_ms = prof["level"]
@@ -497,12 +509,8 @@ def run_wtg(args, rank, world, local_rank):
         for _ in range(e_steps):
             e2e_step()
         torch.cuda.synchronize()
-        e_s = time.perf_counter() - t0
-        if dist:
-            t = torch.tensor([e_s], device=dev, dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e_s = float(t.item())
-        e2e = {"value": world * e_steps * step_bytes / e_s / 1e9, "unit": "GB/s",
+        e_s = slowest_rank(dist, torch, time.perf_counter() - t0, dev)
+        e2e = {"value": job_throughput(world, e_steps, step_bytes, e_s), "unit": "GB/s",
                "h2d_bytes_per_step": 4 * n, "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e_s / e_steps}
         t_e.free()
 
