@@ -310,8 +310,8 @@ __device__ void batch_text(const BatchArgs& a, uint64_t t, BatchSmem<THREADS>& s
       if (a.flags & WTG_RANK) {
         const uint32_t kmax = (b < NB) ? 7u : (r_last > 1 ? (uint32_t)r_last : 1u);
         uint64_t part = (g8 >= 1 && g8 <= kmax) ? ((uint64_t)excl << (63 - 9 * g8)) : 0ull;
-#pragma unroll
-        for (int o = 1; o < 8; o <<= 1) part |= __shfl_xor_sync(0xffffffffu, part, o);
+  #pragma unroll
+      for (int o = 1; o < 8; o <<= 1) part |= __shfl_xor_sync(0xffffffffu, part, o);
         if (g8 == 0 && b <= NB) {
           rank[2 * b] = sb_before;
           rank[2 * b + 1] = part;

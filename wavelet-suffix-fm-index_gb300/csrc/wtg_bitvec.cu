@@ -201,8 +201,8 @@ __global__ void __launch_bounds__(256)
         const uint64_t sb_before = 512 * b - (zl + pres[u]);  // ones before the superblock
         if (flags & WTG_RANK) {
           uint64_t part = g8 >= 1 ? ((uint64_t)excl << (63 - 9 * g8)) : 0ull;
-#pragma unroll
-          for (int o = 1; o < 8; o <<= 1) part |= __shfl_xor_sync(0xffffffffu, part, o);
+    #pragma unroll
+      for (int o = 1; o < 8; o <<= 1) part |= __shfl_xor_sync(0xffffffffu, part, o);
           if (g8 == 0 && valid) {
             rank[2 * b] = sb_before;
             rank[2 * b + 1] = part;

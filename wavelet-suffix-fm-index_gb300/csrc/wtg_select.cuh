@@ -69,37 +69,42 @@ __device__ __forceinline__ uint64_t select_dev(const SelView& v, uint64_t i) {
 // Select marks of one 64-bit word wi, given K1 = ones before it: for
 // select1 (x) and select0 (~x) the position of every 64th arg (low 32 bits,
 // samp[dir * (arg / 64)]), every superblock start (arg 4096q) and end (arg
-// 4096q + 4095).  The next multiple of 64 is (-K) & 63 args into the word
-// (for zeros, K0 = 64 wi - K1, so K1 & 63); one branch-free select per
-// support and word, stores predicated.  zmask clears bits past the end.
+// 4096q + 4095).  The next multiple of 64 is d1 = (-K1) & 63 ones into the
+// word, and d0 = K1 & 63 zeros into it (K0 = 64 wi - K1).  As d1 + d0 is 64
+// or 0, a word holds the next 64th arg of at most one polarity unless K1 is
+// a multiple of 64, and then both are the word's first one and first zero:
+// one branch-free select serves every word.  zmask clears bits past the end.
 __device__ __forceinline__ void word_marks(uint64_t x, uint32_t c, uint64_t K1, uint64_t wi, uint64_t zmask,
                                            bool sel1, bool sel0, uint32_t* __restrict__ samples, uint64_t samp_last,
                                            uint64_t* __restrict__ starts1, uint64_t* __restrict__ starts0,
                                            uint64_t* __restrict__ ends1, uint64_t* __restrict__ ends0,
                                            uint64_t& last1, uint64_t& last0) {
-  if (sel1 && c) {
-    const uint32_t d = (uint32_t)(0u - (uint32_t)K1) & 63u;
-    const uint64_t pos = (wi << 6) + sel64_0(x, d & 63u);
-    if (d < c) {
-      const uint64_t k = K1 + d;
+  const uint64_t z = ~x & zmask;
+  const uint32_t cz = __popcll(z);
+  const uint64_t K0 = (wi << 6) - K1;
+  const uint32_t d1 = (uint32_t)(0u - (uint32_t)K1) & 63u;
+  const uint32_t d0 = (uint32_t)K1 & 63u;
+  const bool s1 = sel1 && d1 < c, s0 = sel0 && d0 < cz;
+  if (s1 || s0) {
+    const uint64_t pos = (wi << 6) + sel64_0(s1 ? x : z, s1 ? d1 : d0);
+    if (s1) {
+      const uint64_t k = K1 + d1;
       samples[k >> 6] = (uint32_t)pos;
       if ((k & 4095) == 0) starts1[k >> 12] = pos;
     }
+    if (s0) {
+      const uint64_t pos0 = s1 ? (wi << 6) + (uint64_t)(__ffsll((long long)z) - 1) : pos;
+      const uint64_t k = K0 + d0;
+      samples[samp_last - (k >> 6)] = (uint32_t)pos0;
+      if ((k & 4095) == 0) starts0[k >> 12] = pos0;
+    }
+  }
+  if (sel1 && c) {
     const uint32_t e = 4095u - ((uint32_t)K1 & 4095u);
     if (e < c) ends1[(K1 + e) >> 12] = (wi << 6) + sel64_0(x, e);
     last1 = max(last1, (wi << 6) + hi64(x) + 1);
   }
-  const uint64_t z = ~x & zmask;
-  const uint32_t cz = __popcll(z);
   if (sel0 && cz) {
-    const uint64_t K0 = (wi << 6) - K1;
-    const uint32_t d = (uint32_t)K1 & 63u;  // == (-K0) & 63
-    const uint64_t pos = (wi << 6) + sel64_0(z, d);
-    if (d < cz) {
-      const uint64_t k = K0 + d;
-      samples[samp_last - (k >> 6)] = (uint32_t)pos;
-      if ((k & 4095) == 0) starts0[k >> 12] = pos;
-    }
     const uint32_t e = 4095u - ((uint32_t)K0 & 4095u);
     if (e < cz) ends0[(K0 + e) >> 12] = (wi << 6) + sel64_0(z, e);
     last0 = max(last0, (wi << 6) + hi64(z) + 1);
