@@ -158,12 +158,20 @@ __device__ void batch_text(const BatchArgs& a, uint64_t t, BatchSmem<THREADS>& s
     uint32_t c[1 << BATCH_LMAX];
 #pragma unroll
     for (int b = 0; b < (1 << BATCH_LMAX); ++b) c[b] = 0;
-    for (uint64_t i0 = (uint64_t)warp * 32; i0 < n; i0 += THREADS) {
-      const uint64_t i = i0 + lane;
-      const uint32_t v = i < n ? (in[i] & vmask) : BATCH_INVALID;
+    // 8 rows of 32 symbols per warp step, all loads issued before the counting
+    constexpr int HR = 8;
+    for (uint64_t i0 = (uint64_t)warp * 32 * HR; i0 < n; i0 += (uint64_t)THREADS * HR) {
+      uint32_t v[HR];
 #pragma unroll
-      for (int b = 0; b < (1 << BATCH_LMAX); ++b)
-        if ((uint32_t)b < nbin) c[b] += __popc(__ballot_sync(0xffffffffu, v == (uint32_t)b));
+      for (int r = 0; r < HR; ++r) {
+        const uint64_t i = i0 + 32 * r + lane;
+        v[r] = i < n ? (in[i] & vmask) : BATCH_INVALID;
+      }
+#pragma unroll
+      for (int r = 0; r < HR; ++r)
+#pragma unroll
+        for (int b = 0; b < (1 << BATCH_LMAX); ++b)
+          if ((uint32_t)b < nbin) c[b] += __popc(__ballot_sync(0xffffffffu, v[r] == (uint32_t)b));
     }
     if (lane == 0) {
 #pragma unroll
