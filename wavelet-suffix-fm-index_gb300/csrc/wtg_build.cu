@@ -388,6 +388,7 @@ __global__ void __launch_bounds__(LV_THREADS, 4)
     }
 
     const uint32_t i0 = (uint32_t)cbase;
+    bool bad = false;                          // a destination outside dst (inconsistent tables)
     uint32_t z = SCATTER ? chunkpre[c] : 0u;  // level-wide zeros before the chunk
     uint32_t p0 = 0;
     bool uniform = true;
@@ -404,7 +405,7 @@ __global__ void __launch_bounds__(LV_THREADS, 4)
         const uint32_t k = r * 32 + lane;
         const bool valid = k < cvalid;
         const uint32_t om = __ballot_sync(0xffffffffu, valid && bit_of(wt[k], shift));
-        if (lane == 0) myw[r] = om;
+        myw[r] = om;  // every lane stores the same word: no branch
         zc += __popc(__ballot_sync(0xffffffffu, valid) & ~om);
       }
       if (chunkcnt_self && lane == 0) chunkcnt_self[c] = zc;
@@ -423,16 +424,17 @@ __global__ void __launch_bounds__(LV_THREADS, 4)
         const T x = wt[k];
         const uint32_t one = bit_of(x, shift);
         const uint32_t om = __ballot_sync(0xffffffffu, one);
-        if (lane == 0) myw[r] = om;
+        myw[r] = om;  // every lane stores the same word: no branch
         const uint32_t zb = z + __popc(~om & ltmask);  // zeros before x (level-wide)
         z += 32u - __popc(om);
         const uint32_t ob = i0 + k - zb;                // ones before x (level-wide)
         const uint32_t d = one ? b.y + ob : b.x + zb;
-        if (d < n32) dst[d] = x;
-        else atomicCAS(err, 0u, (uint32_t)DERR_BAD_INDEX);
+        const bool okd = d < n32;
+        if (okd) dst[d] = x;  // predicated; a bad index is reported after the chunk
+        bad |= !okd;
         if (EMIT_TILES) {
           const uint32_t nzm = __ballot_sync(0xffffffffu, !bit_of(x, shift - 1));  // next-level bit is 0
-          if (lane == 0) mynz[r] = nzm;
+          mynz[r] = nzm;
         }
       }
       if (EMIT_TILES) {
@@ -496,7 +498,7 @@ __global__ void __launch_bounds__(LV_THREADS, 4)
         const bool one = valid && bit_of(x, shift);
         const uint32_t om = __ballot_sync(0xffffffffu, one);
         const uint32_t zm = __ballot_sync(0xffffffffu, valid && !one);
-        if (lane == 0) myw[r] = om;
+        myw[r] = om;  // every lane stores the same word: no branch
         const uint32_t zb = z + __popc(zm & ltmask);
         z += __popc(zm);
         const uint32_t p = prefix_of(x, pshift, pmask);
@@ -514,7 +516,7 @@ __global__ void __launch_bounds__(LV_THREADS, 4)
         const uint32_t d = one ? bb.y + (i0 + k - zb) : bb.x + zb;
         const bool ok = valid && d < n32;
         if (ok) dst[d] = x;
-        else if (valid) atomicCAS(err, 0u, (uint32_t)DERR_BAD_INDEX);
+        bad |= valid && !ok;
         if (EMIT_TILES) {
           const bool nb0 = ok && !bit_of(x, shift - 1);
           slot2_count(tiles_s, nb0, d >> LOG_CHUNK, chunkcnt_next, lane);
@@ -526,6 +528,7 @@ __global__ void __launch_bounds__(LV_THREADS, 4)
         if (EMIT_NODES) slot2_flush(nodes_s, znext, lane);
       }
     }
+    if (SCATTER && __any_sync(0xffffffffu, bad) && lane == 0) atomicCAS(err, 0u, (uint32_t)DERR_BAD_INDEX);
     __syncwarp();
 
     // the chunk's bits: word j covers global bits [g + 32 j, g + 32 j + 32)
