@@ -418,25 +418,37 @@ __global__ void __launch_bounds__(LV_THREADS, 4)
       const uint2 b = cache_b;
       const uint32_t ob0 = i0 - z;                      // ones before the chunk
       const uint32_t zs = z;                            // zeros before the chunk
+      // The chunk's zeros land in b.x + [zs, zs + 512) and its ones in
+      // b.y + [ob0, ob0 + 512): when both ranges lie inside dst, no store of
+      // the chunk needs its own check.
+      const bool in_range = (uint64_t)b.x + zs + CHUNK <= n && (uint64_t)b.y + ob0 + CHUNK <= n;
+      const uint32_t ybase = b.y + i0 + lane;  // a one at row r goes to ybase + 32 r - (zeros before it)
+      auto rows = [&](auto checked) {
+        constexpr bool CHECK = decltype(checked)::value;
 #pragma unroll
-      for (int r = 0; r < WROWS; ++r) {
-        const uint32_t k = r * 32 + lane;
-        const T x = wt[k];
-        const uint32_t one = bit_of(x, shift);
-        const uint32_t om = __ballot_sync(0xffffffffu, one);
-        myw[r] = om;  // every lane stores the same word: no branch
-        const uint32_t zb = z + __popc(~om & ltmask);  // zeros before x (level-wide)
-        z += 32u - __popc(om);
-        const uint32_t ob = i0 + k - zb;                // ones before x (level-wide)
-        const uint32_t d = one ? b.y + ob : b.x + zb;
-        const bool okd = d < n32;
-        if (okd) dst[d] = x;  // predicated; a bad index is reported after the chunk
-        bad |= !okd;
-        if (EMIT_TILES) {
-          const uint32_t nzm = __ballot_sync(0xffffffffu, !bit_of(x, shift - 1));  // next-level bit is 0
-          mynz[r] = nzm;
+        for (int r = 0; r < WROWS; ++r) {
+          const T x = wt[r * 32 + lane];
+          const uint32_t one = bit_of(x, shift);
+          const uint32_t om = __ballot_sync(0xffffffffu, one);
+          myw[r] = om;  // every lane stores the same word: no branch
+          const uint32_t zb = z + __popc(~om & ltmask);  // zeros before x (level-wide)
+          z += 32u - __popc(om);
+          const uint32_t d = one ? ybase + 32u * r - zb : b.x + zb;
+          if (CHECK) {
+            const bool okd = d < n32;
+            if (okd) dst[d] = x;  // predicated; a bad index is reported after the chunk
+            bad |= !okd;
+          } else {
+            dst[d] = x;
+          }
+          if (EMIT_TILES) {
+            const uint32_t nzm = __ballot_sync(0xffffffffu, !bit_of(x, shift - 1));  // next-level bit is 0
+            mynz[r] = nzm;
+          }
         }
-      }
+      };
+      if (in_range) rows(std::false_type{});
+      else rows(std::true_type{});
       if (EMIT_TILES) {
         // Per 512-symbol chunk of the next level, its symbols whose next bit
         // is 0: the chunk's zero run lands at b.x + [zs, ...) and its one run
