@@ -333,8 +333,8 @@ __device__ void batch_text(const BatchArgs& a, uint64_t t, BatchSmem<THREADS>& s
       if (tid == 0) sm.run += all;
       __syncthreads();
     }
-    atomicMax(&sm.last[1], (unsigned long long)last1);
-    atomicMax(&sm.last[0], (unsigned long long)last0);
+    atomicMax(&sm.last[1], (unsigned long long)last_arg_end(bits, last1, W, tailmask, 1));
+    atomicMax(&sm.last[0], (unsigned long long)last_arg_end(bits, last0, W, tailmask, 0));
   }
   __syncthreads();
   const uint64_t m1 = sm.run, m0 = size - m1;

@@ -140,8 +140,8 @@ __global__ void __launch_bounds__(BV_THREADS)
       word_marks(w[j], c[j], sb_before + excl, wi, wi == W - 1 ? tailmask : ~0ull, flags & WTG_SELECT1,
                  flags & WTG_SELECT0, samples, samp_last, starts1, starts0, ends1, ends0, last1, last0);
   }
-  last1 = warp_max_u64(last1);
-  last0 = warp_max_u64(last0);
+  last1 = warp_max_u64(last_arg_end(words, last1, W, tailmask, 1));
+  last0 = warp_max_u64(last_arg_end(words, last0, W, tailmask, 0));
   if (lane == 0) {
     if (last1) atomicMax(&info[INF_LAST1], (unsigned long long)last1);
     if (last0) atomicMax(&info[INF_LAST0], (unsigned long long)last0);
@@ -152,71 +152,47 @@ __global__ void __launch_bounds__(BV_THREADS)
 // when n % 512 == 0: superblock b is chunk c of level l (b = l * n/512 + c),
 // and the zeros before it are the zeros of the levels before l (lvl_zb) plus
 // the chunk's prefix within its level (the level passes' chunk counts,
-// scanned) -- no scan over the bits.  Lane per 64-bit word, 8 lanes per
-// superblock, grid-stride over groups of 4 superblocks.
-constexpr int RS_U = 4;  // 32-word groups per warp step
-
+// scanned) -- no scan over the bits.  Thread per superblock, grid-stride
+// over each level's superblocks.
 __global__ void __launch_bounds__(256)
     rs_levels_kernel(const uint64_t* __restrict__ words, int L, uint64_t chunks_per_level,
                      const uint32_t* __restrict__ chunkpre, uint64_t prestride, const uint64_t* __restrict__ lvl_zb,
                      uint32_t flags, uint64_t* __restrict__ rank, uint32_t* __restrict__ samples, uint64_t samp_last,
                      uint64_t* __restrict__ starts1, uint64_t* __restrict__ starts0, uint64_t* __restrict__ ends1,
                      uint64_t* __restrict__ ends0, unsigned long long* info) {
-  const uint32_t lane = threadIdx.x & 31, g8 = lane & 7;
-  const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-  const uint64_t lw = chunks_per_level * 8;  // words per level
-  const uint64_t ngroups = (lw + 31) / 32;   // groups of 32 words (4 superblocks) per level
-  uint64_t last1 = 0, last0 = 0;
+  const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t W = (uint64_t)L * chunks_per_level * 8;
+  const bool sel1 = flags & WTG_SELECT1, sel0 = flags & WTG_SELECT0;
+  uint64_t lastw1 = 0, lastw0 = 0;
+  // thread per 512-bit superblock: its eight words in four 16-byte loads,
+  // counts and fields in registers, one 16-byte rank entry
   for (int l = 0; l < L; ++l) {
     const uint64_t zl = lvl_zb[l];
     const uint32_t* __restrict__ pre = chunkpre + (uint64_t)l * prestride;
-    const uint64_t w0 = (uint64_t)l * lw;
-    // a warp takes RS_U consecutive groups per step, all loads issued first
-    for (uint64_t grp = gw * RS_U; grp < ngroups; grp += nwarps * RS_U) {
-      uint64_t xs[RS_U];
-      uint32_t pres[RS_U];
+    for (uint64_t c = tid; c < chunks_per_level; c += nthreads) {
+      const uint64_t b = (uint64_t)l * chunks_per_level + c;  // superblock
+      const ulonglong2* p = reinterpret_cast<const ulonglong2*>(words + 8 * b);
+      const ulonglong2 q0 = __ldg(p), q1 = __ldg(p + 1), q2 = __ldg(p + 2), q3 = __ldg(p + 3);
+      const uint64_t w[8] = {q0.x, q0.y, q1.x, q1.y, q2.x, q2.y, q3.x, q3.y};
+      const uint64_t sb_before = 512 * b - (zl + __ldg(pre + c));  // ones before the superblock
+      uint32_t excl = 0;
+      uint64_t part = 0;
 #pragma unroll
-      for (int u = 0; u < RS_U; ++u) {
-        const uint64_t lwi = (grp + u) * 32 + lane;
-        const bool valid = lwi < lw;
-        xs[u] = valid ? __ldg(&words[w0 + lwi]) : 0ull;
-        pres[u] = valid ? __ldg(&pre[lwi >> 3]) : 0u;
+      for (int j = 0; j < 8; ++j) {
+        const uint32_t cj = __popcll(w[j]);
+        if (j) part |= (uint64_t)excl << (63 - 9 * j);
+        if (sel1 || sel0)
+          word_marks(w[j], cj, sb_before + excl, 8 * b + j, ~0ull, sel1, sel0, samples, samp_last, starts1,
+                     starts0, ends1, ends0, lastw1, lastw0);
+        excl += cj;
       }
-#pragma unroll
-      for (int u = 0; u < RS_U; ++u) {
-        const uint64_t lwi = (grp + u) * 32 + lane;  // word within the level
-        const bool valid = lwi < lw;
-        const uint64_t wi = w0 + lwi;
-        const uint64_t x = xs[u];
-        const uint32_t c = __popcll(x);
-        uint32_t inc = c;
-#pragma unroll
-        for (int o = 1; o < 8; o <<= 1) {
-          const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
-          if (g8 >= (uint32_t)o) inc += t;
-        }
-        const uint32_t excl = inc - c;
-        const uint64_t b = wi >> 3;
-        const uint64_t sb_before = 512 * b - (zl + pres[u]);  // ones before the superblock
-        if (flags & WTG_RANK) {
-          uint64_t part = g8 >= 1 ? ((uint64_t)excl << (63 - 9 * g8)) : 0ull;
-    #pragma unroll
-      for (int o = 1; o < 8; o <<= 1) part |= __shfl_xor_sync(0xffffffffu, part, o);
-          if (g8 == 0 && valid) {
-            rank[2 * b] = sb_before;
-            rank[2 * b + 1] = part;
-          }
-        }
-        if (valid)
-          word_marks(x, c, sb_before + excl, wi, ~0ull, flags & WTG_SELECT1, flags & WTG_SELECT0, samples,
-                     samp_last, starts1, starts0, ends1, ends0, last1, last0);
-      }
+      if (flags & WTG_RANK) reinterpret_cast<ulonglong2*>(rank)[b] = make_ulonglong2(sb_before, part);
     }
   }
-  last1 = warp_max_u64(last1);
-  last0 = warp_max_u64(last0);
-  if (lane == 0) {
+  const uint64_t last1 = warp_max_u64(last_arg_end(words, lastw1, W, ~0ull, 1));
+  const uint64_t last0 = warp_max_u64(last_arg_end(words, lastw0, W, ~0ull, 0));
+  if ((threadIdx.x & 31) == 0) {
     if (last1) atomicMax(&info[INF_LAST1], (unsigned long long)last1);
     if (last0) atomicMax(&info[INF_LAST0], (unsigned long long)last0);
   }
@@ -263,10 +239,11 @@ int bv_from_levels(BvSupport& bv, const uint64_t* d_words, uint64_t n, int L, co
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (sms <= 0) sms = 1;
   }
-  const uint64_t groups = (W + 31) / 32;
-  const unsigned grid = (unsigned)std::min<uint64_t>((groups + 8 * RS_U - 1) / (8 * RS_U), (uint64_t)sms * 8);
+  const uint64_t per_level = n / 512;  // superblocks per level, one thread each
+  const unsigned grid = (unsigned)std::max<uint64_t>(
+      1, std::min<uint64_t>((per_level + 255) / 256, (uint64_t)sms * 8));
   prof_begin(PROF_BVPASS, s);
-  rs_levels_kernel<<<grid ? grid : 1, 256, 0, s>>>(
+  rs_levels_kernel<<<grid, 256, 0, s>>>(
       d_words, L, n / 512, chunkpre, stride, lvl_zb, flags, bv.rank.as<uint64_t>(), bv.samples.as<uint32_t>(),
       samp_n - 1, bv.sel[1].starts.as<uint64_t>(), bv.sel[0].starts.as<uint64_t>(), bv.sel[1].ends.as<uint64_t>(),
       bv.sel[0].ends.as<uint64_t>(), bv.info.as<unsigned long long>());

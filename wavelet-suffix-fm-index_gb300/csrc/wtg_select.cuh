@@ -74,11 +74,14 @@ __device__ __forceinline__ uint64_t select_dev(const SelView& v, uint64_t i) {
 // or 0, a word holds the next 64th arg of at most one polarity unless K1 is
 // a multiple of 64, and then both are the word's first one and first zero:
 // one branch-free select serves every word.  zmask clears bits past the end.
+// lastw1 / lastw0 become wi + 1 when the word holds a one / a zero; a caller
+// that visits its words in increasing order turns the final values into
+// the position after its last arg with last_arg_end().
 __device__ __forceinline__ void word_marks(uint64_t x, uint32_t c, uint64_t K1, uint64_t wi, uint64_t zmask,
                                            bool sel1, bool sel0, uint32_t* __restrict__ samples, uint64_t samp_last,
                                            uint64_t* __restrict__ starts1, uint64_t* __restrict__ starts0,
                                            uint64_t* __restrict__ ends1, uint64_t* __restrict__ ends0,
-                                           uint64_t& last1, uint64_t& last0) {
+                                           uint64_t& lastw1, uint64_t& lastw0) {
   const uint64_t z = ~x & zmask;
   const uint32_t cz = __popcll(z);
   const uint64_t K0 = (wi << 6) - K1;
@@ -99,16 +102,27 @@ __device__ __forceinline__ void word_marks(uint64_t x, uint32_t c, uint64_t K1, 
       if ((k & 4095) == 0) starts0[k >> 12] = pos0;
     }
   }
-  if (sel1 && c) {
+  if (sel1) {
     const uint32_t e = 4095u - ((uint32_t)K1 & 4095u);
     if (e < c) ends1[(K1 + e) >> 12] = (wi << 6) + sel64_0(x, e);
-    last1 = max(last1, (wi << 6) + hi64(x) + 1);
+    lastw1 = c ? wi + 1 : lastw1;
   }
-  if (sel0 && cz) {
+  if (sel0) {
     const uint32_t e = 4095u - ((uint32_t)K0 & 4095u);
     if (e < cz) ends0[(K0 + e) >> 12] = (wi << 6) + sel64_0(z, e);
-    last0 = max(last0, (wi << 6) + hi64(z) + 1);
+    lastw0 = cz ? wi + 1 : lastw0;
   }
+}
+
+// Position after the last one (t_b = 1) or zero (t_b = 0) of word lastw - 1
+// of a bitvector of W words (0 when lastw is 0); read through L2
+__device__ __forceinline__ uint64_t last_arg_end(const uint64_t* __restrict__ words, uint64_t lastw, uint64_t W,
+                                                 uint64_t tailmask, int t_b) {
+  if (!lastw) return 0;
+  const uint64_t wi = lastw - 1;
+  uint64_t x = __ldcg(words + wi);
+  if (!t_b) x = ~x & (wi == W - 1 ? tailmask : ~0ull);
+  return (wi << 6) + hi64(x) + 1;
 }
 
 inline SelView sel_view(const BvSupport& bv, int t_b) {
