@@ -73,6 +73,18 @@ def lib():
         L.or_wt_select.restype = u64
         L.or_wt_access_batch.argtypes = [vp, vp, u64, ctypes.c_int, vp, u64, vp]
         L.or_wt_rank_batch.argtypes = [vp, vp, u64, ctypes.c_int, vp, vp, u64, vp]
+        ci = ctypes.c_int
+        L.or_wt_lex_count.argtypes = [vp, vp, u64, ci, u64, u64, u64, vp]
+        L.or_wt_lex_smaller_count.argtypes = [vp, vp, u64, ci, u64, u64, vp]
+        L.or_wt_range_search_2d.argtypes = [vp, vp, vp, vp, u64, ci, u64, u64, u64, u64, ci, u64, vp, vp]
+        L.or_wt_range_search_2d.restype = u64
+        L.or_wt_interval_symbols.argtypes = [vp, vp, u64, ci, u64, u64, u64, vp, vp, vp]
+        L.or_wt_interval_symbols.restype = u64
+        L.or_wt_expand.argtypes = [vp, vp, u64, vp, vp, vp]
+        L.or_wt_expand_ranges.argtypes = [vp, vp, vp, vp, u64, vp, vp]
+        L.or_wt_lex_count_batch.argtypes = [vp, vp, u64, ci, vp, vp, vp, u64, vp]
+        L.or_wt_lex_smaller_count_batch.argtypes = [vp, vp, u64, ci, vp, vp, u64, vp]
+        L.or_wt_range_count_batch.argtypes = [vp, vp, u64, ci, vp, vp, vp, vp, u64, vp]
         L.or_num_threads.restype = ctypes.c_int
         L.or_suffix_array_u8.argtypes = [vp, ctypes.c_int64, vp]
         L.or_suffix_array_u8.restype = ctypes.c_int
@@ -198,6 +210,70 @@ def wt_inverse_select(tree, rtbl, n, levels, i):
 def wt_select(tree, rtbl, sel1, sel0, n, levels, i, c):
     return lib().or_wt_select(_p(tree), _p(rtbl), ctypes.c_void_p(sel1.h), ctypes.c_void_p(sel0.h),
                               n, levels, int(i), int(c))
+
+
+def _u64(a):
+    return np.ascontiguousarray(a, dtype=np.uint64)
+
+
+def wt_lex_count(tree, rtbl, n, levels, i, j, c):
+    """wt_int::lex_count per query: rows (rank(i, c), smaller, greater)."""
+    i, j, c = _u64(i), _u64(j), _u64(c)
+    out = np.zeros((i.size, 3), dtype=np.uint64)
+    lib().or_wt_lex_count_batch(_p(tree), _p(rtbl), n, levels, _p(i), _p(j), _p(c), i.size, _p(out))
+    return out
+
+
+def wt_lex_smaller_count(tree, rtbl, n, levels, i, c):
+    """wt_int::lex_smaller_count per query: rows (rank(i, c), smaller)."""
+    i, c = _u64(i), _u64(c)
+    out = np.zeros((i.size, 2), dtype=np.uint64)
+    lib().or_wt_lex_smaller_count_batch(_p(tree), _p(rtbl), n, levels, _p(i), _p(c), i.size, _p(out))
+    return out
+
+
+def wt_range_count(tree, rtbl, n, levels, lb, rb, vlb, vrb):
+    """range_search_2d(lb, rb, vlb, vrb, report=false).first per query."""
+    lb, rb, vlb, vrb = _u64(lb), _u64(rb), _u64(vlb), _u64(vrb)
+    out = np.zeros(lb.size, dtype=np.uint64)
+    lib().or_wt_range_count_batch(_p(tree), _p(rtbl), n, levels, _p(lb), _p(rb), _p(vlb), _p(vrb), lb.size,
+                                  _p(out))
+    return out
+
+
+def wt_range_report(tree, rtbl, sel1, sel0, n, levels, lb, rb, vlb, vrb):
+    """range_search_2d(lb, rb, vlb, vrb) of one query: (positions, values)."""
+    cnt = lib().or_wt_range_search_2d(_p(tree), _p(rtbl), None, None, n, levels, int(lb), int(rb), int(vlb),
+                                      int(vrb), 0, 0, None, None)
+    pos = np.zeros(max(cnt, 1), dtype=np.uint64)
+    val = np.zeros(max(cnt, 1), dtype=np.uint64)
+    lib().or_wt_range_search_2d(_p(tree), _p(rtbl), ctypes.c_void_p(sel1.h), ctypes.c_void_p(sel0.h), n,
+                                levels, int(lb), int(rb), int(vlb), int(vrb), 1, cnt, _p(pos), _p(val))
+    return pos[:cnt], val[:cnt]
+
+
+def wt_interval_symbols(tree, rtbl, n, levels, i, j):
+    """interval_symbols(i, j) of one query: (symbols, rank(i, c), rank(j, c))."""
+    cap = min(1 << levels, max(int(j) - int(i), 1)) if int(j) >= int(i) else 1
+    cs, ri, rj = (np.zeros(cap, dtype=np.uint64) for _ in range(3))
+    k = lib().or_wt_interval_symbols(_p(tree), _p(rtbl), n, levels, int(i), int(j), cap, _p(cs), _p(ri), _p(rj))
+    return cs[:k], ri[:k], rj[:k]
+
+
+def wt_expand(tree, rtbl, n, node):
+    """expand(v): the children (offset, size, level, sym) of node v."""
+    v = _u64(node)
+    left, right = np.zeros(4, dtype=np.uint64), np.zeros(4, dtype=np.uint64)
+    lib().or_wt_expand(_p(tree), _p(rtbl), n, _p(v), _p(left), _p(right))
+    return left, right
+
+
+def wt_expand_ranges(tree, rtbl, node, ranges):
+    """expand(v, ranges): closed ranges [s, e] (rows) mapped to v's children."""
+    v, r = _u64(node), _u64(ranges).reshape(-1, 2)
+    left, right = np.zeros_like(r), np.zeros_like(r)
+    lib().or_wt_expand_ranges(_p(tree), _p(rtbl), _p(v), _p(r), r.shape[0], _p(left), _p(right))
+    return left, right
 
 
 # ---------------------------------------------------------------- reference
@@ -341,6 +417,116 @@ class RefSelect:
         try:
             if self.h:
                 _ref_rank_select().ref_select_free(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+
+_ref_wi = None
+
+
+def _ref_wt_int():
+    global _ref_wi
+    if _ref_wi is None:
+        L = ctypes.CDLL(os.path.join(REF_DIR, "libref_wt_int.so"))
+        L.ref_wtint_new.argtypes = [vp, ctypes.c_int, u64, ctypes.c_uint32]
+        L.ref_wtint_new.restype = vp
+        L.ref_wtint_free.argtypes = [vp]
+        L.ref_wtint_info.argtypes = [vp, vp]
+        L.ref_wtint_bits.argtypes = [vp, vp]
+        for f in ("ref_wtint_access",):
+            getattr(L, f).argtypes = [vp, u64]
+            getattr(L, f).restype = u64
+        L.ref_wtint_rank.argtypes = [vp, u64, u64]
+        L.ref_wtint_rank.restype = u64
+        L.ref_wtint_select.argtypes = [vp, u64, u64]
+        L.ref_wtint_select.restype = u64
+        L.ref_wtint_inverse_select.argtypes = [vp, u64, vp]
+        L.ref_wtint_lex_count.argtypes = [vp, u64, u64, u64, vp]
+        L.ref_wtint_lex_smaller_count.argtypes = [vp, u64, u64, vp]
+        L.ref_wtint_interval_symbols.argtypes = [vp, u64, u64, u64, vp, vp, vp]
+        L.ref_wtint_interval_symbols.restype = u64
+        L.ref_wtint_range_search_2d.argtypes = [vp, u64, u64, u64, u64, ctypes.c_int, u64, vp, vp]
+        L.ref_wtint_range_search_2d.restype = u64
+        L.ref_wtint_expand.argtypes = [vp, vp, vp, vp]
+        L.ref_wtint_expand_ranges.argtypes = [vp, vp, vp, u64, vp, vp]
+        _ref_wi = L
+    return _ref_wi
+
+
+class RefWtInt:
+    """The reference's own sdsl::wt_int (wt_int/wt_int_par.hpp), built by its
+    constructor and queried through its member functions."""
+
+    def __init__(self, sym, max_level):
+        L = _ref_wt_int()
+        self.sym = np.ascontiguousarray(sym)
+        self.h = L.ref_wtint_new(_p(self.sym), self.sym.dtype.itemsize, self.sym.size, max_level)
+        if not self.h:
+            raise RuntimeError("reference wt_int constructor failed")
+        info = np.zeros(4, dtype=np.uint64)
+        L.ref_wtint_info(self.h, _p(info))
+        self.size, self.sigma, self.levels, nw = [int(x) for x in info]
+        self.bits = np.zeros(max(nw, 1), dtype=np.uint64)
+        L.ref_wtint_bits(self.h, _p(self.bits))
+        self.bits = self.bits[:nw]
+
+    def access(self, i):
+        return int(_ref_wt_int().ref_wtint_access(self.h, int(i)))
+
+    def rank(self, i, c):
+        return int(_ref_wt_int().ref_wtint_rank(self.h, int(i), int(c)))
+
+    def select(self, i, c):
+        return int(_ref_wt_int().ref_wtint_select(self.h, int(i), int(c)))
+
+    def inverse_select(self, i):
+        out = np.zeros(2, dtype=np.uint64)
+        _ref_wt_int().ref_wtint_inverse_select(self.h, int(i), _p(out))
+        return int(out[0]), int(out[1])
+
+    def lex_count(self, i, j, c):
+        out = np.zeros(3, dtype=np.uint64)
+        _ref_wt_int().ref_wtint_lex_count(self.h, int(i), int(j), int(c), _p(out))
+        return out
+
+    def lex_smaller_count(self, i, c):
+        out = np.zeros(2, dtype=np.uint64)
+        _ref_wt_int().ref_wtint_lex_smaller_count(self.h, int(i), int(c), _p(out))
+        return out
+
+    def interval_symbols(self, i, j):
+        cap = min(1 << self.levels, max(int(j) - int(i), 1))  # k <= j - i
+        cs, ri, rj = (np.zeros(cap, dtype=np.uint64) for _ in range(3))
+        k = _ref_wt_int().ref_wtint_interval_symbols(self.h, int(i), int(j), cap, _p(cs), _p(ri), _p(rj))
+        return cs[:k], ri[:k], rj[:k]
+
+    def range_search_2d(self, lb, rb, vlb, vrb, report=True):
+        L = _ref_wt_int()
+        cnt = L.ref_wtint_range_search_2d(self.h, int(lb), int(rb), int(vlb), int(vrb), 0, 0, None, None)
+        if not report:
+            return cnt, None, None
+        pos = np.zeros(max(cnt, 1), dtype=np.uint64)
+        val = np.zeros(max(cnt, 1), dtype=np.uint64)
+        L.ref_wtint_range_search_2d(self.h, int(lb), int(rb), int(vlb), int(vrb), 1, cnt, _p(pos), _p(val))
+        return cnt, pos[:cnt], val[:cnt]
+
+    def expand(self, node):
+        v = _u64(node)
+        left, right = np.zeros(4, dtype=np.uint64), np.zeros(4, dtype=np.uint64)
+        _ref_wt_int().ref_wtint_expand(self.h, _p(v), _p(left), _p(right))
+        return left, right
+
+    def expand_ranges(self, node, ranges):
+        v, r = _u64(node), _u64(ranges).reshape(-1, 2)
+        left, right = np.zeros_like(r), np.zeros_like(r)
+        _ref_wt_int().ref_wtint_expand_ranges(self.h, _p(v), _p(r), r.shape[0], _p(left), _p(right))
+        return left, right
+
+    def __del__(self):
+        try:
+            if self.h:
+                _ref_wt_int().ref_wtint_free(self.h)
                 self.h = None
         except Exception:
             pass

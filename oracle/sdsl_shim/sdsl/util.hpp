@@ -5,6 +5,7 @@
 #include <sstream>
 #include <string>
 #include <typeinfo>
+#include <utility>
 #include "int_vector.hpp"
 
 namespace sdsl {
@@ -30,6 +31,12 @@ void init_support(S& s, const V* v) {
   S tmp(v);
   s = std::move(tmp);
   s.set_vector(v);
+}
+template <class S, class V>
+void swap_support(S& s1, S& s2, const V* v1, const V* v2) {
+  std::swap(s1, s2);
+  s1.set_vector(v1);
+  s2.set_vector(v2);
 }
 }  // namespace util
 }  // namespace sdsl

@@ -575,6 +575,207 @@ uint64_t or_wt_select(const uint64_t* tree, const uint64_t* rt, const or_select*
   return i - 1;
 }
 
+/* wt_int::lex_count (wt_int_par.hpp:715-745): out = (rank(i, c), symbols
+ * smaller than c in [i, j), symbols greater than c in [i, j)) */
+void or_wt_lex_count(const uint64_t* tree, const uint64_t* rt, uint64_t n, int L, uint64_t i, uint64_t j,
+                     uint64_t c, uint64_t* out) {
+  if (L < 64 && (1ull << L) <= c) {
+    out[0] = 0; out[1] = j - i; out[2] = 0;
+    return;
+  }
+  uint64_t offset = 0, smaller = 0, greater = 0, mask = 1ull << (L - 1), node_size = n;
+  for (int k = 0; k < L; k++) {
+    uint64_t o = or_rank1(rt, tree, offset);
+    uint64_t oi = or_rank1(rt, tree, offset + i) - o;
+    uint64_t oj = or_rank1(rt, tree, offset + j) - o;
+    uint64_t oe = or_rank1(rt, tree, offset + node_size) - o;
+    if (c & mask) {
+      offset += node_size - oe; node_size = oe;
+      smaller += j - i - oj + oi; i = oi; j = oj;
+    } else {
+      node_size -= oe;
+      greater += oj - oi; i -= oi; j -= oj;
+    }
+    offset += n;
+    mask >>= 1;
+  }
+  out[0] = i; out[1] = smaller; out[2] = greater;
+}
+
+/* wt_int::lex_smaller_count (wt_int_par.hpp:758-782): out = (rank(i, c),
+ * symbols smaller than c in [0, i)) */
+void or_wt_lex_smaller_count(const uint64_t* tree, const uint64_t* rt, uint64_t n, int L, uint64_t i,
+                             uint64_t c, uint64_t* out) {
+  if (L < 64 && (1ull << L) <= c) {
+    out[0] = 0; out[1] = i;
+    return;
+  }
+  uint64_t offset = 0, result = 0, mask = 1ull << (L - 1), node_size = n;
+  for (int k = 0; k < L && i; k++) {
+    uint64_t o = or_rank1(rt, tree, offset);
+    uint64_t oi = or_rank1(rt, tree, offset + i) - o;
+    uint64_t oe = or_rank1(rt, tree, offset + node_size) - o;
+    if (c & mask) { offset += node_size - oe; node_size = oe; result += i - oi; i = oi; }
+    else { node_size = node_size - oe; i -= oi; }
+    offset += n;
+    mask >>= 1;
+  }
+  out[0] = i; out[1] = result;
+}
+
+/* range_search_2d (wt_int_par.hpp:801-871): points of positions [lb, rb]
+ * with values in [vlb, vrb]; leaves in increasing value order, positions
+ * increasing within a leaf; each reported position is found by walking up
+ * with select1/select0 from the leaf. */
+typedef struct {
+  const uint64_t *tree, *rt;
+  const or_select *s1, *s0;
+  uint64_t n;
+  int L, report;
+  uint64_t cap, cnt;
+  uint64_t *pos, *val;
+  uint64_t offsets[66], obo[66];
+} r2d_ctx;
+
+static void r2d_rec(r2d_ctx* x, uint64_t lb, uint64_t rb, uint64_t vlb, uint64_t vrb, int level, uint64_t ilb,
+                    uint64_t node_size, uint64_t path) {
+  if (lb > rb) return;
+  if (level == x->L) {
+    if (x->report) {
+      for (uint64_t j = lb + 1; j <= rb + 1; ++j) {
+        uint64_t i = j, c = path;
+        for (int k = x->L; k > 0; --k) {
+          uint64_t offset = x->offsets[k - 1], o = x->obo[k - 1];
+          if (c & 1) i = or_select_query(x->s1, x->tree, o + i) - offset + 1;
+          else i = or_select_query(x->s0, x->tree, offset - o + i) - offset + 1;
+          c >>= 1;
+        }
+        uint64_t q = x->cnt + (j - lb - 1);
+        if (q < x->cap) { x->pos[q] = i - 1; x->val[q] = path; }
+      }
+    }
+    x->cnt += rb - lb + 1;
+    return;
+  }
+  uint64_t irb = ilb + (1ull << (x->L - level));
+  uint64_t mid = (irb + ilb) >> 1;
+  uint64_t offset = x->offsets[level];
+  uint64_t o = or_rank1(x->rt, x->tree, offset);
+  x->obo[level] = o;
+  uint64_t olb = or_rank1(x->rt, x->tree, offset + lb);
+  uint64_t orb = or_rank1(x->rt, x->tree, offset + rb + 1);
+  uint64_t oend = or_rank1(x->rt, x->tree, offset + node_size);
+  uint64_t zo = offset - o, zlb = offset + lb - olb, zrb = offset + rb + 1 - orb, zend = offset + node_size - oend;
+  if (vlb < mid && mid) {
+    uint64_t nlb = zlb - zo, nrb = zrb - zo;
+    x->offsets[level + 1] = offset + x->n;
+    if (nrb) r2d_rec(x, nlb, nrb - 1, vlb, vrb < mid - 1 ? vrb : mid - 1, level + 1, ilb, zend - zo, path << 1);
+  }
+  if (vrb >= mid) {
+    uint64_t nlb = olb - o, nrb = orb - o;
+    x->offsets[level + 1] = offset + x->n + (zend - zo);
+    if (nrb) r2d_rec(x, nlb, nrb - 1, mid > vlb ? mid : vlb, vrb, level + 1, mid, oend - o, (path << 1) + 1);
+  }
+}
+
+uint64_t or_wt_range_search_2d(const uint64_t* tree, const uint64_t* rt, const or_select* s1,
+                               const or_select* s0, uint64_t n, int L, uint64_t lb, uint64_t rb, uint64_t vlb,
+                               uint64_t vrb, int report, uint64_t cap, uint64_t* pos, uint64_t* val) {
+  r2d_ctx x;
+  memset(&x, 0, sizeof(x));
+  x.tree = tree; x.rt = rt; x.s1 = s1; x.s0 = s0; x.n = n; x.L = L; x.report = report;
+  x.cap = cap; x.pos = pos; x.val = val;
+  if (L < 64 && vrb > (1ull << L)) vrb = 1ull << L;
+  if (vlb > vrb) return 0;
+  r2d_rec(&x, lb, rb, vlb, vrb, 0, 0, n, 0);
+  return x.cnt;
+}
+
+/* interval_symbols (wt_int_par.hpp:684-702, recursion :119-158): the k
+ * distinct symbols of [i, j) in increasing order with rank(i, c), rank(j, c) */
+typedef struct {
+  const uint64_t *tree, *rt;
+  uint64_t n;
+  int L;
+  uint64_t k, cap;
+  uint64_t *cs, *ri, *rj;
+} isym_ctx;
+
+static void isym_rec(isym_ctx* x, uint64_t i, uint64_t j, int level, uint64_t path, uint64_t node_size,
+                     uint64_t offset) {
+  if (level >= x->L) {
+    if (x->k < x->cap) { x->ri[x->k] = i; x->rj[x->k] = j; x->cs[x->k] = path; }
+    x->k++;
+    return;
+  }
+  uint64_t o = or_rank1(x->rt, x->tree, offset);
+  uint64_t oi = or_rank1(x->rt, x->tree, offset + i) - o;
+  uint64_t oj = or_rank1(x->rt, x->tree, offset + j) - o;
+  uint64_t oe = or_rank1(x->rt, x->tree, offset + node_size) - o;
+  if ((j - i) - (oj - oi) > 0)
+    isym_rec(x, i - oi, j - oj, level + 1, path << 1, node_size - oe, offset + x->n);
+  if (oj - oi > 0)
+    isym_rec(x, oi, oj, level + 1, (path << 1) | 1, oe, offset + (node_size - oe) + x->n);
+}
+
+uint64_t or_wt_interval_symbols(const uint64_t* tree, const uint64_t* rt, uint64_t n, int L, uint64_t i,
+                                uint64_t j, uint64_t cap, uint64_t* cs, uint64_t* ri, uint64_t* rj) {
+  if (i == j) return 0;
+  if (i + 1 == j) {
+    uint64_t c = 0, r = or_wt_inverse_select(tree, rt, n, L, i, &c);
+    if (cap) { cs[0] = c; ri[0] = r; rj[0] = r + 1; }
+    return 1;
+  }
+  isym_ctx x = {tree, rt, n, L, 0, cap, cs, ri, rj};
+  isym_rec(&x, i, j, 0, 0, n, 0);
+  return x.k;
+}
+
+/* expand(v) (wt_int_par.hpp:966-984); nodes are (offset, size, level, sym) */
+void or_wt_expand(const uint64_t* tree, const uint64_t* rt, uint64_t n, const uint64_t* v, uint64_t* left,
+                  uint64_t* right) {
+  uint64_t offset_rank = or_rank1(rt, tree, v[0]);
+  uint64_t ones = or_rank1(rt, tree, v[0] + v[1]) - offset_rank;
+  left[0] = v[0] + n; left[1] = v[1] - ones; left[2] = v[2] + 1; left[3] = v[3] << 1;
+  right[0] = v[0] + n + left[1]; right[1] = ones; right[2] = v[2] + 1; right[3] = (v[3] << 1) | 1;
+}
+
+/* expand(v, ranges) (wt_int_par.hpp:1027-1048): closed ranges [s, e] of v
+ * mapped to its children, in unsigned 64-bit arithmetic */
+void or_wt_expand_ranges(const uint64_t* tree, const uint64_t* rt, const uint64_t* v, const uint64_t* ranges,
+                         uint64_t nr, uint64_t* left, uint64_t* right) {
+  uint64_t v_sp_rank = or_rank1(rt, tree, v[0]);
+  for (uint64_t q = 0; q < nr; q++) {
+    uint64_t s = ranges[2 * q], e = ranges[2 * q + 1];
+    uint64_t sp_rank = or_rank1(rt, tree, v[0] + s);
+    uint64_t right_size = or_rank1(rt, tree, v[0] + e + 1) - sp_rank;
+    uint64_t left_size = (e - s + 1) - right_size;
+    uint64_t right_sp = sp_rank - v_sp_rank, left_sp = s - right_sp;
+    left[2 * q] = left_sp; left[2 * q + 1] = left_sp + left_size - 1;
+    right[2 * q] = right_sp; right[2 * q + 1] = right_sp + right_size - 1;
+  }
+}
+
+void or_wt_lex_count_batch(const uint64_t* tree, const uint64_t* rt, uint64_t n, int L, const uint64_t* i,
+                           const uint64_t* j, const uint64_t* c, uint64_t nq, uint64_t* out) {
+#pragma omp parallel for schedule(static)
+  for (int64_t k = 0; k < (int64_t)nq; k++) or_wt_lex_count(tree, rt, n, L, i[k], j[k], c[k], out + 3 * k);
+}
+
+void or_wt_lex_smaller_count_batch(const uint64_t* tree, const uint64_t* rt, uint64_t n, int L,
+                                   const uint64_t* i, const uint64_t* c, uint64_t nq, uint64_t* out) {
+#pragma omp parallel for schedule(static)
+  for (int64_t k = 0; k < (int64_t)nq; k++) or_wt_lex_smaller_count(tree, rt, n, L, i[k], c[k], out + 2 * k);
+}
+
+void or_wt_range_count_batch(const uint64_t* tree, const uint64_t* rt, uint64_t n, int L, const uint64_t* lb,
+                             const uint64_t* rb, const uint64_t* vlb, const uint64_t* vrb, uint64_t nq,
+                             uint64_t* out) {
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int64_t k = 0; k < (int64_t)nq; k++)
+    out[k] = or_wt_range_search_2d(tree, rt, NULL, NULL, n, L, lb[k], rb[k], vlb[k], vrb[k], 0, 0, NULL, NULL);
+}
+
 void or_wt_access_batch(const uint64_t* tree, const uint64_t* rt, uint64_t n, int L,
                         const uint64_t* idx, uint64_t nq, uint64_t* out) {
 #pragma omp parallel for schedule(static)

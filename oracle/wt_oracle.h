@@ -88,11 +88,41 @@ uint64_t or_wt_select(const uint64_t* tree, const uint64_t* rank_tbl,
                       const or_select* sel1, const or_select* sel0,
                       uint64_t n, int levels, uint64_t i, uint64_t c);
 
+/* wt_int's range queries (wt_int_par.hpp:684-1048).  lex_count writes
+ * (rank(i, c), smaller, greater), lex_smaller_count (rank(i, c), smaller);
+ * range_search_2d returns the point count and, with report, stores the first
+ * cap points (position, value) in the reference's order; interval_symbols
+ * returns k and stores the first cap (symbol, rank(i, c), rank(j, c));
+ * expand maps a node (offset, size, level, sym) to its children, and
+ * expand_ranges closed ranges [s, e] of a node to its children's. */
+void or_wt_lex_count(const uint64_t* tree, const uint64_t* rank_tbl, uint64_t n, int levels, uint64_t i,
+                     uint64_t j, uint64_t c, uint64_t* out);
+void or_wt_lex_smaller_count(const uint64_t* tree, const uint64_t* rank_tbl, uint64_t n, int levels,
+                             uint64_t i, uint64_t c, uint64_t* out);
+uint64_t or_wt_range_search_2d(const uint64_t* tree, const uint64_t* rank_tbl, const or_select* sel1,
+                               const or_select* sel0, uint64_t n, int levels, uint64_t lb, uint64_t rb,
+                               uint64_t vlb, uint64_t vrb, int report, uint64_t cap, uint64_t* pos,
+                               uint64_t* val);
+uint64_t or_wt_interval_symbols(const uint64_t* tree, const uint64_t* rank_tbl, uint64_t n, int levels,
+                                uint64_t i, uint64_t j, uint64_t cap, uint64_t* cs, uint64_t* rank_i,
+                                uint64_t* rank_j);
+void or_wt_expand(const uint64_t* tree, const uint64_t* rank_tbl, uint64_t n, const uint64_t* v, uint64_t* left,
+                  uint64_t* right);
+void or_wt_expand_ranges(const uint64_t* tree, const uint64_t* rank_tbl, const uint64_t* v,
+                         const uint64_t* ranges, uint64_t nr, uint64_t* left, uint64_t* right);
+
 /* Batched query helpers (loop over the scalar functions above, OpenMP). */
 void or_wt_access_batch(const uint64_t* tree, const uint64_t* rank_tbl, uint64_t n, int levels,
                         const uint64_t* idx, uint64_t nq, uint64_t* out);
 void or_wt_rank_batch(const uint64_t* tree, const uint64_t* rank_tbl, uint64_t n, int levels,
                       const uint64_t* idx, const uint64_t* sym, uint64_t nq, uint64_t* out);
+void or_wt_lex_count_batch(const uint64_t* tree, const uint64_t* rank_tbl, uint64_t n, int levels,
+                           const uint64_t* i, const uint64_t* j, const uint64_t* c, uint64_t nq, uint64_t* out);
+void or_wt_lex_smaller_count_batch(const uint64_t* tree, const uint64_t* rank_tbl, uint64_t n, int levels,
+                                   const uint64_t* i, const uint64_t* c, uint64_t nq, uint64_t* out);
+void or_wt_range_count_batch(const uint64_t* tree, const uint64_t* rank_tbl, uint64_t n, int levels,
+                             const uint64_t* lb, const uint64_t* rb, const uint64_t* vlb, const uint64_t* vrb,
+                             uint64_t nq, uint64_t* out);
 void or_select_batch(const or_select* h, const uint64_t* data, const uint64_t* q, uint64_t nq,
                      uint64_t* out);
 
