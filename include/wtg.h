@@ -139,6 +139,50 @@ int wtg_query_access_device(wtg_tree* t, const uint64_t* d_idx, uint64_t nq, uin
 int wtg_query_rank_device(wtg_tree* t, const uint64_t* d_idx, const uint64_t* d_sym, uint64_t nq,
                           uint64_t* d_out, void* stream);
 
+/* ------------------------------------------------------- range queries
+ * wt_int's range queries (wt_int/wt_int_par.hpp:684-1048), batched.  A
+ * query whose bounds leave the sequence (i > j, j > n, or rb >= n with
+ * lb <= rb) answers UINT64_MAX in every field (the reference's precondition).
+ * Variable-size answers are written for all queries back to back, query q's
+ * first answer after the answers of queries 0..q-1 (counts from the same
+ * call, UINT64_MAX read as 0); only the first `cap` answers are stored.  All
+ * need a tree built with WTG_RANK. */
+/* lex_count(i, j, c) -> (rank(i, c), symbols < c in [i, j), symbols > c in
+ * [i, j)) (wt_int_par.hpp:715-745); c >= 2^levels gives (0, j - i, 0) */
+int wtg_query_lex_count(wtg_tree* t, const uint64_t* i, const uint64_t* j, const uint64_t* c, uint64_t nq,
+                        uint64_t* rank_out, uint64_t* smaller_out, uint64_t* greater_out);
+/* lex_smaller_count(i, c) -> (rank(i, c), symbols < c in [0, i))
+ * (wt_int_par.hpp:758-782) */
+int wtg_query_lex_smaller_count(wtg_tree* t, const uint64_t* i, const uint64_t* c, uint64_t nq,
+                                uint64_t* rank_out, uint64_t* smaller_out);
+/* range_search_2d(lb, rb, vlb, vrb, report) (wt_int_par.hpp:801-871): the
+ * positions p in [lb, rb] (inclusive) with value in [vlb, vrb] (vrb clamped
+ * to 2^levels).  count_out gets each query's count; with pos_out / val_out
+ * (report; needs WTG_SELECT1|WTG_SELECT0 too) the points (position, value)
+ * in the reference's order: values increasing, positions increasing. */
+int wtg_query_range_search_2d(wtg_tree* t, const uint64_t* lb, const uint64_t* rb, const uint64_t* vlb,
+                              const uint64_t* vrb, uint64_t nq, uint64_t* count_out, uint64_t cap,
+                              uint64_t* pos_out, uint64_t* val_out);
+/* interval_symbols(i, j) (wt_int_par.hpp:684-702): k_out gets the number of
+ * distinct symbols of [i, j); with cs_out / rank_i_out / rank_j_out, per
+ * symbol in increasing order (c, rank(i, c), rank(j, c)). */
+int wtg_query_interval_symbols(wtg_tree* t, const uint64_t* i, const uint64_t* j, uint64_t nq, uint64_t* k_out,
+                               uint64_t cap, uint64_t* cs_out, uint64_t* rank_i_out, uint64_t* rank_j_out);
+/* expand(v) (wt_int_par.hpp:966-984) for nn nodes v = (offset, size, level,
+ * sym), 4 words each: left and right children in the same form (UINT64_MAX
+ * fields for a leaf or a node reaching past the bits) */
+int wtg_query_expand(wtg_tree* t, const uint64_t* nodes, uint64_t nn, uint64_t* left, uint64_t* right);
+/* expand(v, ranges) (wt_int_par.hpp:1027-1048): nr closed ranges [s, e]
+ * (2 words each) of node v mapped to its children, in the reference's
+ * unsigned 64-bit arithmetic (an empty range is e = s - 1) */
+int wtg_query_expand_ranges(wtg_tree* t, const uint64_t v[4], const uint64_t* ranges, uint64_t nr, uint64_t* left,
+                            uint64_t* right);
+int wtg_query_lex_count_device(wtg_tree* t, const uint64_t* d_i, const uint64_t* d_j, const uint64_t* d_c,
+                               uint64_t nq, uint64_t* d_rank, uint64_t* d_smaller, uint64_t* d_greater,
+                               void* stream);
+int wtg_query_range_count_device(wtg_tree* t, const uint64_t* d_lb, const uint64_t* d_rb, const uint64_t* d_vlb,
+                                 const uint64_t* d_vrb, uint64_t nq, uint64_t* d_count, void* stream);
+
 /* --------------------------------------------- standalone bitvector supports
  * rank_support_v<1> (rank/rank_support_v_par.hpp:69-123) and
  * select_support_mcl<1>/<0> (select/select_support_mcl_par.hpp:120-129,

@@ -875,6 +875,8 @@ void tree_release(TreeImpl& t) {
   t.node_tab_ok = false;
   t.scratch.release(s);
   t.nodes.release(s);
+  t.qbuf.release(s);
+  t.qout.release(s);
   bv_release(t.bv, s);
 }
 

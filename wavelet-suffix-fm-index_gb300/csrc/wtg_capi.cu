@@ -98,6 +98,43 @@ int host_query(DevBuf& qbuf, cudaStream_t s, const uint64_t* const* ins, int nin
   return sync_and_check(s, d_err);
 }
 
+// Variable-size answers: the query arrays go to the device, `count` fills
+// the per-query counts; when `fill` is given (nv output arrays, cap > 0)
+// the counts are scanned into offsets, `fill` writes up to cap answers, and
+// the first min(total, cap) of each output array come back.
+template <typename C, typename F>
+int host_variable_query(TreeImpl& t, const uint64_t* const* ins, int nin, uint64_t nq, uint64_t* counts_out,
+                        uint64_t cap, uint64_t* const* outs, int nv, C count, F fill) {
+  int rc;
+  cudaStream_t s = t.stream;
+  if (nq == 0) return WTG_OK;
+  if ((rc = t.qbuf.ensure((size_t)(nin * nq + nq + nq + 1) * sizeof(uint64_t), s))) return rc;
+  uint64_t* d = t.qbuf.as<uint64_t>();
+  const uint64_t* din[4];
+  for (int k = 0; k < nin; ++k) {
+    WTG_CK(cudaMemcpyAsync(d + k * nq, ins[k], nq * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+    din[k] = d + k * nq;
+  }
+  uint64_t* d_cnt = d + nin * nq;
+  uint64_t* d_off = d_cnt + nq;
+  if ((rc = count(din, d_cnt))) return rc;
+  WTG_CK(cudaMemcpyAsync(counts_out, d_cnt, nq * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+  if (!nv || !cap) return sync_and_check(s, t.err.as<uint32_t>());
+  if ((rc = answer_offsets(d_cnt, nq, d_off, t.scan_tmp, t.err.as<uint32_t>(), s))) return rc;
+  uint64_t total = 0;
+  WTG_CK(cudaMemcpyAsync(&total, d_off + nq, sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+  if ((rc = sync_and_check(s, t.err.as<uint32_t>()))) return rc;
+  const uint64_t m = std::min(total, cap);
+  if (!m) return WTG_OK;
+  if ((rc = t.qout.ensure((size_t)nv * m * sizeof(uint64_t), s))) return rc;
+  uint64_t* dout[4];
+  for (int k = 0; k < nv; ++k) dout[k] = t.qout.as<uint64_t>() + k * m;
+  if ((rc = fill(din, (const uint64_t*)d_off, m, dout))) return rc;
+  for (int k = 0; k < nv; ++k)
+    WTG_CK(cudaMemcpyAsync(outs[k], dout[k], m * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+  return sync_and_check(s, t.err.as<uint32_t>());
+}
+
 void fill_select_info(const BvSupport& bv, int t_b, uint64_t info[8]) {
   const SelectDev& sd = bv.sel[t_b];
   info[0] = bv.size;
@@ -375,6 +412,119 @@ int wtg_query_rank_device(wtg_tree* T, const uint64_t* d_idx, const uint64_t* d_
                           void* stream) {
   if (!T) return fail(WTG_ERR_INVALID, "null tree");
   return launch_wt_rank(T->t, d_idx, d_sym, nq, d_out, (cudaStream_t)stream);
+}
+
+// ------------------------------------------------------- range queries
+
+int wtg_query_lex_count(wtg_tree* T, const uint64_t* i, const uint64_t* j, const uint64_t* c, uint64_t nq,
+                        uint64_t* rank_out, uint64_t* smaller_out, uint64_t* greater_out) {
+  if (!T || (nq && (!i || !j || !c || !rank_out || !smaller_out || !greater_out)))
+    return fail(WTG_ERR_INVALID, "null argument");
+  TreeImpl& t = T->t;
+  const uint64_t* ins[3] = {i, j, c};
+  uint64_t* outs[3] = {rank_out, smaller_out, greater_out};
+  return host_query(t.qbuf, t.stream, ins, 3, nq, outs, 3, t.err.as<uint32_t>(),
+                    [&](const uint64_t** din, uint64_t** dout) {
+                      return launch_wt_lex_count(t, din[0], din[1], din[2], nq, dout[0], dout[1], dout[2],
+                                                 t.stream);
+                    });
+}
+
+int wtg_query_lex_smaller_count(wtg_tree* T, const uint64_t* i, const uint64_t* c, uint64_t nq, uint64_t* rank_out,
+                                uint64_t* smaller_out) {
+  if (!T || (nq && (!i || !c || !rank_out || !smaller_out))) return fail(WTG_ERR_INVALID, "null argument");
+  TreeImpl& t = T->t;
+  const uint64_t* ins[2] = {i, c};
+  uint64_t* outs[2] = {rank_out, smaller_out};
+  return host_query(t.qbuf, t.stream, ins, 2, nq, outs, 2, t.err.as<uint32_t>(),
+                    [&](const uint64_t** din, uint64_t** dout) {
+                      return launch_wt_lex_smaller_count(t, din[0], din[1], nq, dout[0], dout[1], t.stream);
+                    });
+}
+
+int wtg_query_range_search_2d(wtg_tree* T, const uint64_t* lb, const uint64_t* rb, const uint64_t* vlb,
+                              const uint64_t* vrb, uint64_t nq, uint64_t* count_out, uint64_t cap, uint64_t* pos_out,
+                              uint64_t* val_out) {
+  if (!T || (nq && (!lb || !rb || !vlb || !vrb || !count_out))) return fail(WTG_ERR_INVALID, "null argument");
+  if ((pos_out == nullptr) != (val_out == nullptr)) return fail(WTG_ERR_INVALID, "pos_out and val_out go together");
+  TreeImpl& t = T->t;
+  const uint64_t* ins[4] = {lb, rb, vlb, vrb};
+  uint64_t* outs[2] = {pos_out, val_out};
+  const int nv = pos_out ? 2 : 0;
+  if (nv && cap && (t.flags & WTG_ALL) != WTG_ALL)
+    return fail(WTG_ERR_INVALID, "range_search_2d with report needs rank and both selects");
+  return host_variable_query(
+      t, ins, 4, nq, count_out, cap, outs, nv,
+      [&](const uint64_t** din, uint64_t* d_cnt) {
+        return launch_wt_range_count(t, din[0], din[1], din[2], din[3], nq, d_cnt, t.stream);
+      },
+      [&](const uint64_t** din, const uint64_t* d_off, uint64_t m, uint64_t** dout) {
+        return launch_wt_range_report(t, din[0], din[1], din[2], din[3], nq, d_off, m, dout[0], dout[1], t.stream);
+      });
+}
+
+int wtg_query_interval_symbols(wtg_tree* T, const uint64_t* i, const uint64_t* j, uint64_t nq, uint64_t* k_out,
+                               uint64_t cap, uint64_t* cs_out, uint64_t* rank_i_out, uint64_t* rank_j_out) {
+  if (!T || (nq && (!i || !j || !k_out))) return fail(WTG_ERR_INVALID, "null argument");
+  const int given = (cs_out != nullptr) + (rank_i_out != nullptr) + (rank_j_out != nullptr);
+  if (given != 0 && given != 3) return fail(WTG_ERR_INVALID, "cs_out, rank_i_out and rank_j_out go together");
+  TreeImpl& t = T->t;
+  const uint64_t* ins[2] = {i, j};
+  uint64_t* outs[3] = {cs_out, rank_i_out, rank_j_out};
+  return host_variable_query(
+      t, ins, 2, nq, k_out, cap, outs, given,
+      [&](const uint64_t** din, uint64_t* d_cnt) {
+        return launch_wt_interval_symbols(t, din[0], din[1], nq, d_cnt, nullptr, 0, nullptr, nullptr, nullptr,
+                                          t.stream);
+      },
+      [&](const uint64_t** din, const uint64_t* d_off, uint64_t m, uint64_t** dout) {
+        return launch_wt_interval_symbols(t, din[0], din[1], nq, nullptr, d_off, m, dout[0], dout[1], dout[2],
+                                          t.stream);
+      });
+}
+
+int wtg_query_expand(wtg_tree* T, const uint64_t* nodes, uint64_t nn, uint64_t* left, uint64_t* right) {
+  if (!T || (nn && (!nodes || !left || !right))) return fail(WTG_ERR_INVALID, "null argument");
+  TreeImpl& t = T->t;
+  int rc;
+  if (!nn) return WTG_OK;
+  cudaStream_t s = t.stream;
+  if ((rc = t.qbuf.ensure((size_t)12 * nn * sizeof(uint64_t), s))) return rc;
+  uint64_t* d = t.qbuf.as<uint64_t>();
+  WTG_CK(cudaMemcpyAsync(d, nodes, 4 * nn * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+  if ((rc = launch_wt_expand(t, d, nn, d + 4 * nn, d + 8 * nn, s))) return rc;
+  WTG_CK(cudaMemcpyAsync(left, d + 4 * nn, 4 * nn * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+  WTG_CK(cudaMemcpyAsync(right, d + 8 * nn, 4 * nn * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+  return sync_and_check(s, t.err.as<uint32_t>());
+}
+
+int wtg_query_expand_ranges(wtg_tree* T, const uint64_t v[4], const uint64_t* ranges, uint64_t nr, uint64_t* left,
+                            uint64_t* right) {
+  if (!T || !v || (nr && (!ranges || !left || !right))) return fail(WTG_ERR_INVALID, "null argument");
+  TreeImpl& t = T->t;
+  int rc;
+  if (!nr) return WTG_OK;
+  cudaStream_t s = t.stream;
+  if ((rc = t.qbuf.ensure((size_t)6 * nr * sizeof(uint64_t), s))) return rc;
+  uint64_t* d = t.qbuf.as<uint64_t>();
+  WTG_CK(cudaMemcpyAsync(d, ranges, 2 * nr * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+  if ((rc = launch_wt_expand_ranges(t, v[0], d, nr, d + 2 * nr, d + 4 * nr, s))) return rc;
+  WTG_CK(cudaMemcpyAsync(left, d + 2 * nr, 2 * nr * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+  WTG_CK(cudaMemcpyAsync(right, d + 4 * nr, 2 * nr * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+  return sync_and_check(s, t.err.as<uint32_t>());
+}
+
+int wtg_query_lex_count_device(wtg_tree* T, const uint64_t* d_i, const uint64_t* d_j, const uint64_t* d_c,
+                               uint64_t nq, uint64_t* d_rank, uint64_t* d_smaller, uint64_t* d_greater,
+                               void* stream) {
+  if (!T) return fail(WTG_ERR_INVALID, "null tree");
+  return launch_wt_lex_count(T->t, d_i, d_j, d_c, nq, d_rank, d_smaller, d_greater, (cudaStream_t)stream);
+}
+
+int wtg_query_range_count_device(wtg_tree* T, const uint64_t* d_lb, const uint64_t* d_rb, const uint64_t* d_vlb,
+                                 const uint64_t* d_vrb, uint64_t nq, uint64_t* d_count, void* stream) {
+  if (!T) return fail(WTG_ERR_INVALID, "null tree");
+  return launch_wt_range_count(T->t, d_lb, d_rb, d_vlb, d_vrb, nq, d_count, (cudaStream_t)stream);
 }
 
 // ----------------------------------------------------- standalone bitvectors

@@ -27,7 +27,7 @@ struct TreeImpl {
   uint64_t bit_words = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
-  DevBuf seq, lvl[2], bits, hist, zeros, base, status, scan_tmp, err, scratch, nodes, qbuf;
+  DevBuf seq, lvl[2], bits, hist, zeros, base, status, scan_tmp, err, scratch, nodes, qbuf, qout;
   BvSupport bv;
   DevBuf lvl_args;
   bool lvl_args_ok = false;
@@ -63,6 +63,32 @@ int launch_wt_select(const TreeImpl& t, const uint64_t* i, const uint64_t* sym, 
 int launch_bv_rank(const BvSupport& bv, const uint64_t* idx, uint64_t nq, uint64_t* out, cudaStream_t s);
 int launch_bv_select(const BvSupport& bv, int t_b, const uint64_t* i, uint64_t nq, uint64_t* out,
                      cudaStream_t s);
+
+// wt_int's range queries (wtg_range.cu); all arrays are device arrays.
+// Count-type queries give UINT64_MAX for an invalid query (bounds outside
+// the sequence).  Variable-size answers are placed by answer_offsets: the
+// exclusive scan (nq + 1 entries, the last the total) of the per-query
+// counts, invalid ones read as 0; the fill launches then write query q's
+// answers to [off[q], off[q+1]) below cap.
+int answer_offsets(const uint64_t* counts, uint64_t nq, uint64_t* off, DevBuf& scratch, uint32_t* d_err,
+                   cudaStream_t s);
+int launch_wt_lex_count(TreeImpl& t, const uint64_t* i, const uint64_t* j, const uint64_t* c, uint64_t nq,
+                        uint64_t* rank_out, uint64_t* smaller_out, uint64_t* greater_out, cudaStream_t s);
+int launch_wt_lex_smaller_count(TreeImpl& t, const uint64_t* i, const uint64_t* c, uint64_t nq, uint64_t* rank_out,
+                                uint64_t* smaller_out, cudaStream_t s);
+int launch_wt_range_count(TreeImpl& t, const uint64_t* lb, const uint64_t* rb, const uint64_t* vlb,
+                          const uint64_t* vrb, uint64_t nq, uint64_t* count_out, cudaStream_t s);
+int launch_wt_range_report(TreeImpl& t, const uint64_t* lb, const uint64_t* rb, const uint64_t* vlb,
+                           const uint64_t* vrb, uint64_t nq, const uint64_t* off, uint64_t cap, uint64_t* pos,
+                           uint64_t* val, cudaStream_t s);
+// with k_out: the counts; without: the fill into off / cap / cs / ri / rj
+int launch_wt_interval_symbols(TreeImpl& t, const uint64_t* i, const uint64_t* j, uint64_t nq, uint64_t* k_out,
+                               const uint64_t* off, uint64_t cap, uint64_t* cs, uint64_t* ri, uint64_t* rj,
+                               cudaStream_t s);
+int launch_wt_expand(TreeImpl& t, const uint64_t* nodes, uint64_t nn, uint64_t* left, uint64_t* right,
+                     cudaStream_t s);
+int launch_wt_expand_ranges(TreeImpl& t, uint64_t voff, const uint64_t* ranges, uint64_t nr, uint64_t* left,
+                            uint64_t* right, cudaStream_t s);
 
 // per-level select on the tree's concatenated bitvector -- wt_int's select
 // step (m_tree_select1/0(args before the node + i) - node offset,

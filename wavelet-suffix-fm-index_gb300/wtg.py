@@ -68,6 +68,14 @@ _SIGS = {
     "wtg_query_select": ([vp, vp, vp, u64, vp], i32),
     "wtg_query_access_device": ([vp, vp, u64, vp, vp], i32),
     "wtg_query_rank_device": ([vp, vp, vp, u64, vp, vp], i32),
+    "wtg_query_lex_count": ([vp, vp, vp, vp, u64, vp, vp, vp], i32),
+    "wtg_query_lex_smaller_count": ([vp, vp, vp, u64, vp, vp], i32),
+    "wtg_query_range_search_2d": ([vp, vp, vp, vp, vp, u64, vp, u64, vp, vp], i32),
+    "wtg_query_interval_symbols": ([vp, vp, vp, u64, vp, u64, vp, vp, vp], i32),
+    "wtg_query_expand": ([vp, vp, u64, vp, vp], i32),
+    "wtg_query_expand_ranges": ([vp, vp, vp, u64, vp, vp], i32),
+    "wtg_query_lex_count_device": ([vp, vp, vp, vp, u64, vp, vp, vp, vp], i32),
+    "wtg_query_range_count_device": ([vp, vp, vp, vp, vp, u64, vp, vp], i32),
     "wtg_bv_build": ([vp, u64, ctypes.c_uint32, vp], i32),
     "wtg_bv_build_device": ([vp, u64, ctypes.c_uint32, vp, vp], i32),
     "wtg_bv_sync": ([vp], i32),
@@ -291,6 +299,81 @@ class WaveletTree:
         out = np.zeros(i.size, dtype=np.uint64)
         _ck(lib().wtg_query_select(self.h, _p(i), _p(sym), i.size, _p(out)))
         return out
+
+    # wt_int range queries (batched; UINT64_MAX answers for invalid bounds)
+    def lex_count(self, i, j, c):
+        """Rows (rank(i, c), symbols < c in [i, j), symbols > c in [i, j))."""
+        i, j, c = _u64(i), _u64(j), _u64(c)
+        out = np.zeros((3, i.size), dtype=np.uint64)
+        _ck(lib().wtg_query_lex_count(self.h, _p(i), _p(j), _p(c), i.size, _p(out[0]), _p(out[1]), _p(out[2])))
+        return out.T.copy()
+
+    def lex_smaller_count(self, i, c):
+        """Rows (rank(i, c), symbols < c in [0, i))."""
+        i, c = _u64(i), _u64(c)
+        out = np.zeros((2, i.size), dtype=np.uint64)
+        _ck(lib().wtg_query_lex_smaller_count(self.h, _p(i), _p(c), i.size, _p(out[0]), _p(out[1])))
+        return out.T.copy()
+
+    def range_count(self, lb, rb, vlb, vrb):
+        """range_search_2d(lb, rb, vlb, vrb, report=false) counts."""
+        lb, rb, vlb, vrb = _u64(lb), _u64(rb), _u64(vlb), _u64(vrb)
+        cnt = np.zeros(lb.size, dtype=np.uint64)
+        _ck(lib().wtg_query_range_search_2d(self.h, _p(lb), _p(rb), _p(vlb), _p(vrb), lb.size, _p(cnt), 0,
+                                            None, None))
+        return cnt
+
+    def range_search_2d(self, lb, rb, vlb, vrb, cap=None):
+        """range_search_2d with report: (counts, offsets, positions, values);
+        query q's points are positions/values[offsets[q]:offsets[q+1]]."""
+        cnt = self.range_count(lb, rb, vlb, vrb)
+        lb, rb, vlb, vrb = _u64(lb), _u64(rb), _u64(vlb), _u64(vrb)
+        valid = np.where(cnt == NONE, np.uint64(0), cnt)
+        off = np.concatenate([[0], np.cumsum(valid.astype(np.int64))]).astype(np.int64)
+        total = int(off[-1]) if cap is None else min(int(off[-1]), int(cap))
+        pos = np.zeros(max(total, 1), dtype=np.uint64)
+        val = np.zeros(max(total, 1), dtype=np.uint64)
+        if total:
+            _ck(lib().wtg_query_range_search_2d(self.h, _p(lb), _p(rb), _p(vlb), _p(vrb), lb.size, _p(cnt), total,
+                                                _p(pos), _p(val)))
+        return cnt, off, pos[:total], val[:total]
+
+    def interval_symbols(self, i, j):
+        """interval_symbols: (k, offsets, symbols, rank(i, c), rank(j, c));
+        query q's symbols are [offsets[q]:offsets[q+1]]."""
+        i, j = _u64(i), _u64(j)
+        k = np.zeros(i.size, dtype=np.uint64)
+        _ck(lib().wtg_query_interval_symbols(self.h, _p(i), _p(j), i.size, _p(k), 0, None, None, None))
+        valid = np.where(k == NONE, np.uint64(0), k)
+        off = np.concatenate([[0], np.cumsum(valid.astype(np.int64))]).astype(np.int64)
+        total = int(off[-1])
+        cs, ri, rj = (np.zeros(max(total, 1), dtype=np.uint64) for _ in range(3))
+        if total:
+            _ck(lib().wtg_query_interval_symbols(self.h, _p(i), _p(j), i.size, _p(k), total, _p(cs), _p(ri),
+                                                 _p(rj)))
+        return k, off, cs[:total], ri[:total], rj[:total]
+
+    def expand(self, nodes):
+        """Children of nodes (rows (offset, size, level, sym)): (left, right)."""
+        v = _u64(nodes).reshape(-1, 4)
+        left, right = np.zeros_like(v), np.zeros_like(v)
+        _ck(lib().wtg_query_expand(self.h, _p(v), v.shape[0], _p(left), _p(right)))
+        return left, right
+
+    def expand_ranges(self, node, ranges):
+        """Closed ranges [s, e] (rows) of node v mapped to its children."""
+        v, r = _u64(node), _u64(ranges).reshape(-1, 2)
+        left, right = np.zeros_like(r), np.zeros_like(r)
+        _ck(lib().wtg_query_expand_ranges(self.h, _p(v), _p(r), r.shape[0], _p(left), _p(right)))
+        return left, right
+
+    def lex_count_device(self, d_i, d_j, d_c, nq, d_rank, d_smaller, d_greater, stream=0):
+        _ck(lib().wtg_query_lex_count_device(self.h, vp(d_i), vp(d_j), vp(d_c), nq, vp(d_rank), vp(d_smaller),
+                                             vp(d_greater), vp(stream)))
+
+    def range_count_device(self, d_lb, d_rb, d_vlb, d_vrb, nq, d_count, stream=0):
+        _ck(lib().wtg_query_range_count_device(self.h, vp(d_lb), vp(d_rb), vp(d_vlb), vp(d_vrb), nq, vp(d_count),
+                                               vp(stream)))
 
     def access_device(self, d_idx, nq, d_out, stream=0):
         _ck(lib().wtg_query_access_device(self.h, vp(d_idx), nq, vp(d_out), vp(stream)))
