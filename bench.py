@@ -202,8 +202,10 @@ def select_queries(torch, m_levels, nq, gen, dev):
 
 
 def measure_queries(torch, tree, seq, n, dev, stream, log2_q, reps=5):
-    """wt_int access and rank(i, c) throughput: 2^log2_q uniform random
-    positions; for rank, i uniform in [0, n] and c drawn from the input."""
+    """wt_int access, rank(i, c), lex_count(i, j, c) and range_search_2d
+    counts: 2^log2_q queries each; positions uniform, i uniform in [0, n], c
+    drawn from the input, j - i and rb - lb uniform below 2^20, value window
+    [c - 2^12, c + 2^12]."""
     sp = stream.cuda_stream
     nq = 1 << log2_q
     gen = torch.Generator(device=dev)
@@ -212,10 +214,22 @@ def measure_queries(torch, tree, seq, n, dev, stream, log2_q, reps=5):
     ri = torch.randint(0, n + 1, (nq,), device=dev, generator=gen, dtype=torch.int64)
     rc = seq[torch.randint(0, n, (nq,), device=dev, generator=gen, dtype=torch.int64)].to(torch.int64)
     out = torch.empty(nq, device=dev, dtype=torch.int64)
+    # range queries: [i, j) of up to 2^20 positions; value window c +- 2^12
+    span = torch.randint(0, 1 << 20, (nq,), device=dev, generator=gen, dtype=torch.int64)
+    rj = torch.clamp(ri + span, max=n)
+    rb = torch.clamp(idx + span, max=n - 1)
+    vlb = torch.clamp(rc - (1 << 12), min=0)
+    vrb = rc + (1 << 12)
+    o2 = torch.empty(nq, device=dev, dtype=torch.int64)
+    o3 = torch.empty(nq, device=dev, dtype=torch.int64)
     ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
     res = {}
     for name, fn in (("access", lambda: tree.access_device(idx.data_ptr(), nq, out.data_ptr(), sp)),
-                     ("rank", lambda: tree.rank_device(ri.data_ptr(), rc.data_ptr(), nq, out.data_ptr(), sp))):
+                     ("rank", lambda: tree.rank_device(ri.data_ptr(), rc.data_ptr(), nq, out.data_ptr(), sp)),
+                     ("lex_count", lambda: tree.lex_count_device(ri.data_ptr(), rj.data_ptr(), rc.data_ptr(), nq,
+                                                                 out.data_ptr(), o2.data_ptr(), o3.data_ptr(), sp)),
+                     ("range_count", lambda: tree.range_count_device(idx.data_ptr(), rb.data_ptr(), vlb.data_ptr(),
+                                                                     vrb.data_ptr(), nq, out.data_ptr(), sp))):
         for _ in range(3):
             fn()
         torch.cuda.synchronize()
@@ -231,6 +245,12 @@ def measure_queries(torch, tree, seq, n, dev, stream, log2_q, reps=5):
     tree.access_device(idx.data_ptr(), nq, out.data_ptr(), sp)
     torch.cuda.synchronize()
     res["access_exact"] = bool(torch.equal(out, seq[idx].to(torch.int64)))
+    # a full value window counts every position of [lb, rb]
+    zero = torch.zeros_like(idx)
+    top = torch.full_like(idx, 1 << tree.levels)
+    tree.range_count_device(idx.data_ptr(), rb.data_ptr(), zero.data_ptr(), top.data_ptr(), nq, out.data_ptr(), sp)
+    torch.cuda.synchronize()
+    res["range_exact"] = bool(torch.equal(out, rb - idx + 1))
     res["queries"] = nq
     return res
 

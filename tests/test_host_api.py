@@ -65,3 +65,20 @@ def test_cpp_program_matches_oracle(wtg, oracle, tmp_path, variant, kind, n):
     assert np.array_equal(rank, orank)
     assert checks[0] == 0 and checks[1] == 0
     assert checks[2] == int(np.unpackbits(ob.view(np.uint8)).sum())
+    # range queries (the layout the program's header states)
+    rq = checks[3:]
+    assert rq.size == 64 * 9 + 4
+    s1, s0 = oracle.Select(w, n * L, 1), oracle.Select(w, n * L, 0)
+    for q in range(64):
+        i = q * n // 64
+        j = min(n, i + n // 8 + 1)
+        c = int(sym[i]) if i < n else 0
+        row = rq[9 * q:9 * q + 9]
+        assert list(row[:3]) == list(oracle.wt_lex_count(w, orank, n, L, [i], [j], [c])[0])
+        assert list(row[3:5]) == list(oracle.wt_lex_smaller_count(w, orank, n, L, [i], [c])[0])
+        p, _ = oracle.wt_range_report(w, orank, s1, s0, n, L, i, j - 1, c // 2, c)
+        assert row[5] == p.size and row[6] == int(p.sum())
+        cs, _, _ = oracle.wt_interval_symbols(w, orank, n, L, i, j)
+        assert row[7] == cs.size and row[8] == int(cs.sum())
+    left, _ = oracle.wt_expand(w, orank, n, [0, n, 0, 0])
+    assert rq[-4] == 0 and rq[-3] == 1 and rq[-2] == 1 and rq[-1] == 0 and left[2] == 1

@@ -9,9 +9,11 @@
 //     (wavelet/levelWT/WT.h:30-43): outputs are malloc'ed, freed by the caller
 //     with free() (levelWT/WTTime.C:99,135); `symbol`, `uintT` and the WTnode
 //     field width follow the same -DINT / -DLONG knobs (parallel.h:71-81).
-//   * wtg::wt_int (sdsl::wt_int<>, wt_int/wt_int_par.hpp:368-660): operator[],
-//     rank, inverse_select, select, size, sigma-free; std::logic_error where
-//     the reference throws one (wt_int_par.hpp:377,645).
+//   * wtg::wt_int (sdsl::wt_int<>, wt_int/wt_int_par.hpp:368-1048): operator[],
+//     rank, inverse_select, select, size, and the range queries
+//     interval_symbols, lex_count, lex_smaller_count, range_search_2d, root,
+//     expand; std::logic_error where the reference throws one
+//     (wt_int_par.hpp:377,645).
 //   * wtg::rank_support_v / wtg::select_support_mcl<t_b>
 //     (rank/rank_support_v_par.hpp:69-142, select/select_support_mcl_par.hpp:
 //     120-129,564-611) over a bit vector given as 64-bit words.
@@ -23,6 +25,7 @@
 #include <cstring>
 #include <stdexcept>
 #include <string>
+#include <tuple>
 #include <utility>
 #include <vector>
 
@@ -101,6 +104,22 @@ class wt_int {
  public:
   typedef uint64_t size_type;
   typedef uint64_t value_type;
+  typedef std::pair<value_type, size_type> point_type;  // (position, value)
+  typedef std::vector<point_type> point_vec_type;
+  typedef std::pair<size_type, point_vec_type> r2d_res_type;
+  typedef std::pair<size_type, size_type> range_type;  // closed [first, second]
+  typedef std::vector<range_type> range_vec_type;
+  // a node of the tree (wt_int_par.hpp:914-960): its bit offset, size, level
+  // and the symbol prefix of its path
+  struct node_type {
+    size_type offset = 0, size = 0, level = 0;
+    value_type sym = 0;
+    node_type(size_type o = 0, size_type sz = 0, size_type l = 0, value_type sy = 0)
+        : offset(o), size(sz), level(l), sym(sy) {}
+    bool operator==(const node_type& v) const { return offset == v.offset; }
+    bool operator<(const node_type& v) const { return offset < v.offset; }
+    bool operator>(const node_type& v) const { return offset > v.offset; }
+  };
   wt_int() = default;
   // wt_int(buf, size, max_level) (wt_int_par.hpp:368-406); max_level 0 derives
   // hi(max(1, max symbol)) + 1
@@ -143,6 +162,81 @@ class wt_int {
   }
   void rank(const uint64_t* idx, const uint64_t* sym, uint64_t nq, uint64_t* out) const {
     check(wtg_query_rank(t_.get(), idx, sym, nq, out));
+  }
+  // interval_symbols (wt_int_par.hpp:684-702): the k distinct symbols of
+  // [i, j) in cs[0..k-1], increasing, with rank(i, c) and rank(j, c); the
+  // vectors hold at least k entries (sigma is enough)
+  void interval_symbols(size_type i, size_type j, size_type& k, std::vector<value_type>& cs,
+                        std::vector<size_type>& rank_c_i, std::vector<size_type>& rank_c_j) const {
+    if (i > j || j > size()) throw std::logic_error("interval_symbols: need i <= j <= size()");
+    uint64_t kk = 0;
+    check(wtg_query_interval_symbols(t_.get(), &i, &j, 1, &kk, 0, nullptr, nullptr, nullptr));
+    k = kk;
+    if (!kk) return;
+    if (cs.size() < kk || rank_c_i.size() < kk || rank_c_j.size() < kk)
+      throw std::logic_error("interval_symbols: output vectors shorter than the symbol count");
+    check(wtg_query_interval_symbols(t_.get(), &i, &j, 1, &kk, kk, cs.data(), rank_c_i.data(), rank_c_j.data()));
+  }
+  // lex_count (wt_int_par.hpp:715-745): (rank(i, c), #symbols < c in [i, j),
+  // #symbols > c in [i, j))
+  std::tuple<size_type, size_type, size_type> lex_count(size_type i, size_type j, value_type c) const {
+    uint64_t r = 0, sm = 0, gr = 0;
+    check(wtg_query_lex_count(t_.get(), &i, &j, &c, 1, &r, &sm, &gr));
+    return std::make_tuple(r, sm, gr);
+  }
+  // lex_smaller_count (wt_int_par.hpp:758-782): (rank(i, c), #symbols < c in [0, i))
+  std::tuple<size_type, size_type> lex_smaller_count(size_type i, value_type c) const {
+    uint64_t r = 0, sm = 0;
+    check(wtg_query_lex_smaller_count(t_.get(), &i, &c, 1, &r, &sm));
+    return std::make_tuple(r, sm);
+  }
+  // range_search_2d (wt_int_par.hpp:801-815): points of positions [lb, rb]
+  // with values in [vlb, vrb], as (position, value), values increasing
+  r2d_res_type range_search_2d(size_type lb, size_type rb, value_type vlb, value_type vrb,
+                               bool report = true) const {
+    uint64_t cnt = 0;
+    check(wtg_query_range_search_2d(t_.get(), &lb, &rb, &vlb, &vrb, 1, &cnt, 0, nullptr, nullptr));
+    if (cnt == ~0ull) throw std::logic_error("range_search_2d: rb >= size()");
+    point_vec_type pts;
+    if (report && cnt) {
+      std::vector<uint64_t> pos(cnt), val(cnt);
+      check(wtg_query_range_search_2d(t_.get(), &lb, &rb, &vlb, &vrb, 1, &cnt, cnt, pos.data(), val.data()));
+      pts.reserve(cnt);
+      for (uint64_t q = 0; q < cnt; ++q) pts.emplace_back(pos[q], val[q]);
+    }
+    return r2d_res_type(cnt, std::move(pts));
+  }
+  node_type root() const { return node_type(0, size(), 0, 0); }
+  bool is_leaf(const node_type& v) const { return v.level == max_level(); }
+  value_type sym(const node_type& v) const { return v.sym; }
+  bool empty(const node_type& v) const { return v.size == 0; }
+  // expand(v) (wt_int_par.hpp:966-984): the children of inner node v
+  std::pair<node_type, node_type> expand(const node_type& v) const {
+    const uint64_t in[4] = {v.offset, v.size, v.level, v.sym};
+    uint64_t l[4], r[4];
+    check(wtg_query_expand(t_.get(), in, 1, l, r));
+    return std::make_pair(node_type(l[0], l[1], l[2], l[3]), node_type(r[0], r[1], r[2], r[3]));
+  }
+  // expand(v, ranges) (wt_int_par.hpp:1027-1048): each range of v mapped to
+  // the left and the right child
+  std::pair<range_vec_type, range_vec_type> expand(const node_type& v, const range_vec_type& ranges) const {
+    const uint64_t in[4] = {v.offset, v.size, v.level, v.sym};
+    std::vector<uint64_t> r(2 * ranges.size()), lo(r.size()), hi(r.size());
+    for (size_t q = 0; q < ranges.size(); ++q) {
+      r[2 * q] = ranges[q].first;
+      r[2 * q + 1] = ranges[q].second;
+    }
+    check(wtg_query_expand_ranges(t_.get(), in, r.data(), ranges.size(), lo.data(), hi.data()));
+    range_vec_type a(ranges.size()), b(ranges.size());
+    for (size_t q = 0; q < ranges.size(); ++q) {
+      a[q] = range_type(lo[2 * q], lo[2 * q + 1]);
+      b[q] = range_type(hi[2 * q], hi[2 * q + 1]);
+    }
+    return std::make_pair(std::move(a), std::move(b));
+  }
+  std::pair<range_type, range_type> expand(const node_type& v, const range_type& r) const {
+    auto e = expand(v, range_vec_type(1, r));
+    return std::make_pair(e.first[0], e.second[0]);
   }
   // the concatenated level bitvector (wt_int::tree, wt_int_par.hpp:80,290)
   std::vector<uint64_t> tree_words() const {
