@@ -39,20 +39,23 @@
 namespace wtg {
 
 constexpr int LV_THREADS = 256;
-// chunk buffers per warp (prefetch depth + 1): the bits-only last level is
-// latency bound and takes a deeper ring
+// chunk-group buffers per warp (prefetch depth + 1)
 template <bool SCATTER>
-constexpr int lv_stages() { return SCATTER ? 2 : 3; }
+constexpr int lv_stages() { return 2; }
 constexpr int TOP_BITS = 2;  // bits histogrammed by the pre-pass (ballot counted)
 
 constexpr int CHUNK = 512;      // symbols per warp chunk (16 rows of 32)
 constexpr int LOG_CHUNK = 9;
 constexpr int WROWS = CHUNK / 32;
 
+// A warp fetches CPB consecutive chunks with one 4 KB cp.async.bulk: on
+// GB300 a ring of 2 KB bulk copies reads at about 3.5 TB/s, one of 4 KB
+// copies at 6.8-7.4 TB/s (the per-copy cost, not the bytes, sets the rate).
 template <typename T>
 struct LvShape {
+  static constexpr uint32_t CPB = CHUNK * sizeof(T) >= 4096 ? 1 : 4096 / (CHUNK * sizeof(T));
   static constexpr uint32_t TILE = LV_THREADS / 32 * CHUNK;  // symbols per CTA tile
-  static constexpr uint32_t BYTES = TILE * sizeof(T);  // one chunk per warp
+  static constexpr uint32_t BYTES = TILE * sizeof(T) * CPB;  // one chunk group per warp
   template <bool SCATTER>
   static constexpr uint32_t smem() { return lv_stages<SCATTER>() * BYTES; }  // the warps' rings
 };
@@ -60,7 +63,8 @@ struct LvShape {
 // ------------------------------------------------------------ pre-pass
 // One read of the input: the zero count of level 0 (bit levels-1) in every
 // 512-symbol chunk, and the histogram of the top K <= 2 key bits.  A warp per
-// chunk, 16-byte coalesced loads, counts kept in registers.
+// chunk, 16-byte coalesced loads of two chunks in flight per warp, counts
+// kept in registers.
 
 template <typename T>
 __global__ void __launch_bounds__(LV_THREADS) prepass_kernel(const T* __restrict__ s, uint64_t n, int L, int K,
@@ -75,38 +79,54 @@ __global__ void __launch_bounds__(LV_THREADS) prepass_kernel(const T* __restrict
   uint32_t c1 = 0, c2 = 0, c12 = 0, cnt = 0;  // top bit set, second bit set, both, symbols
   constexpr int PER = 16 / sizeof(T);
   constexpr int NV = CHUNK * sizeof(T) / 16 / 32;  // 16-byte loads per lane and chunk
-  for (uint64_t c = gw; c < nchunks; c += nwarps) {
+  auto take = [&](uint64_t x, uint32_t& ones) {
+    const uint32_t b1 = (uint32_t)(x >> top) & 1u;
+    const uint32_t b2 = K > 1 ? (uint32_t)(x >> top2) & 1u : 0u;
+    ones += b1;
+    c2 += b2;
+    c12 += b1 & b2;
+  };
+  // one chunk's counts from its preloaded vectors (full) or scalar loads
+  auto chunk = [&](uint64_t c, bool full, const uint4* v) {
     const uint64_t base = c * CHUNK;
     const uint32_t cv = (uint32_t)min((uint64_t)CHUNK, n - base);
     uint32_t ones = 0;
-    auto take = [&](uint64_t x) {
-      const uint32_t b1 = (uint32_t)(x >> top) & 1u;
-      const uint32_t b2 = K > 1 ? (uint32_t)(x >> top2) & 1u : 0u;
-      ones += b1;
-      c2 += b2;
-      c12 += b1 & b2;
-    };
-    if (vec_ok && cv == CHUNK) {
-      const uint4* q = (const uint4*)(s + base);
+    if (full) {
 #pragma unroll
       for (int j = 0; j < NV; ++j) {
-        uint4 v = __ldg(&q[j * 32 + lane]);
-        const T* e = (const T*)&v;
+        const T* e = (const T*)&v[j];
 #pragma unroll
-        for (int k = 0; k < PER; ++k) take((uint64_t)e[k]);
+        for (int k = 0; k < PER; ++k) take((uint64_t)e[k], ones);
       }
       cnt += CHUNK / 32;
     } else {
       for (uint32_t k = lane; k < cv; k += 32) {
-        take((uint64_t)s[base + k]);
+        take((uint64_t)s[base + k], ones);
         ++cnt;
       }
     }
     c1 += ones;
-    uint32_t wz = ones;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) wz += __shfl_xor_sync(0xffffffffu, wz, o);
+    const uint32_t wz = __reduce_add_sync(0xffffffffu, ones);
     if (lane == 0) chunkcnt[c] = cv - wz;  // zeros of level 0 in this chunk
+  };
+  // two chunks per step, both loaded before either is counted
+  for (uint64_t c = gw; c < nchunks; c += 2 * nwarps) {
+    const uint64_t cb = c + nwarps;
+    const bool fa = vec_ok && (c + 1) * CHUNK <= n;
+    const bool fb = vec_ok && cb < nchunks && (cb + 1) * CHUNK <= n;
+    uint4 va[NV], vb[NV];
+    if (fa) {
+      const uint4* q = (const uint4*)(s + c * CHUNK);
+#pragma unroll
+      for (int j = 0; j < NV; ++j) va[j] = __ldg(&q[j * 32 + lane]);
+    }
+    if (fb) {
+      const uint4* q = (const uint4*)(s + cb * CHUNK);
+#pragma unroll
+      for (int j = 0; j < NV; ++j) vb[j] = __ldg(&q[j * 32 + lane]);
+    }
+    chunk(c, fa, va);
+    if (cb < nchunks) chunk(cb, fb, vb);
   }
   // bins of the top K bits (K = 1: bins 0/1 = top bit 0/1)
   uint32_t h[4] = {cnt - c1 - c2 + c12, c2 - c12, c1 - c12, c12};
@@ -326,28 +346,31 @@ __global__ void __launch_bounds__(LV_THREADS, 4)
                  const uint32_t* __restrict__ chunkpre, uint32_t* __restrict__ chunkcnt_next,
                  uint32_t* __restrict__ znext, uint32_t* err, int bulk_ok, uint32_t* __restrict__ chunkcnt_self) {
   constexpr uint32_t CBYTES = CHUNK * sizeof(T);
+  constexpr uint32_t CPB = LvShape<T>::CPB;
+  constexpr uint32_t GBYTES = CBYTES * CPB;  // one bulk copy: CPB consecutive chunks
   constexpr int LV_STAGES = lv_stages<SCATTER>();
   extern __shared__ __align__(128) unsigned char lv_smem[];
   __shared__ __align__(8) uint64_t mbar[LV_THREADS / 32][LV_STAGES];
   __shared__ uint32_t s_words[LV_THREADS / 32][WROWS];
   __shared__ uint32_t s_nz[LV_THREADS / 32][EMIT_TILES ? WROWS : 1];  // rows' next-level zero masks
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  T* const wring = (T*)(lv_smem + warp * LV_STAGES * CBYTES);  // this warp's LV_STAGES chunk buffers
+  T* const wring = (T*)(lv_smem + warp * LV_STAGES * GBYTES);  // this warp's LV_STAGES group buffers
   uint64_t* const bars = mbar[warp];
   uint32_t* const myw = s_words[warp];
   uint32_t* const mynz = s_nz[warp];
   const uint64_t nchunks = (n + CHUNK - 1) / CHUNK;
-  const uint64_t nfull = bulk_ok ? n / CHUNK : 0;  // chunks fetched with bulk copies
+  const uint64_t ngroups = (nchunks + CPB - 1) / CPB;
+  const uint64_t nfullg = bulk_ok ? n / (CHUNK * CPB) : 0;  // groups fetched with bulk copies
   const uint64_t stride = (uint64_t)gridDim.x * (LV_THREADS / 32);
-  const uint64_t c0 = (uint64_t)blockIdx.x * (LV_THREADS / 32) + warp;
+  const uint64_t g0 = (uint64_t)blockIdx.x * (LV_THREADS / 32) + warp;
   const int shift = L - 1 - level;
   const int pshift = L - level;
   const uint32_t pmask = level ? (uint32_t)((1ull << level) - 1) : 0u;
   const uint32_t ltmask = lanemask_lt();
   const uint32_t n32 = (uint32_t)n;  // n < 2^32
 
-  // ring of LV_STAGES buffers: chunk number j (0, 1, ... of this warp) uses
-  // slot j % LV_STAGES; LV_STAGES - 1 chunks are in flight ahead of the one
+  // ring of LV_STAGES buffers: group number j (0, 1, ... of this warp) uses
+  // slot j % LV_STAGES; LV_STAGES - 1 groups are in flight ahead of the one
   // being processed
   if (lane == 0) {
 #pragma unroll
@@ -355,10 +378,10 @@ __global__ void __launch_bounds__(LV_THREADS, 4)
     mbar_fence_init();
 #pragma unroll
     for (int q = 0; q < LV_STAGES - 1; ++q) {
-      const uint64_t cq = c0 + (uint64_t)q * stride;
-      if (cq < nfull) {
-        mbar_expect_tx(&bars[q], CBYTES);
-        bulk_g2s(wring + q * CHUNK, src + cq * CHUNK, CBYTES, &bars[q]);
+      const uint64_t gq = g0 + (uint64_t)q * stride;
+      if (gq < nfullg) {
+        mbar_expect_tx(&bars[q], GBYTES);
+        bulk_g2s(wring + q * CPB * CHUNK, src + gq * CPB * CHUNK, GBYTES, &bars[q]);
       }
     }
   }
@@ -368,21 +391,27 @@ __global__ void __launch_bounds__(LV_THREADS, 4)
   uint32_t cache_p = 0xFFFFFFFFu;  // base(p) cache
   uint2 cache_b = make_uint2(0, 0);
   uint32_t run_p = 0xFFFFFFFFu, run_e = 0, run_o = 0;  // EMIT_NODES run over uniform chunks
-  for (uint64_t c = c0; c < nchunks; c += stride) {
-    const uint64_t nx = c + (uint64_t)(LV_STAGES - 1) * stride;
+  for (uint64_t g = g0; g < ngroups; g += stride) {
+    const uint64_t nx = g + (uint64_t)(LV_STAGES - 1) * stride;
     const int nslot = slot == 0 ? LV_STAGES - 1 : slot - 1;  // (slot + STAGES - 1) % STAGES
-    if (lane == 0 && nx < nfull) {  // refill the slot freed by the previous chunk
+    if (lane == 0 && nx < nfullg) {  // refill the slot freed by the previous group
       fence_proxy_async_smem();
-      mbar_expect_tx(&bars[nslot], CBYTES);
-      bulk_g2s(wring + nslot * CHUNK, src + nx * CHUNK, CBYTES, &bars[nslot]);
+      mbar_expect_tx(&bars[nslot], GBYTES);
+      bulk_g2s(wring + nslot * CPB * CHUNK, src + nx * CPB * CHUNK, GBYTES, &bars[nslot]);
     }
-    T* const wt = wring + slot * CHUNK;
-    const uint64_t cbase = c * CHUNK;
-    const uint32_t cvalid = (uint32_t)min((uint64_t)CHUNK, n - cbase);
-    if (c < nfull) {
+    const bool gbulk = g < nfullg;
+    if (gbulk) {
       mbar_wait(&bars[slot], (phases >> slot) & 1u, err);
       phases ^= 1u << slot;
-    } else {
+    }
+#pragma unroll 1
+  for (uint32_t j = 0; j < CPB; ++j) {
+    const uint64_t c = g * CPB + j;
+    if (c >= nchunks) break;
+    T* const wt = wring + (slot * CPB + j) * CHUNK;
+    const uint64_t cbase = c * CHUNK;
+    const uint32_t cvalid = (uint32_t)min((uint64_t)CHUNK, n - cbase);
+    if (!gbulk) {
       for (uint32_t k = lane; k < CHUNK; k += 32) wt[k] = k < cvalid ? src[cbase + k] : T(0);
       __syncwarp();
     }
@@ -559,6 +588,7 @@ __global__ void __launch_bounds__(LV_THREADS, 4)
       }
     }
     __syncwarp();
+  }
     slot = slot + 1 == LV_STAGES ? 0 : slot + 1;
   }
   if (EMIT_NODES && lane == 0) emit_flush(znext, run_p, run_e, run_o);
