@@ -259,6 +259,22 @@ int wtg_batch_get_select(wtg_batch* b, uint64_t t, int t_b, uint64_t* sb_words, 
 /* the launch shape the first run chose, and the time of each candidate (ms) */
 int wtg_batch_tuning(wtg_batch* b, int* threads, int* items_per_thread, float ms[8]);
 
+/* ------------------------------------------------- suffix array and BWT
+ * The first two steps of the reference's FM-index construction
+ * (fm-index/par/WT.C:33-41): SA = divsufsort(s) (suffixArray/divsufsort,
+ * 32-bit entries, no sentinel: a suffix that is a prefix of another sorts
+ * first) and bwt[i] = s[SA[i] - 1], or s[n - 1] where SA[i] = 0.  Computed
+ * on the GPU by prefix doubling over radix sorts; identical to divsufsort's
+ * array.  n < 2^31. */
+int wtg_suffix_array(const uint8_t* text, uint64_t n, int32_t* sa_out);
+/* SA and BWT in one call; either output may be NULL (not both) */
+int wtg_bwt(const uint8_t* text, uint64_t n, uint8_t* bwt_out, int32_t* sa_out);
+/* device text / outputs on a stream (d_sa or d_bwt may be NULL); returns
+ * once the stream has finished; rounds (may be NULL) gets the number of
+ * doubling rounds.  Allocates its scratch (about 33 bytes per symbol). */
+int wtg_suffix_array_device(const uint8_t* d_text, uint64_t n, int32_t* d_sa, uint8_t* d_bwt, void* stream,
+                            int* rounds);
+
 /* ------------------------------------------------------------ FM-index count
  * Backward search over a tree built (with WTG_RANK) on the BWT of a text,
  * its symbols coded 0..sigma-1: the reference's FM-index is the wavelet tree

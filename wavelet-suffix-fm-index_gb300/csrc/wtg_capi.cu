@@ -662,6 +662,58 @@ int wtg_bv_select_device(wtg_bv* B, int t_b, const uint64_t* d_i, uint64_t nq, u
   return launch_bv_select(B->bv, t_b, d_i, nq, d_out, (cudaStream_t)stream);
 }
 
+// ------------------------------------------------- suffix array and BWT
+
+int wtg_suffix_array_device(const uint8_t* d_text, uint64_t n, int32_t* d_sa, uint8_t* d_bwt, void* stream,
+                            int* rounds) {
+  int rc;
+  if (n && !d_text) return fail(WTG_ERR_INVALID, "null text");
+  if ((rc = check_device())) return rc;
+  return suffix_array_device(d_text, n, (uint32_t*)d_sa, d_bwt, rounds, (cudaStream_t)stream);
+}
+
+int wtg_bwt(const uint8_t* text, uint64_t n, uint8_t* bwt_out, int32_t* sa_out) {
+  int rc;
+  if (n && (!text || (!bwt_out && !sa_out))) return fail(WTG_ERR_INVALID, "null argument");
+  if (n >= (1ull << 31)) return fail(WTG_ERR_INVALID, "suffix array: n must be below 2^31 (32-bit entries)");
+  if (n == 0) return WTG_OK;
+  if ((rc = check_device())) return rc;
+  cudaStream_t s = nullptr;
+  WTG_CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  DevBuf buf;
+  const uint64_t text_bytes = (n + 15) / 16 * 16;
+  rc = buf.ensure(text_bytes + 5 * n, s);  // text (padded), SA, BWT
+  if (rc == WTG_OK) {
+    uint8_t* d_text = buf.as<uint8_t>();
+    uint32_t* d_sa = (uint32_t*)(d_text + text_bytes);
+    uint8_t* d_bwt = (uint8_t*)(d_sa + n);
+    cudaError_t e = cudaMemcpyAsync(d_text, text, n, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) rc = cuda_fail(e, "copy text");
+    if (rc == WTG_OK) rc = suffix_array_device(d_text, n, d_sa, bwt_out ? d_bwt : nullptr, nullptr, s);
+    if (rc == WTG_OK && sa_out) {
+      e = cudaMemcpyAsync(sa_out, d_sa, n * 4, cudaMemcpyDeviceToHost, s);
+      if (e != cudaSuccess) rc = cuda_fail(e, "copy SA");
+    }
+    if (rc == WTG_OK && bwt_out) {
+      e = cudaMemcpyAsync(bwt_out, d_bwt, n, cudaMemcpyDeviceToHost, s);
+      if (e != cudaSuccess) rc = cuda_fail(e, "copy BWT");
+    }
+    if (rc == WTG_OK) {
+      e = cudaStreamSynchronize(s);
+      if (e != cudaSuccess) rc = cuda_fail(e, "suffix array");
+    }
+  }
+  buf.release(s);
+  cudaStreamSynchronize(s);
+  cudaStreamDestroy(s);
+  return rc;
+}
+
+int wtg_suffix_array(const uint8_t* text, uint64_t n, int32_t* sa_out) {
+  if (n && !sa_out) return fail(WTG_ERR_INVALID, "null argument");
+  return wtg_bwt(text, n, nullptr, sa_out);
+}
+
 // ------------------------------------------------------------ FM-index count
 
 int wtg_fm_count(wtg_tree* T, const uint64_t* C, uint64_t sigma, const uint8_t* pat, const uint64_t* off,

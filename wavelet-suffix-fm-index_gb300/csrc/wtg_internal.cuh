@@ -283,6 +283,12 @@ int scan_exclusive_u32(const uint32_t* in, uint32_t* out, uint64_t n, DevBuf& sc
 int scan_exclusive_u64(const uint64_t* in, uint64_t* out, uint64_t n, DevBuf& scratch, uint32_t* d_err,
                        cudaStream_t s);
 
+// suffix array (and, when d_bwt is given, the BWT) of a device byte text
+// (wtg_sa.cu); n < 2^31; returns after the stream has finished the work;
+// rounds (optional) gets the number of doubling rounds
+int suffix_array_device(const uint8_t* d_text, uint64_t n, uint32_t* d_sa, uint8_t* d_bwt, int* rounds,
+                        cudaStream_t s);
+
 // Flat select_support_mcl on the device.
 struct SelectDev {
   uint64_t arg_cnt = 0, nsb = 0, logn = 0, logn4 = 0, has_long = 0, sb_nwords = 0, pool_nwords = 0;

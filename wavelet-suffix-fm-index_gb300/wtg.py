@@ -68,6 +68,9 @@ _SIGS = {
     "wtg_query_select": ([vp, vp, vp, u64, vp], i32),
     "wtg_query_access_device": ([vp, vp, u64, vp, vp], i32),
     "wtg_query_rank_device": ([vp, vp, vp, u64, vp, vp], i32),
+    "wtg_suffix_array": ([vp, u64, vp], i32),
+    "wtg_bwt": ([vp, u64, vp, vp], i32),
+    "wtg_suffix_array_device": ([vp, u64, vp, vp, vp, vp], i32),
     "wtg_query_lex_count": ([vp, vp, vp, vp, u64, vp, vp, vp], i32),
     "wtg_query_lex_smaller_count": ([vp, vp, vp, u64, vp, vp], i32),
     "wtg_query_range_search_2d": ([vp, vp, vp, vp, vp, u64, vp, u64, vp, vp], i32),
@@ -502,6 +505,30 @@ class LearnedSelect:
         _ck(lib().wtg_lsel_query_device(self.h, t_b, vp(d_level), vp(d_k), nq, vp(d_out), vp(stream)))
 
 
+def suffix_array(text):
+    """Suffix array of a byte text (int32, the order divsufsort gives)."""
+    text = np.ascontiguousarray(text, dtype=np.uint8)
+    sa = np.zeros(max(text.size, 1), dtype=np.int32)
+    _ck(lib().wtg_suffix_array(_p(text), text.size, _p(sa)))
+    return sa[: text.size]
+
+
+def bwt(text, with_sa=False):
+    """BWT of a byte text by fm-index/par/WT.C:38-41 (and its suffix array)."""
+    text = np.ascontiguousarray(text, dtype=np.uint8)
+    out = np.zeros(max(text.size, 1), dtype=np.uint8)
+    sa = np.zeros(max(text.size, 1), dtype=np.int32) if with_sa else None
+    _ck(lib().wtg_bwt(_p(text), text.size, _p(out), _p(sa) if with_sa else None))
+    return (out[: text.size], sa[: text.size]) if with_sa else out[: text.size]
+
+
+def suffix_array_device(d_text, n, d_sa=0, d_bwt=0, stream=0):
+    """Device variant; returns the number of doubling rounds."""
+    r = ctypes.c_int(0)
+    _ck(lib().wtg_suffix_array_device(vp(d_text), n, vp(d_sa), vp(d_bwt), vp(stream), ctypes.byref(r)))
+    return r.value
+
+
 class FMIndex:
     """FM-index core over a BWT (fm-index/par/WT.C:33-46: the wavelet tree of
     s[SA[i]-1]): a GPU wavelet tree over the BWT's symbol codes
@@ -513,6 +540,18 @@ class FMIndex:
         self.tree = WaveletTree(bwt_codes, levels=levels_for_sigma(self.sigma), flags=ALL)
         occ = self.tree.rank(np.full(self.sigma, self.n), np.arange(self.sigma))
         self.C = np.concatenate([[0], np.cumsum(occ)[:-1]]).astype(np.uint64)
+
+    @classmethod
+    def from_text(cls, text):
+        """FM-index of a byte text, built as fm-index/par/WT.C:33-44 does:
+        suffix array and BWT on the GPU, the BWT's bytes coded 0..sigma-1 in
+        byte order, its wavelet tree.  Returns (index, byte -> code table)."""
+        b = bwt(text)
+        present = np.zeros(256, dtype=bool)
+        present[np.unique(b)] = True
+        code = np.cumsum(present).astype(np.int64) - 1
+        fm = cls(code[b].astype(np.uint8), int(present.sum()))
+        return fm, np.where(present, code, -1)
 
     @staticmethod
     def pack(patterns):
