@@ -255,6 +255,109 @@ def measure_queries(torch, tree, seq, n, dev, stream, log2_q, reps=5):
     return res
 
 
+def measure_fm(torch, wtg, oracle_mod, dev, log2_n, log2_q, cpu_log2):
+    """FM-index core on an order-2 Markov DNA text of 2^log2_n symbols with
+    0.1 % N runs and a '$' terminator: suffix array + BWT
+    (fm-index/par/WT.C:33-41) on the GPU,
+    the 3-level wavelet tree of the BWT codes with rank + select, and 2^log2_q
+    backward-search counts of patterns of U[8, 32] symbols copied from the
+    text (each occurs, so every count must be >= 1: counts_below_1 = 0).  The CPU figure is the
+    oracle's suffix array on a 2^cpu_log2 sample (single thread)."""
+    import datagen
+    n = 1 << log2_n
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+    with torch.cuda.stream(stream):
+        text = datagen.dna_markov_device(n, torch, dev, seed=SEED + 17)
+        # a unique smallest last symbol: suffix order is then rotation order,
+        # so backward search over the sentinel-free BWT counts exactly
+        text[n - 1] = ord("$")
+        sa = torch.empty(n, dtype=torch.int32, device=dev)
+        bw = torch.empty(n, dtype=torch.uint8, device=dev)
+    torch.cuda.synchronize()
+    rounds = wtg.suffix_array_device(text.data_ptr(), n, sa.data_ptr(), bw.data_ptr(), sp)  # warm-up
+    reps = 2
+    e0, e1 = ev(), ev()
+    e0.record(stream)
+    for _ in range(reps):
+        wtg.suffix_array_device(text.data_ptr(), n, sa.data_ptr(), bw.data_ptr(), sp)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    sa_ms = e0.elapsed_time(e1) / reps
+    # BWT bytes -> codes 0..sigma-1 in byte order, then its wavelet tree
+    with torch.cuda.stream(stream):
+        present = torch.zeros(256, dtype=torch.int64, device=dev)
+        present[torch.unique(bw).long()] = 1
+        lut = (torch.cumsum(present, 0) - 1).to(torch.uint8)
+        codes = lut[bw.long()].contiguous()
+        tcodes = lut[text.long()].contiguous()
+    torch.cuda.synchronize()
+    sigma = int(present.sum().item())
+    fm = wtg.FMIndex.from_device(codes.data_ptr(), n, sigma, sp)
+    e0, e1 = ev(), ev()
+    e0.record(stream)
+    fm2 = wtg.FMIndex.from_device(codes.data_ptr(), n, sigma, sp)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    wt_ms = e0.elapsed_time(e1)
+    del fm2
+    # count queries
+    nq = 1 << log2_q
+    g = torch.Generator(device=dev)
+    g.manual_seed(SEED + 19)
+    lens = torch.randint(8, 33, (nq,), device=dev, generator=g)
+    starts = torch.randint(0, n - 32, (nq,), device=dev, generator=g)
+    off = torch.zeros(nq + 1, dtype=torch.int64, device=dev)
+    off[1:] = torch.cumsum(lens, 0)
+    total = int(off[-1].item())
+    qid = torch.repeat_interleave(torch.arange(nq, device=dev), lens)
+    pos = starts[qid] + (torch.arange(total, device=dev) - off[:-1][qid])
+    pat = tcodes[pos].contiguous()
+    del qid, pos
+    dC = torch.from_numpy(fm.C.view(np.int64)).to(dev)
+    out = torch.empty(nq, dtype=torch.int64, device=dev)
+    run = lambda: fm.count_device(dC.data_ptr(), pat.data_ptr(), off.data_ptr(), nq, out.data_ptr(), sp)  # noqa: E731
+    run()
+    torch.cuda.synchronize()
+    e0, e1 = ev(), ev()
+    e0.record(stream)
+    for _ in range(3):
+        run()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    q_ms = e0.elapsed_time(e1) / 3
+    zero = int((out < 1).sum().item())
+    # sorted-order spot check of the suffix array: adjacent suffixes compare
+    # by first symbol, then by the inverse array one position on
+    s_h = text.cpu().numpy()
+    sa_h = sa.cpu().numpy().astype(np.int64)
+    inv = np.empty(n + 1, np.int64)
+    inv[sa_h] = np.arange(n)
+    inv[n] = -1
+    a_, b_ = sa_h[:-1], sa_h[1:]
+    sa_exact = bool(((s_h[a_] < s_h[b_]) | ((s_h[a_] == s_h[b_]) & (inv[a_ + 1] < inv[b_ + 1]))).all())
+    del s_h, sa_h, inv, a_, b_
+    cpu = None
+    if oracle_mod is not None and cpu_log2:
+        m = 1 << cpu_log2
+        sample = text[:m].cpu().numpy()
+        t0 = time.perf_counter()
+        oracle_mod.suffix_array(sample)
+        cpu_s = time.perf_counter() - t0
+        cpu = {"symbols_per_s": m / cpu_s, "sample": f"first 2^{cpu_log2} symbols, oracle prefix doubling, 1 thread",
+               "s": cpu_s}
+    res = {"workload": f"order-2 Markov DNA text + '$', n=2^{log2_n}, 0.1% N runs; SA+BWT, 3-level WT + rank + select "
+                       f"of the BWT, 2^{log2_q} counts of patterns of U[8,32] symbols",
+           "n": n, "sigma": sigma, "sa_bwt_ms": sa_ms, "sa_rounds": rounds,
+           "sa_msym_per_s": n / (sa_ms / 1e3) / 1e6, "wt_ms": wt_ms, "fm_build_ms": sa_ms + wt_ms,
+           "count_queries": nq, "count_ms": q_ms, "count_mqs": nq / (q_ms / 1e3) / 1e6,
+           "counts_below_1": zero, "sa_order_exact": sa_exact, "cpu_suffix_array": cpu}
+    del text, sa, bw, codes, tcodes, pat, fm
+    torch.cuda.empty_cache()
+    return res
+
+
 def measure_batch(torch, wtg, stream, ntexts, reps=5):
     """Batched build of ntexts DNA-like texts (lengths floor(2^U[10,20]),
     i.i.d. uniform over 4 symbols, 2 levels, rank + select1 + select0): one
@@ -484,6 +587,13 @@ def run_wtg(args, rank, world, local_rank):
         queries = measure_queries(torch, tree, seq, n, dev, stream, args.select_log2)
     if args.batch_texts:
         batch = measure_batch(torch, wtg, stream, args.batch_texts)
+    fm = None
+    if args.fm_log2:
+        orc = None
+        if not args.no_cpu:
+            from oracle import oracle as orc
+            orc.build(ref=False)
+        fm = measure_fm(torch, wtg, orc, dev, args.fm_log2, args.fm_queries_log2, args.fm_cpu_log2)
 
     # ---- e2e: host API with pinned host buffers, outputs copied back
     e2e = None
@@ -562,6 +672,7 @@ def run_wtg(args, rank, world, local_rank):
         "kernel_time": kernel_share,
         "select": select,
         "queries": queries,
+        "fm": fm,
         "batch": batch,
         "cpu_baseline": cpu,
         "e2e": e2e,
@@ -585,6 +696,10 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-select", action="store_true")
+    ap.add_argument("--fm-log2", type=int, default=28,
+                    help="FM-index core (suffix array, BWT, tree, counts) on a 2^k DNA text; 0 skips")
+    ap.add_argument("--fm-queries-log2", type=int, default=24)
+    ap.add_argument("--fm-cpu-log2", type=int, default=22)
     ap.add_argument("--batch-texts", type=int, default=4096,
                     help="texts of the batched-build comparison (0: skip it)")
     ap.add_argument("--select-log2", type=int, default=26,

@@ -82,19 +82,28 @@ __global__ void __launch_bounds__(SA_THREADS) radix_count_kernel(const uint64_t*
   }
 }
 
-// stable scatter of one tile: offs = exclusive scan of counts; a warp ranks
-// its 512 elements in order (equal digits of one step ranked by lane)
+// stable scatter of one tile: offs = exclusive scan of counts.  A warp ranks
+// its 512 elements in order (equal digits of one step ranked by lane) into a
+// digit-sorted copy of the tile in shared memory; the block then writes the
+// copy out in order, so each digit's run goes out as consecutive stores.
 __global__ void __launch_bounds__(SA_THREADS) radix_scatter_kernel(const uint64_t* __restrict__ key,
                                                                   const uint32_t* __restrict__ val, uint64_t n,
                                                                   int shift, const uint32_t* __restrict__ offs,
                                                                   uint32_t ntiles, uint64_t* __restrict__ key_out,
                                                                   uint32_t* __restrict__ val_out) {
-  __shared__ uint32_t wc[SA_WARPS][RADIX];
+  extern __shared__ __align__(16) unsigned char sa_smem[];
+  uint64_t* const skey = (uint64_t*)sa_smem;                  // SA_TILE keys
+  uint32_t* const sval = (uint32_t*)(skey + SA_TILE);         // SA_TILE values
+  __shared__ uint32_t wc[SA_WARPS][RADIX];                    // per warp: count, then local base
+  __shared__ int64_t gdelta[RADIX];                           // global position - local index
+  __shared__ uint32_t wsum[SA_WARPS];
   for (uint32_t i = threadIdx.x; i < SA_WARPS * RADIX; i += SA_THREADS) (&wc[0][0])[i] = 0;
   __syncthreads();
   const uint32_t w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t lt = (1u << lane) - 1u;
-  const uint64_t base = (uint64_t)blockIdx.x * SA_TILE + (uint64_t)w * SA_IPW;
+  const uint64_t tile0 = (uint64_t)blockIdx.x * SA_TILE;
+  const uint32_t tn = (uint32_t)min((uint64_t)SA_TILE, n - tile0);  // elements in this tile
+  const uint64_t base = tile0 + (uint64_t)w * SA_IPW;
   for (int it = 0; it < SA_IPW / 32; ++it) {
     const uint64_t idx = base + it * 32 + lane;
     const bool valid = idx < n;
@@ -104,34 +113,55 @@ __global__ void __launch_bounds__(SA_THREADS) radix_scatter_kernel(const uint64_
     __syncwarp();
   }
   __syncthreads();
-  for (uint32_t d = threadIdx.x; d < RADIX; d += SA_THREADS) {
-    uint32_t run = offs[(uint64_t)d * ntiles + blockIdx.x];
-    for (int k = 0; k < SA_WARPS; ++k) {
-      const uint32_t c = wc[k][d];
-      wc[k][d] = run;
-      run += c;
-    }
+  // thread d: the tile's count of digit d, its exclusive scan over digits
+  // (the digit's first local index) and each warp's local base
+  const uint32_t d = threadIdx.x;  // SA_THREADS == RADIX
+  uint32_t tot = 0;
+  for (int k = 0; k < SA_WARPS; ++k) tot += wc[k][d];
+  uint32_t inc = tot;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t q = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= (uint32_t)o) inc += q;
+  }
+  if (lane == 31) wsum[w] = inc;
+  __syncthreads();
+  uint32_t start = inc - tot;
+  for (uint32_t k = 0; k < w; ++k) start += wsum[k];
+  gdelta[d] = (int64_t)offs[(uint64_t)d * ntiles + blockIdx.x] - (int64_t)start;
+  uint32_t run = start;
+  for (int k = 0; k < SA_WARPS; ++k) {
+    const uint32_t c = wc[k][d];
+    wc[k][d] = run;
+    run += c;
   }
   __syncthreads();
   for (int it = 0; it < SA_IPW / 32; ++it) {
     const uint64_t idx = base + it * 32 + lane;
     const bool valid = idx < n;
     uint64_t k = 0;
-    uint32_t v = 0, d = 0xFFFFu;
+    uint32_t v = 0, dg = 0xFFFFu;
     if (valid) {
       k = key[idx];
       v = val[idx];
-      d = (uint32_t)(k >> shift) & (RADIX - 1);
+      dg = (uint32_t)(k >> shift) & (RADIX - 1);
     }
-    const uint32_t peers = __match_any_sync(0xffffffffu, d);
+    const uint32_t peers = __match_any_sync(0xffffffffu, dg);
     if (valid) {
-      const uint32_t pos = wc[w][d] + __popc(peers & lt);
-      key_out[pos] = k;
-      val_out[pos] = v;
+      const uint32_t lp = wc[w][dg] + __popc(peers & lt);
+      skey[lp] = k;
+      sval[lp] = v;
     }
     __syncwarp();
-    if (valid && lane == (uint32_t)(__ffs(peers) - 1)) wc[w][d] += __popc(peers);
+    if (valid && lane == (uint32_t)(__ffs(peers) - 1)) wc[w][dg] += __popc(peers);
     __syncwarp();
+  }
+  __syncthreads();
+  for (uint32_t j = threadIdx.x; j < tn; j += SA_THREADS) {
+    const uint64_t k = skey[j];
+    const uint64_t g = (uint64_t)((int64_t)j + gdelta[(uint32_t)(k >> shift) & (RADIX - 1)]);
+    key_out[g] = k;
+    val_out[g] = sval[j];
   }
 }
 
@@ -190,8 +220,15 @@ struct SaScratch {
 
 // LSD radix sort of (key, val) pairs on key bits [lo, hi); the result is in
 // key[cur] / val[cur] (cur flips once per pass)
+constexpr int SCATTER_SMEM = SA_TILE * (8 + 4);  // the tile's keys and values
+
 static int radix_sort(SaScratch& x, uint64_t n, int lo, int hi, int& cur) {
   int rc;
+  static bool attr = false;
+  if (!attr) {
+    WTG_CK(cudaFuncSetAttribute(radix_scatter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SCATTER_SMEM));
+    attr = true;
+  }
   const uint32_t ntiles = (uint32_t)((n + SA_TILE - 1) / SA_TILE);
   for (int shift = lo; shift < hi; shift += RBITS) {
     radix_count_kernel<<<ntiles, SA_THREADS, 0, x.s>>>(x.key[cur].as<uint64_t>(), n, shift, x.counts.as<uint32_t>(),
@@ -201,7 +238,7 @@ static int radix_sort(SaScratch& x, uint64_t n, int lo, int hi, int& cur) {
     if ((rc = scan_exclusive_u32(x.counts.as<uint32_t>(), x.counts.as<uint32_t>(), (uint64_t)RADIX * ntiles,
                                  x.scan_tmp, x.err.as<uint32_t>(), x.s)))
       return rc;
-    radix_scatter_kernel<<<ntiles, SA_THREADS, 0, x.s>>>(x.key[cur].as<uint64_t>(), x.val[cur].as<uint32_t>(), n,
+    radix_scatter_kernel<<<ntiles, SA_THREADS, SCATTER_SMEM, x.s>>>(x.key[cur].as<uint64_t>(), x.val[cur].as<uint32_t>(), n,
                                                          shift, x.counts.as<uint32_t>(), ntiles,
                                                          x.key[cur ^ 1].as<uint64_t>(), x.val[cur ^ 1].as<uint32_t>());
     count_launch();

@@ -76,6 +76,38 @@ def dna_markov(n, seed=0, n_frac=0.001):
     return text
 
 
+def dna_markov_device(n, torch, device, seed=0, n_frac=0.001, block=4096):
+    """dna_markov's distribution generated on the GPU for large n: the text
+    is cut into blocks of `block` symbols, each an order-2 chain from a
+    uniform start (restarts cost a few symbols of mixing per block); N runs
+    of U[1, 100] symbols until about n_frac of the text is N.  uint8 ACGTN."""
+    rng = np.random.default_rng(seed)
+    trans = rng.dirichlet(np.ones(4), size=16)
+    cdf = torch.tensor(np.cumsum(trans, axis=1)[:, :3], dtype=torch.float32, device=device)
+    nb = (n + block - 1) // block
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    a = torch.randint(0, 4, (nb,), device=device, generator=g)
+    b = torch.randint(0, 4, (nb,), device=device, generator=g)
+    codes = torch.empty((block, nb), dtype=torch.uint8, device=device)
+    for i in range(block):
+        u = torch.rand(nb, device=device, generator=g)
+        row = cdf[a * 4 + b]
+        c = (u.unsqueeze(1) > row).sum(dim=1)
+        codes[i] = c.to(torch.uint8)
+        a, b = b, c
+    lut = torch.tensor(np.frombuffer(b"ACGT", np.uint8).copy(), device=device)
+    text = lut[codes.t().reshape(-1)[:n].long()]
+    runs = int(round(n * n_frac / 50.5))
+    if runs:
+        ln = torch.randint(1, 101, (runs,), device=device, generator=g)
+        st = torch.randint(0, max(1, n - 100), (runs,), device=device, generator=g)
+        idx = (st.unsqueeze(1) + torch.arange(100, device=device).unsqueeze(0))
+        idx = idx[torch.arange(100, device=device).unsqueeze(0) < ln.unsqueeze(1)]
+        text[idx] = ord("N")
+    return text.contiguous()
+
+
 def batch_texts(k=4096, lo=10, hi=20, seed=0):
     rng = np.random.default_rng(seed)
     lens = np.floor(2.0 ** rng.uniform(lo, hi, k)).astype(np.int64)

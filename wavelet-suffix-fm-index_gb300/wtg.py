@@ -542,6 +542,17 @@ class FMIndex:
         self.C = np.concatenate([[0], np.cumsum(occ)[:-1]]).astype(np.uint64)
 
     @classmethod
+    def from_device(cls, d_codes, n, sigma, stream=0):
+        """FM-index over a BWT already on the device (codes 0..sigma-1, u8)."""
+        fm = cls.__new__(cls)
+        fm.n, fm.sigma = int(n), int(sigma)
+        fm.tree = WaveletTree.from_device(d_codes, n, 1, levels_for_sigma(fm.sigma), ALL, stream)
+        fm.tree.sync()
+        occ = fm.tree.rank(np.full(fm.sigma, fm.n), np.arange(fm.sigma))
+        fm.C = np.concatenate([[0], np.cumsum(occ)[:-1]]).astype(np.uint64)
+        return fm
+
+    @classmethod
     def from_text(cls, text):
         """FM-index of a byte text, built as fm-index/par/WT.C:33-44 does:
         suffix array and BWT on the GPU, the BWT's bytes coded 0..sigma-1 in
