@@ -8,9 +8,11 @@
 //     each; a suffix's first K = floor(64 / b) characters, packed
 //     most-significant first, are its initial 64-bit key, so key order is the
 //     order of the K-character prefixes (a prefix cut by the end sorts first);
-//   * after a sort, rank[i] = number of distinct keys before suffix i's key;
-//     while some ranks are shared, the next key of suffix i is
-//     (rank[i], rank[i + h] + 1 or 0 past the end) and h doubles.
+//   * after a sort, rank[i] = the suffix-array position of the first slot of
+//     suffix i's group (suffixes with equal keys); while groups of several
+//     suffixes remain, only their members are re-keyed by
+//     (rank[i], rank[i + h] + 1 or 0 past the end) and re-sorted, and h
+//     doubles (finished groups are never touched again).
 // The sort is stable and every rank is a function of the key, so the result
 // is the unique suffix order, the same array divsufsort gives.
 #include <algorithm>
@@ -165,30 +167,77 @@ __global__ void __launch_bounds__(SA_THREADS) radix_scatter_kernel(const uint64_
   }
 }
 
-// g[j] = 1 where sorted key j starts a new run of equal keys; g[n] = 0
-__global__ void run_flags_kernel(const uint64_t* __restrict__ key, uint64_t n, uint32_t* __restrict__ g) {
-  for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j <= n; j += (uint64_t)gridDim.x * blockDim.x)
-    g[j] = j < n && (j == 0 || key[j] != key[j - 1]) ? 1u : 0u;
+// Doubling rounds work on the active list: the suffix-array positions
+// act[0..m) (ascending) of the suffixes whose group still holds more than
+// one suffix.  A group occupies consecutive positions, its members share
+// rank = the position of the group's first slot, and sorting the active
+// suffixes by (rank, rank of the suffix h on) lays the groups out in
+// position order again, so the k-th sorted suffix goes to position act[k].
+
+__device__ __forceinline__ bool run_start(const uint64_t* __restrict__ key, uint64_t k) {
+  return k == 0 || key[k] != key[k - 1];
 }
 
-// rank[val[j]] = distinct keys before sorted key j (g = exclusive scan of the
-// flags, so g[j] + flag(j) - 1)
-__global__ void ranks_kernel(const uint64_t* __restrict__ key, const uint32_t* __restrict__ val,
-                             const uint32_t* __restrict__ g, uint64_t n, uint32_t* __restrict__ rank) {
-  for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t f = (j == 0 || key[j] != key[j - 1]) ? 1u : 0u;
-    rank[val[j]] = g[j] + f - 1u;
-  }
-}
-
-// doubling key of suffix i: (rank[i], rank[i + h] + 1, or 0 past the end)
-__global__ void double_keys_kernel(const uint32_t* __restrict__ rank, uint64_t n, uint64_t h, int B,
+// key of active suffix k: the first K codes (round 0, suffix k, act is the
+// identity) or (rank[i], rank[i + h] + 1, or 0 past the end) for i = sa[act[k]]
+__global__ void active_keys_kernel(const uint32_t* __restrict__ act, const uint32_t* __restrict__ sa,
+                                   const uint32_t* __restrict__ rank, uint64_t m, uint64_t n, uint64_t h, int B,
                                    uint64_t* __restrict__ key, uint32_t* __restrict__ val) {
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < m; k += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t i = sa[act[k]];
     const uint64_t sec = i + h < n ? (uint64_t)rank[i + h] + 1 : 0;
-    key[i] = ((uint64_t)rank[i] << B) | sec;
-    val[i] = (uint32_t)i;
+    key[k] = ((uint64_t)rank[i] << B) | sec;
+    val[k] = i;
   }
+}
+
+// g[k] = 1 where sorted key k starts a run of equal keys; g[m] = 0
+__global__ void run_flags_kernel(const uint64_t* __restrict__ key, uint64_t m, uint32_t* __restrict__ g) {
+  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k <= m; k += (uint64_t)gridDim.x * blockDim.x)
+    g[k] = k < m && run_start(key, k) ? 1u : 0u;
+}
+
+// after the scan of the run flags: first[r] = sorted index of run r's first key
+__global__ void run_first_kernel(const uint64_t* __restrict__ key, const uint32_t* __restrict__ g, uint64_t m,
+                                 uint32_t* __restrict__ first) {
+  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < m; k += (uint64_t)gridDim.x * blockDim.x)
+    if (run_start(key, k)) first[g[k]] = (uint32_t)k;
+}
+
+// place the sorted active suffixes, give each the position of its new
+// group's first slot as rank, and flag the ones still sharing a group
+// (ga[k] = 1, ga[m] = 0, for the scan that compacts the next active list)
+__global__ void place_kernel(const uint64_t* __restrict__ key, const uint32_t* __restrict__ val,
+                             const uint32_t* __restrict__ g, const uint32_t* __restrict__ first,
+                             const uint32_t* __restrict__ act, uint64_t m, uint32_t* __restrict__ sa,
+                             uint32_t* __restrict__ rank, uint32_t* __restrict__ ga) {
+  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k <= m; k += (uint64_t)gridDim.x * blockDim.x) {
+    if (k == m) {
+      ga[m] = 0;
+      continue;
+    }
+    const bool st = run_start(key, k);
+    const bool next_st = k + 1 == m || key[k + 1] != key[k];
+    const uint32_t i = val[k];
+    sa[act[k]] = i;
+    rank[i] = act[first[g[k] + (st ? 1u : 0u) - 1u]];
+    ga[k] = (st && next_st) ? 0u : 1u;
+  }
+}
+
+// next active list: act_next[ga[k]] = act[k] for the suffixes still shared
+__global__ void compact_active_kernel(const uint64_t* __restrict__ key, const uint32_t* __restrict__ ga,
+                                      const uint32_t* __restrict__ act, uint64_t m, uint32_t* __restrict__ act_next) {
+  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < m; k += (uint64_t)gridDim.x * blockDim.x) {
+    const bool st = run_start(key, k);
+    const bool next_st = k + 1 == m || key[k + 1] != key[k];
+    if (!(st && next_st)) act_next[ga[k]] = act[k];
+  }
+}
+
+__global__ void iota_kernel(uint32_t* __restrict__ a, uint64_t m) {
+  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < m; k += (uint64_t)gridDim.x * blockDim.x)
+    a[k] = (uint32_t)k;
 }
 
 // fm-index/par/WT.C:38-41: bwt[j] = s[SA[j] - 1], or s[n - 1] where SA[j] = 0
@@ -210,11 +259,13 @@ unsigned grid_for(uint64_t n) {
 
 // Scratch of one suffix-array run, released when it ends.
 struct SaScratch {
-  DevBuf key[2], val[2], rank, g, counts, scan_tmp, err, small;
+  DevBuf key[2], val[2], rank, sa, act[2], g, first, counts, scan_tmp, err, small;
   cudaStream_t s;
   explicit SaScratch(cudaStream_t st) : s(st) {}
   ~SaScratch() {
-    for (auto* b : {&key[0], &key[1], &val[0], &val[1], &rank, &g, &counts, &scan_tmp, &err, &small}) b->release(s);
+    for (auto* b : {&key[0], &key[1], &val[0], &val[1], &rank, &sa, &act[0], &act[1], &g, &first, &counts,
+                    &scan_tmp, &err, &small})
+      b->release(s);
   }
 };
 
@@ -248,26 +299,46 @@ static int radix_sort(SaScratch& x, uint64_t n, int lo, int hi, int& cur) {
   return WTG_OK;
 }
 
-// distinct keys of the sorted pairs; fills rank[] for every suffix
-static int assign_ranks(SaScratch& x, uint64_t n, int cur, uint64_t* groups) {
-  const unsigned grid = grid_for(n + 1);
-  run_flags_kernel<<<grid, 256, 0, x.s>>>(x.key[cur].as<uint64_t>(), n, x.g.as<uint32_t>());
-  count_launch();
-  WTG_CK(cudaGetLastError());
+static int scan_u32(SaScratch& x, uint32_t* a, uint64_t m, uint32_t* total) {
   int rc;
-  if ((rc = scan_exclusive_u32(x.g.as<uint32_t>(), x.g.as<uint32_t>(), n + 1, x.scan_tmp, x.err.as<uint32_t>(), x.s)))
-    return rc;
-  ranks_kernel<<<grid, 256, 0, x.s>>>(x.key[cur].as<uint64_t>(), x.val[cur].as<uint32_t>(), x.g.as<uint32_t>(), n,
-                                      x.rank.as<uint32_t>());
-  count_launch();
-  WTG_CK(cudaGetLastError());
-  uint32_t G = 0;
-  WTG_CK(cudaMemcpyAsync(&G, x.g.as<uint32_t>() + n, sizeof(G), cudaMemcpyDeviceToHost, x.s));
+  if ((rc = scan_exclusive_u32(a, a, m + 1, x.scan_tmp, x.err.as<uint32_t>(), x.s))) return rc;
+  WTG_CK(cudaMemcpyAsync(total, a + m, sizeof(uint32_t), cudaMemcpyDeviceToHost, x.s));
   WTG_CK(cudaStreamSynchronize(x.s));
   uint32_t e = 0;
   WTG_CK(cudaMemcpy(&e, x.err.p, sizeof(e), cudaMemcpyDeviceToHost));
   if (e) return fail(WTG_ERR_TIMEOUT, "suffix array: a scan wait timed out");
-  *groups = G;
+  return WTG_OK;
+}
+
+// after a sort of the m active pairs (in key[cur] / val[cur]): place them,
+// refresh their ranks and compact the still-shared ones into act[ac ^ 1]
+static int settle_round(SaScratch& x, uint64_t m, int cur, int& ac, uint64_t* m_next) {
+  int rc;
+  const unsigned grid = grid_for(m + 1);
+  const uint64_t* key = x.key[cur].as<uint64_t>();
+  uint32_t* g = x.g.as<uint32_t>();
+  run_flags_kernel<<<grid, 256, 0, x.s>>>(key, m, g);
+  count_launch();
+  WTG_CK(cudaGetLastError());
+  uint32_t runs = 0;
+  if ((rc = scan_u32(x, g, m, &runs))) return rc;
+  run_first_kernel<<<grid, 256, 0, x.s>>>(key, g, m, x.first.as<uint32_t>());
+  count_launch();
+  WTG_CK(cudaGetLastError());
+  uint32_t* ga = x.key[cur ^ 1].as<uint32_t>();  // the other key buffer is free until the next sort
+  place_kernel<<<grid, 256, 0, x.s>>>(key, x.val[cur].as<uint32_t>(), g, x.first.as<uint32_t>(),
+                                      x.act[ac].as<uint32_t>(), m, x.sa.as<uint32_t>(), x.rank.as<uint32_t>(), ga);
+  count_launch();
+  WTG_CK(cudaGetLastError());
+  uint32_t still = 0;
+  if ((rc = scan_u32(x, ga, m, &still))) return rc;
+  if (still) {
+    compact_active_kernel<<<grid, 256, 0, x.s>>>(key, ga, x.act[ac].as<uint32_t>(), m, x.act[ac ^ 1].as<uint32_t>());
+    count_launch();
+    WTG_CK(cudaGetLastError());
+    ac ^= 1;
+  }
+  *m_next = still;
   return WTG_OK;
 }
 
@@ -279,8 +350,10 @@ int suffix_array_device(const uint8_t* d_text, uint64_t n, uint32_t* d_sa, uint8
   if (n >= (1ull << 31)) return fail(WTG_ERR_INVALID, "suffix array: n must be below 2^31 (32-bit entries)");
   SaScratch x(s);
   const uint64_t ntiles = (n + SA_TILE - 1) / SA_TILE;
-  if ((rc = x.key[0].ensure(n * 8, s)) || (rc = x.key[1].ensure(n * 8, s)) || (rc = x.val[0].ensure(n * 4, s)) ||
-      (rc = x.val[1].ensure(n * 4, s)) || (rc = x.rank.ensure(n * 4, s)) || (rc = x.g.ensure((n + 1) * 4, s)) ||
+  if ((rc = x.key[0].ensure(n * 8 + 8, s)) || (rc = x.key[1].ensure(n * 8 + 8, s)) ||
+      (rc = x.val[0].ensure(n * 4, s)) || (rc = x.val[1].ensure(n * 4, s)) || (rc = x.rank.ensure(n * 4, s)) ||
+      (rc = x.sa.ensure(n * 4, s)) || (rc = x.act[0].ensure(n * 4, s)) || (rc = x.act[1].ensure(n * 4, s)) ||
+      (rc = x.g.ensure((n + 1) * 4, s)) || (rc = x.first.ensure(n * 4, s)) ||
       (rc = x.counts.ensure(RADIX * ntiles * 4, s)) || (rc = x.err.ensure(4, s)) || (rc = x.small.ensure(2048, s)))
     return rc;
   WTG_CK(cudaMemsetAsync(x.err.p, 0, 4, s));
@@ -300,32 +373,36 @@ int suffix_array_device(const uint8_t* d_text, uint64_t n, uint32_t* d_sa, uint8
   const int K = 64 / b;
   uint16_t* d_code = (uint16_t*)(x.small.as<uint32_t>() + 256);
   WTG_CK(cudaMemcpyAsync(d_code, code, sizeof(code), cudaMemcpyHostToDevice, s));
+  // round 0: every suffix, keyed by its first K codes
   init_keys_kernel<<<grid_for(n), 256, 0, s>>>(d_text, n, d_code, b, K, x.key[0].as<uint64_t>(),
                                                x.val[0].as<uint32_t>());
   count_launch();
+  iota_kernel<<<grid_for(n), 256, 0, s>>>(x.act[0].as<uint32_t>(), n);
+  count_launch();
   WTG_CK(cudaGetLastError());
-  int cur = 0;
+  int cur = 0, ac = 0;
   if ((rc = radix_sort(x, n, (64 - b * K) / RBITS * RBITS, 64, cur))) return rc;
-  uint64_t groups = 0;
-  if ((rc = assign_ranks(x, n, cur, &groups))) return rc;
+  uint64_t m = 0;
+  if ((rc = settle_round(x, n, cur, ac, &m))) return rc;
   uint64_t h = (uint64_t)K;
   int r = 0;
-  const int B = bit_width64(n);  // rank[i + h] + 1 <= n
-  while (groups < n) {
-    double_keys_kernel<<<grid_for(n), 256, 0, s>>>(x.rank.as<uint32_t>(), n, h, B, x.key[cur].as<uint64_t>(),
+  const int B = bit_width64(n);               // rank[i + h] + 1 <= n
+  const int hi = B + bit_width64(n - 1);      // rank < n
+  while (m) {
+    active_keys_kernel<<<grid_for(m), 256, 0, s>>>(x.act[ac].as<uint32_t>(), x.sa.as<uint32_t>(),
+                                                   x.rank.as<uint32_t>(), m, n, h, B, x.key[cur].as<uint64_t>(),
                                                    x.val[cur].as<uint32_t>());
     count_launch();
     WTG_CK(cudaGetLastError());
-    const int hi = B + bit_width64(groups - 1);
-    if ((rc = radix_sort(x, n, 0, hi, cur))) return rc;
-    if ((rc = assign_ranks(x, n, cur, &groups))) return rc;
+    if ((rc = radix_sort(x, m, 0, hi, cur))) return rc;
+    if ((rc = settle_round(x, m, cur, ac, &m))) return rc;
     h *= 2;
     ++r;
   }
   if (rounds) *rounds = r;
-  if (d_sa) WTG_CK(cudaMemcpyAsync(d_sa, x.val[cur].p, n * 4, cudaMemcpyDeviceToDevice, s));
+  if (d_sa) WTG_CK(cudaMemcpyAsync(d_sa, x.sa.p, n * 4, cudaMemcpyDeviceToDevice, s));
   if (d_bwt) {
-    bwt_kernel<<<grid_for(n), 256, 0, s>>>(d_text, x.val[cur].as<uint32_t>(), n, d_bwt);
+    bwt_kernel<<<grid_for(n), 256, 0, s>>>(d_text, x.sa.as<uint32_t>(), n, d_bwt);
     count_launch();
     WTG_CK(cudaGetLastError());
   }
