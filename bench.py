@@ -581,30 +581,14 @@ def run_wtg(args, rank, world, local_rank):
     roofline["frac"] = roofline["achieved"] / peak
     kernel_share = {k: {"launches": v[0], "ms": v[1]} for k, v in prof.items()}
 
-    select = queries = batch = None
-    if not args.no_select:
-        select = measure_select(torch, wtg, tree, n, L, dev, stream, args.select_log2)
-        queries = measure_queries(torch, tree, seq, n, dev, stream, args.select_log2)
-    if args.batch_texts:
-        batch = measure_batch(torch, wtg, stream, args.batch_texts)
-    fm = None
-    if args.fm_log2:
-        orc = None
-        if not args.no_cpu:
-            from oracle import oracle as orc
-            orc.build(ref=False)
-        fm = measure_fm(torch, wtg, orc, dev, args.fm_log2, args.fm_queries_log2, args.fm_cpu_log2)
-
-    # ---- e2e: host API with pinned host buffers, outputs copied back
+    # ---- e2e: host API with pinned host buffers, outputs copied back (run
+    # before the other sections, so that the pinned buffers are placed as
+    # in a fresh process)
     e2e = None
     if not args.no_e2e:
         import ctypes
         host_in = torch.empty(n, dtype=torch.int32, pin_memory=True)
         host_in.copy_(seq)
-        del seq
-        torch.cuda.empty_cache()
-        tree.free()
-        tree = None
         h = ctypes.c_void_p()
         L_ = wtg.lib()
         wtg._ck(L_.wtg_tree_build(ctypes.c_void_p(host_in.data_ptr()), n, 4, L, wtg.ALL, ctypes.byref(h)))
@@ -643,6 +627,20 @@ def run_wtg(args, rank, world, local_rank):
         e2e = {"value": job_throughput(world, e_steps, step_bytes, e_s), "unit": "GB/s",
                "h2d_bytes_per_step": 4 * n, "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e_s / e_steps}
         t_e.free()
+
+    select = queries = batch = None
+    if not args.no_select:
+        select = measure_select(torch, wtg, tree, n, L, dev, stream, args.select_log2)
+        queries = measure_queries(torch, tree, seq, n, dev, stream, args.select_log2)
+    if args.batch_texts:
+        batch = measure_batch(torch, wtg, stream, args.batch_texts)
+    fm = None
+    if args.fm_log2:
+        orc = None
+        if not args.no_cpu:
+            from oracle import oracle as orc
+            orc.build(ref=False)
+        fm = measure_fm(torch, wtg, orc, dev, args.fm_log2, args.fm_queries_log2, args.fm_cpu_log2)
 
     if rank != 0:
         if dist:
