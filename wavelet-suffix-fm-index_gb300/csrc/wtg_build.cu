@@ -340,7 +340,7 @@ __device__ __forceinline__ uint32_t prefix_of(T x, int s, uint32_t mask) {
 // most two destination chunks, so emission is per-lane counting and four
 // atomics per chunk.  Other chunks take a compact general path.
 template <typename T, bool SCATTER, bool EMIT_NODES, bool EMIT_TILES>
-__global__ void __launch_bounds__(LV_THREADS, 4)
+__global__ void __launch_bounds__(LV_THREADS, 3)
     level_kernel(const T* __restrict__ src, T* __restrict__ dst, uint64_t n, int L, int level,
                  const uint2* __restrict__ base_lvl, uint32_t* __restrict__ bits32, uint64_t bit_off,
                  const uint32_t* __restrict__ chunkpre, uint32_t* __restrict__ chunkcnt_next,
