@@ -151,33 +151,60 @@ __device__ void batch_text(const BatchArgs& a, uint64_t t, BatchSmem<THREADS>& s
   const uint8_t* __restrict__ in = a.sym + a.so[t];
   uint64_t* __restrict__ bits = a.bits + a.bo[t];
 
-  // ---- H: histogram and run starts
+  // ---- H: histogram and run starts.  The order of the symbols does not
+  // matter here, so each thread reads 16 at a time and counts the low-L-bit
+  // values of a 32-bit word bit-sliced (L <= 2) or bytewise (L = 3, 4);
+  // bin 0 is what remains.
   if (tid < (1u << BATCH_LMAX)) sm.hist[tid] = 0;
   __syncthreads();
   {
     uint32_t c[1 << BATCH_LMAX];
 #pragma unroll
     for (int b = 0; b < (1 << BATCH_LMAX); ++b) c[b] = 0;
-    // 8 rows of 32 symbols per warp step, all loads issued before the counting
-    constexpr int HR = 8;
-    for (uint64_t i0 = (uint64_t)warp * 32 * HR; i0 < n; i0 += (uint64_t)THREADS * HR) {
-      uint32_t v[HR];
+    const uint32_t bmask = vmask * 0x01010101u;
+    auto count_word = [&](uint32_t w) {  // four symbols
+      const uint32_t x = w & bmask;
+      if (L == 1) {
+        c[1] += __popc(x);
+      } else if (L == 2) {
+        const uint32_t lo = x & 0x01010101u, hi = (x >> 1) & 0x01010101u, both = __popc(lo & hi);
+        c[1] += __popc(lo) - both;
+        c[2] += __popc(hi) - both;
+        c[3] += both;
+      } else {
 #pragma unroll
-      for (int r = 0; r < HR; ++r) {
-        const uint64_t i = i0 + 32 * r + lane;
-        v[r] = i < n ? (in[i] & vmask) : BATCH_INVALID;
+        for (int b = 1; b < (1 << BATCH_LMAX); ++b)
+          if ((uint32_t)b < nbin) c[b] += __popc(__vcmpeq4(x, (uint32_t)b * 0x01010101u)) >> 3;
       }
-#pragma unroll
-      for (int r = 0; r < HR; ++r)
-#pragma unroll
-        for (int b = 0; b < (1 << BATCH_LMAX); ++b)
-          if ((uint32_t)b < nbin) c[b] += __popc(__ballot_sync(0xffffffffu, v[r] == (uint32_t)b));
+    };
+    const uint64_t head = min(n, (uint64_t)((16u - ((uintptr_t)in & 15u)) & 15u));  // bytes before a 16-byte boundary
+    const uint64_t nvec = (n - head) / 16;
+    const uint64_t rest = head + nvec * 16;
+    if (tid < head) count_word(in[tid]);
+    if (tid < n - rest) count_word(in[rest + tid]);
+    const uint4* vin = reinterpret_cast<const uint4*>(in + head);
+    uint64_t q = tid;
+    for (; q + THREADS < nvec; q += 2 * THREADS) {
+      const uint4 u = __ldg(vin + q), v = __ldg(vin + q + THREADS);
+      count_word(u.x); count_word(u.y); count_word(u.z); count_word(u.w);
+      count_word(v.x); count_word(v.y); count_word(v.z); count_word(v.w);
     }
-    if (lane == 0) {
-#pragma unroll
-      for (int b = 0; b < (1 << BATCH_LMAX); ++b)
-        if ((uint32_t)b < nbin && c[b]) atomicAdd(&sm.hist[b], c[b]);
+    if (q < nvec) {
+      const uint4 u = __ldg(vin + q);
+      count_word(u.x); count_word(u.y); count_word(u.z); count_word(u.w);
     }
+#pragma unroll
+    for (int b = 1; b < (1 << BATCH_LMAX); ++b) {
+      if ((uint32_t)b >= nbin) continue;
+      const uint32_t t = __reduce_add_sync(0xffffffffu, c[b]);
+      if (lane == 0 && t) atomicAdd(&sm.hist[b], t);
+    }
+  }
+  __syncthreads();
+  if (tid == 0) {
+    uint64_t others = 0;
+    for (uint32_t b = 1; b < nbin; ++b) others += sm.hist[b];
+    sm.hist[0] = (uint32_t)(n - others);
   }
   __syncthreads();
   if (tid < (uint32_t)nslot) {
