@@ -140,6 +140,127 @@ __device__ __forceinline__ uint64_t batch_select_by_rank(int t_b, const uint64_t
   return 0;
 }
 
+// Run of (level l, key k) in a row: the valid lanes whose symbol's bits
+// above level l spell k (planes P[j] = ballot of bit j, V = valid lanes)
+template <int LL>
+__device__ __forceinline__ uint32_t batch_run_mask(const uint32_t* P, uint32_t V, int l, uint32_t k) {
+  uint32_t m = V;
+#pragma unroll
+  for (int j = LL - 1; j >= 0; --j)
+    if (j >= LL - l) m &= ((k >> (j - (LL - l))) & 1u) ? P[j] : ~P[j];
+  return m;
+}
+
+// The level bits of one text: every (level, key) run is one contiguous bit
+// range of its level, so per chunk of THREADS * IPT symbols a warp counts
+// its rows' members of every run (one ballot per bit plane and row; run
+// masks from logic ops), the block places the warps' pieces, and each warp
+// appends its pieces: level 0's run is the valid lanes, a prefix of the row,
+// so its bits are the plane itself; deeper runs compact the plane to the
+// run with one OR-reduction of 1 << rank.  All runs are carried through the
+// rows together, their words written whole or, at a run's first and last
+// word (shared with the neighbouring pieces), ORed.
+template <int THREADS, int IPT, int LL>
+__device__ void batch_write_bits(const uint8_t* __restrict__ in, uint64_t n, uint64_t* __restrict__ bits,
+                                 BatchSmem<THREADS>& sm) {
+  constexpr int NW = THREADS / 32;
+  constexpr int NS = (1 << LL) - 1;  // runs: (level, key) slots
+  constexpr uint64_t CH = (uint64_t)THREADS * IPT;
+  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t vmask = (1u << LL) - 1, lt = (1u << lane) - 1;
+  for (uint64_t c0 = 0; c0 < n; c0 += CH) {
+    const uint64_t s0 = c0 + (uint64_t)warp * 32 * IPT;
+    uint32_t v[IPT];
+#pragma unroll
+    for (int r = 0; r < IPT; ++r) {
+      const uint64_t i = s0 + 32 * r + lane;
+      v[r] = i < n ? (in[i] & vmask) : BATCH_INVALID;
+    }
+    uint32_t cnt[NS];
+#pragma unroll
+    for (int q = 0; q < NS; ++q) cnt[q] = 0;
+#pragma unroll
+    for (int r = 0; r < IPT; ++r) {
+      const bool valid = v[r] != BATCH_INVALID;
+      uint32_t P[LL];
+#pragma unroll
+      for (int j = 0; j < LL; ++j) P[j] = __ballot_sync(0xffffffffu, valid && ((v[r] >> j) & 1u));
+      const uint32_t V = __ballot_sync(0xffffffffu, valid);
+#pragma unroll
+      for (int l = 0, q = 0; l < LL; ++l)
+#pragma unroll
+        for (uint32_t k = 0; k < (1u << l); ++k, ++q) cnt[q] += __popc(batch_run_mask<LL>(P, V, l, k));
+    }
+    if (lane == 0) {
+#pragma unroll
+      for (int q = 0; q < NS; ++q) sm.cnt[warp][q] = cnt[q];
+    }
+    __syncthreads();
+    if (tid < (uint32_t)NS) {
+      uint64_t run = sm.carry[tid];
+      for (int w = 0; w < NW; ++w) {
+        sm.start[w][tid] = run;
+        run += sm.cnt[w][tid];
+      }
+      sm.carry[tid] = run;
+    }
+    __syncthreads();
+    uint64_t acc[NS], word[NS];
+    uint32_t fill[NS];
+    bool shared_word[NS];
+#pragma unroll
+    for (int q = 0; q < NS; ++q) {
+      const uint64_t dest = sm.base[q] + sm.start[warp][q];
+      word[q] = dest >> 6;
+      fill[q] = (uint32_t)(dest & 63);
+      shared_word[q] = fill[q] != 0;  // the first word may hold the previous piece's tail
+      acc[q] = 0;
+    }
+#pragma unroll
+    for (int r = 0; r < IPT; ++r) {
+      const bool valid = v[r] != BATCH_INVALID;
+      uint32_t P[LL];
+#pragma unroll
+      for (int j = 0; j < LL; ++j) P[j] = __ballot_sync(0xffffffffu, valid && ((v[r] >> j) & 1u));
+      const uint32_t V = __ballot_sync(0xffffffffu, valid);
+#pragma unroll
+      for (int l = 0, q = 0; l < LL; ++l) {
+        const int bs = LL - 1 - l;
+#pragma unroll
+        for (uint32_t k = 0; k < (1u << l); ++k, ++q) {
+          const uint32_t m = batch_run_mask<LL>(P, V, l, k);
+          const uint32_t cm = __popc(m);
+          if (cm == 0) continue;
+          uint32_t comp;
+          if (l == 0) {
+            comp = P[bs] & V;  // the run is the valid lanes, a prefix of the row
+          } else {
+            const uint32_t one = ((m & P[bs]) >> lane) & 1u ? (1u << __popc(m & lt)) : 0u;
+            comp = __reduce_or_sync(0xffffffffu, one);
+          }
+          acc[q] |= (uint64_t)comp << fill[q];
+          if (fill[q] + cm >= 64) {
+            if (lane == 0 && acc[q]) {
+              if (shared_word[q]) atomicOr((unsigned long long*)&bits[word[q]], (unsigned long long)acc[q]);
+              else bits[word[q]] = acc[q];
+            }
+            acc[q] = fill[q] ? ((uint64_t)comp >> (64 - fill[q])) : 0;
+            fill[q] = fill[q] + cm - 64;
+            ++word[q];
+            shared_word[q] = false;
+          } else {
+            fill[q] += cm;
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < NS; ++q)
+      if (lane == 0 && fill[q] && acc[q]) atomicOr((unsigned long long*)&bits[word[q]], (unsigned long long)acc[q]);
+    __syncthreads();
+  }
+}
+
 template <int THREADS, int IPT>
 __device__ void batch_text(const BatchArgs& a, uint64_t t, BatchSmem<THREADS>& sm) {
   constexpr int NW = THREADS / 32;
@@ -219,71 +340,12 @@ __device__ void batch_text(const BatchArgs& a, uint64_t t, BatchSmem<THREADS>& s
   }
   __syncthreads();
 
-  // ---- W: level bits
-  constexpr uint64_t CH = (uint64_t)THREADS * IPT;
-  for (uint64_t c0 = 0; c0 < n; c0 += CH) {
-    const uint64_t s0 = c0 + (uint64_t)warp * 32 * IPT;
-    uint32_t v[IPT];
-#pragma unroll
-    for (int r = 0; r < IPT; ++r) {
-      const uint64_t i = s0 + 32 * r + lane;
-      v[r] = i < n ? (in[i] & vmask) : BATCH_INVALID;
-    }
-    for (int l = 0, slot = 0; l < L; ++l) {
-      const int sh = L - l;
-      for (uint32_t k = 0; k < (1u << l); ++k, ++slot) {
-        uint32_t cnt = 0;
-#pragma unroll
-        for (int r = 0; r < IPT; ++r)
-          cnt += __popc(__ballot_sync(0xffffffffu, v[r] != BATCH_INVALID && (v[r] >> sh) == k));
-        if (lane == 0) sm.cnt[warp][slot] = cnt;
-      }
-    }
-    __syncthreads();
-    if (tid < (uint32_t)nslot) {
-      uint64_t run = sm.carry[tid];
-      for (int w = 0; w < NW; ++w) {
-        sm.start[w][tid] = run;
-        run += sm.cnt[w][tid];
-      }
-      sm.carry[tid] = run;
-    }
-    __syncthreads();
-    const uint32_t lt = (1u << lane) - 1;
-    for (int l = 0, slot = 0; l < L; ++l) {
-      const int sh = L - l, bs = L - 1 - l;
-      for (uint32_t k = 0; k < (1u << l); ++k, ++slot) {
-        const uint64_t dest = sm.base[slot] + sm.start[warp][slot];
-        uint64_t word = dest >> 6;
-        uint32_t fill = (uint32_t)(dest & 63);
-        bool shared_word = fill != 0;  // the first word may hold the previous run's tail
-        uint64_t acc = 0;
-#pragma unroll
-        for (int r = 0; r < IPT; ++r) {
-          const bool in_run = v[r] != BATCH_INVALID && (v[r] >> sh) == k;
-          const uint32_t m = __ballot_sync(0xffffffffu, in_run);
-          const uint32_t one = (in_run && ((v[r] >> bs) & 1)) ? (1u << __popc(m & lt)) : 0u;
-          const uint32_t comp = __reduce_or_sync(0xffffffffu, one);
-          const uint32_t cnt = __popc(m);
-          if (cnt == 0) continue;
-          acc |= (uint64_t)comp << fill;
-          if (fill + cnt >= 64) {
-            if (lane == 0 && acc) {
-              if (shared_word) atomicOr((unsigned long long*)&bits[word], (unsigned long long)acc);
-              else bits[word] = acc;
-            }
-            acc = fill ? ((uint64_t)comp >> (64 - fill)) : 0;
-            fill = fill + cnt - 64;
-            ++word;
-            shared_word = false;
-          } else {
-            fill += cnt;
-          }
-        }
-        if (lane == 0 && fill && acc) atomicOr((unsigned long long*)&bits[word], (unsigned long long)acc);
-      }
-    }
-    __syncthreads();
+  // ---- W: level bits (batch_write_bits, compiled per level count)
+  switch (L) {
+    case 1: batch_write_bits<THREADS, IPT, 1>(in, n, bits, sm); break;
+    case 2: batch_write_bits<THREADS, IPT, 2>(in, n, bits, sm); break;
+    case 3: batch_write_bits<THREADS, IPT, 3>(in, n, bits, sm); break;
+    default: batch_write_bits<THREADS, IPT, 4>(in, n, bits, sm); break;
   }
   __syncthreads();
 
