@@ -39,6 +39,7 @@ namespace wtg {
 constexpr int BATCH_LMAX = 4;
 constexpr int BATCH_SLOTS = (1 << BATCH_LMAX) - 1;  // (level, key) pairs
 constexpr uint32_t BATCH_INVALID = 0xFFFFFFFFu;
+constexpr int BATCH_MAX_CHUNK = 8192;  // THREADS * IPT of every launch shape
 
 struct BatchArgs {
   const uint8_t* sym;     // concatenated texts
@@ -80,6 +81,10 @@ struct BatchSmem {
   unsigned long long last[2];
   uint32_t nlong;
   uint64_t ent[NW][64];
+  // phase W: two staging buffers for chunks of up to BATCH_MAX_CHUNK symbols
+  // (plus the text's offset from a 16-byte boundary), filled by cp.async.bulk
+  alignas(16) uint8_t stage[2][BATCH_MAX_CHUNK + 32];
+  alignas(8) uint64_t bar[2];
 };
 
 __device__ __forceinline__ uint64_t batch_logn(uint64_t size) {
@@ -162,19 +167,37 @@ __device__ __forceinline__ uint32_t batch_run_mask(const uint32_t* P, uint32_t V
 // word (shared with the neighbouring pieces), ORed.
 template <int THREADS, int IPT, int LL>
 __device__ void batch_write_bits(const uint8_t* __restrict__ in, uint64_t n, uint64_t* __restrict__ bits,
-                                 BatchSmem<THREADS>& sm) {
+                                 BatchSmem<THREADS>& sm, uint32_t& phases, uint32_t* err) {
   constexpr int NW = THREADS / 32;
   constexpr int NS = (1 << LL) - 1;  // runs: (level, key) slots
   constexpr uint64_t CH = (uint64_t)THREADS * IPT;
+  static_assert(CH <= BATCH_MAX_CHUNK, "chunk larger than the staging buffers");
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t vmask = (1u << LL) - 1, lt = (1u << lane) - 1;
-  for (uint64_t c0 = 0; c0 < n; c0 += CH) {
+  // chunks are staged by thread 0 one ahead: from the 16-byte boundary at
+  // or below the chunk (the input has 16 bytes of padding after the last
+  // text, so the rounded-up tail stays inside it)
+  const uint32_t off = (uint32_t)((uintptr_t)in & 15u);
+  auto stage_chunk = [&](uint64_t c, int buf) {
+    const uint64_t cnt = min(CH, n - c);
+    const uint32_t bytes = (uint32_t)((off + cnt + 15) & ~15ull);
+    fence_proxy_async_smem();
+    mbar_expect_tx(&sm.bar[buf], bytes);
+    bulk_g2s(sm.stage[buf], in + c - off, bytes, &sm.bar[buf]);
+  };
+  int cur = 0;
+  if (tid == 0 && n) stage_chunk(0, 0);
+  for (uint64_t c0 = 0; c0 < n; c0 += CH, cur ^= 1) {
+    if (tid == 0 && c0 + CH < n) stage_chunk(c0 + CH, cur ^ 1);  // its last readers passed the previous barrier
+    mbar_wait(&sm.bar[cur], (phases >> cur) & 1u, err);
+    phases ^= 1u << cur;
+    const uint8_t* const st = sm.stage[cur] + off;
     const uint64_t s0 = c0 + (uint64_t)warp * 32 * IPT;
     uint32_t v[IPT];
 #pragma unroll
     for (int r = 0; r < IPT; ++r) {
       const uint64_t i = s0 + 32 * r + lane;
-      v[r] = i < n ? (in[i] & vmask) : BATCH_INVALID;
+      v[r] = i < n ? (st[i - c0] & vmask) : BATCH_INVALID;
     }
     uint32_t cnt[NS];
 #pragma unroll
@@ -208,6 +231,7 @@ __device__ void batch_write_bits(const uint8_t* __restrict__ in, uint64_t n, uin
     uint64_t acc[NS], word[NS];
     uint32_t fill[NS];
     bool shared_word[NS];
+    const uint64_t lvl0_dest = sm.base[0] + sm.start[warp][0];
 #pragma unroll
     for (int q = 0; q < NS; ++q) {
       const uint64_t dest = sm.base[q] + sm.start[warp][q];
@@ -233,7 +257,16 @@ __device__ void batch_write_bits(const uint8_t* __restrict__ in, uint64_t n, uin
           if (cm == 0) continue;
           uint32_t comp;
           if (l == 0) {
-            comp = P[bs] & V;  // the run is the valid lanes, a prefix of the row
+            // level 0 holds every symbol in order: row r of this warp is the
+            // 32-bit word (dest >> 5) + r (dest = its first bit, a multiple
+            // of 32); a partial row shares its word with level 1's first bits
+            comp = P[bs] & V;
+            if (lane == 0) {
+              uint32_t* const w32 = reinterpret_cast<uint32_t*>(bits) + (lvl0_dest >> 5) + r;
+              if (V == 0xffffffffu) *w32 = comp;
+              else if (comp) atomicOr(w32, comp);
+            }
+            continue;
           } else {
             const uint32_t one = ((m & P[bs]) >> lane) & 1u ? (1u << __popc(m & lt)) : 0u;
             comp = __reduce_or_sync(0xffffffffu, one);
@@ -262,7 +295,7 @@ __device__ void batch_write_bits(const uint8_t* __restrict__ in, uint64_t n, uin
 }
 
 template <int THREADS, int IPT>
-__device__ void batch_text(const BatchArgs& a, uint64_t t, BatchSmem<THREADS>& sm) {
+__device__ void batch_text(const BatchArgs& a, uint64_t t, BatchSmem<THREADS>& sm, uint32_t& phases) {
   constexpr int NW = THREADS / 32;
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int L = a.L;
@@ -342,10 +375,10 @@ __device__ void batch_text(const BatchArgs& a, uint64_t t, BatchSmem<THREADS>& s
 
   // ---- W: level bits (batch_write_bits, compiled per level count)
   switch (L) {
-    case 1: batch_write_bits<THREADS, IPT, 1>(in, n, bits, sm); break;
-    case 2: batch_write_bits<THREADS, IPT, 2>(in, n, bits, sm); break;
-    case 3: batch_write_bits<THREADS, IPT, 3>(in, n, bits, sm); break;
-    default: batch_write_bits<THREADS, IPT, 4>(in, n, bits, sm); break;
+    case 1: batch_write_bits<THREADS, IPT, 1>(in, n, bits, sm, phases, a.err); break;
+    case 2: batch_write_bits<THREADS, IPT, 2>(in, n, bits, sm, phases, a.err); break;
+    case 3: batch_write_bits<THREADS, IPT, 3>(in, n, bits, sm, phases, a.err); break;
+    default: batch_write_bits<THREADS, IPT, 4>(in, n, bits, sm, phases, a.err); break;
   }
   __syncthreads();
 
@@ -528,13 +561,20 @@ __device__ void batch_text(const BatchArgs& a, uint64_t t, BatchSmem<THREADS>& s
 template <int THREADS, int IPT>
 __global__ void __launch_bounds__(THREADS, 2048 / THREADS / 2) batch_build_kernel(BatchArgs a) {
   __shared__ BatchSmem<THREADS> sm;
+  if (threadIdx.x == 0) {
+    mbar_init(&sm.bar[0], 1);
+    mbar_init(&sm.bar[1], 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  uint32_t phases = 0;  // bit b: parity of staging buffer b's next completion
   for (;;) {
     if (threadIdx.x == 0) sm.item = atomicAdd(a.queue, 1u);
     __syncthreads();
     const uint32_t item = sm.item;
     __syncthreads();
     if (item >= a.T) break;
-    batch_text<THREADS, IPT>(a, a.order[item], sm);
+    batch_text<THREADS, IPT>(a, a.order[item], sm, phases);
     __syncthreads();
   }
 }
