@@ -309,12 +309,7 @@ __device__ __forceinline__ void slot2_flush(Slot2& s, uint32_t* __restrict__ tar
   s = Slot2();
 }
 
-// 32-bit shifts for symbols of up to 4 bytes, 64-bit otherwise
-template <typename T>
-__device__ __forceinline__ uint32_t bit_of(T x, int s) {
-  if constexpr (sizeof(T) <= 4) return ((uint32_t)x >> s) & 1u;
-  else return (uint32_t)((uint64_t)x >> s) & 1u;
-}
+// node of a symbol: 32-bit shifts for symbols of up to 4 bytes, 64-bit otherwise
 template <typename T>
 __device__ __forceinline__ uint32_t prefix_of(T x, int s, uint32_t mask) {
   if constexpr (sizeof(T) <= 4) return (s >= 32 ? 0u : ((uint32_t)x >> s)) & mask;
@@ -351,19 +346,19 @@ __global__ void __launch_bounds__(LV_THREADS, 3)
   constexpr int LV_STAGES = lv_stages<SCATTER>();
   extern __shared__ __align__(128) unsigned char lv_smem[];
   __shared__ __align__(8) uint64_t mbar[LV_THREADS / 32][LV_STAGES];
-  __shared__ uint32_t s_words[LV_THREADS / 32][WROWS];
-  __shared__ uint32_t s_nz[LV_THREADS / 32][EMIT_TILES ? WROWS : 1];  // rows' next-level zero masks
+  __shared__ uint2 s_rows[LV_THREADS / 32][WROWS];  // per row: its bits, its next-level zero mask
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   T* const wring = (T*)(lv_smem + warp * LV_STAGES * GBYTES);  // this warp's LV_STAGES group buffers
   uint64_t* const bars = mbar[warp];
-  uint32_t* const myw = s_words[warp];
-  uint32_t* const mynz = s_nz[warp];
+  uint2* const myrow = s_rows[warp];
   const uint64_t nchunks = (n + CHUNK - 1) / CHUNK;
   const uint64_t ngroups = (nchunks + CPB - 1) / CPB;
   const uint64_t nfullg = bulk_ok ? n / (CHUNK * CPB) : 0;  // groups fetched with bulk copies
   const uint64_t stride = (uint64_t)gridDim.x * (LV_THREADS / 32);
   const uint64_t g0 = (uint64_t)blockIdx.x * (LV_THREADS / 32) + warp;
   const int shift = L - 1 - level;
+  // L <= 24: the bits a pass tests lie in the low 32 bits of every symbol
+  const uint32_t m1 = 1u << shift, mnext = m1 >> 1;
   const int pshift = L - level;
   const uint32_t pmask = level ? (uint32_t)((1ull << level) - 1) : 0u;
   const uint32_t ltmask = lanemask_lt();
@@ -433,8 +428,8 @@ __global__ void __launch_bounds__(LV_THREADS, 3)
       for (int r = 0; r < WROWS; ++r) {
         const uint32_t k = r * 32 + lane;
         const bool valid = k < cvalid;
-        const uint32_t om = __ballot_sync(0xffffffffu, valid && bit_of(wt[k], shift));
-        myw[r] = om;  // every lane stores the same word: no branch
+        const uint32_t om = __ballot_sync(0xffffffffu, valid && ((uint32_t)wt[k] & m1));
+        myrow[r].x = om;  // every lane stores the same word: no branch
         zc += __popc(__ballot_sync(0xffffffffu, valid) & ~om);
       }
       if (chunkcnt_self && lane == 0) chunkcnt_self[c] = zc;
@@ -457,9 +452,8 @@ __global__ void __launch_bounds__(LV_THREADS, 3)
 #pragma unroll
         for (int r = 0; r < WROWS; ++r) {
           const T x = wt[r * 32 + lane];
-          const uint32_t one = bit_of(x, shift);
+          const bool one = (uint32_t)x & m1;
           const uint32_t om = __ballot_sync(0xffffffffu, one);
-          myw[r] = om;  // every lane stores the same word: no branch
           const uint32_t zb = z + __popc(~om & ltmask);  // zeros before x (level-wide)
           z += 32u - __popc(om);
           const uint32_t d = one ? ybase + 32u * r - zb : b.x + zb;
@@ -470,10 +464,9 @@ __global__ void __launch_bounds__(LV_THREADS, 3)
           } else {
             dst[d] = x;
           }
-          if (EMIT_TILES) {
-            const uint32_t nzm = __ballot_sync(0xffffffffu, !bit_of(x, shift - 1));  // next-level bit is 0
-            mynz[r] = nzm;
-          }
+          // every lane stores the same words: no branch
+          if (EMIT_TILES) myrow[r] = make_uint2(om, __ballot_sync(0xffffffffu, !((uint32_t)x & mnext)));
+          else myrow[r].x = om;
         }
       };
       if (in_range) rows(std::false_type{});
@@ -488,7 +481,8 @@ __global__ void __launch_bounds__(LV_THREADS, 3)
         const uint32_t olim = ((b.y + ob0 + CHUNK) & ~(uint32_t)(CHUNK - 1)) - b.y;
         __syncwarp();
         const bool row = lane < (uint32_t)WROWS;
-        const uint32_t omr = row ? myw[lane] : 0u, nzm = row ? mynz[lane] : 0u;
+        const uint2 rw = row ? myrow[lane] : make_uint2(0u, 0u);
+        const uint32_t omr = rw.x, nzm = rw.y;
         const uint32_t zmr = row ? ~omr : 0u;
         const uint32_t zc = __popc(zmr), oc = __popc(omr);
         uint32_t zpre = zc;
@@ -536,10 +530,10 @@ __global__ void __launch_bounds__(LV_THREADS, 3)
         const uint32_t k = r * 32 + lane;
         const bool valid = k < cvalid;
         const T x = wt[k];
-        const bool one = valid && bit_of(x, shift);
+        const bool one = valid && ((uint32_t)x & m1);
         const uint32_t om = __ballot_sync(0xffffffffu, one);
         const uint32_t zm = __ballot_sync(0xffffffffu, valid && !one);
-        myw[r] = om;  // every lane stores the same word: no branch
+        myrow[r].x = om;  // every lane stores the same word: no branch
         const uint32_t zb = z + __popc(zm & ltmask);
         z += __popc(zm);
         const uint32_t p = prefix_of(x, pshift, pmask);
@@ -559,7 +553,7 @@ __global__ void __launch_bounds__(LV_THREADS, 3)
         if (ok) dst[d] = x;
         bad |= valid && !ok;
         if (EMIT_TILES) {
-          const bool nb0 = ok && !bit_of(x, shift - 1);
+          const bool nb0 = ok && !((uint32_t)x & mnext);
           slot2_count(tiles_s, nb0, d >> LOG_CHUNK, chunkcnt_next, lane);
           if (EMIT_NODES) slot2_count(nodes_s, nb0, 2 * p + (one ? 1u : 0u), znext, lane);
         }
@@ -577,8 +571,8 @@ __global__ void __launch_bounds__(LV_THREADS, 3)
     const uint32_t g0 = (uint32_t)(g & 31);
     const uint64_t G = g >> 5;
     if (lane <= (uint32_t)WROWS && !(g0 == 0 && lane == (uint32_t)WROWS)) {
-      const uint32_t curw = lane < (uint32_t)WROWS ? myw[lane] : 0u;
-      const uint32_t prev = lane ? myw[lane - 1] : 0u;
+      const uint32_t curw = lane < (uint32_t)WROWS ? myrow[lane].x : 0u;
+      const uint32_t prev = lane ? myrow[lane - 1].x : 0u;
       const uint32_t val = g0 ? ((curw << g0) | (prev >> (32 - g0))) : curw;
       const uint64_t wlo = (G + lane) * 32;
       if (wlo < g + cvalid) {
