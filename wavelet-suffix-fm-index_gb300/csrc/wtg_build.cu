@@ -394,6 +394,9 @@ __global__ void __launch_bounds__(LV_THREADS, 3)
       mbar_expect_tx(&bars[nslot], GBYTES);
       bulk_g2s(wring + nslot * CPB * CHUNK, src + nx * CPB * CHUNK, GBYTES, &bars[nslot]);
     }
+    // the group's chunk prefixes, loaded before the wait: lane j holds chunk g * CPB + j's
+    uint32_t zpre_g = 0;
+    if (SCATTER && lane < CPB && g * CPB + lane < nchunks) zpre_g = chunkpre[g * CPB + lane];
     const bool gbulk = g < nfullg;
     if (gbulk) {
       mbar_wait(&bars[slot], (phases >> slot) & 1u, err);
@@ -413,7 +416,7 @@ __global__ void __launch_bounds__(LV_THREADS, 3)
 
     const uint32_t i0 = (uint32_t)cbase;
     bool bad = false;                          // a destination outside dst (inconsistent tables)
-    uint32_t z = SCATTER ? chunkpre[c] : 0u;  // level-wide zeros before the chunk
+    uint32_t z = SCATTER ? __shfl_sync(0xffffffffu, zpre_g, j) : 0u;  // level-wide zeros before the chunk
     uint32_t p0 = 0;
     bool uniform = true;
     if (SCATTER && level) {
@@ -476,7 +479,9 @@ __global__ void __launch_bounds__(LV_THREADS, 3)
         // is 0: the chunk's zero run lands at b.x + [zs, ...) and its one run
         // at b.y + [ob0, ...), each crossing at most one destination chunk
         // boundary (zero rank zlim, one rank olim).  Lane r < WROWS counts
-        // row r from the rows' masks; one warp reduction per value.
+        // row r from the rows' masks; one warp reduction per value.  The row
+        // that holds a boundary is split with one ballot: lane j takes bit j
+        // when its rank in the run lies below the boundary.
         const uint32_t zlim = ((b.x + zs + CHUNK) & ~(uint32_t)(CHUNK - 1)) - b.x;
         const uint32_t olim = ((b.y + ob0 + CHUNK) & ~(uint32_t)(CHUNK - 1)) - b.y;
         __syncwarp();
@@ -497,20 +502,28 @@ __global__ void __launch_bounds__(LV_THREADS, 3)
         const uint32_t nzz = nzm & zmr, nzo = nzm & omr;
         uint32_t t0 = __popc(nzz), t1 = __popc(nzo);
         uint32_t a0 = zlim >= zrow + zc ? t0 : 0u, a1 = olim >= orow + oc ? t1 : 0u;
-        if (zlim > zrow && zlim < zrow + zc)
-          a0 = __popc(nzz & ((1u << sel64_0((uint64_t)zmr, zlim - zrow)) - 1u));
-        if (olim > orow && olim < orow + oc)
-          a1 = __popc(nzo & ((1u << sel64_0((uint64_t)omr, olim - orow)) - 1u));
+        const uint32_t zx = __ballot_sync(0xffffffffu, zlim > zrow && zlim < zrow + zc);
+        const uint32_t ox = __ballot_sync(0xffffffffu, olim > orow && olim < orow + oc);
         t0 = __reduce_add_sync(0xffffffffu, t0);
         t1 = __reduce_add_sync(0xffffffffu, t1);
         a0 = __reduce_add_sync(0xffffffffu, a0);
         a1 = __reduce_add_sync(0xffffffffu, a1);
+        if (zx) {
+          const int sr = __ffs(zx) - 1;
+          const uint32_t m = __shfl_sync(0xffffffffu, zmr, sr), nm = __shfl_sync(0xffffffffu, nzz, sr);
+          const uint32_t q = __shfl_sync(0xffffffffu, zlim - zrow, sr);
+          a0 += __popc(__ballot_sync(0xffffffffu, ((nm >> lane) & 1u) && __popc(m & ltmask) < q));
+        }
+        if (ox) {
+          const int sr = __ffs(ox) - 1;
+          const uint32_t m = __shfl_sync(0xffffffffu, omr, sr), nm = __shfl_sync(0xffffffffu, nzo, sr);
+          const uint32_t q = __shfl_sync(0xffffffffu, olim - orow, sr);
+          a1 += __popc(__ballot_sync(0xffffffffu, ((nm >> lane) & 1u) && __popc(m & ltmask) < q));
+        }
         const uint32_t k0 = (b.x + zs) >> LOG_CHUNK, k1 = (b.y + ob0) >> LOG_CHUNK;
-        if (lane == 0) {
-          if (a0) atomicAdd(&chunkcnt_next[k0], a0);
-          if (t0 - a0) atomicAdd(&chunkcnt_next[k0 + 1], t0 - a0);
-          if (a1) atomicAdd(&chunkcnt_next[k1], a1);
-          if (t1 - a1) atomicAdd(&chunkcnt_next[k1 + 1], t1 - a1);
+        if (lane < 4) {  // lanes 0, 1: the zero run's two destination chunks; 2, 3: the one run's
+          const uint32_t v = lane == 0 ? a0 : lane == 1 ? t0 - a0 : lane == 2 ? a1 : t1 - a1;
+          if (v) atomicAdd(&chunkcnt_next[(lane < 2 ? k0 : k1) + (lane & 1u)], v);
         }
         if (EMIT_NODES) {
           if (p0 != run_p) {
@@ -570,7 +583,9 @@ __global__ void __launch_bounds__(LV_THREADS, 3)
     const uint64_t g = bit_off + cbase;
     const uint32_t g0 = (uint32_t)(g & 31);
     const uint64_t G = g >> 5;
-    if (lane <= (uint32_t)WROWS && !(g0 == 0 && lane == (uint32_t)WROWS)) {
+    if (g0 == 0 && cvalid == CHUNK) {  // whole words of this chunk only
+      if (lane < (uint32_t)WROWS) bits32[G + lane] = myrow[lane].x;
+    } else if (lane <= (uint32_t)WROWS && !(g0 == 0 && lane == (uint32_t)WROWS)) {
       const uint32_t curw = lane < (uint32_t)WROWS ? myrow[lane].x : 0u;
       const uint32_t prev = lane ? myrow[lane - 1].x : 0u;
       const uint32_t val = g0 ? ((curw << g0) | (prev >> (32 - g0))) : curw;
