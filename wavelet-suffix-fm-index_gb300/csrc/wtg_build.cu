@@ -295,12 +295,6 @@ __device__ __forceinline__ void slot2_count(Slot2& s, bool pend, uint32_t key, u
   }
 }
 
-__device__ __forceinline__ void emit_flush(uint32_t* __restrict__ znext, uint32_t p, uint32_t ce, uint32_t co) {
-  if (p == 0xFFFFFFFFu) return;
-  if (ce) atomicAdd(&znext[2 * p], ce);
-  if (co) atomicAdd(&znext[2 * p + 1], co);
-}
-
 __device__ __forceinline__ void slot2_flush(Slot2& s, uint32_t* __restrict__ target, uint32_t lane) {
   if (lane == 0) {
     if (s.ca) atomicAdd(&target[s.ka], s.ca);
@@ -329,7 +323,13 @@ __device__ __forceinline__ uint32_t prefix_of(T x, int s, uint32_t mask) {
 //     (C - Zb, zeros + Zb) and the level-wide zero rank;
 //   * EMIT_TILES: per 512-symbol chunk of the next level, the number of its
 //     symbols whose next bit is 0 (the next pass's chunkpre input);
-//   * EMIT_NODES: per node of the next level, its left-child size.
+//   * EMIT_NODES: per node of the next level, its left-child size: a chunk
+//     inside one node p stores its two counts (for nodes 2p and 2p+1) in
+//     nc0[c], nc1[c], which the host-side scans and node_sum_kernel add up
+//     per node; a chunk across node boundaries adds its counts with atomics.
+//     (Counting with per-warp runs and atomics on the node counters put
+//     one atomic per group on the few nodes a grid stride spans at the
+//     middle levels -- a hot L2 slice that slowed those levels by a third.)
 // A full chunk inside one node (the common case) takes a lean unrolled path:
 // one base(p), its zero run and one run contiguous in dst, each touching at
 // most two destination chunks, so emission is per-lane counting and four
@@ -339,6 +339,7 @@ __global__ void __launch_bounds__(LV_THREADS, 3)
     level_kernel(const T* __restrict__ src, T* __restrict__ dst, uint64_t n, int L, int level,
                  const uint2* __restrict__ base_lvl, uint32_t* __restrict__ bits32, uint64_t bit_off,
                  const uint32_t* __restrict__ chunkpre, uint32_t* __restrict__ chunkcnt_next,
+                 uint32_t* __restrict__ nc0, uint32_t* __restrict__ nc1,
                  uint32_t* __restrict__ znext, uint32_t* err, int bulk_ok, uint32_t* __restrict__ chunkcnt_self) {
   constexpr uint32_t CBYTES = CHUNK * sizeof(T);
   constexpr uint32_t CPB = LvShape<T>::CPB;
@@ -385,7 +386,6 @@ __global__ void __launch_bounds__(LV_THREADS, 3)
   int slot = 0;
   uint32_t cache_p = 0xFFFFFFFFu;  // base(p) cache
   uint2 cache_b = make_uint2(0, 0);
-  uint32_t run_p = 0xFFFFFFFFu, run_e = 0, run_o = 0;  // EMIT_NODES run over uniform chunks
   for (uint64_t g = g0; g < ngroups; g += stride) {
     const uint64_t nx = g + (uint64_t)(LV_STAGES - 1) * stride;
     const int nslot = slot == 0 ? LV_STAGES - 1 : slot - 1;  // (slot + STAGES - 1) % STAGES
@@ -525,15 +525,7 @@ __global__ void __launch_bounds__(LV_THREADS, 3)
           const uint32_t v = lane == 0 ? a0 : lane == 1 ? t0 - a0 : lane == 2 ? a1 : t1 - a1;
           if (v) atomicAdd(&chunkcnt_next[(lane < 2 ? k0 : k1) + (lane & 1u)], v);
         }
-        if (EMIT_NODES) {
-          if (p0 != run_p) {
-            if (lane == 0) emit_flush(znext, run_p, run_e, run_o);
-            run_p = p0;
-            run_e = run_o = 0;
-          }
-          run_e += t0;
-          run_o += t1;
-        }
+        if (EMIT_NODES && lane < 2) (lane ? nc1 : nc0)[c] = lane ? t1 : t0;
       }
     } else {
       // ---- general path: a node boundary inside the chunk, or its last chunk
@@ -575,6 +567,7 @@ __global__ void __launch_bounds__(LV_THREADS, 3)
         slot2_flush(tiles_s, chunkcnt_next, lane);
         if (EMIT_NODES) slot2_flush(nodes_s, znext, lane);
       }
+      if (EMIT_NODES && lane < 2) (lane ? nc1 : nc0)[c] = 0u;  // counted by the atomics above
     }
     if (SCATTER && __any_sync(0xffffffffu, bad) && lane == 0) atomicCAS(err, 0u, (uint32_t)DERR_BAD_INDEX);
     __syncwarp();
@@ -600,7 +593,6 @@ __global__ void __launch_bounds__(LV_THREADS, 3)
   }
     slot = slot + 1 == LV_STAGES ? 0 : slot + 1;
   }
-  if (EMIT_NODES && lane == 0) emit_flush(znext, run_p, run_e, run_o);
 }
 
 // ------------------------------------------------------------------ host
@@ -639,6 +631,24 @@ static int level_grid(uint64_t n) {
   return (int)std::min<uint64_t>(tiles, (uint64_t)per_sm * sm_count());
 }
 
+// Node sizes of level l+1 from the per-chunk counts of the pass over level l:
+// the chunks lying inside node p are [ceil(C(p)/512), floor(C(p+1)/512)), and
+// the exclusive scans S0, S1 of their counts (zeros of 2p, of 2p+1) give
+// their sums as S[end] - S[begin].  The chunks across node boundaries added
+// theirs with atomics during the pass.
+__global__ void node_sum_kernel(const uint32_t* __restrict__ Cl, uint64_t cnt, uint64_t n,
+                                const uint32_t* __restrict__ S0, const uint32_t* __restrict__ S1,
+                                uint32_t* __restrict__ znext) {
+  for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < cnt; p += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t b = ((uint64_t)Cl[p] + CHUNK - 1) / CHUNK;
+    const uint64_t e = (p + 1 < cnt ? (uint64_t)Cl[p + 1] : n) / CHUNK;
+    if (e > b) {
+      znext[2 * p] += S0[e] - S0[b];
+      znext[2 * p + 1] += S1[e] - S1[b];
+    }
+  }
+}
+
 struct LevelArgs {
   const void* src;
   void* dst;
@@ -649,6 +659,7 @@ struct LevelArgs {
   uint64_t bit_off;
   const uint32_t* chunkpre;
   uint32_t* chunkcnt_next;
+  uint32_t *nc0, *nc1;  // per chunk: counts of the next level's two nodes (emit_nodes)
   uint32_t* znext;
   uint32_t* err;
   uint32_t* chunkcnt_self;
@@ -661,7 +672,7 @@ static void launch_level_v(const LevelArgs& a, cudaStream_t st) {
   const size_t shm = LvShape<T>::template smem<SC>();
   level_kernel<T, SC, EN, ET><<<level_grid<T, SC, EN, ET>(a.n), LV_THREADS, shm, st>>>(
       (const T*)a.src, (T*)a.dst, a.n, a.L, a.level, a.base_lvl, a.bits32, a.bit_off, a.chunkpre,
-      a.chunkcnt_next, a.znext, a.err, bulk_ok, a.chunkcnt_self);
+      a.chunkcnt_next, a.nc0, a.nc1, a.znext, a.err, bulk_ok, a.chunkcnt_self);
 }
 
 template <typename T>
@@ -782,6 +793,12 @@ int tree_build(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int L, uint32
     WTG_CK(cudaGetLastError());
   }
 
+  // per-chunk node counts of a pass and their scans: [nc0 | nc1 | S0 | S1]
+  if (n && L > K) {
+    if ((rc = t.nodecnt.ensure(4 * (tiles + 1) * sizeof(uint32_t), s))) return rc;
+    WTG_CK(cudaMemsetAsync(t.nodecnt.p, 0, 2 * (tiles + 1) * sizeof(uint32_t), s));
+  }
+
   // level passes; each scattering pass feeds the next level's chunk counts
   // and (from level K on) its node tables.  With n % 512 == 0 the chunk
   // counts of every level also give the rank/select pass its prefixes.
@@ -810,6 +827,8 @@ int tree_build(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int L, uint32
       a.chunkcnt_next = tilecnt + (uint64_t)(l + 1) * (tiles + 1);
       a.chunkcnt_self = (!a.scatter && rs_from_levels) ? tilecnt + (uint64_t)l * (tiles + 1) : nullptr;
       a.znext = Z + ((1ull << (l + 1)) - 1);
+      a.nc0 = a.emit_nodes ? t.nodecnt.as<uint32_t>() : nullptr;
+      a.nc1 = a.emit_nodes ? a.nc0 + (tiles + 1) : nullptr;
       a.err = d_err;
       if (a.scatter)
         if ((rc = scan_exclusive_u32(tilecnt + (uint64_t)l * (tiles + 1), tilepre, tiles, t.scan_tmp, d_err, s)))
@@ -819,6 +838,20 @@ int tree_build(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int L, uint32
       prof_end(a.scatter ? PROF_LEVEL : PROF_LEVEL_LAST, s);
       count_launch();
       WTG_CK(cudaGetLastError());
+      if (a.emit_nodes) {
+        // the in-node chunks' counts: scans, then one sum per node of level l
+        uint32_t* S0 = a.nc0 + 2 * (tiles + 1);
+        uint32_t* S1 = a.nc0 + 3 * (tiles + 1);
+        if ((rc = scan_exclusive_u32(a.nc0, S0, tiles + 1, t.scan_tmp, d_err, s))) return rc;
+        if ((rc = scan_exclusive_u32(a.nc1, S1, tiles + 1, t.scan_tmp, d_err, s))) return rc;
+        const uint64_t cnt = 1ull << l;
+        unsigned grid = (unsigned)std::min<uint64_t>((cnt + 255) / 256, 2048);
+        prof_begin(PROF_TABLES, s);
+        node_sum_kernel<<<grid, 256, 0, s>>>(C + cnt - 1, cnt, n, S0, S1, a.znext);
+        prof_end(PROF_TABLES, s);
+        count_launch();
+        WTG_CK(cudaGetLastError());
+      }
       src = a.dst;
       if (t.host_bits) {
         // words holding only bits of levels <= l are final now; the word
@@ -914,6 +947,7 @@ void tree_release(TreeImpl& t) {
   t.node_tab_ok = false;
   t.scratch.release(s);
   t.nodes.release(s);
+  t.nodecnt.release(s);
   t.qbuf.release(s);
   t.qout.release(s);
   bv_release(t.bv, s);

@@ -28,6 +28,7 @@ struct TreeImpl {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   DevBuf seq, lvl[2], bits, hist, zeros, base, status, scan_tmp, err, scratch, nodes, qbuf, qout;
+  DevBuf nodecnt;  // per chunk: the node counts of a level pass, then their scans
   BvSupport bv;
   DevBuf lvl_args;
   bool lvl_args_ok = false;
