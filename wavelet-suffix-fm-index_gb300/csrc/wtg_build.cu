@@ -631,6 +631,100 @@ static int level_grid(uint64_t n) {
   return (int)std::min<uint64_t>(tiles, (uint64_t)per_sm * sm_count());
 }
 
+// Three exclusive scans in one single-pass launch (decoupled look-back, one
+// status word array per field; warps 0-2 run the three look-backs side by
+// side): after a pass, the next level's chunk zero counts and the two
+// per-chunk node counts.  Every prefix stays below n < 2^32.
+constexpr int S3_THREADS = 256;
+constexpr int S3_IPT = 16;
+constexpr int S3_TILE = S3_THREADS * S3_IPT;
+
+__global__ void __launch_bounds__(S3_THREADS)
+    scan3_kernel(const uint32_t* __restrict__ in0, const uint32_t* __restrict__ in1,
+                 const uint32_t* __restrict__ in2, uint32_t* __restrict__ out0, uint32_t* __restrict__ out1,
+                 uint32_t* __restrict__ out2, uint64_t n, uint64_t* status, uint64_t sstride, uint32_t* counter,
+                 uint32_t* err) {
+  __shared__ uint32_t s_tile;
+  __shared__ uint32_t s_wsum[3][S3_THREADS / 32];
+  __shared__ uint32_t s_prefix[3];
+  if (threadIdx.x == 0) s_tile = atomicAdd(counter, 1u);
+  __syncthreads();
+  const uint32_t tile = s_tile;
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint64_t base = (uint64_t)tile * S3_TILE + (uint64_t)threadIdx.x * S3_IPT;
+  const uint32_t* const in[3] = {in0, in1, in2};
+  uint32_t v[3][S3_IPT], sum[3], incl[3];
+#pragma unroll
+  for (int f = 0; f < 3; ++f) {
+    sum[f] = 0;
+#pragma unroll
+    for (int k = 0; k < S3_IPT; ++k) {
+      v[f][k] = base + k < n ? in[f][base + k] : 0u;
+      sum[f] += v[f][k];
+    }
+    incl[f] = sum[f];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, incl[f], o);
+      if (lane >= (uint32_t)o) incl[f] += t;
+    }
+    if (lane == 31) s_wsum[f][warp] = incl[f];
+  }
+  __syncthreads();
+  if (warp < 3) {
+    // warp f: the scan of field f's warp sums, then its look-back
+    const uint32_t f = warp;
+    const uint32_t w = lane < S3_THREADS / 32 ? s_wsum[f][lane] : 0u;
+    uint32_t winc = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, winc, o);
+      if (lane >= (uint32_t)o) winc += t;
+    }
+    if (lane < S3_THREADS / 32) s_wsum[f][lane] = winc - w;
+    const uint32_t total = __shfl_sync(0xffffffffu, winc, S3_THREADS / 32 - 1);
+    uint64_t* st = status + f * sstride;
+    uint32_t prefix = 0;
+    if (tile == 0) {
+      if (lane == 0) lb_publish(st, tile, LB_FLAG_INC, total);
+    } else {
+      if (lane == 0) lb_publish(st, tile, LB_FLAG_AGG, total);
+      prefix = (uint32_t)lb_lookback_warp(st, tile, err);
+      if (lane == 0) lb_publish(st, tile, LB_FLAG_INC, (uint64_t)prefix + total);
+    }
+    if (lane == 0) s_prefix[f] = prefix;
+  }
+  __syncthreads();
+  uint32_t* const out[3] = {out0, out1, out2};
+#pragma unroll
+  for (int f = 0; f < 3; ++f) {
+    uint32_t run = s_prefix[f] + s_wsum[f][warp] + incl[f] - sum[f];
+#pragma unroll
+    for (int k = 0; k < S3_IPT; ++k) {
+      if (base + k < n) out[f][base + k] = run;
+      run += v[f][k];
+    }
+  }
+}
+
+static int scan3_u32(const uint32_t* in0, const uint32_t* in1, const uint32_t* in2, uint32_t* out0, uint32_t* out1,
+                     uint32_t* out2, uint64_t n, DevBuf& scratch, uint32_t* d_err, cudaStream_t s) {
+  if (n == 0) return WTG_OK;
+  const uint64_t tiles = (n + S3_TILE - 1) / S3_TILE;
+  const size_t bytes = (3 * tiles + 1) * sizeof(uint64_t);
+  int rc = scratch.ensure(bytes, s);
+  if (rc) return rc;
+  WTG_CK(cudaMemsetAsync(scratch.p, 0, bytes, s));
+  prof_begin(PROF_TABLES, s);
+  scan3_kernel<<<(unsigned)tiles, S3_THREADS, 0, s>>>(in0, in1, in2, out0, out1, out2, n,
+                                                       scratch.as<uint64_t>() + 1, tiles, scratch.as<uint32_t>(),
+                                                       d_err);
+  prof_end(PROF_TABLES, s);
+  count_launch();
+  WTG_CK(cudaGetLastError());
+  return WTG_OK;
+}
+
 // Node sizes of level l+1 from the per-chunk counts of the pass over level l:
 // the chunks lying inside node p are [ceil(C(p)/512), floor(C(p+1)/512)), and
 // the exclusive scans S0, S1 of their counts (zeros of 2p, of 2p+1) give
@@ -809,6 +903,7 @@ int tree_build(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int L, uint32
       if ((rc = t.lvl[1].ensure(n * eb + 16, s))) return rc;
     }
     const void* src = d_seq;
+    bool pre_ready = false;  // the level's chunk prefixes were scanned with the previous pass's counts
     for (int l = 0; l < L; ++l) {
       LevelArgs a{};
       a.scatter = l < L - 1;
@@ -830,20 +925,24 @@ int tree_build(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int L, uint32
       a.nc0 = a.emit_nodes ? t.nodecnt.as<uint32_t>() : nullptr;
       a.nc1 = a.emit_nodes ? a.nc0 + (tiles + 1) : nullptr;
       a.err = d_err;
-      if (a.scatter)
+      if (a.scatter && !pre_ready)
         if ((rc = scan_exclusive_u32(tilecnt + (uint64_t)l * (tiles + 1), tilepre, tiles, t.scan_tmp, d_err, s)))
           return rc;
+      pre_ready = false;
       prof_begin(a.scatter ? PROF_LEVEL : PROF_LEVEL_LAST, s);
       WTG_DISPATCH(eb, launch_level, a, s);
       prof_end(a.scatter ? PROF_LEVEL : PROF_LEVEL_LAST, s);
       count_launch();
       WTG_CK(cudaGetLastError());
       if (a.emit_nodes) {
-        // the in-node chunks' counts: scans, then one sum per node of level l
+        // the next level's chunk prefixes and the in-node chunks' counts in
+        // one scan, then one sum per node of level l
         uint32_t* S0 = a.nc0 + 2 * (tiles + 1);
         uint32_t* S1 = a.nc0 + 3 * (tiles + 1);
-        if ((rc = scan_exclusive_u32(a.nc0, S0, tiles + 1, t.scan_tmp, d_err, s))) return rc;
-        if ((rc = scan_exclusive_u32(a.nc1, S1, tiles + 1, t.scan_tmp, d_err, s))) return rc;
+        if ((rc = scan3_u32(a.chunkcnt_next, a.nc0, a.nc1, tilepre_all + (uint64_t)(l + 1) * (tiles + 1), S0, S1,
+                            tiles + 1, t.scan_tmp, d_err, s)))
+          return rc;
+        pre_ready = true;
         const uint64_t cnt = 1ull << l;
         unsigned grid = (unsigned)std::min<uint64_t>((cnt + 255) / 256, 2048);
         prof_begin(PROF_TABLES, s);
