@@ -291,32 +291,45 @@ __global__ void select_pool_total_kernel(int t_b, unsigned long long* info, cons
   info[t_b ? INF_POOL1 : INF_POOL0] = nsb ? offs[nsb - 1] + sizes[nsb - 1] : 0;
 }
 
-// warp per superblock: final descriptors, and the 64-entry mini blocks
+// Two superblocks per warp (lanes 0-15 pack superblock 2w's words, lanes
+// 16-31 superblock 2w+1's): final descriptors and the 64-entry mini blocks.
+// A mini block's words are few (its width, at most 32), so one superblock per
+// warp left half of the lanes idle while the others packed.
 __global__ void __launch_bounds__(256)
     select_mini_kernel(int t_b, uint64_t nsb, uint64_t m, const uint32_t* __restrict__ samples, uint64_t samp_last,
                        const uint64_t* __restrict__ descw, const uint64_t* __restrict__ offs,
                        uint64_t* __restrict__ desc, uint64_t* __restrict__ pool) {
-  __shared__ uint64_t ent[256 / 32][64];
+  __shared__ uint64_t ent[256 / 32][2][64];
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (i >= nsb) return;
-  const uint64_t d = descw[i];
-  const uint64_t off = offs[i];
-  if (lane == 0) desc[i] = (off << 8) | (d & 255);
-  if ((d >> 7) & 1) return;  // long block
-  const uint32_t wdt = (uint32_t)(d & 127);
+  const uint64_t i0 = (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 2;
+  if (i0 >= nsb) return;
   auto samp = [&](uint64_t k) { return t_b ? samples[k] : samples[samp_last - k]; };
   // positions are kept mod 2^32; a mini block spans at most log^4 n < 2^32
   // bits, so the offsets are exact
-  const uint32_t start = samp(64 * i);
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
-    uint32_t j = lane + 32 * h;
-    uint64_t k = 4096 * i + 64 * (uint64_t)j;
-    ent[warp][j] = (k < m) ? (uint64_t)(uint32_t)(samp(64 * i + j) - start) : 0;
+    const uint64_t i = i0 + h;
+    if (i < nsb) {  // warp-uniform
+      const uint32_t start = samp(64 * i);
+#pragma unroll
+      for (int g = 0; g < 2; ++g) {
+        const uint32_t j = lane + 32 * g;
+        const uint64_t k = 4096 * i + 64 * (uint64_t)j;
+        ent[warp][h][j] = (k < m) ? (uint64_t)(uint32_t)(samp(64 * i + j) - start) : 0;
+      }
+    }
   }
   __syncwarp();
-  if (lane < wdt) pool[off + lane] = packed_word(lane, wdt, 64, [&](uint64_t j) { return ent[warp][j]; });
+  const uint32_t h = lane >> 4, ql = lane & 15;
+  const uint64_t i = i0 + h;
+  if (i >= nsb) return;
+  const uint64_t d = descw[i];
+  const uint64_t off = offs[i];
+  if (ql == 0) desc[i] = (off << 8) | (d & 255);
+  if ((d >> 7) & 1) return;  // long block
+  const uint32_t wdt = (uint32_t)(d & 127);
+  for (uint32_t q = ql; q < wdt; q += 16)
+    pool[off + q] = packed_word(q, wdt, 64, [&](uint64_t j) { return ent[warp][h][j]; });
 }
 
 // m_superblock: entry i = position of arg 4096*i, width logn
@@ -527,7 +540,7 @@ int bv_finish(BvSupport& bv, uint32_t* d_err, cudaStream_t s) {
     uint64_t* descw = sd.desc.as<uint64_t>() + nsb_cap;
     uint64_t* offs = sd.sizes.as<uint64_t>() + nsb_cap;
     prof_begin(PROF_SELECT, s);
-    select_mini_kernel<<<(unsigned)((sd.nsb * 32 + 255) / 256), 256, 0, s>>>(
+    select_mini_kernel<<<(unsigned)(((sd.nsb + 1) / 2 * 32 + 255) / 256), 256, 0, s>>>(
         t_b, sd.nsb, m, samples, samp_n - 1, descw, offs, sd.desc.as<uint64_t>(), sd.pool.as<uint64_t>());
     prof_end(PROF_SELECT, s);
     count_launch();

@@ -636,7 +636,7 @@ static int level_grid(uint64_t n) {
 // side): after a pass, the next level's chunk zero counts and the two
 // per-chunk node counts.  Every prefix stays below n < 2^32.
 constexpr int S3_THREADS = 256;
-constexpr int S3_IPT = 16;
+constexpr int S3_IPT = 8;
 constexpr int S3_TILE = S3_THREADS * S3_IPT;
 
 __global__ void __launch_bounds__(S3_THREADS)
