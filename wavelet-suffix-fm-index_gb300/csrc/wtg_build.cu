@@ -634,7 +634,9 @@ static int level_grid(uint64_t n) {
 // Three exclusive scans in one single-pass launch (decoupled look-back, one
 // status word array per field; warps 0-2 run the three look-backs side by
 // side): after a pass, the next level's chunk zero counts and the two
-// per-chunk node counts.  Every prefix stays below n < 2^32.
+// per-chunk node counts.  Every prefix stays below n < 2^32.  The arrays are
+// 16-byte aligned (per-level strides are whole vectors), so a thread moves
+// its 8 items of a field as two 16-byte vectors.
 constexpr int S3_THREADS = 256;
 constexpr int S3_IPT = 8;
 constexpr int S3_TILE = S3_THREADS * S3_IPT;
@@ -654,14 +656,21 @@ __global__ void __launch_bounds__(S3_THREADS)
   const uint64_t base = (uint64_t)tile * S3_TILE + (uint64_t)threadIdx.x * S3_IPT;
   const uint32_t* const in[3] = {in0, in1, in2};
   uint32_t v[3][S3_IPT], sum[3], incl[3];
+  const bool whole = base + S3_IPT <= n;  // the thread's items as two 16-byte vectors
 #pragma unroll
   for (int f = 0; f < 3; ++f) {
     sum[f] = 0;
+    if (whole) {
+      const uint4 a = __ldg(reinterpret_cast<const uint4*>(in[f] + base));
+      const uint4 b = __ldg(reinterpret_cast<const uint4*>(in[f] + base) + 1);
+      v[f][0] = a.x; v[f][1] = a.y; v[f][2] = a.z; v[f][3] = a.w;
+      v[f][4] = b.x; v[f][5] = b.y; v[f][6] = b.z; v[f][7] = b.w;
+    } else {
 #pragma unroll
-    for (int k = 0; k < S3_IPT; ++k) {
-      v[f][k] = base + k < n ? in[f][base + k] : 0u;
-      sum[f] += v[f][k];
+      for (int k = 0; k < S3_IPT; ++k) v[f][k] = base + k < n ? in[f][base + k] : 0u;
     }
+#pragma unroll
+    for (int k = 0; k < S3_IPT; ++k) sum[f] += v[f][k];
     incl[f] = sum[f];
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -699,10 +708,19 @@ __global__ void __launch_bounds__(S3_THREADS)
 #pragma unroll
   for (int f = 0; f < 3; ++f) {
     uint32_t run = s_prefix[f] + s_wsum[f][warp] + incl[f] - sum[f];
+    uint32_t o[S3_IPT];
 #pragma unroll
     for (int k = 0; k < S3_IPT; ++k) {
-      if (base + k < n) out[f][base + k] = run;
+      o[k] = run;
       run += v[f][k];
+    }
+    if (whole) {
+      reinterpret_cast<uint4*>(out[f] + base)[0] = make_uint4(o[0], o[1], o[2], o[3]);
+      reinterpret_cast<uint4*>(out[f] + base)[1] = make_uint4(o[4], o[5], o[6], o[7]);
+    } else {
+#pragma unroll
+      for (int k = 0; k < S3_IPT; ++k)
+        if (base + k < n) out[f][base + k] = o[k];
     }
   }
 }
@@ -857,12 +875,14 @@ int tree_build(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int L, uint32
 
   // per-level tile zero counts [L x tiles] and their scan (tilepre)
   const uint64_t tiles = n ? (n + tile_elems(eb) - 1) / tile_elems(eb) : 0;
-  // [L + 1][tiles + 1] counts, then [L][tiles + 1] prefixes (kept per level:
+  // [L + 1][tst] counts, then [L][tst] prefixes (kept per level:
   // the rank/select pass reads them all)
-  if ((rc = t.status.ensure((2 * (uint64_t)L + 1) * (tiles + 1) * sizeof(uint32_t), s))) return rc;
+  // per-level stride: tiles + 1 entries, rounded up to whole 16-byte vectors
+  const uint64_t tst = (tiles + 4) & ~3ull;
+  if ((rc = t.status.ensure((2 * (uint64_t)L + 1) * tst * sizeof(uint32_t), s))) return rc;
   uint32_t* tilecnt = t.status.as<uint32_t>();
-  uint32_t* tilepre_all = tilecnt + ((uint64_t)L + 1) * (tiles + 1);
-  if (n) WTG_CK(cudaMemsetAsync(tilecnt, 0, (uint64_t)L * (tiles + 1) * sizeof(uint32_t), s));
+  uint32_t* tilepre_all = tilecnt + ((uint64_t)L + 1) * tst;
+  if (n) WTG_CK(cudaMemsetAsync(tilecnt, 0, (uint64_t)L * tst * sizeof(uint32_t), s));
 
   if (n) {
     prof_begin(PROF_HIST, s);
@@ -889,8 +909,8 @@ int tree_build(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int L, uint32
 
   // per-chunk node counts of a pass and their scans: [nc0 | nc1 | S0 | S1]
   if (n && L > K) {
-    if ((rc = t.nodecnt.ensure(4 * (tiles + 1) * sizeof(uint32_t), s))) return rc;
-    WTG_CK(cudaMemsetAsync(t.nodecnt.p, 0, 2 * (tiles + 1) * sizeof(uint32_t), s));
+    if ((rc = t.nodecnt.ensure(4 * tst * sizeof(uint32_t), s))) return rc;
+    WTG_CK(cudaMemsetAsync(t.nodecnt.p, 0, 2 * tst * sizeof(uint32_t), s));
   }
 
   // level passes; each scattering pass feeds the next level's chunk counts
@@ -917,16 +937,16 @@ int tree_build(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int L, uint32
       a.base_lvl = base + ((1ull << l) - 1);
       a.bits32 = t.bits.as<uint32_t>();
       a.bit_off = (uint64_t)l * n;
-      uint32_t* tilepre = tilepre_all + (uint64_t)l * (tiles + 1);
+      uint32_t* tilepre = tilepre_all + (uint64_t)l * tst;
       a.chunkpre = tilepre;
-      a.chunkcnt_next = tilecnt + (uint64_t)(l + 1) * (tiles + 1);
-      a.chunkcnt_self = (!a.scatter && rs_from_levels) ? tilecnt + (uint64_t)l * (tiles + 1) : nullptr;
+      a.chunkcnt_next = tilecnt + (uint64_t)(l + 1) * tst;
+      a.chunkcnt_self = (!a.scatter && rs_from_levels) ? tilecnt + (uint64_t)l * tst : nullptr;
       a.znext = Z + ((1ull << (l + 1)) - 1);
       a.nc0 = a.emit_nodes ? t.nodecnt.as<uint32_t>() : nullptr;
-      a.nc1 = a.emit_nodes ? a.nc0 + (tiles + 1) : nullptr;
+      a.nc1 = a.emit_nodes ? a.nc0 + tst : nullptr;
       a.err = d_err;
       if (a.scatter && !pre_ready)
-        if ((rc = scan_exclusive_u32(tilecnt + (uint64_t)l * (tiles + 1), tilepre, tiles, t.scan_tmp, d_err, s)))
+        if ((rc = scan_exclusive_u32(tilecnt + (uint64_t)l * tst, tilepre, tiles, t.scan_tmp, d_err, s)))
           return rc;
       pre_ready = false;
       prof_begin(a.scatter ? PROF_LEVEL : PROF_LEVEL_LAST, s);
@@ -937,9 +957,9 @@ int tree_build(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int L, uint32
       if (a.emit_nodes) {
         // the next level's chunk prefixes and the in-node chunks' counts in
         // one scan, then one sum per node of level l
-        uint32_t* S0 = a.nc0 + 2 * (tiles + 1);
-        uint32_t* S1 = a.nc0 + 3 * (tiles + 1);
-        if ((rc = scan3_u32(a.chunkcnt_next, a.nc0, a.nc1, tilepre_all + (uint64_t)(l + 1) * (tiles + 1), S0, S1,
+        uint32_t* S0 = a.nc0 + 2 * tst;
+        uint32_t* S1 = a.nc0 + 3 * tst;
+        if ((rc = scan3_u32(a.chunkcnt_next, a.nc0, a.nc1, tilepre_all + (uint64_t)(l + 1) * tst, S0, S1,
                             tiles + 1, t.scan_tmp, d_err, s)))
           return rc;
         pre_ready = true;
@@ -983,11 +1003,11 @@ int tree_build(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int L, uint32
   // rank / select over the concatenated bitvector
   t.bv.rank_done = (t.host_rank && (flags & WTG_RANK)) ? t.rank_ev : nullptr;
   if (rs_from_levels) {
-    uint32_t* last_cnt = tilecnt + (uint64_t)(L - 1) * (tiles + 1);
-    uint32_t* last_pre = tilepre_all + (uint64_t)(L - 1) * (tiles + 1);
+    uint32_t* last_cnt = tilecnt + (uint64_t)(L - 1) * tst;
+    uint32_t* last_pre = tilepre_all + (uint64_t)(L - 1) * tst;
     if ((rc = scan_exclusive_u32(last_cnt, last_pre, tiles, t.scan_tmp, d_err, s))) return rc;
     if ((rc = t.scratch.ensure(((uint64_t)L + 1) * sizeof(uint64_t), s))) return rc;
-    if ((rc = bv_from_levels(t.bv, t.bits.as<uint64_t>(), n, L, tilecnt, tilepre_all, tiles + 1, tiles,
+    if ((rc = bv_from_levels(t.bv, t.bits.as<uint64_t>(), n, L, tilecnt, tilepre_all, tst, tiles,
                              t.scratch.as<uint64_t>(), flags, d_err, s)))
       return rc;
   } else if (flags) {
