@@ -52,10 +52,10 @@ def algorithmic_bytes(n, L, w, sel_words=0):
 
 # DRAM bytes (read + write) per symbol of one uint32 partitioning level pass,
 # from ncu's dram__bytes_read.sum + dram__bytes_write.sum over levels 9-11 of
-# an n=2^26 build (491.7 MB per launch: 269.8 MB read, 221.9 MB written, the
+# an n=2^26 build (491.9 MB per launch: 269.6 MB read, 222.3 MB written, the
 # rest of the writes still in L2 when the launch ends); traffic grows
 # linearly with n, so a full launch's traffic is this figure times n.
-LEVEL_DRAM_BYTES_PER_SYMBOL_U32 = 491.7e6 / 2 ** 26
+LEVEL_DRAM_BYTES_PER_SYMBOL_U32 = 491.9e6 / 2 ** 26
 
 
 def level_launch_bytes(n, w):
