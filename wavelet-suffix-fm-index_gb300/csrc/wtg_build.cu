@@ -10,26 +10,32 @@
 //   * the level's bits are a coalesced map: one __ballot_sync per warp and row
 //     yields 32 bits, staged in shared memory and stored as whole words;
 //   * the stable partition is a scatter: with Z(i) = number of zeros before
-//     position i at this level (one decoupled look-back scan per level) an
-//     element of node p with bit 0 goes to  C_l(p) + Z(i) - Zb(p)  and one with
-//     bit 1 to  C_l(p) + zeros(p) + (i - Z(i)) - (C_l(p) - Zb(p)), where
-//     zeros(p) is the size of p's left child and Zb(p) the zeros of the
-//     level's nodes before p; base_kernel / level_table_kernel fold them into
-//     two per-node constants.
+//     position i at this level, an element of node p with bit 0 goes to
+//     C_l(p) + Z(i) - Zb(p)  and one with bit 1 to
+//     C_l(p) + zeros(p) + (i - Z(i)) - (C_l(p) - Zb(p)), where zeros(p) is
+//     the size of p's left child and Zb(p) the zeros of the level's nodes
+//     before p; base_kernel / level_table_kernel fold them into two per-node
+//     constants.  Z at every 512-symbol chunk start is the exclusive scan of
+//     the per-chunk zero counts the previous pass emitted for its
+//     destination chunks (level 0: the pre-pass), so no pass waits on
+//     another chunk's result.
 //
-// Node sizes: a pre-pass histograms the top K = min(L, 12) bits in shared
-// memory, which gives C and zeros for levels < K.  For deeper levels the pass
-// over level l counts, per node of level l+1, the symbols whose next bit is 0
-// (the level order keeps each node contiguous, so a warp aggregates a run of
-// rows into one atomic per node), and a small table kernel derives level
-// l+1's constants before its pass.
+// Node sizes: the pre-pass histograms the top K = 2 bits, which gives C and
+// zeros for levels 0 and 1.  For deeper levels the pass over level l counts,
+// per node of level l+1, the symbols whose next bit is 0: a chunk inside one
+// node p stores its two counts (nodes 2p, 2p+1) per chunk, a scan and
+// node_sum_kernel add them up per node, and chunks across node boundaries
+// add theirs with atomics; level_table_kernel then derives level l+1's
+// constants before its pass.
 //
-// Each level pass is a persistent kernel: CTAs take 16 KB tiles from an atomic
-// counter and prefetch the next tile with cp.async.bulk into the other half
-// of a double buffer while they process the current one.  Per level the
-// sequence is read once and written once, plus n/8 bytes of bits.  The node
-// table (WT.C:110,156-159,234-257) follows from the per-node starts and zero
-// counts alone.
+// Each level pass is a persistent kernel in which every warp runs its own
+// pipeline: it fetches groups of 512-symbol chunks (4 KB) with cp.async.bulk
+// into a private two-stage ring and waits on its own mbarriers, the chunks of
+// the level taken in a grid stride (a narrow moving window of the order, so
+// the writes advance in a few dense fronts).  Per level the sequence is read
+// once and written once, plus n/8 bytes of bits.  The node table
+// (WT.C:110,156-159,234-257) follows from the per-node starts and zero counts
+// alone.
 #include <algorithm>
 #include <type_traits>
 
