@@ -266,15 +266,6 @@ __global__ void node_kernel(const uint32_t* __restrict__ C, const uint32_t* __re
 // registers and added to `target` (one atomic) when a key is evicted.  Keys
 // of a row arrive sorted by node or by destination, so two entries catch
 // almost every repeat.
-__device__ __forceinline__ uint64_t warp_max64(uint64_t v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    const uint64_t t = __shfl_xor_sync(0xffffffffu, v, o);
-    v = t > v ? t : v;
-  }
-  return v;
-}
-
 struct Slot2 {
   uint32_t ka = 0xFFFFFFFFu, ca = 0, kb = 0xFFFFFFFFu, cb = 0;
 };
@@ -317,11 +308,13 @@ __device__ __forceinline__ uint32_t prefix_of(T x, int s, uint32_t mask) {
 }
 
 // One level over the level-l order in src.  Every warp runs its own
-// pipeline over 512-symbol chunks (chunk = global warp id + k * warps): it
-// prefetches its next chunk with cp.async.bulk into the other half of its
-// private double buffer and waits on its own mbarrier, so warps never
-// synchronise with each other.  The chunk's zeros-before come from chunkpre
-// (the scan of the counts the previous pass emitted).  Per chunk:
+// pipeline over groups of CPB consecutive 512-symbol chunks (4 KB; group =
+// global warp id + k * warps): it prefetches its next group with one
+// cp.async.bulk into the other half of its private double buffer and waits
+// on its own mbarrier, so warps never synchronise with each other.  A
+// chunk's zeros-before come from chunkpre (the scan of the counts the
+// previous pass emitted), read for the whole group before the wait.  Per
+// chunk:
 //   * the level's bits: one ballot per 32 symbols, stored as whole words;
 //   * SCATTER: every symbol goes straight to its place in the next level's
 //     order: bit 0 -> C(p) + zeros before it in node p, bit 1 ->
@@ -338,8 +331,9 @@ __device__ __forceinline__ uint32_t prefix_of(T x, int s, uint32_t mask) {
 //     middle levels -- a hot L2 slice that slowed those levels by a third.)
 // A full chunk inside one node (the common case) takes a lean unrolled path:
 // one base(p), its zero run and one run contiguous in dst, each touching at
-// most two destination chunks, so emission is per-lane counting and four
-// atomics per chunk.  Other chunks take a compact general path.
+// most two destination chunks, so emission is per-row counting, one ballot
+// for the row that holds a destination boundary, and four atomics per chunk.
+// Other chunks take a compact general path.
 template <typename T, bool SCATTER, bool EMIT_NODES, bool EMIT_TILES>
 __global__ void __launch_bounds__(LV_THREADS, 3)
     level_kernel(const T* __restrict__ src, T* __restrict__ dst, uint64_t n, int L, int level,
