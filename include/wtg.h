@@ -12,7 +12,7 @@
  * Layouts (bit-exact with the reference):
  *   bits   : level l of the tree occupies bits [l*n, (l+1)*n) of one array of
  *            ceil(n*levels/64) 64-bit words, LSB first
- *            (wavelet/levelWT/WT.C:97,104,136; wt_int/wt_int_par.hpp:397-398).
+ *            (wavelet/levelWT/WT.C:54,61,93; wt_int/wt_int_par.hpp:397-398).
  *   nodes  : WTnode records {bitmapPtr, length, parent, leftChild, rightChild}
  *            in heap order, with 4-byte (uintT) or 8-byte (-DLONG) fields and
  *            UINT_T_MAX for absent links (wavelet/levelWT/WT.h:30-35).  Node
@@ -62,12 +62,12 @@ uint64_t wtg_launch_count(void);
 
 /* ------------------------------------------------------------ tree build
  * Replaces WT(symbol* s, uintT n, uintT sigma) (wavelet/levelWT/WT.h:43,
- * levelWT/WT.C:86-270; same contract in ddWT/recWT/serialWT) and the
+ * levelWT/WT.C:43-227; same contract in ddWT/recWT/serialWT) and the
  * sdsl::wt_int<> constructor (wt_int/wt_int_par.hpp:368-406) with its
  * util::init_support calls for rank and select (:402-404).
  *   seq        : n symbols of elem_bytes (1, 2, 4 or 8) bytes, host memory
  *   levels     : tree height; symbols are read through their low `levels`
- *                bits, bit (levels-1-l) at level l (levelWT/WT.C:105,
+ *                bits, bit (levels-1-l) at level l (levelWT/WT.C:62,
  *                wt_int_par.hpp:173).  levels = max(1, log2Up(sigma)) gives
  *                levelWT's tree; 0 derives wt_int's hi(max(1,max symbol))+1
  *                (wt_int_par.hpp:385-395).  1..24 supported.
@@ -112,7 +112,7 @@ int wtg_tree_select_info(wtg_tree* t, int t_b, uint64_t info[8]);
  * Host destinations; sizes must match wtg_tree_info / wtg_tree_select_info. */
 int wtg_tree_get_bits(wtg_tree* t, uint64_t* dst, uint64_t nwords);
 /* WTnode records for heap ids [0, n_entries) with index_bytes (4 or 8) per
- * field: the reference's 2*sigma-entry node array (levelWT/WT.C:89). */
+ * field: the reference's 2*sigma-entry node array (levelWT/WT.C:46). */
 int wtg_tree_get_nodes(wtg_tree* t, int index_bytes, uint64_t n_entries, void* dst);
 int wtg_tree_get_rank(wtg_tree* t, uint64_t* dst, uint64_t nwords);
 int wtg_tree_get_select(wtg_tree* t, int t_b, uint64_t* sb_words, uint64_t* desc, uint64_t* pool);
@@ -208,14 +208,18 @@ int wtg_bv_select_device(wtg_bv* b, int t_b, const uint64_t* d_i, uint64_t nq, u
  * inside a memory budget owned by another framework, or in a phase where a
  * cudaMalloc would synchronise the device or is forbidden by the pool in use.
  * Builds the same rank_support_v<1> table as wtg_bv_build (WTG_RANK) from
- * d_words (size_bits bits, device memory) into d_rank (((capacity>>9)+1)*2
- * words, device memory), on `stream`, and waits for it.  It calls no
+ * d_words (size_bits bits, device memory) into d_rank (device memory of
+ * 2*(floor(ceil(size_bits/64)/8)+1) words, the size wtg_bv_rank_words gives),
+ * on `stream`; the calling thread then waits for that stream (not for the
+ * whole device) to read the pass's error word.  It calls no
  * cudaMalloc/cudaFree: its scratch is one fixed device array inside the
  * library (about 1 MB, held on every GPU that loads the library until exit),
  * which limits size_bits to 2^34; larger inputs return WTG_ERR_RANGE.  The
  * first call on a device looks up that array's device address (make it
- * before any stream capture).  All calls share the array, so calls that
- * overlap on the GPU (other threads or streams) race. */
+ * before any stream capture); the address is kept until the process exits,
+ * so the entry point must not be used after a cudaDeviceReset.  All calls
+ * share the array, so calls that overlap on the GPU (other threads or
+ * streams) race. */
 int wtg_rank_build_noalloc(const uint64_t* d_words, uint64_t size_bits, uint64_t* d_rank, void* stream);
 
 /* ------------------------------------------------------------ batched builds
@@ -279,7 +283,7 @@ int wtg_suffix_array_device(const uint8_t* d_text, uint64_t n, int32_t* d_sa, ui
  * Backward search over a tree built (with WTG_RANK) on the BWT of a text,
  * its symbols coded 0..sigma-1: the reference's FM-index is the wavelet tree
  * of s[SA[i]-1] (s[n-1] where SA[i] == 0) with SA from divsufsort
- * (fm-index/par/WT.C:33-46); the reference stops at construction, and this
+ * (fm-index/par/WT.C:33-45); the reference stops at construction, and this
  * adds the count query.  C[c] = number of BWT symbols below c (sigma
  * entries).  Pattern p is pat[off[p] .. off[p+1]) (byte codes); out[p] is
  * the size of its suffix-array range, i.e. its number of occurrences.  A

@@ -14,6 +14,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
+# The reference checkout: $WTG_REFERENCE_DIR, else "reference" beside the repo root.
+REF_SRC = os.environ.get("WTG_REFERENCE_DIR") or os.path.abspath(os.path.join(HERE, "..", "..", "reference"))
 
 u64 = ctypes.c_uint64
 vp = ctypes.c_void_p
@@ -26,8 +28,8 @@ def build(ref=True):
     import shutil
     if shutil.which("make"):
         subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
-        if ref and os.path.isdir("/root/reference"):
-            subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+        if ref and os.path.isdir(REF_SRC):
+            subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + REF_SRC], check=True)
         return
     os.makedirs(os.path.join(HERE, "_build"), exist_ok=True)
     subprocess.run(["gcc", "-O2", "-fPIC", "-fopenmp", "-std=gnu11", "-shared", "-o", LIB_PATH,

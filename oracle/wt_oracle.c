@@ -17,7 +17,7 @@
 #endif
 
 #define OR_NONE UINT64_MAX
-#define OR_THRESHOLD 10000 /* wavelet/levelWT/WT.C:72 */
+#define OR_THRESHOLD 10000 /* wavelet/levelWT/WT.C:29 */
 
 typedef struct { uint64_t start, length, nodeID, zc; } or_chunk;
 
@@ -30,7 +30,7 @@ int or_num_threads(void) {
 }
 
 static inline void or_word(uint64_t* w, uint64_t v) {
-  if (v) __atomic_fetch_or(w, v, __ATOMIC_RELAXED); /* writeOr, WT.C:74-78 */
+  if (v) __atomic_fetch_or(w, v, __ATOMIC_RELAXED); /* writeOr, WT.C:31-35 */
 }
 
 static inline int popc(uint64_t x) { return __builtin_popcountll(x); }

@@ -28,10 +28,10 @@ typedef struct {
 int or_log2_up(uint64_t i);
 /* sdsl bits::hi: position of the most significant set bit, 0 for x == 0. */
 int or_hi(uint64_t x);
-/* levels = max(1, log2Up(sigma)) (wavelet/levelWT/WT.C:96). */
+/* levels = max(1, log2Up(sigma)) (wavelet/levelWT/WT.C:53). */
 int or_levels_for_sigma(uint64_t sigma);
 
-/* levelWT WT() (wavelet/levelWT/WT.C:86-270).  Symbols are elem_bytes wide
+/* levelWT WT() (wavelet/levelWT/WT.C:43-227).  Symbols are elem_bytes wide
  * (1, 2, 4 or 8); the tree has `levels` levels over codes [0, 2^levels).
  * wt receives ceil(n*levels/64) words (level l at bits [l*n,(l+1)*n), LSB
  * first).  nodes (may be NULL) receives n_nodes entries in heap order; entries
@@ -126,7 +126,7 @@ void or_wt_range_count_batch(const uint64_t* tree, const uint64_t* rank_tbl, uin
 void or_select_batch(const or_select* h, const uint64_t* data, const uint64_t* q, uint64_t nq,
                      uint64_t* out);
 
-/* FM-index core (fm-index/par/WT.C:33-46): suffix array, BWT, and counting
+/* FM-index core (fm-index/par/WT.C:33-45): suffix array, BWT, and counting
  * by backward search over the wavelet tree of the BWT. */
 /* Suffix array of the n bytes at s: all suffixes, no sentinel, a proper
  * prefix before its extensions -- the array divsufsort returns

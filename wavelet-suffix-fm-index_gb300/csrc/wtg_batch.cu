@@ -2,7 +2,7 @@
 // wavelet tree (level bitvector of L <= 4 levels), rank_support_v<1> and
 // select_support_mcl<1>/<0>, all in one persistent launch.
 //
-// The reference builds one sequence per WT() call (levelWT/WT.C:86-270,
+// The reference builds one sequence per WT() call (levelWT/WT.C:43-227,
 // driven by levelWT/WTTime.C:78-103); a batch there is a loop of calls.  Here
 // one persistent kernel pulls texts from a device queue, largest first, and
 // one CTA builds a whole text -- the data of a text (at most a few MB) stays
@@ -10,7 +10,7 @@
 //   H  symbol histogram -> per level l and node key k (the top l bits) the
 //      bit position where that node's bits start: l*n + (symbols whose key
 //      is below k).  Level l is the text stably sorted by the top l bits
-//      (levelWT/WT.C:118-188), so a symbol's bit at level l lands at
+//      (levelWT/WT.C:118-190), so a symbol's bit at level l lands at
 //      start(l, key) + (symbols of the same key before it): every level is
 //      written from one read of the text, no level-by-level passes.
 //   W  per chunk, warp slices count their symbols per (level, key), a block

@@ -606,7 +606,9 @@ static uint64_t* noalloc_scratch_ptr(int dev, int* rc) {
     return nullptr;
   }
   std::lock_guard<std::mutex> lk(mu);
-  if (!ptrs[dev]) {  // set-up, once per device, with that device current
+  // set-up, once per device, with that device current.  The address is kept
+  // for the life of the process, so it is not valid after a cudaDeviceReset.
+  if (!ptrs[dev]) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) {
@@ -646,9 +648,10 @@ extern "C" int wtg_rank_build_noalloc(const uint64_t* d_words, uint64_t size_bit
                                                        nullptr, nullptr, nullptr, nullptr, info, status, counter, err);
   count_launch();
   WTG_CK(cudaGetLastError());
-  WTG_CK(cudaStreamSynchronize(s));
+  // read the error word on the caller's stream only: no device-wide wait
   uint32_t e = 0;
-  WTG_CK(cudaMemcpy(&e, err, sizeof(e), cudaMemcpyDeviceToHost));
+  WTG_CK(cudaMemcpyAsync(&e, err, sizeof(e), cudaMemcpyDeviceToHost, s));
+  WTG_CK(cudaStreamSynchronize(s));
   if (e) return fail(WTG_ERR_TIMEOUT, "a device-side wait of the rank pass timed out; the table is invalid");
   return WTG_OK;
 }

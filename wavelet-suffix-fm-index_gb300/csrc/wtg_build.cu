@@ -1,6 +1,6 @@
 // wtg_build.cu -- level-by-level wavelet-tree construction on the GPU.
 //
-// The reference (wavelet/levelWT/WT.C:86-270) walks the tree node by node:
+// The reference (wavelet/levelWT/WT.C:43-227) walks the tree node by node:
 // at level l every node writes bit (levels-l-1) of its symbols at
 // l*n + position and stably partitions them, zeros first, into the next
 // level's buffer.  Here a level is one flat pass over the whole sequence:
@@ -34,7 +34,7 @@
 // the level taken in a grid stride (a narrow moving window of the order, so
 // the writes advance in a few dense fronts).  Per level the sequence is read
 // once and written once, plus n/8 bytes of bits.  The node table
-// (WT.C:110,156-159,234-257) follows from the per-node starts and zero counts
+// (WT.C:67,113-116,191-214) follows from the per-node starts and zero counts
 // alone.
 #include <algorithm>
 #include <type_traits>
@@ -168,7 +168,7 @@ __global__ void max_kernel(const T* __restrict__ s, uint64_t n, unsigned long lo
 }
 
 // ------------------------------------------------------ per-node tables
-// Heap id h = 2^l - 1 + p names node p of level l (levelWT/WT.C:236-252).
+// Heap id h = 2^l - 1 + p names node p of level l (levelWT/WT.C:191-214).
 // C[h] = start of node h in its level, Z[h] = size of its left child.
 
 __device__ __forceinline__ void heap_split(uint64_t h, int& l, uint64_t& p) {
@@ -224,7 +224,7 @@ __global__ void level_table_kernel(int m, int with_base, uint32_t* __restrict__ 
   }
 }
 
-// WTnode records in heap order (levelWT/WT.C:89-110,156-159,234-257).
+// WTnode records in heap order (levelWT/WT.C:46-67,113-116,191-214).
 __global__ void node_kernel(const uint32_t* __restrict__ C, const uint32_t* __restrict__ Z, int L, uint64_t n,
                             uint64_t n_entries, int ib, void* __restrict__ out) {
   uint64_t h = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;

@@ -3,7 +3,7 @@
 //
 // The reference builds the FM-index -- suffix array by divsufsort, the BWT
 // s[SA[i]-1] (s[n-1] where SA[i] == 0), a wavelet tree over it
-// (fm-index/par/WT.C:33-46) -- and stops there.  Counting is the standard
+// (fm-index/par/WT.C:33-45) -- and stops there.  Counting is the standard
 // backward search: [sp, ep) = [0, n), then for the pattern's symbols from the
 // last to the first  sp = C[c] + rank(sp, c),  ep = C[c] + rank(ep, c), where
 // rank is wt_int's (wt_int/wt_int_par.hpp:553-577) over the tree of the BWT

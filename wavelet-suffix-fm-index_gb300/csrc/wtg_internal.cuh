@@ -3,7 +3,7 @@
 //
 // Data layouts kept bit-exact with the reference (jlabeit/wavelet-suffix-fm-index):
 //   * level bitvector: level l occupies bits [l*n, (l+1)*n) of one array of
-//     64-bit words, LSB first (wavelet/levelWT/WT.C:97,104,136);
+//     64-bit words, LSB first (wavelet/levelWT/WT.C:54,61,93);
 //   * rank_support_v<1> table: interleaved (absolute count, seven 9-bit
 //     cumulative block counts) per 512-bit superblock
 //     (rank/rank_support_v_par.hpp:78-113);

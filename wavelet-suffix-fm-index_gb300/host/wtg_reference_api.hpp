@@ -56,7 +56,7 @@ inline void check(int rc) {
   if (rc != WTG_OK) throw std::runtime_error(std::string("wtg: ") + wtg_last_error());
 }
 
-// max(1, log2Up(sigma)) (wavelet/levelWT/WT.C:96)
+// max(1, log2Up(sigma)) (wavelet/levelWT/WT.C:53)
 inline int levels_for_sigma(uint64_t sigma) {
   int a = 0;
   for (uint64_t b = sigma - 1; b > 0; b >>= 1) ++a;
@@ -307,7 +307,7 @@ class select_support_mcl {
 }  // namespace wtg
 
 #ifndef WTG_NO_REFERENCE_TYPES
-// levelWT's WT() (wavelet/levelWT/WT.h:43, WT.C:86-270): the level-concatenated
+// levelWT's WT() (wavelet/levelWT/WT.h:43, WT.C:43-227): the level-concatenated
 // bitvector of ceil(n*levels/64) words and 2*sigma WTnode records, both
 // malloc'ed; the caller frees them with free().
 inline std::pair<WTnode*, long*> WT(symbol* s, uintT n, uintT sigma) {

@@ -165,7 +165,7 @@ def profile_read():
 
 
 def levels_for_sigma(sigma):
-    """max(1, log2Up(sigma)) (wavelet/levelWT/WT.C:96)."""
+    """max(1, log2Up(sigma)) (wavelet/levelWT/WT.C:53)."""
     a, b = 0, int(sigma) - 1
     while b > 0:
         b >>= 1
@@ -398,7 +398,7 @@ class WaveletTree:
 
 def WT(s, sigma, index_bytes=4):
     """levelWT's WT(s, n, sigma): returns (nodes [2*sigma, 5], bits) with
-    levels = max(1, log2Up(sigma)) (wavelet/levelWT/WT.C:86-270)."""
+    levels = max(1, log2Up(sigma)) (wavelet/levelWT/WT.C:43-227)."""
     t = WaveletTree(s, levels=levels_for_sigma(sigma), flags=0)
     try:
         return t.nodes(2 * int(sigma), index_bytes), t.bits()
@@ -530,7 +530,7 @@ def suffix_array_device(d_text, n, d_sa=0, d_bwt=0, stream=0):
 
 
 class FMIndex:
-    """FM-index core over a BWT (fm-index/par/WT.C:33-46: the wavelet tree of
+    """FM-index core over a BWT (fm-index/par/WT.C:33-45: the wavelet tree of
     s[SA[i]-1]): a GPU wavelet tree over the BWT's symbol codes
     (0..sigma-1), the C array, and backward-search counting on the GPU."""
 
