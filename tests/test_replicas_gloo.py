@@ -1,7 +1,10 @@
 """The multi-process path of bench.py on CPU: two gloo ranks, each building
 its own seeded sequence with the oracle (the GPU path shards the same way,
 one independent sequence per rank, no collective on the data path), joined
-by the job-time reduction (maximum over ranks) and the whole-job throughput."""
+by the job-time reduction (maximum over ranks) and the whole-job throughput;
+and two gloo ranks that each drive libwtg's C ABI in their own process
+(a real build checked against the oracle where a GPU is present, the
+no-GPU, argument and injected-allocation-failure paths otherwise)."""
 import os
 import socket
 
@@ -61,3 +64,68 @@ def test_two_gloo_ranks():
             assert job == pytest.approx(1.5)              # the slowest rank's time
             assert value == pytest.approx(2 * 3 * 1.0 / 1.5)  # both ranks' bytes over that time
             assert checks[0] != checks[1]                 # independent sequences
+
+
+def _libwtg_rank(rank, world, port, out):
+    import sys
+    for p in (ROOT, os.path.join(ROOT, "wavelet-suffix-fm-index_gb300")):
+        if p not in sys.path:
+            sys.path.insert(0, p)
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    import datagen
+    import wtg
+    from oracle import oracle as O
+    sym = datagen.exp_u32(1 << 15, seed=77 + rank)  # one sequence per rank
+    codes = []
+    try:  # argument check, before any device work
+        wtg.WaveletTree(sym, levels=25)
+    except wtg.WtgError as e:
+        codes.append(e.code)
+    checksum = 0
+    try:
+        wtg.inject_alloc_failure(1)
+        try:
+            wtg.WaveletTree(sym, levels=20)
+        except wtg.WtgError as e:
+            codes.append(e.code)  # ERR_OOM with a GPU, ERR_CUDA without
+        wtg.inject_alloc_failure(0)
+        t = wtg.WaveletTree(sym, levels=20)
+        bits = t.bits()
+        ref, _ = O.wt_build(sym, 20)
+        codes.append(0 if np.array_equal(bits, ref) else -1)
+        checksum = int(np.bitwise_xor.reduce(bits)) & 0xFFFFFFFF
+        t.free()
+    except wtg.WtgError as e:
+        codes.append(e.code)
+    finally:
+        wtg.inject_alloc_failure(0)
+    mine = torch.tensor(codes + [checksum], dtype=torch.int64)
+    gathered = [torch.zeros_like(mine) for _ in range(world)]
+    dist.all_gather(gathered, mine)
+    out[rank] = [g.tolist() for g in gathered]
+    dist.destroy_process_group()
+
+
+def test_two_gloo_ranks_through_libwtg():
+    ctx = mp.get_context("spawn")
+    port = _free_port()
+    has_gpu = torch.cuda.is_available()
+    with ctx.Manager() as m:
+        out = m.dict()
+        procs = [ctx.Process(target=_libwtg_rank, args=(r, 2, port, out)) for r in range(2)]
+        for p in procs:
+            p.start()
+        for p in procs:
+            p.join(300)
+            assert p.exitcode == 0
+        assert out[0] == out[1]  # both ranks see both ranks' results
+        for codes in out[0]:
+            assert codes[0] == 1  # ERR_INVALID: levels above 24
+            if has_gpu:
+                assert codes[1:3] == [2, 0]  # ERR_OOM injected, then an exact build
+            else:
+                assert codes[1:3] == [3, 3]  # ERR_CUDA: no GPU, no CPU fallback
+        if has_gpu:
+            assert out[0][0][-1] != out[0][1][-1]  # independent sequences

@@ -36,6 +36,8 @@
 
 namespace wtg {
 
+WTG_WAIT_LIMIT_SETTER(batch)
+
 constexpr int BATCH_LMAX = 4;
 constexpr int BATCH_SLOTS = (1 << BATCH_LMAX) - 1;  // (level, key) pairs
 constexpr uint32_t BATCH_INVALID = 0xFFFFFFFFu;

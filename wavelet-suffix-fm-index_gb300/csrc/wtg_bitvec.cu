@@ -25,6 +25,8 @@
 
 namespace wtg {
 
+WTG_WAIT_LIMIT_SETTER(bitvec)
+
 constexpr int BV_THREADS = 256;  // one 512-bit superblock per thread
 
 __device__ __forceinline__ uint64_t warp_max_u64(uint64_t v) {
@@ -54,6 +56,7 @@ __global__ void __launch_bounds__(BV_THREADS)
   if (threadIdx.x == 0) s_tile = atomicAdd(counter, 1u);
   __syncthreads();
   const uint32_t tile = s_tile;
+  if (tile >= gridDim.x) return;  // only when the counter did not start at 0 (a stalled pass)
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, g8 = lane & 7;
   const uint64_t wbase = (uint64_t)tile * (BVT_ITER * BV_THREADS);
   const uint64_t tailmask = (size & 63) ? ((1ull << (size & 63)) - 1) : ~0ull;
@@ -471,6 +474,10 @@ int bv_pass(BvSupport& bv, uint32_t* d_err, cudaStream_t s) {
   if (tiles > 0x7fffffffull) return fail(WTG_ERR_INVALID, "bitvector too large");
   if ((rc = bv.status.ensure((tiles + 1) * sizeof(uint64_t), s))) return rc;
   WTG_CK(cudaMemsetAsync(bv.status.p, 0, (tiles + 1) * sizeof(uint64_t), s));
+  if (test_take_lookback_stall()) {  // tile 0 is never taken: every look-back wait on it runs out
+    static const uint32_t one = 1;
+    WTG_CK(cudaMemcpyAsync(bv.status.p, &one, sizeof(one), cudaMemcpyHostToDevice, s));
+  }
   prof_begin(PROF_BVPASS, s);
   bv_pass_kernel<<<(unsigned)tiles, BV_THREADS, 0, s>>>(
       bv.words, size, W, NB, bv.flags, bv.rank.as<uint64_t>(), bv.samples.as<uint32_t>(), samp_n - 1,

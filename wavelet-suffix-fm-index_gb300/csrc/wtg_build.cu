@@ -44,6 +44,8 @@
 
 namespace wtg {
 
+WTG_WAIT_LIMIT_SETTER(build)
+
 constexpr int LV_THREADS = 256;
 // chunk-group buffers per warp (prefetch depth + 1)
 template <bool SCATTER>

@@ -10,6 +10,8 @@
 
 namespace wtg {
 
+WTG_WAIT_LIMIT_SETTER(core)
+
 static thread_local std::string g_last_error;
 std::atomic<uint64_t> g_launches{0};
 
@@ -45,10 +47,34 @@ static int ensure_pool_setup() {
   return WTG_OK;
 }
 
+// ------------------------------------------------------- test hooks
+// Failure injection on the host side only: an armed countdown makes one
+// device allocation report WTG_ERR_OOM, and an armed stall makes the next
+// rank/select pass's look-back waits run out (see wtg_internal.cuh).
+static std::atomic<int64_t> g_alloc_fail_countdown{0};
+static std::atomic<int> g_lookback_stall{0};
+
+void test_arm_alloc_failure(int64_t nth) { g_alloc_fail_countdown.store(nth > 0 ? nth : 0); }
+void test_arm_lookback_stall(int on) { g_lookback_stall.store(on ? 1 : 0); }
+
+bool test_take_alloc_failure() {
+  int64_t c = g_alloc_fail_countdown.load();
+  while (c > 0)
+    if (g_alloc_fail_countdown.compare_exchange_weak(c, c - 1)) return c == 1;
+  return false;
+}
+
+bool test_take_lookback_stall() {
+  int armed = 1;
+  return g_lookback_stall.compare_exchange_strong(armed, 0);
+}
+
 int DevBuf::ensure(size_t need, cudaStream_t s) {
   if (need <= bytes && p) return WTG_OK;
   int rc = ensure_pool_setup();
   if (rc) return rc;
+  // an injected failure leaves the buffer as it was, like a failed cudaMallocAsync
+  if (test_take_alloc_failure()) return fail(WTG_ERR_OOM, "device allocation failed (injected by wtg_test_fail_alloc)");
   if (p) {
     cudaFreeAsync(p, s);
     p = nullptr;

@@ -139,6 +139,33 @@ __device__ __forceinline__ uint64_t packed_word(uint64_t q, uint32_t w, uint64_t
 // multiple of 16.  Every wait is bounded.
 
 constexpr uint32_t MBAR_SPIN_LIMIT = 1u << 24;
+constexpr uint32_t LB_SPIN_LIMIT = 1u << 22;  // ~ seconds with the look-back backoff below
+
+// Limits of the bounded device waits: [0] look-back spins, [1] mbarrier
+// tries.  Every translation unit that waits holds its own copy (the library
+// is built without relocatable device code); wtg_set_wait_limits rewrites
+// them all through the setters declared below, for the current device.
+static __constant__ uint32_t c_wait_limit[2] = {LB_SPIN_LIMIT, MBAR_SPIN_LIMIT};
+#define WTG_WAIT_LIMIT_SETTER(name)                                                    \
+  int set_wait_limits_##name(const uint32_t lim[2]) {                                   \
+    cudaError_t e = cudaMemcpyToSymbol(c_wait_limit, lim, 2 * sizeof(uint32_t));        \
+    return e == cudaSuccess ? (int)WTG_OK : cuda_fail(e, "cudaMemcpyToSymbol(wait limits)"); \
+  }
+int set_wait_limits_build(const uint32_t lim[2]);
+int set_wait_limits_batch(const uint32_t lim[2]);
+int set_wait_limits_bitvec(const uint32_t lim[2]);
+int set_wait_limits_core(const uint32_t lim[2]);
+
+// Host-side failure injection for the tests (no device fault is ever made):
+// test_take_alloc_failure() is true for the one device allocation the armed
+// countdown selects (DevBuf::ensure then reports WTG_ERR_OOM);
+// test_take_lookback_stall() is true once after arming, and the rank/select
+// pass then starts its tile counter at 1, so tile 0 never publishes and the
+// other tiles' bounded look-back waits run out.
+bool test_take_alloc_failure();
+bool test_take_lookback_stall();
+void test_arm_alloc_failure(int64_t nth);
+void test_arm_lookback_stall(int on);
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -181,7 +208,9 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 
 // waits for phase `parity` of bar to complete; false (and err set) on timeout
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t* err) {
-  for (uint32_t k = 0; k < MBAR_SPIN_LIMIT; ++k)
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint32_t limit = c_wait_limit[1];
+  for (uint32_t k = 1; k < limit; ++k)
     if (mbar_try_wait(bar, parity)) return true;
   atomicCAS(err, 0u, (uint32_t)DERR_LOOKBACK_TIMEOUT);
   return false;
@@ -200,7 +229,6 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32
 constexpr uint64_t LB_FLAG_AGG = 1ull << 62;
 constexpr uint64_t LB_FLAG_INC = 2ull << 62;
 constexpr uint64_t LB_VALUE_MASK = (1ull << 62) - 1;
-constexpr uint32_t LB_SPIN_LIMIT = 1u << 22;  // ~ seconds with the backoff below
 
 __device__ __forceinline__ void lb_publish(uint64_t* status, uint32_t tile, uint64_t flag, uint64_t v) {
   __threadfence();
@@ -224,7 +252,7 @@ __device__ __forceinline__ uint64_t lb_lookback_warp(uint64_t* status, uint32_t 
       uint32_t spins = 0, ns = 32;
       s = lb_load(status, (uint64_t)j);
       while ((s >> 62) == 0) {
-        if (++spins > LB_SPIN_LIMIT) {
+        if (++spins > c_wait_limit[0]) {
           atomicCAS(err, 0u, (uint32_t)DERR_LOOKBACK_TIMEOUT);
           s = LB_FLAG_INC;  // give up: treat as an inclusive zero
           break;
