@@ -346,6 +346,49 @@ int wtg_lsel_query_device(wtg_lsel* m, int t_b, const uint64_t* d_level, const u
 int wtg_profile_enable(int on);
 int wtg_profile_read(uint64_t launches[WTG_PROF_CLASSES], double ms[WTG_PROF_CLASSES]);
 
+/* ---------------------------------------------- sdsl serialize() streams
+ * The byte streams sdsl's serialize() writes (what sdsl::store_to_file puts
+ * in a file), so that sdsl consumers load GPU-built structures with their
+ * own load(), and so that outputs compare byte for byte as the reference's
+ * own check does (wt_int/compareResults.py:1-15).
+ * wtg_tree_serialize: wt_int<>::serialize (wt_int/wt_int_par.hpp:887-899):
+ *   size (u64), sigma (u64, the non-empty leaves), the level bit_vector, the
+ *   rank_support_v, select_support_mcl<1>, select_support_mcl<0>, max_level
+ *   (u32) -- needs a tree built with WTG_ALL.
+ * wtg_bv_serialize: part WTG_RANK gives rank_support_v<1>::serialize
+ *   (rank/rank_support_v_par.hpp:154-164), WTG_SELECT1 / WTG_SELECT0
+ *   select_support_mcl<1/0>::serialize (select/select_support_mcl_par.hpp:
+ *   644-681).
+ * Each int_vector inside is its size in bits (u64), its width (one byte, for
+ * run-time widths only) and its ceil(bits/64) words.  With dst == NULL only
+ * *len is set; otherwise dst (host memory) must hold cap >= *len bytes.
+ * wtg_tree_sigma: wt_int's sigma, the number of non-empty leaves. */
+int wtg_tree_serialize(wtg_tree* t, void* dst, uint64_t cap, uint64_t* len);
+int wtg_tree_sigma(wtg_tree* t, uint64_t* sigma);
+int wtg_bv_serialize(wtg_bv* b, uint32_t part, void* dst, uint64_t cap, uint64_t* len);
+
+/* ----------------------------------------------- failure handling knobs
+ * No counterpart in the reference (its CPU code has no device waits; its
+ * error sites throw std::logic_error, wt_int/wt_int_par.hpp:377,645).
+ *
+ * Every device-side wait of the builds is bounded: a decoupled look-back
+ * spins at most `lookback_spins` times (with a backoff of up to 1 us each,
+ * default 2^22: seconds), an mbarrier wait tries at most `mbarrier_tries`
+ * times (default 2^24).  On expiry the kernel records the failure and
+ * returns, and the build's sync reports WTG_ERR_TIMEOUT; the context stays
+ * usable.  wtg_set_wait_limits changes both limits for later launches on the
+ * current device (0 restores a default).
+ *
+ * Test hooks, host side only (they never make a device fault):
+ * wtg_test_fail_alloc(k), k >= 1, makes the k-th next device allocation of
+ * the library fail with WTG_ERR_OOM (0 disarms); wtg_test_stall_lookback(1)
+ * makes the next rank/select pass over a caller bitvector start its tile
+ * counter at 1, so tile 0 never publishes its count and the other tiles'
+ * look-back waits run out (WTG_ERR_TIMEOUT). */
+int wtg_set_wait_limits(uint32_t lookback_spins, uint32_t mbarrier_tries);
+int wtg_test_fail_alloc(int64_t nth);
+int wtg_test_stall_lookback(int on);
+
 /* --------------------------------------------------------------- helpers */
 /* Alphabet remap of levelWT/WTTime.C:80-94: every symbol becomes its rank
  * among the distinct values present; *sigma_out = number of distinct values.

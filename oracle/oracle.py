@@ -7,6 +7,7 @@ baseline -- never as the product path.
 """
 import ctypes
 import os
+import struct
 import subprocess
 
 import numpy as np
@@ -120,11 +121,13 @@ def wt_words(n, levels):
     return (n * levels + 63) // 64
 
 
-def wt_build(sym, levels, n_nodes=None, serial=False):
-    """levelWT (or serialWT) build. Returns (words u64[], nodes u64[n_nodes,5] or None)."""
+def wt_build(sym, levels, n_nodes=None, serial=False, tail=False):
+    """levelWT (or serialWT) build. Returns (words u64[], nodes u64[n_nodes,5] or None).
+    With tail=True the words carry one extra zero word (the padding word
+    rank_support_v reads past a bitvector whose size is a multiple of 512)."""
     sym = np.ascontiguousarray(sym)
     n = sym.size
-    words = np.zeros(max(wt_words(n, levels), 1), dtype=np.uint64)
+    words = np.zeros(max(wt_words(n, levels), 1) + (1 if tail else 0), dtype=np.uint64)
     nodes = None
     if n_nodes:
         nodes = np.zeros((n_nodes, 5), dtype=np.uint64)
@@ -132,7 +135,7 @@ def wt_build(sym, levels, n_nodes=None, serial=False):
     rc = fn(_p(sym), sym.dtype.itemsize, n, levels, _p(words), _p(nodes), n_nodes or 0)
     if rc != 0:
         raise RuntimeError(f"oracle wt build failed rc={rc}")
-    return words[: wt_words(n, levels)], nodes
+    return words[: wt_words(n, levels) + (1 if tail else 0)], nodes
 
 
 def remap_alphabet(sym):
@@ -278,6 +281,63 @@ def wt_expand_ranges(tree, rtbl, node, ranges):
     return left, right
 
 
+# ------------------------------------------------------ sdsl serialize()
+# The byte streams of sdsl's serialize(), restated from the reference's
+# members (wt_int/wt_int_par.hpp:887-899, rank/rank_support_v_par.hpp:154-164,
+# select/select_support_mcl_par.hpp:644-681) and sdsl's int_vector format:
+# size in bits (u64), width (u8, run-time widths only), ceil(bits/64) words.
+
+
+def _iv(bits, words, width=None):
+    head = struct.pack("<Q", int(bits)) + (b"" if width is None else struct.pack("<B", int(width)))
+    w = np.ascontiguousarray(words, dtype="<u8")[: (int(bits) + 63) // 64]
+    return head + w.tobytes()
+
+
+def serialize_rank(tbl):
+    """rank_support_v<1>::serialize: m_basic_block as an int_vector<64>."""
+    return np.frombuffer(_iv(np.asarray(tbl).size * 64, tbl), dtype=np.uint8)
+
+
+def serialize_select(sel):
+    """select_support_mcl<t_b>::serialize of a Select (or RefSelect) built here."""
+    out = [struct.pack("<Q", sel.arg_cnt)]
+    if sel.arg_cnt:
+        nsb = sel.nsb
+        out.append(_iv(nsb * sel.logn, sel.sb_words, sel.logn))
+        desc = np.asarray(sel.desc, dtype=np.uint64)
+        if sel.has_long:
+            mini = np.zeros((nsb + 63) // 64 * 64, dtype=bool)
+            mini[:nsb] = ((desc >> np.uint64(7)) & np.uint64(1)) == 0
+            out.append(_iv(nsb, np.packbits(mini, bitorder="little").view(np.uint64)))
+        else:
+            out.append(_iv(0, np.zeros(0, np.uint64)))
+        pool = np.asarray(sel.pool, dtype=np.uint64)
+        for d in desc.tolist():
+            w, at = d & 0x7F, d >> 8
+            entries = 4096 if (d >> 7) & 1 else 64
+            out.append(_iv(entries * w, pool[at: at + entries * w // 64], w))
+    return np.frombuffer(b"".join(out), dtype=np.uint8)
+
+
+def serialize_wt_int(sym, levels):
+    """wt_int<>(sym, n, levels)::serialize, built with this oracle."""
+    sym = np.ascontiguousarray(sym)
+    n = sym.size
+    if n == 0:  # the constructor returns before building anything
+        b = struct.pack("<QQ", 0, 0) + _iv(0, []) + _iv(0, []) + struct.pack("<QQI", 0, 0, 0)
+        return np.frombuffer(b, dtype=np.uint8)
+    w, _ = wt_build(sym, levels, tail=True)
+    size = n * levels
+    mask = (1 << levels) - 1
+    sigma = np.unique(sym.astype(np.uint64) & np.uint64(mask)).size
+    parts = [struct.pack("<QQ", n, sigma), _iv(size, w),
+             serialize_rank(rank_build(w, size)).tobytes(),
+             serialize_select(Select(w, size, 1)).tobytes(), serialize_select(Select(w, size, 0)).tobytes(),
+             struct.pack("<I", levels)]
+    return np.frombuffer(b"".join(parts), dtype=np.uint8)
+
+
 # ---------------------------------------------------------------- reference
 
 _ref_libs = {}
@@ -380,6 +440,10 @@ def _ref_rank_select():
         L.ref_select_query.argtypes = [vp, u64]
         L.ref_select_query.restype = u64
         L.ref_select_free.argtypes = [vp]
+        L.ref_rank_serialize.argtypes = [vp, u64, vp, u64]
+        L.ref_rank_serialize.restype = u64
+        L.ref_select_serialize.argtypes = [vp, vp, u64]
+        L.ref_select_serialize.restype = u64
         _ref_rs = L
     return _ref_rs
 
@@ -391,6 +455,16 @@ def ref_rank_build(words, size_bits):
     if _ref_rank_select().ref_rank_build(_p(words), size_bits, _p(tbl), tbl.size) != 0:
         raise RuntimeError("reference rank table size mismatch")
     return tbl
+
+
+def ref_rank_serialize(words, size_bits):
+    """The reference's rank_support_v<1>::serialize stream."""
+    words = np.ascontiguousarray(words, dtype=np.uint64)
+    L = _ref_rank_select()
+    n = L.ref_rank_serialize(_p(words), size_bits, None, 0)
+    out = np.zeros(n, dtype=np.uint8)
+    L.ref_rank_serialize(_p(words), size_bits, _p(out), n)
+    return out
 
 
 class RefSelect:
@@ -414,6 +488,14 @@ class RefSelect:
 
     def query(self, i):
         return _ref_rank_select().ref_select_query(self.h, int(i))
+
+    def serialize(self):
+        """The reference's select_support_mcl::serialize stream."""
+        L = _ref_rank_select()
+        n = L.ref_select_serialize(self.h, None, 0)
+        out = np.zeros(n, dtype=np.uint8)
+        L.ref_select_serialize(self.h, _p(out), n)
+        return out
 
     def __del__(self):
         try:
@@ -452,6 +534,10 @@ def _ref_wt_int():
         L.ref_wtint_range_search_2d.restype = u64
         L.ref_wtint_expand.argtypes = [vp, vp, vp, vp]
         L.ref_wtint_expand_ranges.argtypes = [vp, vp, vp, u64, vp, vp]
+        L.ref_wtint_serialize.argtypes = [vp, vp, u64]
+        L.ref_wtint_serialize.restype = u64
+        L.ref_wtint_load.argtypes = [vp, u64]
+        L.ref_wtint_load.restype = vp
         _ref_wi = L
     return _ref_wi
 
@@ -460,10 +546,17 @@ class RefWtInt:
     """The reference's own sdsl::wt_int (wt_int/wt_int_par.hpp), built by its
     constructor and queried through its member functions."""
 
-    def __init__(self, sym, max_level):
+    def __init__(self, sym, max_level, stream=None):
         L = _ref_wt_int()
-        self.sym = np.ascontiguousarray(sym)
-        self.h = L.ref_wtint_new(_p(self.sym), self.sym.dtype.itemsize, self.sym.size, max_level)
+        if stream is not None:  # wt_int::load of a serialized stream
+            self.sym = None
+            b = np.ascontiguousarray(stream, dtype=np.uint8)
+            self.h = L.ref_wtint_load(_p(b), b.size)
+            if not self.h:
+                raise RuntimeError("reference wt_int::load failed")
+        else:
+            self.sym = np.ascontiguousarray(sym)
+            self.h = L.ref_wtint_new(_p(self.sym), self.sym.dtype.itemsize, self.sym.size, max_level)
         if not self.h:
             raise RuntimeError("reference wt_int constructor failed")
         info = np.zeros(4, dtype=np.uint64)
@@ -472,6 +565,19 @@ class RefWtInt:
         self.bits = np.zeros(max(nw, 1), dtype=np.uint64)
         L.ref_wtint_bits(self.h, _p(self.bits))
         self.bits = self.bits[:nw]
+
+    @classmethod
+    def load(cls, stream):
+        """The reference's wt_int::load of a serialized stream."""
+        return cls(None, 0, stream=stream)
+
+    def serialize(self):
+        """The reference's wt_int::serialize stream (uint8 array)."""
+        L = _ref_wt_int()
+        n = L.ref_wtint_serialize(self.h, None, 0)
+        out = np.zeros(n, dtype=np.uint8)
+        L.ref_wtint_serialize(self.h, _p(out), n)
+        return out
 
     def access(self, i):
         return int(_ref_wt_int().ref_wtint_access(self.h, int(i)))

@@ -53,6 +53,7 @@ struct sel_any {
   virtual void info(uint64_t* out) = 0;
   virtual void copy(uint64_t* sb_words, uint64_t* desc, uint64_t* pool) = 0;
   virtual uint64_t query(uint64_t i) = 0;
+  virtual std::string serialize() = 0;
 };
 
 template <uint8_t t_b>
@@ -95,7 +96,17 @@ struct sel_impl : sel_any {
     }
   }
   uint64_t query(uint64_t i) override { return ss->select(i); }
+  std::string serialize() override {
+    std::ostringstream os;
+    ss->serialize(os);
+    return os.str();
+  }
 };
+
+uint64_t emit(const std::string& b, uint8_t* dst, uint64_t cap) {
+  if (dst && cap >= b.size()) memcpy(dst, b.data(), b.size());
+  return b.size();
+}
 
 }  // namespace
 
@@ -126,4 +137,20 @@ void ref_select_copy(void* h, uint64_t* sb_words, uint64_t* desc, uint64_t* pool
 }
 uint64_t ref_select_query(void* h, uint64_t i) { return ((sel_any*)h)->query(i); }
 void ref_select_free(void* h) { delete (sel_any*)h; }
+
+// rank_support_v::serialize (rank/rank_support_v_par.hpp:154-164) of the
+// table over the first `size` bits of `words`; returns the stream length and
+// fills dst when cap suffices (dst may be NULL)
+uint64_t ref_rank_serialize(const uint64_t* words, uint64_t size, uint8_t* dst, uint64_t cap) {
+  sdsl::bit_vector bv = make_bv(words, size);
+  sdsl::rank_support_v<1, 1> rs(&bv);
+  std::ostringstream os;
+  rs.serialize(os);
+  return emit(os.str(), dst, cap);
+}
+
+// select_support_mcl::serialize (select/select_support_mcl_par.hpp:644-681)
+uint64_t ref_select_serialize(void* h, uint8_t* dst, uint64_t cap) {
+  return emit(((sel_any*)h)->serialize(), dst, cap);
+}
 }

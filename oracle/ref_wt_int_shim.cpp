@@ -15,7 +15,9 @@
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
+#include <sstream>
 #include <stdexcept>
+#include <string>
 #include <tuple>
 #include <vector>
 
@@ -66,6 +68,29 @@ void* ref_wtint_new(const void* seq, int elem_bytes, uint64_t n, uint32_t max_le
 }
 
 void ref_wtint_free(void* h) { delete (wt_t*)h; }
+
+// wt_int::serialize (wt_int_par.hpp:887-899) into dst when it holds cap >=
+// the stream's length bytes; returns that length (dst may be NULL)
+uint64_t ref_wtint_serialize(void* h, uint8_t* dst, uint64_t cap) {
+  std::ostringstream os;
+  ((const wt_t*)h)->serialize(os);
+  const std::string b = os.str();
+  if (dst && cap >= b.size()) memcpy(dst, b.data(), b.size());
+  return b.size();
+}
+
+// wt_int::load (wt_int_par.hpp:902-911) from len bytes; NULL when the
+// stream ends early
+void* ref_wtint_load(const uint8_t* src, uint64_t len) {
+  std::istringstream is(std::string((const char*)src, len));
+  wt_t* w = new wt_t();
+  w->load(is);
+  if (is.fail()) {
+    delete w;
+    return nullptr;
+  }
+  return w;
+}
 
 // size, sigma, max_level, words of m_tree
 void ref_wtint_info(void* h, uint64_t* out) {

@@ -13,12 +13,16 @@
 //     capacity is a multiple of 512).
 //   * int_vector<0> has its width chosen at run time (default 64).
 //   * int_vector<64>::operator[] yields a real uint64_t&.
+//   * serialize() writes the size in bits as a uint64, then -- for the
+//     run-time width int_vector<0> only -- the width as one byte, then the
+//     ceil(bits/64) data words; load() reads the same stream.
 #ifndef WTG_SDSL_SHIM_INT_VECTOR
 #define WTG_SDSL_SHIM_INT_VECTOR
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
-#include <iosfwd>
+#include <istream>
+#include <ostream>
 #include <string>
 #include <type_traits>
 #include <utility>
@@ -174,10 +178,32 @@ class int_vector {
     std::swap(m_width, o.m_width);
   }
 
-  // Serialization is not exercised by the pin; declared so the reference
-  // headers compile.
-  size_type serialize(std::ostream&, structure_tree_node* = nullptr, std::string = "") const { return 0; }
-  void load(std::istream&) {}
+  size_type serialize(std::ostream& out, structure_tree_node* = nullptr, std::string = "") const {
+    const uint64_t bits = m_size;
+    out.write(reinterpret_cast<const char*>(&bits), sizeof(bits));
+    size_type written = sizeof(bits);
+    if (t_width == 0) {
+      const uint8_t w = m_width;
+      out.write(reinterpret_cast<const char*>(&w), 1);
+      written += 1;
+    }
+    const uint64_t nw = (bits + 63) >> 6;
+    if (nw) out.write(reinterpret_cast<const char*>(m_data), (std::streamsize)(nw * 8));
+    return written + nw * 8;
+  }
+  void load(std::istream& in) {
+    uint64_t bits = 0;
+    in.read(reinterpret_cast<char*>(&bits), sizeof(bits));
+    if (t_width == 0) {
+      uint8_t w = 64;
+      in.read(reinterpret_cast<char*>(&w), 1);
+      m_width = w;
+    }
+    free(m_data);
+    alloc(bits);
+    const uint64_t nw = (bits + 63) >> 6;
+    if (nw) in.read(reinterpret_cast<char*>(m_data), (std::streamsize)(nw * 8));
+  }
 };
 
 typedef int_vector<1> bit_vector;

@@ -944,6 +944,53 @@ int wtg_batch_tuning(wtg_batch* B, int* threads, int* items_per_thread, float ms
   return batch_tuning(*B->b, threads, items_per_thread, ms, 8);
 }
 
+// ------------------------------------------------ sdsl serialize() streams
+
+int wtg_tree_serialize(wtg_tree* T, void* dst, uint64_t cap, uint64_t* len) {
+  if (!T || !len) return fail(WTG_ERR_INVALID, "null argument");
+  int rc = tree_serialize(T->t, (uint8_t*)dst, cap, len);
+  if (rc) return rc;
+  return dst ? sync_and_check(T->t.stream, T->t.err.as<uint32_t>()) : WTG_OK;
+}
+
+int wtg_tree_sigma(wtg_tree* T, uint64_t* sigma) {
+  if (!T || !sigma) return fail(WTG_ERR_INVALID, "null argument");
+  int rc = tree_leaf_count(T->t, sigma, T->t.stream);
+  if (rc) return rc;
+  return sync_and_check(T->t.stream, T->t.err.as<uint32_t>());
+}
+
+int wtg_bv_serialize(wtg_bv* B, uint32_t part, void* dst, uint64_t cap, uint64_t* len) {
+  if (!B || !len) return fail(WTG_ERR_INVALID, "null argument");
+  int rc = bv_serialize(B->bv, part, (uint8_t*)dst, cap, len, B->stream);
+  if (rc) return rc;
+  return dst ? sync_and_check(B->stream, B->err.as<uint32_t>()) : WTG_OK;
+}
+
+// ------------------------------------------------ failure handling knobs
+
+int wtg_set_wait_limits(uint32_t lookback_spins, uint32_t mbarrier_tries) {
+  int rc;
+  if ((rc = check_device())) return rc;
+  const uint32_t lim[2] = {lookback_spins ? lookback_spins : LB_SPIN_LIMIT,
+                           mbarrier_tries ? mbarrier_tries : MBAR_SPIN_LIMIT};
+  if ((rc = set_wait_limits_build(lim))) return rc;
+  if ((rc = set_wait_limits_batch(lim))) return rc;
+  if ((rc = set_wait_limits_bitvec(lim))) return rc;
+  return set_wait_limits_core(lim);
+}
+
+int wtg_test_fail_alloc(int64_t nth) {
+  if (nth < 0) return fail(WTG_ERR_INVALID, "nth must be >= 0");
+  test_arm_alloc_failure(nth);
+  return WTG_OK;
+}
+
+int wtg_test_stall_lookback(int on) {
+  test_arm_lookback_stall(on);
+  return WTG_OK;
+}
+
 // ------------------------------------------------------------------ helpers
 
 int wtg_remap_alphabet(void* seq, uint64_t n, int elem_bytes, uint64_t* sigma_out) {

@@ -138,6 +138,12 @@ cudaStream_t batch_stream(const BatchImpl& b);
 uint64_t batch_total_symbols(const BatchImpl& b);
 int batch_tuning(const BatchImpl& b, int* threads, int* ipt, float* ms, int nms);
 
+// sdsl serialize() streams (wtg_serialize.cu): with dst NULL only *len is
+// set; otherwise dst (host memory, cap bytes) receives the stream
+int tree_leaf_count(TreeImpl& t, uint64_t* sigma, cudaStream_t s);
+int tree_serialize(TreeImpl& t, uint8_t* dst, uint64_t cap, uint64_t* len);
+int bv_serialize(BvSupport& bv, uint32_t part, uint8_t* dst, uint64_t cap, uint64_t* len, cudaStream_t s);
+
 // alphabet remap (levelWT/WTTime.C:80-94) on a device sequence, in place
 int remap_alphabet_device(void* d_seq, uint64_t n, int eb, uint64_t* sigma, DevBuf& tmp, DevBuf& scan_tmp,
                           uint32_t* d_err, cudaStream_t s);

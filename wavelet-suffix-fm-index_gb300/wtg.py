@@ -117,6 +117,12 @@ _SIGS = {
     "wtg_rank_build_noalloc": ([vp, u64, vp, vp], i32),
     "wtg_profile_enable": ([i32], i32),
     "wtg_profile_read": ([vp, vp], i32),
+    "wtg_tree_serialize": ([vp, vp, u64, vp], i32),
+    "wtg_tree_sigma": ([vp, vp], i32),
+    "wtg_bv_serialize": ([vp, ctypes.c_uint32, vp, u64, vp], i32),
+    "wtg_set_wait_limits": ([ctypes.c_uint32, ctypes.c_uint32], i32),
+    "wtg_test_fail_alloc": ([ctypes.c_int64], i32),
+    "wtg_test_stall_lookback": ([i32], i32),
 }
 
 
@@ -147,6 +153,22 @@ def _ck(rc):
 
 def launch_count():
     return int(lib().wtg_launch_count())
+
+
+def set_wait_limits(lookback_spins=0, mbarrier_tries=0):
+    """Limits of the bounded device waits on the current device (0: default)."""
+    _ck(lib().wtg_set_wait_limits(int(lookback_spins), int(mbarrier_tries)))
+
+
+def inject_alloc_failure(nth):
+    """Test hook: the nth next device allocation fails with ERR_OOM (0 disarms)."""
+    _ck(lib().wtg_test_fail_alloc(int(nth)))
+
+
+def inject_lookback_stall(on=True):
+    """Test hook: the next rank/select pass over a caller bitvector never
+    publishes its first tile, so its look-back waits run out (ERR_TIMEOUT)."""
+    _ck(lib().wtg_test_stall_lookback(1 if on else 0))
 
 
 PROF_CLASSES = ("level", "level_last", "hist", "tables", "bvpass", "select")
@@ -384,6 +406,20 @@ class WaveletTree:
     def rank_device(self, d_idx, d_sym, nq, d_out, stream=0):
         _ck(lib().wtg_query_rank_device(self.h, vp(d_idx), vp(d_sym), nq, vp(d_out), vp(stream)))
 
+    def serialize(self):
+        """sdsl wt_int<>::serialize stream of the tree (uint8 array)."""
+        n = ctypes.c_uint64(0)
+        _ck(lib().wtg_tree_serialize(self.h, None, 0, ctypes.byref(n)))
+        out = np.empty(n.value, dtype=np.uint8)
+        _ck(lib().wtg_tree_serialize(self.h, _p(out), out.size, ctypes.byref(n)))
+        return out
+
+    def sigma(self):
+        """wt_int's sigma: the number of non-empty leaves."""
+        v = ctypes.c_uint64(0)
+        _ck(lib().wtg_tree_sigma(self.h, ctypes.byref(v)))
+        return int(v.value)
+
     def level_select(self, level, k, t_b=1):
         """Position inside level `level` of its k-th one (t_b=1) or zero
         (t_b=0) through select_support_mcl (wt_int_par.hpp:651-656)."""
@@ -448,6 +484,15 @@ class BitVectorSupport:
         idx = _u64(idx)
         out = np.zeros(idx.size, dtype=np.uint64)
         _ck(lib().wtg_bv_rank(self.h, _p(idx), idx.size, _p(out)))
+        return out
+
+    def serialize(self, part):
+        """sdsl serialize() stream of one support: part RANK gives
+        rank_support_v, SELECT1 / SELECT0 select_support_mcl<1> / <0>."""
+        n = ctypes.c_uint64(0)
+        _ck(lib().wtg_bv_serialize(self.h, part, None, 0, ctypes.byref(n)))
+        out = np.empty(n.value, dtype=np.uint8)
+        _ck(lib().wtg_bv_serialize(self.h, part, _p(out), out.size, ctypes.byref(n)))
         return out
 
     def select(self, i, t_b=1):
