@@ -15,9 +15,12 @@ The algorithmic bytes of one build are
   + [L*n/8 + 16*((L*n>>9)+1)] (rank: read bits, write table)
   + 2 * [L*n/8 + select sample bytes written] (select1, select0).
 
---impl reference times the reference algorithm on the host cores instead (the
-CPU restatement of levelWT + rank_support_v_par + select_support_mcl_par, all
-threads), on a bounded sample per step.
+--impl reference times the reference's own CPU code on the host cores instead:
+levelWT's WT() (-DLONG -DINT, OpenMP) and rank_support_v_par +
+select_support_mcl_par<1>/<0> (OpenMP), built from the reference's sources by
+oracle/Makefile (bench-ref), on a bounded sample of the workload per step; where
+those builds are absent it times the oracle's restatement of the same code
+("kind": "port").
 
 Run: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl wtg|reference]
 Multi-GPU (torchrun): every rank builds its own independent sequence; no
@@ -147,6 +150,28 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+def workload_config(n, world):
+    """The `config` of both arms' lines (the workload, not the sample)."""
+    return {"workload": WORKLOAD, "n": n, "levels": LEVELS, "sigma": 1 << LEVELS, "elem_bytes": 4,
+            "l2": "inputs larger than L2 (4 GiB per level pass, 2.5 GiB of bits)",
+            "parallelism": f"replicas x{world} (independent sequences)"}
+
+
+def cpu_reference_seconds(n):
+    """One build of an n-symbol sample of the workload by the reference's own
+    code (levelWT WT() with -DLONG -DINT, then rank_support_v_par and
+    select_support_mcl_par<1>/<0> over its bits, all OpenMP threads).
+    Returns (seconds, algorithmic bytes, cores), or None where the
+    reference's builders are not built."""
+    import datagen
+    from oracle import oracle as O
+    if O.ref_bench() is None:
+        return None
+    sym = datagen.exp_u32(n, mean=MEAN, cap=CAP, seed=SEED)
+    t_wt, t_r, t_s1, t_s0, sel_words = O.ref_bench_times(sym, LEVELS)
+    return t_wt + t_r + t_s1 + t_s0, algorithmic_bytes(n, LEVELS, 4, sel_words), O.num_threads()
+
+
 def cpu_build_seconds(n, threads_note=True):
     """One full CPU build (oracle restatement, all OpenMP threads) of an n-symbol
     sample of the workload; returns (seconds, sample bytes, cores)."""
@@ -168,23 +193,27 @@ def run_reference(args, rank):
     if rank != 0:
         return
     from oracle import oracle as O
-    O.build(ref=False)
+    O.build(ref=True)
     n = 1 << args.cpu_log2
+    kind = "reference" if O.ref_bench() is not None else "port"
+    timed = cpu_reference_seconds if kind == "reference" else cpu_build_seconds
     for _ in range(args.warmup):
-        cpu_build_seconds(n)
+        timed(n)
     tot_t, tot_b, cores = 0.0, 0.0, 1
     for _ in range(args.steps):
-        dt, b, cores = cpu_build_seconds(n)
+        dt, b, cores = timed(n)
         tot_t += dt
         tot_b += b
     gbs = tot_b / tot_t / 1e9
-    sample = f"n=2^{args.cpu_log2} uint32 symbols of the same distribution, 20 levels, full build per step"
+    what = ("the reference's levelWT WT() (-DLONG -DINT) + rank_support_v_par + select_support_mcl_par<1>/<0>, "
+            "OpenMP" if kind == "reference" else "the oracle's restatement of levelWT + rank/select, OpenMP")
+    sample = f"n=2^{args.cpu_log2} uint32 symbols of the same distribution, 20 levels, one full build per step: {what}"
     line = {
         "impl": "reference", "metric": METRIC, "value": gbs, "unit": "GB/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "n": 1 << 30, "levels": LEVELS, "sample_n": n},
-        "cpu_baseline": {"value": gbs, "unit": "GB/s", "cores": cores, "kind": "port", "sample": sample},
+        "config": workload_config(1 << args.n_log2, 1),
+        "cpu_baseline": {"value": gbs, "unit": "GB/s", "cores": cores, "kind": kind, "sample": sample},
         "e2e": {"value": gbs, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -652,20 +681,29 @@ def run_wtg(args, rank, world, local_rank):
     cpu = None
     if not args.no_cpu:
         from oracle import oracle as O
-        O.build(ref=False)
+        O.build(ref=True)
         cn = 1 << args.cpu_log2
+        r = cpu_reference_seconds(cn)
+        if r is not None:
+            dt, b, cores = r
+            cpu = {"value": b / dt / 1e9, "unit": "GB/s", "cores": cores, "kind": "reference",
+                   "sample": f"n=2^{args.cpu_log2} of the same distribution, 20 levels, one full build ({dt:.2f} s) "
+                             "by the reference's levelWT WT() + rank_support_v_par + select_support_mcl_par, OpenMP"}
         dt, b, cores = cpu_build_seconds(cn)
-        cpu = {"value": b / dt / 1e9, "unit": "GB/s", "cores": cores, "kind": "port",
-               "sample": f"n=2^{args.cpu_log2} of the same distribution, 20 levels, one full build ({dt:.2f} s)"}
+        port = {"value": b / dt / 1e9, "unit": "GB/s", "cores": cores, "kind": "port",
+                "sample": f"n=2^{args.cpu_log2} of the same distribution, 20 levels, one full build ({dt:.2f} s) "
+                          "by the oracle's restatement, OpenMP"}
+        if cpu is None:
+            cpu = port
+        else:
+            cpu["port"] = port
 
     line = {
         "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "n": n, "levels": L, "sigma": 1 << L, "elem_bytes": 4,
-                   "algorithmic_bytes_per_step": step_bytes,
-                   "l2": "inputs larger than L2 (4 GiB per level pass, 2.5 GiB of bits)",
-                   "parallelism": f"replicas x{world} (independent sequences)"},
+        "config": workload_config(n, world),
+        "algorithmic_bytes_per_step": step_bytes,
         "hbm_frac": value / peak,
         "roofline": roofline,
         "kernel_time": kernel_share,
@@ -691,7 +729,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="wtg", choices=["wtg", "reference"])
     ap.add_argument("--n-log2", type=int, default=30)
-    ap.add_argument("--cpu-log2", type=int, default=27)
+    ap.add_argument("--cpu-log2", type=int, default=25,
+                    help="log2 of the CPU baseline's sample (the reference arm: at most 26)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-select", action="store_true")

@@ -24,13 +24,18 @@ NONE = np.uint64(0xFFFFFFFFFFFFFFFF)
 
 
 def build(ref=True):
-    """Compile the oracle (and, when the reference checkout exists, the
-    reference's own builders into _ref/)."""
+    """Compile the oracle; with ref=True also the reference's own builders:
+    the pins (_ref/libref_*.so, where the reference checkout exists) and the
+    timed CPU baseline (_ref/libref_bench_*.so, from the staged copy of the
+    reference's sources in _ref/src, which also builds where the checkout
+    does not exist)."""
     import shutil
     if shutil.which("make"):
         subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
         if ref and os.path.isdir(REF_SRC):
-            subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + REF_SRC], check=True)
+            subprocess.run(["make", "-s", "-C", HERE, "ref", "ref-src", "REF=" + REF_SRC], check=True)
+        if ref and os.path.isdir(os.path.join(REF_DIR, "src")):
+            subprocess.run(["make", "-s", "-C", HERE, "bench-ref"], check=True)
         return
     os.makedirs(os.path.join(HERE, "_build"), exist_ok=True)
     subprocess.run(["gcc", "-O2", "-fPIC", "-fopenmp", "-std=gnu11", "-shared", "-o", LIB_PATH,
@@ -383,6 +388,43 @@ def ref_divsufsort(s):
     if L.divsufsort(_p(s), _p(sa), s.size) != 0:
         raise RuntimeError("divsufsort failed")
     return sa[: s.size]
+
+
+_ref_bench = None
+
+
+def ref_bench():
+    """The reference's own CPU builders compiled for the timed baseline
+    (levelWT with -DLONG -DINT, rank_support_v_par and select_support_mcl_par,
+    all with OpenMP), or None where they were not built."""
+    global _ref_bench
+    if _ref_bench is None:
+        a = os.path.join(REF_DIR, "libref_bench_levelwt.so")
+        b = os.path.join(REF_DIR, "libref_bench_rs.so")
+        if not (os.path.exists(a) and os.path.exists(b)):
+            return None
+        wt, rs = ctypes.CDLL(a), ctypes.CDLL(b)
+        wt.ref_wt_time.argtypes = [vp, ctypes.c_int, u64, u64]
+        wt.ref_wt_time.restype = ctypes.c_double
+        rs.ref_rank_select_time.argtypes = [vp, u64, vp]
+        _ref_bench = (wt, rs)
+    return _ref_bench
+
+
+def ref_bench_times(sym, levels):
+    """Seconds of the reference's WT(s, n, 2^levels), and of its
+    rank_support_v / select_support_mcl<1> / <0> constructors over those
+    bits, for one sample; plus the select structures' words (for the
+    algorithmic bytes).  Returns (t_wt, t_rank, t_sel1, t_sel0, sel_words)."""
+    wt, rs = ref_bench()
+    sym = np.ascontiguousarray(sym)
+    t_wt = wt.ref_wt_time(_p(sym), sym.dtype.itemsize, sym.size, 1 << levels)
+    if t_wt < 0:
+        raise MemoryError("reference WT() sample")
+    w, _ = wt_build(sym, levels, tail=True)  # the same bits (pinned), to feed the supports
+    out = np.zeros(5)
+    rs.ref_rank_select_time(_p(w), sym.size * levels, _p(out))
+    return t_wt, out[0], out[1], out[2], int(out[3] + out[4])
 
 
 def ref_available(variant="levelwt_u8"):

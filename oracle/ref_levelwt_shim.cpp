@@ -8,6 +8,7 @@
 // The symbol and index widths follow the reference's own compile-time knobs:
 // -DINT makes symbols uintT, -DLONG makes uintT 64-bit (wavelet/levelWT/WT.h:24-43,
 // parallel.h:71-81).
+#include <chrono>
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
@@ -38,5 +39,24 @@ int ref_wt(const void* s, uint64_t n, uint64_t sigma, uint64_t* words, uint64_t 
   free(R.second);
   free(in);
   return 0;
+}
+
+// Seconds of one WT(s, n, sigma) call -- the timed CPU baseline.  The input
+// (n symbols of in_bytes bytes) is widened to the build's symbol type before
+// the clock starts; the outputs are freed after it stops.  Returns < 0 when
+// memory runs out.
+double ref_wt_time(const void* s, int in_bytes, uint64_t n, uint64_t sigma) {
+  symbol* in = (symbol*)malloc(sizeof(symbol) * (n ? n : 1));
+  if (!in) return -1.0;
+  for (uint64_t i = 0; i < n; ++i)
+    in[i] = in_bytes == 1 ? (symbol)((const uint8_t*)s)[i]
+            : in_bytes == 4 ? (symbol)((const uint32_t*)s)[i] : (symbol)((const uint64_t*)s)[i];
+  const auto t0 = std::chrono::steady_clock::now();
+  std::pair<WTnode*, long*> R = WT(in, (uintT)n, (uintT)sigma);
+  const auto t1 = std::chrono::steady_clock::now();
+  free(R.first);
+  free(R.second);
+  free(in);
+  return std::chrono::duration<double>(t1 - t0).count();
 }
 }

@@ -13,6 +13,7 @@
 // holding every long or mini block's int_vector<0> words in superblock order.
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cassert>
 #include <cstdint>
 #include <cstdlib>
@@ -62,6 +63,10 @@ struct sel_impl : sel_any {
   sdsl::select_support_mcl<t_b, 1>* ss;
   sel_impl(const uint64_t* words, uint64_t size) : bv(make_bv(words, size)) {
     ss = new sdsl::select_support_mcl<t_b, 1>(&bv);
+  }
+  // over a bit_vector the caller keeps alive (no copy)
+  sel_impl(const uint64_t*, uint64_t, const sdsl::bit_vector* ext) {
+    ss = new sdsl::select_support_mcl<t_b, 1>(ext);
   }
   ~sel_impl() { delete ss; }
   uint64_t nsb() const { return (ss->m_arg_cnt + 4095) >> 12; }
@@ -147,6 +152,31 @@ uint64_t ref_rank_serialize(const uint64_t* words, uint64_t size, uint8_t* dst, 
   std::ostringstream os;
   rs.serialize(os);
   return emit(os.str(), dst, cap);
+}
+
+// Seconds of the rank_support_v<1>, select_support_mcl<1> and
+// select_support_mcl<0> constructors over the first `size` bits of `words`
+// (the timed CPU baseline; the bit_vector is filled before the clock
+// starts): out = {t_rank, t_select1, t_select0, select1 words, select0
+// words}, the words being m_superblock's plus every block's.
+void ref_rank_select_time(const uint64_t* words, uint64_t size, double* out) {
+  sdsl::bit_vector bv = make_bv(words, size);
+  auto t0 = std::chrono::steady_clock::now();
+  { sdsl::rank_support_v<1, 1> rs(&bv); }
+  auto t1 = std::chrono::steady_clock::now();
+  out[0] = std::chrono::duration<double>(t1 - t0).count();
+  for (int t_b = 1; t_b >= 0; --t_b) {
+    sel_any* h = nullptr;
+    t0 = std::chrono::steady_clock::now();
+    if (t_b) h = new sel_impl<1>(words, size, &bv);
+    else h = new sel_impl<0>(words, size, &bv);
+    t1 = std::chrono::steady_clock::now();
+    uint64_t info[8];
+    h->info(info);
+    out[t_b ? 1 : 2] = std::chrono::duration<double>(t1 - t0).count();
+    out[t_b ? 3 : 4] = (double)(info[6] + info[4] + info[7]);
+    delete h;
+  }
 }
 
 // select_support_mcl::serialize (select/select_support_mcl_par.hpp:644-681)

@@ -10,10 +10,13 @@
 // range_search_2d(i, j-1, c/2, c) count and its points' position sum (2),
 // interval_symbols k and sum of its symbols (2), then four u64 checks of the
 // root's expand (left size + right size - n, left.level, right.sym, and the
-// expanded range sizes minus the range size).
+// expanded range sizes minus the range size).  The sdsl serialize() streams of
+// the wt_int, the rank_support_v and the select_support_mcl<1> go to
+// out.bin.wt_int, out.bin.rank and out.bin.sel1 (wtg::store_to_file).
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
+#include <string>
 #include <vector>
 
 #include "../../wavelet-suffix-fm-index_gb300/host/wtg_reference_api.hpp"
@@ -85,6 +88,11 @@ int main(int argc, char** argv) {
   std::fwrite(checks, sizeof(uint64_t), 3, o);
   std::fwrite(rq.data(), sizeof(uint64_t), rq.size(), o);
   std::fclose(o);
+  // sdsl streams, as store_to_file writes them: <out>.wt_int, .rank, .sel1
+  const std::string base(argv[4]);
+  if (!wtg::store_to_file(wt, base + ".wt_int") || !wtg::store_to_file(rs, base + ".rank") ||
+      !wtg::store_to_file(ss, base + ".sel1"))
+    return 5;
   std::free(r.first);
   std::free(r.second);
   return 0;

@@ -82,3 +82,8 @@ def test_cpp_program_matches_oracle(wtg, oracle, tmp_path, variant, kind, n):
         assert row[7] == cs.size and row[8] == int(cs.sum())
     left, _ = oracle.wt_expand(w, orank, n, [0, n, 0, 0])
     assert rq[-4] == 0 and rq[-3] == 1 and rq[-2] == 1 and rq[-1] == 0 and left[2] == 1
+    # sdsl streams written by store_to_file
+    out = str(tmp_path / "o.bin")
+    assert np.array_equal(np.fromfile(out + ".wt_int", dtype=np.uint8), oracle.serialize_wt_int(sym, L))
+    assert np.array_equal(np.fromfile(out + ".rank", dtype=np.uint8), oracle.serialize_rank(orank))
+    assert np.array_equal(np.fromfile(out + ".sel1", dtype=np.uint8), oracle.serialize_select(s1))

@@ -17,12 +17,17 @@
 //   * wtg::rank_support_v / wtg::select_support_mcl<t_b>
 //     (rank/rank_support_v_par.hpp:69-142, select/select_support_mcl_par.hpp:
 //     120-129,564-611) over a bit vector given as 64-bit words.
+//   * serialize(std::ostream&) on all three, writing sdsl's byte streams
+//     (wt_int_par.hpp:887-899, rank_support_v_par.hpp:154-164,
+//     select_support_mcl_par.hpp:644-681), and wtg::store_to_file.
 // Every call runs on the current CUDA device; failures other than the
 // reference's own exceptions raise std::runtime_error with wtg_last_error().
 #pragma once
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
+#include <fstream>
+#include <ostream>
 #include <stdexcept>
 #include <string>
 #include <tuple>
@@ -61,6 +66,18 @@ inline int levels_for_sigma(uint64_t sigma) {
   int a = 0;
   for (uint64_t b = sigma - 1; b > 0; b >>= 1) ++a;
   return a < 1 ? 1 : a;
+}
+
+// Writes the stream `fill(dst, cap, len)` produces (dst NULL: length only) to
+// `out`; returns the bytes written, as sdsl's serialize() does.
+template <typename F>
+inline uint64_t write_stream(std::ostream& out, F fill) {
+  uint64_t len = 0;
+  check(fill(nullptr, 0, &len));
+  std::vector<char> buf(len);
+  check(fill(buf.data(), len, &len));
+  out.write(buf.data(), (std::streamsize)len);
+  return len;
 }
 
 // Owning handle of a GPU-built tree.
@@ -238,6 +255,16 @@ class wt_int {
     auto e = expand(v, range_vec_type(1, r));
     return std::make_pair(e.first[0], e.second[0]);
   }
+  // wt_int::serialize (wt_int_par.hpp:887-899): sdsl's byte stream
+  uint64_t serialize(std::ostream& out) const {
+    tree empty;
+    wtg_tree* h = t_.get();
+    if (!h) {  // the reference serializes an empty wt_int too
+      empty = tree(nullptr, 0, 1, 1, WTG_ALL);
+      h = empty.get();
+    }
+    return write_stream(out, [h](void* d, uint64_t c, uint64_t* l) { return wtg_tree_serialize(h, d, c, l); });
+  }
   // the concatenated level bitvector (wt_int::tree, wt_int_par.hpp:80,290)
   std::vector<uint64_t> tree_words() const {
     std::vector<uint64_t> w(t_.bit_words());
@@ -264,6 +291,11 @@ class rank_support_v {
     return out;
   }
   uint64_t operator()(uint64_t idx) const { return rank(idx); }
+  // rank_support_v::serialize (rank_support_v_par.hpp:154-164)
+  uint64_t serialize(std::ostream& out) const {
+    wtg_bv* b = b_;
+    return write_stream(out, [b](void* d, uint64_t c, uint64_t* l) { return wtg_bv_serialize(b, WTG_RANK, d, c, l); });
+  }
   // m_basic_block in the reference layout
   std::vector<uint64_t> basic_block() const {
     uint64_t nw = 0;
@@ -299,10 +331,25 @@ class select_support_mcl {
     check(wtg_bv_select_info(b_, t_b, info));
     return info[1];
   }
+  // select_support_mcl::serialize (select_support_mcl_par.hpp:644-681)
+  uint64_t serialize(std::ostream& out) const {
+    wtg_bv* b = b_;
+    const uint32_t part = t_b ? WTG_SELECT1 : WTG_SELECT0;
+    return write_stream(out, [b, part](void* d, uint64_t c, uint64_t* l) { return wtg_bv_serialize(b, part, d, c, l); });
+  }
 
  private:
   wtg_bv* b_ = nullptr;
 };
+
+// sdsl's store_to_file(v, file): v's serialize() stream in a file
+template <typename T>
+inline bool store_to_file(const T& v, const std::string& file) {
+  std::ofstream out(file, std::ios::binary | std::ios::trunc);
+  if (!out) return false;
+  v.serialize(out);
+  return (bool)out;
+}
 
 }  // namespace wtg
 
