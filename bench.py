@@ -388,7 +388,16 @@ def measure_fm(torch, wtg, oracle_mod, dev, log2_n, log2_q, cpu_log2):
     return res
 
 
-def measure_batch(torch, wtg, stream, ntexts, reps=5):
+def b_texts_host(texts_seed, ntexts):
+    """The batch workload's texts on the host (the generator of measure_batch)."""
+    rng = np.random.default_rng(texts_seed)
+    lengths = np.floor(2.0 ** rng.uniform(10, 20, ntexts)).astype(np.uint64)
+    concat = rng.integers(0, 4, int(lengths.sum()), dtype=np.uint8)
+    offs = np.concatenate([[0], np.cumsum(lengths)]).astype(np.int64)
+    return [concat[offs[t]:offs[t + 1]] for t in range(ntexts)]
+
+
+def measure_batch(torch, wtg, stream, ntexts, reps=5, cpu_texts=0):
     """Batched build of ntexts DNA-like texts (lengths floor(2^U[10,20]),
     i.i.d. uniform over 4 symbols, 2 levels, rank + select1 + select0): one
     persistent launch replayed from a CUDA graph, against the same texts
@@ -445,9 +454,26 @@ def measure_batch(torch, wtg, stream, ntexts, reps=5):
             np.array_equal(b.select_tables(t, 0).pool, ref.select_tables(0).pool)
         ref.free()
     b.free()
+    cpu = None
+    if cpu_texts:
+        from oracle import oracle as O
+        if O.ref_bench() is not None:
+            # every (ntexts / cpu_texts)-th text: the reference's WT() per text
+            # and its rank/select constructors per text, OpenMP across texts
+            pick = np.arange(0, ntexts, max(1, ntexts // cpu_texts))
+            h_texts = b_texts_host(texts_seed=SEED + 13, ntexts=ntexts)
+            lens_s = lengths[pick]
+            concat_s = np.concatenate([h_texts[int(t)] for t in pick])
+            t_wt, t_rs = O.ref_bench_batch(concat_s, lens_s, 2)
+            sb = sum(algorithmic_bytes(int(m), 2, 1) for m in lens_s)
+            cpu = {"value": sb / (t_wt + t_rs) / 1e9, "unit": "GB/s", "cores": O.num_threads(), "kind": "reference",
+                   "sample": f"{pick.size} of the {ntexts} texts ({int(lens_s.sum())} symbols): the reference's WT() "
+                             "and rank_support_v + select_support_mcl<1>/<0> constructors per text, OpenMP across texts",
+                   "wt_s": t_wt, "supports_s": t_rs}
     return {
         "workload": f"{ntexts} texts, lengths floor(2^U[10,20]), uniform over 4 symbols, 2 levels, "
                     "rank + select1 + select0 per text",
+        "cpu_baseline": cpu,
         "texts": ntexts, "symbols": total, "algorithmic_bytes": step_bytes,
         "ms": ms, "gbs": step_bytes / (ms / 1e3) / 1e9, "first_run_s": first_s,
         "launch_shape": {"threads": threads, "symbols_per_thread": ipt,
@@ -457,10 +483,51 @@ def measure_batch(torch, wtg, stream, ntexts, reps=5):
     }
 
 
+def measure_byte_text(torch, wtg, dev, log2_n, reps=10, cpu=True):
+    """The byte-text build: n = 2^log2_n uint8 symbols, Zipf(1.0) over the 256
+    byte values (seeded rank -> byte permutation), 8 levels (levelWT's tree
+    for sigma 256), rank_support_v over the level bits; the input resident on
+    the device.  CPU baseline: the reference's levelWT WT() (byte symbols,
+    OpenMP) and its rank_support_v constructor on the same text."""
+    import datagen
+    n, L = 1 << log2_n, 8
+    sym = datagen.zipf_bytes(n, seed=SEED + 29)
+    d = torch.from_numpy(sym).to(dev)
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    torch.cuda.synchronize()
+    t = None
+    for _ in range(3):
+        t = wtg.WaveletTree.from_device(d.data_ptr(), n, 1, L, wtg.RANK, sp, tree=t)
+    t.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        t = wtg.WaveletTree.from_device(d.data_ptr(), n, 1, L, wtg.RANK, sp, tree=t)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    nb = n * L
+    step_bytes = L * n + (L - 1) * n + nb / 8 + nb / 8 + 16 * ((nb >> 9) + 1)
+    t.free()
+    res = {"workload": f"byte text, n=2^{log2_n} uint8, Zipf(1.0) over 256 byte values, 8 levels, rank_support_v",
+           "n": n, "levels": L, "ms": ms, "gbs": step_bytes / (ms / 1e3) / 1e9, "algorithmic_bytes": step_bytes,
+           "cpu_baseline": None}
+    if cpu:
+        from oracle import oracle as O
+        if O.ref_bench() is not None:
+            t_wt, t_r = O.ref_bench_byte_text(sym, L)
+            res["cpu_baseline"] = {"value": step_bytes / (t_wt + t_r) / 1e9, "unit": "GB/s",
+                                   "cores": O.num_threads(), "kind": "reference",
+                                   "sample": "the whole text: the reference's levelWT WT() (byte symbols) and "
+                                             "rank_support_v constructor, OpenMP", "wt_s": t_wt, "rank_s": t_r}
+    return res
+
+
 LSEL_CONFIGS = (1024, 65536)  # segments per level and polarity: the named model, and a larger one
 
 
-def measure_select(torch, wtg, tree, n, L, dev, stream, log2_q, reps=5):
+def measure_select(torch, wtg, tree, n, L, dev, stream, log2_q, reps=5, cpu_log2=0):
     """Learned select against plain select_support_mcl on the tree's levels:
     2^log2_q select1 and 2^log2_q select0 queries per pass (uniform level,
     uniform k), every learned answer compared with the plain one.  The first
@@ -528,6 +595,7 @@ def measure_select(torch, wtg, tree, n, L, dev, stream, log2_q, reps=5):
         ls.free()
     sel_tables = [tree.select_tables(t_b) for t_b in (0, 1)]
     mcl_words = sum(s.sb_nwords + s.nsb + s.pool_nwords for s in sel_tables)
+    cpu = select_cpu_baseline(cpu_log2) if cpu_log2 else None
     return {
         "queries_per_pass": 2 * nq, "query_mix": f"2^{log2_q} select1 + 2^{log2_q} select0, uniform level and k",
         "plain_mqs": 2 * nq / (plain_ms / 1e3) / 1e6, "plain_ms": plain_ms,
@@ -536,7 +604,36 @@ def measure_select(torch, wtg, tree, n, L, dev, stream, log2_q, reps=5):
                  "exact error windows searched through rank_support_v",
         "mcl_space_bits_per_bit": 64 * mcl_words / bits,
         "learned": learned,
+        "cpu_baseline": cpu,
     }
+
+
+def select_cpu_baseline(log2_n, log2_q=22):
+    """The reference's select_support_mcl<1>/<0>::select on the host cores
+    (OpenMP over the queries) over the 20 levels of a 2^log2_n-symbol sample
+    of the workload: 2^log2_q uniform select1 and select0 queries on the
+    concatenated level bitvector, answers checked against the oracle."""
+    import datagen
+    from oracle import oracle as O
+    if O.ref_bench() is None:
+        return None
+    n = 1 << log2_n
+    sym = datagen.exp_u32(n, mean=MEAN, cap=CAP, seed=SEED)
+    w, _ = O.wt_build(sym, LEVELS, tail=True)
+    size = n * LEVELS
+    ones = int(O.rank_build(w, size)[-2])
+    rng = np.random.default_rng(SEED + 3)
+    secs, nq = 0.0, 0
+    for t_b, m in ((1, ones), (0, size - ones)):
+        q = rng.integers(1, m + 1, 1 << log2_q).astype(np.uint64)
+        dt, ans = O.ref_bench_select(w, size, t_b, q)
+        if not np.array_equal(ans[:4096], O.Select(w, size, t_b).query_batch(q[:4096])):
+            raise RuntimeError("reference select disagrees with the oracle")
+        secs += dt
+        nq += q.size
+    return {"value": nq / secs / 1e6, "unit": "Mq/s", "cores": O.num_threads(), "kind": "reference",
+            "sample": f"select_support_mcl<1>/<0>::select over the 20 x 2^{log2_n} level bits of a 2^{log2_n}-symbol "
+                      f"sample, 2^{log2_q} uniform select1 + 2^{log2_q} select0 queries, OpenMP over queries"}
 
 
 def run_wtg(args, rank, world, local_rank):
@@ -658,12 +755,19 @@ def run_wtg(args, rank, world, local_rank):
                "h2d_bytes_per_step": 4 * n, "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e_s / e_steps}
         t_e.free()
 
-    select = queries = batch = None
+    select = queries = batch = byte_text = None
+    cpu_on = not args.no_cpu and rank == 0
+    if cpu_on:
+        from oracle import oracle as O
+        O.build(ref=True)
     if not args.no_select:
-        select = measure_select(torch, wtg, tree, n, L, dev, stream, args.select_log2)
+        select = measure_select(torch, wtg, tree, n, L, dev, stream, args.select_log2,
+                                cpu_log2=24 if cpu_on else 0)
         queries = measure_queries(torch, tree, seq, n, dev, stream, args.select_log2)
     if args.batch_texts:
-        batch = measure_batch(torch, wtg, stream, args.batch_texts)
+        batch = measure_batch(torch, wtg, stream, args.batch_texts, cpu_texts=512 if cpu_on else 0)
+    if args.bytes_log2:
+        byte_text = measure_byte_text(torch, wtg, dev, args.bytes_log2, cpu=cpu_on)
     fm = None
     if args.fm_log2:
         orc = None
@@ -711,6 +815,7 @@ def run_wtg(args, rank, world, local_rank):
         "queries": queries,
         "fm": fm,
         "batch": batch,
+        "byte_text": byte_text,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "clocks": clocks.summary(),
@@ -738,6 +843,8 @@ def main():
                     help="FM-index core (suffix array, BWT, tree, counts) on a 2^k DNA text; 0 skips")
     ap.add_argument("--fm-queries-log2", type=int, default=24)
     ap.add_argument("--fm-cpu-log2", type=int, default=22)
+    ap.add_argument("--bytes-log2", type=int, default=24,
+                    help="byte-text build (Zipf bytes, 8 levels, rank) of 2^k symbols; 0 skips")
     ap.add_argument("--batch-texts", type=int, default=4096,
                     help="texts of the batched-build comparison (0: skip it)")
     ap.add_argument("--select-log2", type=int, default=26,

@@ -395,20 +395,79 @@ _ref_bench = None
 
 def ref_bench():
     """The reference's own CPU builders compiled for the timed baseline
-    (levelWT with -DLONG -DINT, rank_support_v_par and select_support_mcl_par,
-    all with OpenMP), or None where they were not built."""
+    (levelWT with -DLONG -DINT and with byte symbols, rank_support_v_par and
+    select_support_mcl_par, all with OpenMP) as (wt_long_int, rs, wt_u8), or
+    None where they were not built."""
     global _ref_bench
     if _ref_bench is None:
-        a = os.path.join(REF_DIR, "libref_bench_levelwt.so")
-        b = os.path.join(REF_DIR, "libref_bench_rs.so")
-        if not (os.path.exists(a) and os.path.exists(b)):
+        paths = [os.path.join(REF_DIR, f"libref_bench_{v}.so") for v in ("levelwt", "rs", "levelwt_u8")]
+        if not all(os.path.exists(p) for p in paths):
             return None
-        wt, rs = ctypes.CDLL(a), ctypes.CDLL(b)
-        wt.ref_wt_time.argtypes = [vp, ctypes.c_int, u64, u64]
-        wt.ref_wt_time.restype = ctypes.c_double
+        wt, rs, wt8 = (ctypes.CDLL(p) for p in paths)
+        for w in (wt, wt8):
+            w.ref_wt_time.argtypes = [vp, ctypes.c_int, u64, u64]
+            w.ref_wt_time.restype = ctypes.c_double
+            w.ref_wt_batch_time.argtypes = [vp, vp, u64, u64]
+            w.ref_wt_batch_time.restype = ctypes.c_double
         rs.ref_rank_select_time.argtypes = [vp, u64, vp]
-        _ref_bench = (wt, rs)
+        rs.ref_rank_select_batch_time.argtypes = [vp, vp, vp, u64]
+        rs.ref_rank_select_batch_time.restype = ctypes.c_double
+        rs.ref_select_new.argtypes = [vp, u64, ctypes.c_int]
+        rs.ref_select_new.restype = vp
+        rs.ref_select_free.argtypes = [vp]
+        rs.ref_select_batch.argtypes = [vp, vp, u64, vp]
+        rs.ref_select_batch.restype = ctypes.c_double
+        _ref_bench = (wt, rs, wt8)
     return _ref_bench
+
+
+def ref_bench_byte_text(sym, levels):
+    """Seconds of the reference's WT() over a byte text (sigma 2^levels) and
+    of its rank_support_v constructor over those bits: (t_wt, t_rank)."""
+    wt, rs, wt8 = ref_bench()
+    sym = np.ascontiguousarray(sym, dtype=np.uint8)
+    t_wt = wt8.ref_wt_time(_p(sym), 1, sym.size, 1 << levels)
+    w, _ = wt_build(sym, levels, tail=True)
+    out = np.zeros(5)
+    rs.ref_rank_select_time(_p(w), sym.size * levels, _p(out))
+    return t_wt, float(out[0])
+
+
+def ref_bench_batch(concat, lengths, levels):
+    """Seconds of the reference's WT() per text and of its rank_support_v +
+    select_support_mcl<1> + <0> per text, the texts spread over the OpenMP
+    threads: (t_wt, t_supports)."""
+    wt, rs, wt8 = ref_bench()
+    concat = np.ascontiguousarray(concat, dtype=np.uint8)
+    lengths = np.asarray(lengths, dtype=np.uint64)
+    offs = np.concatenate([[0], np.cumsum(lengths)]).astype(np.uint64)
+    t_wt = wt8.ref_wt_batch_time(_p(concat), _p(offs), lengths.size, 1 << levels)
+    words, woffs, sizes = [], [0], []
+    for t in range(lengths.size):
+        w, _ = wt_build(concat[int(offs[t]):int(offs[t + 1])], levels, tail=True)
+        words.append(w)
+        woffs.append(woffs[-1] + w.size)
+        sizes.append(int(lengths[t]) * levels)
+    allw = np.concatenate(words) if words else np.zeros(1, np.uint64)
+    wo = np.asarray(woffs[:-1], dtype=np.uint64)  # kept alive across the call
+    sz = np.asarray(sizes, dtype=np.uint64)
+    t_rs = rs.ref_rank_select_batch_time(_p(allw), _p(wo), _p(sz), lengths.size)
+    return t_wt, t_rs
+
+
+def ref_bench_select(words, size_bits, t_b, queries):
+    """The reference's select_support_mcl<t_b>::select over a bitvector for
+    every query (OpenMP over the queries): (seconds, answers)."""
+    wt, rs, wt8 = ref_bench()
+    words = np.ascontiguousarray(words, dtype=np.uint64)
+    q = np.ascontiguousarray(queries, dtype=np.uint64)
+    out = np.zeros(q.size, dtype=np.uint64)
+    h = rs.ref_select_new(_p(words), size_bits, t_b)
+    try:
+        secs = rs.ref_select_batch(h, _p(q), q.size, _p(out))
+    finally:
+        rs.ref_select_free(h)
+    return secs, out
 
 
 def ref_bench_times(sym, levels):
@@ -416,7 +475,7 @@ def ref_bench_times(sym, levels):
     rank_support_v / select_support_mcl<1> / <0> constructors over those
     bits, for one sample; plus the select structures' words (for the
     algorithmic bytes).  Returns (t_wt, t_rank, t_sel1, t_sel0, sel_words)."""
-    wt, rs = ref_bench()
+    wt, rs, _ = ref_bench()
     sym = np.ascontiguousarray(sym)
     t_wt = wt.ref_wt_time(_p(sym), sym.dtype.itemsize, sym.size, 1 << levels)
     if t_wt < 0:

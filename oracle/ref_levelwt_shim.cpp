@@ -13,6 +13,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <utility>
+#include <vector>
 #include "parallel.h"
 #include "utils.h"
 #include "WT.h"
@@ -39,6 +40,39 @@ int ref_wt(const void* s, uint64_t n, uint64_t sigma, uint64_t* words, uint64_t 
   free(R.second);
   free(in);
   return 0;
+}
+
+// Seconds of WT(text, n_t, sigma) over T texts laid end to end (offs[t] ..
+// offs[t + 1]), the texts spread over the OpenMP threads (each WT() call
+// then runs on its thread: the reference's own parallel_for inside it is a
+// nested region).  Inputs are copied to per-text buffers before the clock
+// starts and the outputs freed after it stops.  < 0 when memory runs out.
+double ref_wt_batch_time(const uint8_t* concat, const uint64_t* offs, uint64_t T, uint64_t sigma) {
+  std::vector<symbol*> in(T, nullptr);
+  std::vector<std::pair<WTnode*, long*>> out(T);
+  bool ok = true;
+  for (uint64_t t = 0; t < T; ++t) {
+    const uint64_t n = offs[t + 1] - offs[t];
+    in[t] = (symbol*)malloc(sizeof(symbol) * (n ? n : 1));
+    if (!in[t]) ok = false;
+    else for (uint64_t i = 0; i < n; ++i) in[t][i] = (symbol)concat[offs[t] + i];
+  }
+  double secs = -1.0;
+  if (ok) {
+    const auto t0 = std::chrono::steady_clock::now();
+#if defined(OPENMP)
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+    for (long t = 0; t < (long)T; ++t) out[t] = WT(in[t], (uintT)(offs[t + 1] - offs[t]), (uintT)sigma);
+    const auto t1 = std::chrono::steady_clock::now();
+    secs = std::chrono::duration<double>(t1 - t0).count();
+    for (uint64_t t = 0; t < T; ++t) {
+      free(out[t].first);
+      free(out[t].second);
+    }
+  }
+  for (uint64_t t = 0; t < T; ++t) free(in[t]);
+  return secs;
 }
 
 // Seconds of one WT(s, n, sigma) call -- the timed CPU baseline.  The input

@@ -179,6 +179,40 @@ void ref_rank_select_time(const uint64_t* words, uint64_t size, double* out) {
   }
 }
 
+// Seconds of the rank_support_v<1>, select_support_mcl<1> and <0>
+// constructors over T bitvectors (bitvector t: sizes[t] bits at word
+// woffs[t] of words), the bitvectors spread over the OpenMP threads; the
+// bit_vectors are filled before the clock starts.
+double ref_rank_select_batch_time(const uint64_t* words, const uint64_t* woffs, const uint64_t* sizes, uint64_t T) {
+  std::vector<sdsl::bit_vector> bvs;
+  bvs.reserve(T);
+  for (uint64_t t = 0; t < T; ++t) bvs.push_back(make_bv(words + woffs[t], sizes[t]));
+  const auto t0 = std::chrono::steady_clock::now();
+#if defined(OPENMP)
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+  for (long t = 0; t < (long)T; ++t) {
+    sdsl::rank_support_v<1, 1> rs(&bvs[t]);
+    sdsl::select_support_mcl<1, 1> s1(&bvs[t]);
+    sdsl::select_support_mcl<0, 1> s0(&bvs[t]);
+  }
+  const auto t1 = std::chrono::steady_clock::now();
+  return std::chrono::duration<double>(t1 - t0).count();
+}
+
+// select(q[i]) for nq queries on a select structure (OpenMP over the
+// queries); returns the seconds
+double ref_select_batch(void* h, const uint64_t* q, uint64_t nq, uint64_t* out) {
+  sel_any* s = (sel_any*)h;
+  const auto t0 = std::chrono::steady_clock::now();
+#if defined(OPENMP)
+#pragma omp parallel for schedule(static, 4096)
+#endif
+  for (long i = 0; i < (long)nq; ++i) out[i] = s->query(q[i]);
+  const auto t1 = std::chrono::steady_clock::now();
+  return std::chrono::duration<double>(t1 - t0).count();
+}
+
 // select_support_mcl::serialize (select/select_support_mcl_par.hpp:644-681)
 uint64_t ref_select_serialize(void* h, uint8_t* dst, uint64_t cap) {
   return emit(((sel_any*)h)->serialize(), dst, cap);

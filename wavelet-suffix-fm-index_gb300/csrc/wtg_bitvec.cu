@@ -157,17 +157,67 @@ __global__ void __launch_bounds__(BV_THREADS)
 // the chunk's prefix within its level (the level passes' chunk counts,
 // scanned) -- no scan over the bits.  Thread per superblock, grid-stride
 // over each level's superblocks.
+//
+// Per word, the work is one in-word select at most (the next 64th one or
+// zero, see word_marks) in 32-bit arithmetic on per-superblock 64-bit bases:
+// the select1 samples of a superblock are consecutive from index
+// ceil(ones before / 64), the select0 samples consecutive (descending from
+// the back) from ceil(zeros before / 64).  The last two steps of the select
+// read a 256 x 8 table of in-byte selects from shared memory.  A superblock
+// holds at most one superblock end per polarity (512 < 4096 args), resolved
+// once per superblock; the last word holding a one / a zero is resolved once
+// per thread from the last such superblock.
+__device__ __forceinline__ uint32_t sel64_lut(uint64_t v, uint32_t d, uint32_t cl, const uint8_t* __restrict__ lut) {
+  // d-th (0-based) set bit of v; cl = popcount of its low 32 bits
+  const bool up = d >= cl;
+  uint32_t w = up ? (uint32_t)(v >> 32) : (uint32_t)v;
+  d -= up ? cl : 0u;
+  uint32_t pos = up ? 32u : 0u;
+  const uint32_t c16 = __popc(w & 0xFFFFu);
+  const bool u16 = d >= c16;
+  w = u16 ? (w >> 16) : w;
+  d -= u16 ? c16 : 0u;
+  pos += u16 ? 16u : 0u;
+  const uint32_t c8 = __popc(w & 0xFFu);
+  const bool u8 = d >= c8;
+  w = u8 ? (w >> 8) : w;
+  d -= u8 ? c8 : 0u;
+  pos += u8 ? 8u : 0u;
+  return pos + lut[((w & 0xFFu) << 3) | (d & 7u)];
+}
+
+// position after the last one (t_b = 1) or zero (t_b = 0) of superblock sb
+// (eight words, all inside the bitvector); read through L2
+__device__ __forceinline__ uint64_t last_arg_end_sb(const uint64_t* __restrict__ words, uint64_t sb, int t_b) {
+  for (int j = 7; j >= 0; --j) {
+    uint64_t x = __ldcg(words + 8 * sb + j);
+    if (!t_b) x = ~x;
+    if (x) return ((8 * sb + j) << 6) + hi64(x) + 1;
+  }
+  return 0;
+}
+
 __global__ void __launch_bounds__(256)
     rs_levels_kernel(const uint64_t* __restrict__ words, int L, uint64_t chunks_per_level,
                      const uint32_t* __restrict__ chunkpre, uint64_t prestride, const uint64_t* __restrict__ lvl_zb,
                      uint32_t flags, uint64_t* __restrict__ rank, uint32_t* __restrict__ samples, uint64_t samp_last,
                      uint64_t* __restrict__ starts1, uint64_t* __restrict__ starts0, uint64_t* __restrict__ ends1,
                      uint64_t* __restrict__ ends0, unsigned long long* info) {
+  __shared__ uint8_t lut[256 * 8];  // lut[byte * 8 + r] = position of the r-th set bit of byte
+  for (uint32_t e = threadIdx.x; e < 256 * 8; e += blockDim.x) {
+    uint32_t byte = e >> 3, r = e & 7, pos = 0;
+    for (uint32_t k = 0; k < 8; ++k)
+      if ((byte >> k) & 1u) {
+        if (r == 0) { pos = k; break; }
+        --r;
+      }
+    lut[e] = (uint8_t)pos;
+  }
+  __syncthreads();
   const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
-  const uint64_t W = (uint64_t)L * chunks_per_level * 8;
-  const bool sel1 = flags & WTG_SELECT1, sel0 = flags & WTG_SELECT0;
-  uint64_t lastw1 = 0, lastw0 = 0;
+  const bool sel1 = flags & WTG_SELECT1, sel0 = flags & WTG_SELECT0, sel = sel1 || sel0;
+  uint64_t last_sb1 = ~0ull, last_sb0 = ~0ull;  // last superblocks holding a one / a zero
   // thread per 512-bit superblock: its eight words in four 16-byte loads,
   // counts and fields in registers, one 16-byte rank entry
   for (int l = 0; l < L; ++l) {
@@ -178,26 +228,89 @@ __global__ void __launch_bounds__(256)
       const ulonglong2* p = reinterpret_cast<const ulonglong2*>(words + 8 * b);
       const ulonglong2 q0 = __ldg(p), q1 = __ldg(p + 1), q2 = __ldg(p + 2), q3 = __ldg(p + 3);
       const uint64_t w[8] = {q0.x, q0.y, q1.x, q1.y, q2.x, q2.y, q3.x, q3.y};
-      const uint64_t sb_before = 512 * b - (zl + __ldg(pre + c));  // ones before the superblock
-      uint32_t excl = 0;
+      const uint64_t zb = zl + __ldg(pre + c);  // zeros before the superblock
+      const uint64_t sb_before = 512 * b - zb;  // ones before the superblock
+      const uint32_t pos_base = (uint32_t)(512 * b);
+      const uint32_t k1_base = (uint32_t)sb_before, k0_base = (uint32_t)zb;
+      // next samples of this superblock: select1 from the front, select0 from the back
+      uint32_t* __restrict__ p1 = samples + ((sb_before + 63) >> 6);
+      uint32_t* __restrict__ p0 = samples + (samp_last - ((zb + 63) >> 6));
+      uint32_t excl = 0;  // ones before the word within the superblock
+      uint32_t n1 = 0, n0 = 0;
       uint64_t part = 0;
+      uint32_t cnt[8];
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
-        const uint32_t cj = __popcll(w[j]);
+        const uint64_t x = w[j];
+        const uint32_t cl = __popc((uint32_t)x);
+        const uint32_t cj = cl + __popc((uint32_t)(x >> 32));
+        cnt[j] = cj;
         if (j) part |= (uint64_t)excl << (63 - 9 * j);
-        if (sel1 || sel0)
-          word_marks(w[j], cj, sb_before + excl, 8 * b + j, ~0ull, sel1, sel0, samples, samp_last, starts1,
-                     starts0, ends1, ends0, lastw1, lastw0);
+        if (sel) {
+          const uint32_t K1 = k1_base + excl;                         // ones before the word (mod 2^32)
+          const uint32_t K0 = k0_base + 64u * j - excl;               // zeros before it
+          const uint32_t d1 = (0u - K1) & 63u, d0 = K1 & 63u;
+          const bool s1 = sel1 && d1 < cj, s0 = sel0 && d0 < 64u - cj;
+          if (s1 || s0) {
+            const uint64_t v = s1 ? x : ~x;
+            const uint32_t off = sel64_lut(v, s1 ? d1 : d0, s1 ? cl : 32u - cl, lut);
+            const uint32_t pos = pos_base + 64u * j + off;
+            if (s1) {
+              p1[n1++] = pos;
+              if (((K1 + d1) & 4095u) == 0) starts1[((sb_before + excl + d1) >> 12)] = 512 * b + 64 * j + off;
+            }
+            if (s0) {
+              // both polarities only when K1 % 64 == 0: the word's first one and first zero
+              const uint32_t off0 = s1 ? (uint32_t)(__ffsll((long long)~x) - 1) : off;
+              *(p0 - n0) = pos_base + 64u * j + off0;
+              ++n0;
+              if (((K0 + d0) & 4095u) == 0)
+                starts0[((zb + 64 * j - excl + d0) >> 12)] = 512 * b + 64 * j + off0;
+            }
+          }
+        }
         excl += cj;
       }
       if (flags & WTG_RANK) reinterpret_cast<ulonglong2*>(rank)[b] = make_ulonglong2(sb_before, part);
+      if (sel) {
+        // superblock ends: the arg 4095 of a 4096-arg superblock, at most one per polarity here
+        const uint32_t cz = 512u - excl;
+        const uint32_t e1 = 4095u - (k1_base & 4095u), e0 = 4095u - (k0_base & 4095u);
+        const bool h1 = sel1 && e1 < excl, h0 = sel0 && e0 < cz;
+        if (h1 || h0) {
+          // which polarity (both can end here) is resolved one after the other
+#pragma unroll
+          for (int t = 1; t >= 0; --t) {
+            if (!(t ? h1 : h0)) continue;
+            const uint32_t e = t ? e1 : e0;
+            uint32_t before = 0, r = 0, jj = 0;
+            uint64_t xx = 0;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+              const uint32_t cj = t ? cnt[j] : 64u - cnt[j];
+              const bool here = before <= e && e < before + cj;
+              xx = here ? (t ? w[j] : ~w[j]) : xx;
+              r = here ? e - before : r;
+              jj = here ? (uint32_t)j : jj;
+              before += cj;
+            }
+            const uint64_t pos = 512 * b + 64 * jj + sel64_lut(xx, r, __popc((uint32_t)xx), lut);
+            if (t) ends1[(sb_before + e) >> 12] = pos;
+            else ends0[(zb + e) >> 12] = pos;
+          }
+        }
+        last_sb1 = excl ? b : last_sb1;
+        last_sb0 = cz ? b : last_sb0;
+      }
     }
   }
-  const uint64_t last1 = warp_max_u64(last_arg_end(words, lastw1, W, ~0ull, 1));
-  const uint64_t last0 = warp_max_u64(last_arg_end(words, lastw0, W, ~0ull, 0));
-  if ((threadIdx.x & 31) == 0) {
-    if (last1) atomicMax(&info[INF_LAST1], (unsigned long long)last1);
-    if (last0) atomicMax(&info[INF_LAST0], (unsigned long long)last0);
+  if (sel) {
+    const uint64_t last1 = warp_max_u64(last_sb1 == ~0ull ? 0 : last_arg_end_sb(words, last_sb1, 1));
+    const uint64_t last0 = warp_max_u64(last_sb0 == ~0ull ? 0 : last_arg_end_sb(words, last_sb0, 0));
+    if ((threadIdx.x & 31) == 0) {
+      if (last1) atomicMax(&info[INF_LAST1], (unsigned long long)last1);
+      if (last0) atomicMax(&info[INF_LAST0], (unsigned long long)last0);
+    }
   }
 }
 
