@@ -427,7 +427,7 @@ def measure_batch(torch, wtg, stream, ntexts, reps=5, cpu_texts=0):
     b.sync()
     ms = e0.elapsed_time(e1) / reps
     step_bytes = sum(algorithmic_bytes(int(n), 2, 1) for n in lengths)
-    threads, ipt, tune_ms = b.tuning()
+    tile, ipt, tune_ms = b.tuning()
     # the same texts, one single-sequence build each
     d_in, _ = b.input_device()
     offs = np.concatenate([[0], np.cumsum(lengths)]).astype(np.uint64)
@@ -476,7 +476,7 @@ def measure_batch(torch, wtg, stream, ntexts, reps=5, cpu_texts=0):
         "cpu_baseline": cpu,
         "texts": ntexts, "symbols": total, "algorithmic_bytes": step_bytes,
         "ms": ms, "gbs": step_bytes / (ms / 1e3) / 1e9, "first_run_s": first_s,
-        "launch_shape": {"threads": threads, "symbols_per_thread": ipt,
+        "launch_shape": {"tile_symbols": tile, "symbols_per_thread": ipt,
                          "candidates_ms": [round(float(x), 3) for x in tune_ms]},
         "per_text_plain_ms": plain_s * 1e3, "per_text_plain_gbs": step_bytes / plain_s / 1e9,
         "speedup_vs_per_text": plain_s * 1e3 / ms, "exact_spot_check": bool(exact),
@@ -659,6 +659,60 @@ def run_wtg(args, rank, world, local_rank):
     del x
     torch.cuda.synchronize()
 
+    # ---- e2e first, in a fresh process state: the host API from pinned host
+    # buffers, the input copied in and every output copied back per step
+    e2e = None
+    if not args.no_e2e:
+        import ctypes
+        host_in = torch.empty(n, dtype=torch.int32, pin_memory=True)
+        host_in.copy_(seq)
+        h = ctypes.c_void_p()
+        L_ = wtg.lib()
+        wtg._ck(L_.wtg_tree_build(ctypes.c_void_p(host_in.data_ptr()), n, 4, L, wtg.ALL, ctypes.byref(h)))
+        t_e = wtg.WaveletTree(_handle=h)
+        s1, s0 = t_e.select_tables(1), t_e.select_tables(0)
+        e2e_bytes = algorithmic_bytes(n, L, 4, sum(s.sb_nwords + s.nsb + s.pool_nwords for s in (s1, s0)))
+        outs = {
+            "bits": torch.empty(t_e.bit_words, dtype=torch.int64, pin_memory=True),
+            "rank": torch.empty(t_e.rank_words, dtype=torch.int64, pin_memory=True),
+        }
+        for tb, s in ((1, s1), (0, s0)):
+            outs[f"sb{tb}"] = torch.empty(max(s.sb_nwords, 1), dtype=torch.int64, pin_memory=True)
+            outs[f"desc{tb}"] = torch.empty(max(s.nsb, 1), dtype=torch.int64, pin_memory=True)
+            outs[f"pool{tb}"] = torch.empty(max(s.pool_nwords, 1), dtype=torch.int64, pin_memory=True)
+        d2h = 8 * (t_e.bit_words + t_e.rank_words + sum(s.sb_nwords + s.nsb + s.pool_nwords for s in (s1, s0)))
+        vp = ctypes.c_void_p
+
+        def e2e_step():
+            # bits and rank table come back while the build runs; then the
+            # select tables (their sizes are known only after the build)
+            wtg._ck(L_.wtg_tree_build_out(vp(host_in.data_ptr()), n, 4, L, wtg.ALL, vp(outs["bits"].data_ptr()),
+                                          vp(outs["rank"].data_ptr()), ctypes.byref(h)))
+            for tb in (1, 0):
+                wtg._ck(L_.wtg_tree_get_select(h, tb, vp(outs[f"sb{tb}"].data_ptr()),
+                                               vp(outs[f"desc{tb}"].data_ptr()), vp(outs[f"pool{tb}"].data_ptr())))
+
+        for _ in range(max(1, args.warmup)):
+            e2e_step()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        e_steps = max(1, args.steps)
+        step_ms = []
+        t0 = time.perf_counter()
+        for _ in range(e_steps):
+            ts = time.perf_counter()
+            e2e_step()
+            step_ms.append(1e3 * (time.perf_counter() - ts))
+        torch.cuda.synchronize()
+        e_s = slowest_rank(dist, torch, time.perf_counter() - t0, dev)
+        e2e = {"value": job_throughput(world, e_steps, e2e_bytes, e_s), "unit": "GB/s",
+               "h2d_bytes_per_step": 4 * n, "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e_s / e_steps,
+               "step_ms": [round(x, 2) for x in step_ms]}
+        t_e.free()
+        del outs, host_in, t_e
+        torch.cuda.empty_cache()
+
     stream = torch.cuda.current_stream(dev)
     sp = stream.cuda_stream
 
@@ -707,53 +761,6 @@ def run_wtg(args, rank, world, local_rank):
     }
     roofline["frac"] = roofline["achieved"] / peak
     kernel_share = {k: {"launches": v[0], "ms": v[1]} for k, v in prof.items()}
-
-    # ---- e2e: host API with pinned host buffers, outputs copied back (run
-    # before the other sections, so that the pinned buffers are placed as
-    # in a fresh process)
-    e2e = None
-    if not args.no_e2e:
-        import ctypes
-        host_in = torch.empty(n, dtype=torch.int32, pin_memory=True)
-        host_in.copy_(seq)
-        h = ctypes.c_void_p()
-        L_ = wtg.lib()
-        wtg._ck(L_.wtg_tree_build(ctypes.c_void_p(host_in.data_ptr()), n, 4, L, wtg.ALL, ctypes.byref(h)))
-        t_e = wtg.WaveletTree(_handle=h)
-        s1, s0 = t_e.select_tables(1), t_e.select_tables(0)
-        outs = {
-            "bits": torch.empty(t_e.bit_words, dtype=torch.int64, pin_memory=True),
-            "rank": torch.empty(t_e.rank_words, dtype=torch.int64, pin_memory=True),
-        }
-        for tb, s in ((1, s1), (0, s0)):
-            outs[f"sb{tb}"] = torch.empty(max(s.sb_nwords, 1), dtype=torch.int64, pin_memory=True)
-            outs[f"desc{tb}"] = torch.empty(max(s.nsb, 1), dtype=torch.int64, pin_memory=True)
-            outs[f"pool{tb}"] = torch.empty(max(s.pool_nwords, 1), dtype=torch.int64, pin_memory=True)
-        d2h = 8 * (t_e.bit_words + t_e.rank_words + sum(s.sb_nwords + s.nsb + s.pool_nwords for s in (s1, s0)))
-        vp = ctypes.c_void_p
-
-        def e2e_step():
-            # bits and rank table come back while the build runs; then the
-            # select tables (their sizes are known only after the build)
-            wtg._ck(L_.wtg_tree_build_out(vp(host_in.data_ptr()), n, 4, L, wtg.ALL, vp(outs["bits"].data_ptr()),
-                                          vp(outs["rank"].data_ptr()), ctypes.byref(h)))
-            for tb in (1, 0):
-                wtg._ck(L_.wtg_tree_get_select(h, tb, vp(outs[f"sb{tb}"].data_ptr()),
-                                               vp(outs[f"desc{tb}"].data_ptr()), vp(outs[f"pool{tb}"].data_ptr())))
-
-        e2e_step()
-        if dist:
-            dist.barrier()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        e_steps = max(1, args.steps)
-        for _ in range(e_steps):
-            e2e_step()
-        torch.cuda.synchronize()
-        e_s = slowest_rank(dist, torch, time.perf_counter() - t0, dev)
-        e2e = {"value": job_throughput(world, e_steps, step_bytes, e_s), "unit": "GB/s",
-               "h2d_bytes_per_step": 4 * n, "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e_s / e_steps}
-        t_e.free()
 
     select = queries = batch = byte_text = None
     cpu_on = not args.no_cpu and rank == 0

@@ -54,6 +54,7 @@ typedef struct wtg_tree wtg_tree; /* wavelet tree + supports, owns device memory
 typedef struct wtg_bv wtg_bv;     /* rank/select supports over a caller bitvector */
 typedef struct wtg_lsel wtg_lsel; /* learned select index over a tree's levels */
 typedef struct wtg_batch wtg_batch; /* batched builds of many short texts */
+typedef struct wtg_huff wtg_huff;   /* Huffman-shaped wavelet tree of a byte text */
 
 const char* wtg_last_error(void);
 int wtg_version(void);
@@ -227,19 +228,23 @@ int wtg_rank_build_noalloc(const uint64_t* d_words, uint64_t size_bits, uint64_t
  * and select_support_mcl<1>/<0> -- what a loop of WT() calls
  * (wavelet/levelWT/WT.h:43) or of wt_int constructions
  * (wt_int/wt_int_par.hpp:368-406) plus init_support would give, one text per
- * call -- built in one persistent launch that pulls texts from a device
- * queue, replayed from a CUDA graph after the first run.
+ * call -- built in one persistent launch that pulls work items from a
+ * device queue, replayed from a CUDA graph after the first run.  The items,
+ * in phase order: (text, tile) key histograms, (text, level, tile) level
+ * bits, (text, rank tile) rank_support_v entries and select samples, (text)
+ * select_support_mcl finishing; each waits for its text's previous phase.
  *   lengths : symbols of each text (ntexts entries); texts are u8 symbols
  *             read through their low `levels` bits, concatenated in order
  *   levels  : 1..4
  *   flags   : WTG_RANK | WTG_SELECT1 | WTG_SELECT0 (select implies rank)
  *   stream  : the stream the batch runs on (NULL: the batch makes its own)
  * The plan allocates every output region (sizes follow from the lengths).
- * The first wtg_batch_run times each launch shape (threads per CTA x symbols
- * per thread) on the loaded input, keeps the fastest and captures the build
- * in a CUDA graph; later runs replay the graph.  Per-text outputs have the
- * single-sequence layouts (wtg_tree_get_bits / _get_rank / _get_select of a
- * tree built with the same levels). */
+ * The first wtg_batch_run times each launch shape (symbols per histogram /
+ * level-bits tile x symbols per thread per chunk) on the loaded input, keeps
+ * the fastest and captures the build in a CUDA graph; later runs replay the
+ * graph.  Per-text outputs have the single-sequence layouts
+ * (wtg_tree_get_bits / _get_rank / _get_select of a tree built with the same
+ * levels). */
 int wtg_batch_plan(const uint64_t* lengths, uint64_t ntexts, int levels, uint32_t flags, void* stream,
                    wtg_batch** out);
 /* device address and size of the input buffer (the concatenated texts) */
@@ -248,12 +253,14 @@ int wtg_batch_input(wtg_batch* b, void** d_input, uint64_t* nbytes);
 int wtg_batch_load(wtg_batch* b, const void* texts);
 int wtg_batch_run(wtg_batch* b);
 /* fix the launch shape instead of timing the candidates on the first run:
- * threads per CTA 256, 512 or 1024; symbols per thread per chunk 4, 8 or 16 */
-int wtg_batch_set_shape(wtg_batch* b, int threads, int items_per_thread);
+ * (symbols per tile, symbols per thread per chunk) one of (4096, 4),
+ * (8192, 4), (4096, 8), (8192, 8), (16384, 8), (8192, 16), (16384, 16),
+ * (32768, 16) */
+int wtg_batch_set_shape(wtg_batch* b, int tile, int items_per_thread);
 int wtg_batch_sync(wtg_batch* b);
 int wtg_batch_free(wtg_batch* b);
 /* after wtg_batch_sync.  text info: n, levels, bit words, rank words, ones,
- * zeros, and the chosen threads per CTA and symbols per thread */
+ * zeros, and the chosen symbols per tile and symbols per thread */
 int wtg_batch_text_info(wtg_batch* b, uint64_t t, uint64_t info[8]);
 /* select info[8] of text t, as wtg_tree_select_info */
 int wtg_batch_select_info(wtg_batch* b, uint64_t t, int t_b, uint64_t info[8]);
@@ -261,7 +268,7 @@ int wtg_batch_get_bits(wtg_batch* b, uint64_t t, uint64_t* dst, uint64_t nwords)
 int wtg_batch_get_rank(wtg_batch* b, uint64_t t, uint64_t* dst, uint64_t nwords);
 int wtg_batch_get_select(wtg_batch* b, uint64_t t, int t_b, uint64_t* sb_words, uint64_t* desc, uint64_t* pool);
 /* the launch shape the first run chose, and the time of each candidate (ms) */
-int wtg_batch_tuning(wtg_batch* b, int* threads, int* items_per_thread, float ms[8]);
+int wtg_batch_tuning(wtg_batch* b, int* tile, int* items_per_thread, float ms[8]);
 
 /* ------------------------------------------------- suffix array and BWT
  * The first two steps of the reference's FM-index construction
@@ -345,6 +352,41 @@ int wtg_lsel_query_device(wtg_lsel* m, int t_b, const uint64_t* d_level, const u
 #define WTG_PROF_CLASSES 6
 int wtg_profile_enable(int on);
 int wtg_profile_read(uint64_t launches[WTG_PROF_CLASSES], double ms[WTG_PROF_CLASSES]);
+
+/* ------------------------------------------- Huffman-shaped wavelet tree
+ * sdsl::wt_huff<> over a byte text (wt_huff/wt_huff_par.hpp, built as
+ * wt_huff/wt_pc_par.hpp:321-361 builds it), the tree of the reference's
+ * FM-index (fm-index/par/WT.C:44).  Shape: Huffman code of the byte counts,
+ * ties broken by (frequency, node number) with leaves numbered by byte value
+ * and merged nodes after them (wt_huff_par.hpp:82-117); nodes in breadth-first
+ * order, each inner node's bitvector at bv_pos = the sizes of the inner nodes
+ * before it; rank_support_v<1> / select_support_mcl over the concatenated
+ * bitvector as flags ask (select implies rank).
+ *   info[5]  : n, sigma, bitvector bits, tree nodes, rank table words
+ *   get_tree : per node (bv_pos, bv_pos_rank -- the ones before bv_pos, or a
+ *              leaf's byte --, parent, child0, child1), 0xFFFF for none, 5
+ *              words each; per byte its leaf (0xFFFF: absent) and path (bit d
+ *              set when the (d+1)-th edge goes right, length << 56)
+ *   access / rank / select / inverse_select: wt_pc's operator[], rank(i, c),
+ *              select(i, c), inverse_select(i) (wt_huff/wt_pc_par.hpp:430-552);
+ *              select gives n for a byte not in the text and UINT64_MAX for i
+ *              beyond its occurrences (the reference asserts)
+ *   fm_count : backward search over a BWT's tree, C[256] = bytes below c */
+int wtg_huff_build(const uint8_t* text, uint64_t n, uint32_t flags, wtg_huff** out);
+int wtg_huff_build_device(const uint8_t* d_text, uint64_t n, uint32_t flags, void* stream, wtg_huff** out);
+int wtg_huff_free(wtg_huff* h);
+int wtg_huff_info(wtg_huff* h, uint64_t info[5]);
+int wtg_huff_get_bits(wtg_huff* h, uint64_t* dst, uint64_t nwords);
+int wtg_huff_get_tree(wtg_huff* h, uint64_t* nodes, uint64_t* leaves, uint64_t* paths);
+int wtg_huff_get_rank(wtg_huff* h, uint64_t* dst, uint64_t nwords);
+int wtg_huff_select_info(wtg_huff* h, int t_b, uint64_t info[8]);
+int wtg_huff_get_select(wtg_huff* h, int t_b, uint64_t* sb_words, uint64_t* desc, uint64_t* pool);
+int wtg_huff_access(wtg_huff* h, const uint64_t* idx, uint64_t nq, uint64_t* out);
+int wtg_huff_rank(wtg_huff* h, const uint64_t* idx, const uint64_t* sym, uint64_t nq, uint64_t* out);
+int wtg_huff_select(wtg_huff* h, const uint64_t* i, const uint64_t* sym, uint64_t nq, uint64_t* out);
+int wtg_huff_inverse_select(wtg_huff* h, const uint64_t* idx, uint64_t nq, uint64_t* rank_out, uint64_t* sym_out);
+int wtg_huff_fm_count(wtg_huff* h, const uint64_t* C, const uint8_t* pat, const uint64_t* off, uint64_t npat,
+                      uint64_t* out);
 
 /* ---------------------------------------------- sdsl serialize() streams
  * The byte streams sdsl's serialize() writes (what sdsl::store_to_file puts

@@ -343,6 +343,169 @@ def serialize_wt_int(sym, levels):
     return np.frombuffer(b"".join(parts), dtype=np.uint8)
 
 
+# ------------------------------------------------- Huffman-shaped tree
+# Restates the reference's wt_huff build (wt_huff/wt_huff_par.hpp:82-117 for
+# the shape, wt_huff/wt_pc_par.hpp:193-258,321-361 for the bits) over the
+# breadth-first byte code tree of sdsl's byte_tree.
+
+
+class HuffShape:
+    """The code tree of a byte text: nodes in breadth-first order (root 0) as
+    rows (bv_pos, freq, sym, parent, child0, child1) -- -1 for no parent /
+    child -- and per byte its path (bit d set: the (d+1)-th edge goes right)
+    and path length (0: not in the text).  bv_size = the concatenated
+    bitvector's length (the inner nodes' sizes)."""
+
+    def __init__(self, counts):
+        import heapq
+        counts = [int(c) for c in counts]
+        shape = []  # [freq, sym, child0, child1]
+        heap = []
+        for c, f in enumerate(counts):
+            if f > 0:
+                heap.append((f, len(shape)))
+                shape.append([f, c, -1, -1])
+        heapq.heapify(heap)
+        while len(heap) > 1:  # the two smallest (frequency, node number) pairs merge
+            f1, i1 = heapq.heappop(heap)
+            f2, i2 = heapq.heappop(heap)
+            heapq.heappush(heap, (f1 + f2, len(shape)))
+            shape.append([f1 + f2, 0, i1, i2])
+        rows, order = [], []
+        if shape:
+            order = [len(shape) - 1]
+            rows = [[0, 0, 0, -1, -1, -1]]
+        bv = 0
+        k = 0
+        while k < len(order):  # first in, first out: the placed nodes are the queue
+            f, sym, c0, c1 = shape[order[k]]
+            rows[k][0], rows[k][1], rows[k][2] = bv, f, sym
+            if c0 >= 0:
+                bv += f
+                for j, c in enumerate((c0, c1)):
+                    rows[k][4 + j] = len(order)
+                    order.append(c)
+                    rows.append([0, 0, 0, k, -1, -1])
+            k += 1
+        self.nodes = np.array(rows, dtype=np.int64).reshape(-1, 6)
+        self.bv_size = bv
+        self.sigma = sum(1 for f in counts if f > 0)
+        self.leaf = np.full(256, -1, dtype=np.int64)
+        self.path = np.zeros(256, dtype=np.uint64)
+        self.plen = np.zeros(256, dtype=np.int64)
+        for v in range(self.nodes.shape[0]):
+            if self.nodes[v, 4] < 0:
+                c = int(self.nodes[v, 2])
+                self.leaf[c] = v
+                p, ln, u = 0, 0, v
+                while u != 0:
+                    par = int(self.nodes[u, 3])
+                    p = (p << 1) | (1 if int(self.nodes[par, 5]) == u else 0)
+                    ln += 1
+                    u = par
+                self.path[c], self.plen[c] = p, ln
+
+
+def huff_build(text):
+    """wt_huff over a byte text: (HuffShape, words of the concatenated
+    bitvector with one zero word after the data)."""
+    text = np.ascontiguousarray(text, dtype=np.uint8)
+    counts = np.bincount(text, minlength=256) if text.size else np.zeros(256, np.int64)
+    sh = HuffShape(counts[: int(text.max()) + 1] if text.size else [])
+    nwords = (sh.bv_size + 63) // 64
+    words = np.zeros(nwords + 1, dtype=np.uint64)
+    if text.size == 0 or sh.bv_size == 0:
+        return sh, words
+    plen = sh.plen[text]
+    path = sh.path[text]
+    bits = np.zeros(sh.bv_size, dtype=np.uint8)
+    # depth d: the symbols whose code is longer than d, stably ordered by the
+    # depth-d node on their path (breadth-first = left to right), give the
+    # bits of the depth-d inner nodes, which lie consecutively from the first
+    # one's bv_pos
+    node = np.zeros(text.size, dtype=np.int64)  # each symbol's node at depth d
+    for d in range(int(plen.max())):
+        live = plen > d
+        idx = np.nonzero(live)[0]
+        if idx.size == 0:
+            break
+        nd = node[idx]
+        o = np.argsort(sh.nodes[nd, 0], kind="stable")
+        b = ((path[idx] >> np.uint64(d)) & np.uint64(1)).astype(np.int64)
+        start = int(sh.nodes[nd[o[0]], 0])
+        bits[start:start + idx.size] = b[o]
+        node[idx] = sh.nodes[nd, 4 + b]
+    words[:nwords] = np.packbits(np.concatenate([bits, np.zeros(nwords * 64 - bits.size, np.uint8)]),
+                                 bitorder="little").view(np.uint64)
+    return sh, words
+
+
+class HuffOracle:
+    """wt_huff built here, with rank_support_v / select_support_mcl over its
+    bitvector and the wt_pc queries (wt_huff/wt_pc_par.hpp:430-552)."""
+
+    def __init__(self, text):
+        self.text = np.ascontiguousarray(text, dtype=np.uint8)
+        self.n = self.text.size
+        self.shape, self.words = huff_build(self.text)
+        self.size = self.shape.bv_size
+        self.rank_tbl = rank_build(self.words, self.size)
+        nd = self.shape.nodes
+        self.node_rank = np.array([rank1(self.rank_tbl, self.words, int(nd[v, 0])) if nd[v, 4] >= 0 else int(nd[v, 2])
+                                   for v in range(nd.shape[0])], dtype=np.uint64)
+        self.sel = {t_b: Select(self.words, self.size, t_b) for t_b in (0, 1)}
+
+    def _bit(self, p):
+        return (int(self.words[p >> 6]) >> (p & 63)) & 1
+
+    def _r1(self, p):
+        return rank1(self.rank_tbl, self.words, p)
+
+    def access(self, i):
+        nd, v = self.shape.nodes, 0
+        while nd[v, 4] >= 0:
+            p = int(nd[v, 0]) + i
+            r = self._r1(p) - int(self.node_rank[v])
+            if self._bit(p):
+                i, v = r, int(nd[v, 5])
+            else:
+                i, v = i - r, int(nd[v, 4])
+        return int(nd[v, 2])
+
+    def rank(self, i, c):
+        sh, nd = self.shape, self.shape.nodes
+        if sh.leaf[c] < 0:
+            return 0
+        if sh.sigma == 1:
+            return i
+        p, ln, res, v = int(sh.path[c]), int(sh.plen[c]), i, 0
+        for _ in range(ln):
+            if res == 0:
+                break
+            r = self._r1(int(nd[v, 0]) + res) - int(self.node_rank[v])
+            res = r if p & 1 else res - r
+            v = int(nd[v, 5 if p & 1 else 4])
+            p >>= 1
+        return res
+
+    def select(self, i, c):
+        sh, nd = self.shape, self.shape.nodes
+        v = int(sh.leaf[c])
+        if v < 0:
+            return self.n
+        if sh.sigma == 1:
+            return min(i - 1, self.n)
+        res = i - 1
+        for _ in range(int(sh.plen[c])):
+            par = int(nd[v, 3])
+            if int(nd[par, 5]) == v:
+                res = self.sel[1].query(int(self.node_rank[par]) + res + 1) - int(nd[par, 0])
+            else:
+                res = self.sel[0].query(int(nd[par, 0]) - int(self.node_rank[par]) + res + 1) - int(nd[par, 0])
+            v = par
+        return res
+
+
 # ---------------------------------------------------------------- reference
 
 _ref_libs = {}
@@ -641,6 +804,75 @@ def _ref_wt_int():
         L.ref_wtint_load.restype = vp
         _ref_wi = L
     return _ref_wi
+
+
+class RefWtHuff:
+    """The reference's own wt_huff (wt_huff/wt_huff_par.hpp over
+    wt_huff/wt_pc_par.hpp), built by its constructor and queried through its
+    members; its tree in the shim's breadth-first node layout."""
+
+    def __init__(self, text):
+        L = ctypes.CDLL(os.path.join(REF_DIR, "libref_wt_huff.so"))
+        L.ref_huff_new.argtypes = [vp, u64]
+        L.ref_huff_new.restype = vp
+        L.ref_huff_free.argtypes = [vp]
+        for f in ("ref_huff_info", "ref_huff_bits", "ref_huff_rank"):
+            getattr(L, f).argtypes = [vp, vp]
+        L.ref_huff_rank_words.argtypes = [vp]
+        L.ref_huff_rank_words.restype = u64
+        L.ref_huff_nodes.argtypes = [vp, vp, vp, vp]
+        L.ref_huff_select.argtypes = [vp, ctypes.c_int, vp, vp, vp, vp]
+        L.ref_huff_access.argtypes = [vp, u64]
+        L.ref_huff_access.restype = u64
+        L.ref_huff_rank_query.argtypes = [vp, u64, u64]
+        L.ref_huff_rank_query.restype = u64
+        L.ref_huff_select_query.argtypes = [vp, u64, u64]
+        L.ref_huff_select_query.restype = u64
+        self.L = L
+        self.text = np.ascontiguousarray(text, dtype=np.uint8)
+        self.h = L.ref_huff_new(_p(self.text), self.text.size)
+        if not self.h:
+            raise RuntimeError("reference wt_huff constructor failed")
+        info = np.zeros(4, dtype=np.uint64)
+        L.ref_huff_info(self.h, _p(info))
+        self.n, self.sigma, self.size, nn = [int(x) for x in info]
+        self.words = np.zeros((self.size + 63) // 64 + 1, dtype=np.uint64)
+        L.ref_huff_bits(self.h, _p(self.words))
+        self.words = self.words[: (self.size + 63) // 64]
+        self.rank_tbl = np.zeros(max(L.ref_huff_rank_words(self.h), 1), dtype=np.uint64)
+        L.ref_huff_rank(self.h, _p(self.rank_tbl))
+        self.rank_tbl = self.rank_tbl[: L.ref_huff_rank_words(self.h)]
+        self.nodes = np.zeros((max(nn, 1), 5), dtype=np.uint64)
+        self.leaf = np.zeros(256, dtype=np.uint64)
+        self.path = np.zeros(256, dtype=np.uint64)
+        L.ref_huff_nodes(self.h, _p(self.nodes), _p(self.leaf), _p(self.path))
+        self.nodes = self.nodes[:nn]
+
+    def select_tables(self, t_b):
+        info = np.zeros(8, dtype=np.uint64)
+        self.L.ref_huff_select(self.h, t_b, _p(info), None, None, None)
+        sb = np.zeros(max(int(info[6]), 1), dtype=np.uint64)
+        desc = np.zeros(max(int(info[4]), 1), dtype=np.uint64)
+        pool = np.zeros(max(int(info[7]), 1), dtype=np.uint64)
+        self.L.ref_huff_select(self.h, t_b, _p(info), _p(sb), _p(desc), _p(pool))
+        return info, sb[: int(info[6])], desc[: int(info[4])], pool[: int(info[7])]
+
+    def access(self, i):
+        return int(self.L.ref_huff_access(self.h, int(i)))
+
+    def rank(self, i, c):
+        return int(self.L.ref_huff_rank_query(self.h, int(i), int(c)))
+
+    def select(self, i, c):
+        return int(self.L.ref_huff_select_query(self.h, int(i), int(c)))
+
+    def __del__(self):
+        try:
+            if self.h:
+                self.L.ref_huff_free(self.h)
+                self.h = None
+        except Exception:
+            pass
 
 
 class RefWtInt:

@@ -46,6 +46,12 @@ inline uint32_t sel(uint64_t x, uint32_t i) {
   return (uint32_t)__builtin_ctzll(x);
 }
 inline uint64_t lo_set_f(uint32_t k) { return k >= 64 ? ~0ull : ((1ull << k) - 1); }
+// x with its 64 bits in reverse order
+inline uint64_t rev(uint64_t x) {
+  uint64_t r = 0;
+  for (int k = 0; k < 64; ++k, x >>= 1) r = (r << 1) | (x & 1);
+  return r;
+}
 inline uint64_t lo_unset_f(uint32_t k) { return k >= 64 ? 0ull : (~0ull << k); }
 }  // namespace bits
 
@@ -163,6 +169,15 @@ class int_vector {
     if (sh + m_width > 64) {
       uint32_t r = 64 - sh;
       m_data[wi + 1] = (m_data[wi + 1] & ~(mask >> r)) | (x >> r);
+    }
+  }
+
+  // the `len` (<= 64) low bits of x at bit position idx
+  void set_int(size_type idx, uint64_t x, uint8_t len = 64) {
+    for (uint8_t k = 0; k < len; ++k) {
+      const uint64_t p = idx + k;
+      const uint64_t m = 1ull << (p & 63);
+      m_data[p >> 6] = ((x >> k) & 1) ? (m_data[p >> 6] | m) : (m_data[p >> 6] & ~m);
     }
   }
 

@@ -41,8 +41,8 @@ def test_batch_matches_single_builds(wtg, L):
     b.run()
     b.sync()
     _compare(wtg, b, texts, L)
-    threads, ipt, ms = b.tuning()
-    assert threads in (256, 512, 1024) and ipt in (4, 8, 16) and (ms > 0).sum() >= 1
+    tile, ipt, ms = b.tuning()
+    assert tile in (4096, 8192, 16384, 32768) and ipt in (4, 8, 16) and (ms > 0).sum() >= 1
 
 
 def test_sparse_texts_take_long_blocks(wtg):

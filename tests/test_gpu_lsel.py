@@ -69,7 +69,10 @@ def _check_windows(ls, lb, t_b):
 
 
 CASES = [("exp20", 300001, 20, 1024), ("exp20", 1 << 18, 20, 1024), ("zipf8", 100003, 8, 1024),
-         ("bin1", 65, 1, 1024), ("tiny5", 37, 5, 4), ("u16_12", 77777, 12, 64), ("allsame", 4099, 3, 1024)]
+         ("bin1", 65, 1, 1024), ("tiny5", 37, 5, 4), ("u16_12", 77777, 12, 64), ("allsame", 4099, 3, 1024),
+         # n % 512 == 0: the levels start on superblocks and queries go through the compact rank directory
+         ("zipf8", 1 << 17, 8, 1024), ("u16_12", 153600, 12, 64), ("bin1", 512, 1, 1024),
+         ("exp20", 1 << 20, 20, 65536), ("tiny5", 1024, 5, 4), ("allsame", 4096, 3, 1024)]
 
 
 def _gen(kind, n, seed):
@@ -107,8 +110,9 @@ def test_learned_and_plain_level_select_match_oracle(wtg, oracle, kind, n, L, se
     assert info["segments"] == sum(ls.level_model(tb, l)[0]["nseg"] for tb in (0, 1) for l in range(L))
 
 
-def test_every_k_of_small_tree(wtg, oracle):
-    sym = datagen.exp_u32(5000, mean=2 ** 6, seed=11)
+@pytest.mark.parametrize("n", [5000, 5120])  # 5120 % 512 == 0: through the compact rank directory
+def test_every_k_of_small_tree(wtg, oracle, n):
+    sym = datagen.exp_u32(n, mean=2 ** 6, seed=11)
     L = 12
     t, w = _tree(wtg, oracle, sym, L)
     lb = _level_bits(w, sym.size, L)
@@ -122,8 +126,9 @@ def test_every_k_of_small_tree(wtg, oracle):
         assert np.array_equal(t.level_select(lv, k, t_b), exp)
 
 
-def test_fallback_paths_stay_exact(wtg, oracle):
-    sym = datagen.exp_u32(200000, seed=5)
+@pytest.mark.parametrize("n", [200000, 204800])
+def test_fallback_paths_stay_exact(wtg, oracle, n):
+    sym = datagen.exp_u32(n, seed=5)
     L = 20
     t, w = _tree(wtg, oracle, sym, L)
     lb = _level_bits(w, sym.size, L)

@@ -247,57 +247,55 @@ __global__ void __launch_bounds__(256)
         cnt[j] = cj;
         if (j) part |= (uint64_t)excl << (63 - 9 * j);
         if (sel) {
-          const uint32_t K1 = k1_base + excl;                         // ones before the word (mod 2^32)
-          const uint32_t K0 = k0_base + 64u * j - excl;               // zeros before it
+          // branch-free: the select runs for every word, the stores are predicated
+          const uint32_t K1 = k1_base + excl;            // ones before the word (mod 2^32)
+          const uint32_t K0 = k0_base + 64u * j - excl;  // zeros before it
           const uint32_t d1 = (0u - K1) & 63u, d0 = K1 & 63u;
           const bool s1 = sel1 && d1 < cj, s0 = sel0 && d0 < 64u - cj;
-          if (s1 || s0) {
-            const uint64_t v = s1 ? x : ~x;
-            const uint32_t off = sel64_lut(v, s1 ? d1 : d0, s1 ? cl : 32u - cl, lut);
-            const uint32_t pos = pos_base + 64u * j + off;
-            if (s1) {
-              p1[n1++] = pos;
-              if (((K1 + d1) & 4095u) == 0) starts1[((sb_before + excl + d1) >> 12)] = 512 * b + 64 * j + off;
-            }
-            if (s0) {
-              // both polarities only when K1 % 64 == 0: the word's first one and first zero
-              const uint32_t off0 = s1 ? (uint32_t)(__ffsll((long long)~x) - 1) : off;
-              *(p0 - n0) = pos_base + 64u * j + off0;
-              ++n0;
-              if (((K0 + d0) & 4095u) == 0)
-                starts0[((zb + 64 * j - excl + d0) >> 12)] = 512 * b + 64 * j + off0;
-            }
-          }
+          const uint32_t off = sel64_lut(s1 ? x : ~x, s1 ? d1 : d0, s1 ? cl : 32u - cl, lut);
+          // both polarities only when K1 % 64 == 0: the word's first one and first zero
+          const uint32_t off0 = s1 ? (uint32_t)(__ffsll((long long)~x) - 1) : off;
+          const uint32_t pos = pos_base + 64u * j;
+          if (s1) p1[n1] = pos + off;
+          if (s0) *(p0 - n0) = pos + off0;
+          if (s1 && ((K1 + d1) & 4095u) == 0) starts1[(sb_before + excl + d1) >> 12] = 512 * b + 64 * j + off;
+          if (s0 && ((K0 + d0) & 4095u) == 0)
+            starts0[(zb + 64 * j - excl + d0) >> 12] = 512 * b + 64 * j + off0;
+          n1 += s1;
+          n0 += s0;
         }
         excl += cj;
       }
       if (flags & WTG_RANK) reinterpret_cast<ulonglong2*>(rank)[b] = make_ulonglong2(sb_before, part);
       if (sel) {
-        // superblock ends: the arg 4095 of a 4096-arg superblock, at most one per polarity here
+        // superblock ends: arg 4095 of a 4096-arg superblock, at most one per
+        // polarity in 512 bits; one scan serves the lane's first polarity,
+        // the rare superblock that ends one of each takes a second
         const uint32_t cz = 512u - excl;
         const uint32_t e1 = 4095u - (k1_base & 4095u), e0 = 4095u - (k0_base & 4095u);
-        const bool h1 = sel1 && e1 < excl, h0 = sel0 && e0 < cz;
-        if (h1 || h0) {
-          // which polarity (both can end here) is resolved one after the other
+        bool h1 = sel1 && e1 < excl, h0 = sel0 && e0 < cz;
+        // the lanes still inside the superblock loop (its last round may hold fewer)
+        const uint32_t live = __activemask();
+        while (__any_sync(live, h1 || h0)) {
+          const bool t1 = h1;  // this round's polarity
+          const uint32_t e = t1 ? e1 : e0;
+          uint32_t before = 0, r = 0;
+          uint64_t xx = 0, jj = 0;
 #pragma unroll
-          for (int t = 1; t >= 0; --t) {
-            if (!(t ? h1 : h0)) continue;
-            const uint32_t e = t ? e1 : e0;
-            uint32_t before = 0, r = 0, jj = 0;
-            uint64_t xx = 0;
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-              const uint32_t cj = t ? cnt[j] : 64u - cnt[j];
-              const bool here = before <= e && e < before + cj;
-              xx = here ? (t ? w[j] : ~w[j]) : xx;
-              r = here ? e - before : r;
-              jj = here ? (uint32_t)j : jj;
-              before += cj;
-            }
-            const uint64_t pos = 512 * b + 64 * jj + sel64_lut(xx, r, __popc((uint32_t)xx), lut);
-            if (t) ends1[(sb_before + e) >> 12] = pos;
-            else ends0[(zb + e) >> 12] = pos;
+          for (int j = 0; j < 8; ++j) {
+            const uint32_t cj = t1 ? cnt[j] : 64u - cnt[j];
+            const bool here = before <= e && e < before + cj;
+            xx = here ? w[j] : xx;
+            r = here ? e - before : r;
+            jj = here ? (uint64_t)j : jj;
+            before += cj;
           }
+          xx = t1 ? xx : ~xx;
+          const uint64_t pos = 512 * b + 64 * jj + sel64_lut(xx, r, __popc((uint32_t)xx), lut);
+          if (h1) ends1[(sb_before + e1) >> 12] = pos;
+          else if (h0) ends0[(zb + e0) >> 12] = pos;
+          if (h1) h1 = false;
+          else h0 = false;
         }
         last_sb1 = excl ? b : last_sb1;
         last_sb0 = cz ? b : last_sb0;

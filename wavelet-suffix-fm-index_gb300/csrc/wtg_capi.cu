@@ -19,6 +19,10 @@ struct wtg_lsel {
   wtg::DevBuf qbuf;
 };
 
+struct wtg_huff {
+  wtg::HuffImpl* h = nullptr;
+};
+
 struct wtg_bv {
   wtg::BvSupport bv;
   wtg::DevBuf words;  // device copy for host-input builds
@@ -881,9 +885,9 @@ int wtg_batch_load(wtg_batch* B, const void* texts) {
   return WTG_OK;
 }
 
-int wtg_batch_set_shape(wtg_batch* B, int threads, int items_per_thread) {
+int wtg_batch_set_shape(wtg_batch* B, int tile, int items_per_thread) {
   if (!B) return fail(WTG_ERR_INVALID, "null batch");
-  return batch_set_shape(*B->b, threads, items_per_thread);
+  return batch_set_shape(*B->b, tile, items_per_thread);
 }
 
 int wtg_batch_run(wtg_batch* B) {
@@ -939,9 +943,182 @@ int wtg_batch_get_select(wtg_batch* B, uint64_t t, int t_b, uint64_t* sb_words, 
   return batch_get(*B->b, t, 4, t_b, pool, si[7]);
 }
 
-int wtg_batch_tuning(wtg_batch* B, int* threads, int* items_per_thread, float ms[8]) {
-  if (!B || !threads || !items_per_thread || !ms) return fail(WTG_ERR_INVALID, "null argument");
-  return batch_tuning(*B->b, threads, items_per_thread, ms, 8);
+int wtg_batch_tuning(wtg_batch* B, int* tile, int* items_per_thread, float ms[8]) {
+  if (!B || !tile || !items_per_thread || !ms) return fail(WTG_ERR_INVALID, "null argument");
+  return batch_tuning(*B->b, tile, items_per_thread, ms, 8);
+}
+
+// ------------------------------------------------ Huffman-shaped trees
+
+static int huff_common(wtg_huff* H, const uint8_t* d_text, uint64_t n, uint32_t flags) {
+  int rc = huff_build(*H->h, d_text, n, flags);
+  if (rc) return rc;
+  return sync_and_check(huff_stream(*H->h), huff_err(*H->h));
+}
+
+int wtg_huff_build(const uint8_t* text, uint64_t n, uint32_t flags, wtg_huff** out) {
+  int rc;
+  if (!out || (!text && n)) return fail(WTG_ERR_INVALID, "null argument");
+  *out = nullptr;
+  if ((rc = check_device())) return rc;
+  wtg_huff* H = new (std::nothrow) wtg_huff();
+  if (!H || !(H->h = huff_new())) {
+    delete H;
+    return fail(WTG_ERR_OOM, "host allocation failed");
+  }
+  cudaStream_t s = nullptr;
+  cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    huff_delete(H->h);
+    delete H;
+    return cuda_fail(e, "cudaStreamCreate");
+  }
+  huff_set_stream(*H->h, s, true);
+  DevBuf& t = huff_text(*H->h);
+  rc = t.ensure(n + 16, s);
+  if (rc == WTG_OK && n) {
+    const cudaError_t ce = cudaMemcpyAsync(t.p, text, n, cudaMemcpyHostToDevice, s);
+    if (ce != cudaSuccess) rc = cuda_fail(ce, "cudaMemcpyAsync(text)");
+  }
+  if (rc == WTG_OK) rc = huff_common(H, t.as<uint8_t>(), n, flags);
+  if (rc != WTG_OK) {
+    wtg_huff_free(H);
+    return rc;
+  }
+  *out = H;
+  return WTG_OK;
+}
+
+int wtg_huff_build_device(const uint8_t* d_text, uint64_t n, uint32_t flags, void* stream, wtg_huff** out) {
+  int rc;
+  if (!out || (!d_text && n)) return fail(WTG_ERR_INVALID, "null argument");
+  *out = nullptr;
+  if ((rc = check_device())) return rc;
+  wtg_huff* H = new (std::nothrow) wtg_huff();
+  if (!H || !(H->h = huff_new())) {
+    delete H;
+    return fail(WTG_ERR_OOM, "host allocation failed");
+  }
+  huff_set_stream(*H->h, (cudaStream_t)stream, false);
+  if ((rc = huff_common(H, d_text, n, flags))) {
+    wtg_huff_free(H);
+    return rc;
+  }
+  *out = H;
+  return WTG_OK;
+}
+
+int wtg_huff_free(wtg_huff* H) {
+  if (!H) return WTG_OK;
+  huff_delete(H->h);
+  delete H;
+  return WTG_OK;
+}
+
+int wtg_huff_info(wtg_huff* H, uint64_t info[5]) {
+  if (!H || !info) return fail(WTG_ERR_INVALID, "null argument");
+  return huff_info(*H->h, info);
+}
+
+int wtg_huff_get_bits(wtg_huff* H, uint64_t* dst, uint64_t nwords) {
+  if (!H || (!dst && nwords)) return fail(WTG_ERR_INVALID, "null argument");
+  uint64_t info[5];
+  huff_info(*H->h, info);
+  if (nwords != (info[2] + 63) / 64) return fail(WTG_ERR_INVALID, "nwords does not match the tree");
+  cudaStream_t s = huff_stream(*H->h);
+  if (nwords) WTG_CK(cudaMemcpyAsync(dst, huff_bits(*H->h), nwords * 8, cudaMemcpyDeviceToHost, s));
+  return sync_and_check(s, huff_err(*H->h));
+}
+
+int wtg_huff_get_tree(wtg_huff* H, uint64_t* nodes, uint64_t* leaves, uint64_t* paths) {
+  if (!H || !nodes || !leaves || !paths) return fail(WTG_ERR_INVALID, "null argument");
+  return huff_tree(*H->h, nodes, leaves, paths);
+}
+
+int wtg_huff_get_rank(wtg_huff* H, uint64_t* dst, uint64_t nwords) {
+  if (!H || !dst) return fail(WTG_ERR_INVALID, "null argument");
+  uint64_t info[5];
+  huff_info(*H->h, info);
+  if (!info[4]) return fail(WTG_ERR_INVALID, "rank support not built");
+  if (nwords != info[4]) return fail(WTG_ERR_INVALID, "nwords mismatch");
+  cudaStream_t s = huff_stream(*H->h);
+  WTG_CK(cudaMemcpyAsync(dst, huff_bv(*H->h).rank.p, nwords * 8, cudaMemcpyDeviceToHost, s));
+  return sync_and_check(s, huff_err(*H->h));
+}
+
+int wtg_huff_select_info(wtg_huff* H, int t_b, uint64_t info[8]) {
+  if (!H || !info || (t_b != 0 && t_b != 1)) return fail(WTG_ERR_INVALID, "bad argument");
+  BvSupport& bv = huff_bv(*H->h);
+  if (!(bv.flags & (t_b ? WTG_SELECT1 : WTG_SELECT0))) return fail(WTG_ERR_INVALID, "select support not built");
+  fill_select_info(bv, t_b, info);
+  return WTG_OK;
+}
+
+int wtg_huff_get_select(wtg_huff* H, int t_b, uint64_t* sb_words, uint64_t* desc, uint64_t* pool) {
+  if (!H || (t_b != 0 && t_b != 1)) return fail(WTG_ERR_INVALID, "bad argument");
+  int rc = copy_select(huff_bv(*H->h), t_b, sb_words, desc, pool, huff_stream(*H->h));
+  if (rc) return rc;
+  return sync_and_check(huff_stream(*H->h), huff_err(*H->h));
+}
+
+static int huff_host_query(wtg_huff* H, int what, const uint64_t* a, const uint64_t* b, uint64_t nq, uint64_t* out,
+                           uint64_t* out2) {
+  HuffImpl& h = *H->h;
+  const uint64_t* ins[2] = {a, b};
+  uint64_t* outs[2] = {out, out2};
+  const int nin = (what == 1 || what == 2) ? 2 : 1, nout = what == 3 ? 2 : 1;
+  cudaStream_t s = huff_stream(h);
+  return host_query(huff_qbuf(h), s, ins, nin, nq, outs, nout, huff_err(h),
+                    [&](const uint64_t** din, uint64_t** dout) {
+                      return launch_huff_query(h, what, din[0], nin > 1 ? din[1] : nullptr, nq, dout[0],
+                                               nout > 1 ? dout[1] : nullptr, s);
+                    });
+}
+
+int wtg_huff_access(wtg_huff* H, const uint64_t* idx, uint64_t nq, uint64_t* out) {
+  if (!H || (nq && (!idx || !out))) return fail(WTG_ERR_INVALID, "null argument");
+  return huff_host_query(H, 0, idx, nullptr, nq, out, nullptr);
+}
+
+int wtg_huff_rank(wtg_huff* H, const uint64_t* idx, const uint64_t* sym, uint64_t nq, uint64_t* out) {
+  if (!H || (nq && (!idx || !sym || !out))) return fail(WTG_ERR_INVALID, "null argument");
+  return huff_host_query(H, 1, idx, sym, nq, out, nullptr);
+}
+
+int wtg_huff_select(wtg_huff* H, const uint64_t* i, const uint64_t* sym, uint64_t nq, uint64_t* out) {
+  if (!H || (nq && (!i || !sym || !out))) return fail(WTG_ERR_INVALID, "null argument");
+  return huff_host_query(H, 2, i, sym, nq, out, nullptr);
+}
+
+int wtg_huff_inverse_select(wtg_huff* H, const uint64_t* idx, uint64_t nq, uint64_t* rank_out, uint64_t* sym_out) {
+  if (!H || (nq && (!idx || !rank_out || !sym_out))) return fail(WTG_ERR_INVALID, "null argument");
+  return huff_host_query(H, 3, idx, nullptr, nq, rank_out, sym_out);
+}
+
+int wtg_huff_fm_count(wtg_huff* H, const uint64_t* C, const uint8_t* pat, const uint64_t* off, uint64_t npat,
+                      uint64_t* out) {
+  int rc;
+  if (!H || !C || (npat && (!off || !out))) return fail(WTG_ERR_INVALID, "null argument");
+  if (npat == 0) return WTG_OK;
+  const uint64_t total = off[npat];
+  if (total && !pat) return fail(WTG_ERR_INVALID, "null patterns");
+  for (uint64_t p = 0; p < npat; ++p)
+    if (off[p] > off[p + 1]) return fail(WTG_ERR_INVALID, "pattern offsets must not decrease");
+  HuffImpl& h = *H->h;
+  cudaStream_t s = huff_stream(h);
+  DevBuf& q = huff_qbuf(h);
+  const uint64_t words = 256 + (npat + 1) + npat + (total + 7) / 8;
+  if ((rc = q.ensure(words * sizeof(uint64_t), s))) return rc;
+  uint64_t* dC = q.as<uint64_t>();
+  uint64_t* dOff = dC + 256;
+  uint64_t* dOut = dOff + npat + 1;
+  uint8_t* dPat = (uint8_t*)(dOut + npat);
+  WTG_CK(cudaMemcpyAsync(dC, C, 256 * 8, cudaMemcpyHostToDevice, s));
+  WTG_CK(cudaMemcpyAsync(dOff, off, (npat + 1) * 8, cudaMemcpyHostToDevice, s));
+  if (total) WTG_CK(cudaMemcpyAsync(dPat, pat, total, cudaMemcpyHostToDevice, s));
+  if ((rc = launch_huff_fm_count(h, dC, dPat, dOff, npat, dOut, s))) return rc;
+  WTG_CK(cudaMemcpyAsync(out, dOut, npat * 8, cudaMemcpyDeviceToHost, s));
+  return sync_and_check(s, huff_err(h));
 }
 
 // ------------------------------------------------ sdsl serialize() streams

@@ -127,7 +127,7 @@ void batch_delete(BatchImpl* b);
 int batch_plan(BatchImpl& b, const uint64_t* lengths, uint64_t T, int L, uint32_t flags, cudaStream_t s,
                bool own_stream);
 int batch_run(BatchImpl& b);
-int batch_set_shape(BatchImpl& b, int threads, int ipt);
+int batch_set_shape(BatchImpl& b, int tile, int ipt);
 int batch_sync(BatchImpl& b, uint32_t* err_out);
 int batch_text_info(const BatchImpl& b, uint64_t t, uint64_t info[8]);
 int batch_select_info(const BatchImpl& b, uint64_t t, int t_b, uint64_t info[8]);
@@ -136,7 +136,27 @@ int batch_get(const BatchImpl& b, uint64_t t, int what, int t_b, void* dst, uint
 void* batch_input(BatchImpl& b);
 cudaStream_t batch_stream(const BatchImpl& b);
 uint64_t batch_total_symbols(const BatchImpl& b);
-int batch_tuning(const BatchImpl& b, int* threads, int* ipt, float* ms, int nms);
+int batch_tuning(const BatchImpl& b, int* tile, int* ipt, float* ms, int nms);
+
+// Huffman-shaped wavelet tree of a byte text (wtg_huff.cu)
+struct HuffImpl;
+HuffImpl* huff_new();
+void huff_delete(HuffImpl* h);
+void huff_set_stream(HuffImpl& h, cudaStream_t s, bool own);
+cudaStream_t huff_stream(const HuffImpl& h);
+int huff_build(HuffImpl& h, const uint8_t* d_text, uint64_t n, uint32_t flags);
+int huff_info(const HuffImpl& h, uint64_t info[5]);  // n, sigma, bits, nodes, rank words
+int huff_tree(HuffImpl& h, uint64_t* nodes, uint64_t* leaves, uint64_t* paths);
+BvSupport& huff_bv(HuffImpl& h);
+const uint64_t* huff_bits(const HuffImpl& h);
+DevBuf& huff_text(HuffImpl& h);
+DevBuf& huff_qbuf(HuffImpl& h);
+const uint32_t* huff_err(const HuffImpl& h);
+// what: 0 access, 1 rank(a, b), 2 select(a, b), 3 inverse_select (out, out2)
+int launch_huff_query(HuffImpl& h, int what, const uint64_t* a, const uint64_t* b, uint64_t nq, uint64_t* out,
+                      uint64_t* out2, cudaStream_t s);
+int launch_huff_fm_count(HuffImpl& h, const uint64_t* C, const uint8_t* pat, const uint64_t* off, uint64_t npat,
+                         uint64_t* out, cudaStream_t s);
 
 // sdsl serialize() streams (wtg_serialize.cu): with dst NULL only *len is
 // set; otherwise dst (host memory, cap bytes) receives the stream

@@ -117,6 +117,20 @@ _SIGS = {
     "wtg_rank_build_noalloc": ([vp, u64, vp, vp], i32),
     "wtg_profile_enable": ([i32], i32),
     "wtg_profile_read": ([vp, vp], i32),
+    "wtg_huff_build": ([vp, u64, ctypes.c_uint32, vp], i32),
+    "wtg_huff_build_device": ([vp, u64, ctypes.c_uint32, vp, vp], i32),
+    "wtg_huff_free": ([vp], i32),
+    "wtg_huff_info": ([vp, vp], i32),
+    "wtg_huff_get_bits": ([vp, vp, u64], i32),
+    "wtg_huff_get_tree": ([vp, vp, vp, vp], i32),
+    "wtg_huff_get_rank": ([vp, vp, u64], i32),
+    "wtg_huff_select_info": ([vp, i32, vp], i32),
+    "wtg_huff_get_select": ([vp, i32, vp, vp, vp], i32),
+    "wtg_huff_access": ([vp, vp, u64, vp], i32),
+    "wtg_huff_rank": ([vp, vp, vp, u64, vp], i32),
+    "wtg_huff_select": ([vp, vp, vp, u64, vp], i32),
+    "wtg_huff_inverse_select": ([vp, vp, u64, vp, vp], i32),
+    "wtg_huff_fm_count": ([vp, vp, vp, vp, u64, vp], i32),
     "wtg_tree_serialize": ([vp, vp, u64, vp], i32),
     "wtg_tree_sigma": ([vp, vp], i32),
     "wtg_bv_serialize": ([vp, ctypes.c_uint32, vp, u64, vp], i32),
@@ -630,6 +644,100 @@ class FMIndex:
                                       vp(stream)))
 
 
+class HuffmanTree:
+    """Huffman-shaped wavelet tree of a byte text (sdsl::wt_huff<>) built on
+    the GPU, with rank_support_v / select_support_mcl over its bitvector
+    (include/wtg.h: wtg_huff_build)."""
+
+    def __init__(self, text=None, flags=ALL, _handle=None):
+        self.h = vp()
+        if _handle is not None:
+            self.h = _handle
+        else:
+            text = np.ascontiguousarray(text, dtype=np.uint8)
+            _ck(lib().wtg_huff_build(_p(text), text.size, flags, ctypes.byref(self.h)))
+        info = np.zeros(5, dtype=np.uint64)
+        _ck(lib().wtg_huff_info(self.h, _p(info)))
+        self.n, self.sigma, self.size, self.num_nodes, self.rank_words = [int(x) for x in info]
+
+    @classmethod
+    def from_device(cls, d_text, n, flags=ALL, stream=0):
+        h = vp()
+        _ck(lib().wtg_huff_build_device(vp(d_text), int(n), flags, vp(stream), ctypes.byref(h)))
+        return cls(_handle=h)
+
+    def free(self):
+        if self.h:
+            lib().wtg_huff_free(self.h)
+            self.h = vp()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def bits(self):
+        out = np.zeros((self.size + 63) // 64, dtype=np.uint64)
+        _ck(lib().wtg_huff_get_bits(self.h, _p(out), out.size))
+        return out
+
+    def tree(self):
+        """(nodes [m, 5]: bv_pos, bv_pos_rank, parent, child0, child1; leaf
+        per byte; path per byte, length in the top 8 bits)."""
+        nodes = np.zeros((max(self.num_nodes, 1), 5), dtype=np.uint64)
+        leaves, paths = np.zeros(256, dtype=np.uint64), np.zeros(256, dtype=np.uint64)
+        _ck(lib().wtg_huff_get_tree(self.h, _p(nodes), _p(leaves), _p(paths)))
+        return nodes[: self.num_nodes], leaves, paths
+
+    def rank_table(self):
+        out = np.zeros(self.rank_words, dtype=np.uint64)
+        _ck(lib().wtg_huff_get_rank(self.h, _p(out), out.size))
+        return out
+
+    def select_tables(self, t_b):
+        info = np.zeros(8, dtype=np.uint64)
+        _ck(lib().wtg_huff_select_info(self.h, t_b, _p(info)))
+        sb = np.zeros(max(int(info[6]), 1), dtype=np.uint64)
+        desc = np.zeros(max(int(info[4]), 1), dtype=np.uint64)
+        pool = np.zeros(max(int(info[7]), 1), dtype=np.uint64)
+        _ck(lib().wtg_huff_get_select(self.h, t_b, _p(sb), _p(desc), _p(pool)))
+        return _SelectTables(info, sb[: int(info[6])], desc[: int(info[4])], pool[: int(info[7])])
+
+    def access(self, idx):
+        idx = _u64(idx)
+        out = np.zeros(idx.size, dtype=np.uint64)
+        _ck(lib().wtg_huff_access(self.h, _p(idx), idx.size, _p(out)))
+        return out
+
+    def rank(self, idx, sym):
+        idx, sym = _u64(idx), _u64(sym)
+        out = np.zeros(idx.size, dtype=np.uint64)
+        _ck(lib().wtg_huff_rank(self.h, _p(idx), _p(sym), idx.size, _p(out)))
+        return out
+
+    def select(self, i, sym):
+        i, sym = _u64(i), _u64(sym)
+        out = np.zeros(i.size, dtype=np.uint64)
+        _ck(lib().wtg_huff_select(self.h, _p(i), _p(sym), i.size, _p(out)))
+        return out
+
+    def inverse_select(self, idx):
+        idx = _u64(idx)
+        r, c = np.zeros(idx.size, dtype=np.uint64), np.zeros(idx.size, dtype=np.uint64)
+        _ck(lib().wtg_huff_inverse_select(self.h, _p(idx), idx.size, _p(r), _p(c)))
+        return r, c
+
+    def fm_count(self, C, pat, off):
+        """Backward-search counts over the tree of a BWT: C[c] = bytes below c
+        (256 entries), patterns pat[off[q]:off[q+1]] (bytes)."""
+        C, off = _u64(C), _u64(off)
+        pat = np.ascontiguousarray(pat, dtype=np.uint8)
+        out = np.zeros(off.size - 1, dtype=np.uint64)
+        _ck(lib().wtg_huff_fm_count(self.h, _p(C), _p(pat) if pat.size else None, _p(off), out.size, _p(out)))
+        return out
+
+
 class Batch:
     """Many independent texts (u8 symbols, 1..4 levels), each with its own
     wavelet tree, rank_support_v and select_support_mcl, built in one
@@ -660,8 +768,9 @@ class Batch:
     def run(self):
         _ck(lib().wtg_batch_run(self.h))
 
-    def set_shape(self, threads, items_per_thread):
-        _ck(lib().wtg_batch_set_shape(self.h, threads, items_per_thread))
+    def set_shape(self, tile, items_per_thread):
+        """Fix the launch shape: symbols per H / W work item and per thread per chunk."""
+        _ck(lib().wtg_batch_set_shape(self.h, tile, items_per_thread))
 
     def sync(self):
         _ck(lib().wtg_batch_sync(self.h))
@@ -680,7 +789,7 @@ class Batch:
     def text_info(self, t):
         a = np.zeros(8, dtype=np.uint64)
         _ck(lib().wtg_batch_text_info(self.h, t, _p(a)))
-        return dict(zip(("n", "levels", "bit_words", "rank_words", "ones", "zeros", "threads", "ipt"),
+        return dict(zip(("n", "levels", "bit_words", "rank_words", "ones", "zeros", "tile", "ipt"),
                         (int(x) for x in a)))
 
     def bits(self, t):
