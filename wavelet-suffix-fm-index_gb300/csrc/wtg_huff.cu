@@ -116,7 +116,8 @@ __global__ void __launch_bounds__(HUFF_THREADS)
 
 // scatter constants of the children of depth-d inner node v: left child gets
 // the symbols going 0 at base0 + (zeros before them at this depth), right
-// child the 1s at base1 + (ones before them); UINT64_MAX for a leaf child
+// child the 1s at base1 + (ones before them), modulo 2^64 (unused for a leaf
+// child)
 __global__ void huff_node_kernel(const HuffNodeDev* __restrict__ nodes, const uint16_t* __restrict__ ids, int count,
                                  uint64_t D, uint64_t Dnext, const uint32_t* __restrict__ chunkpre,
                                  const uint64_t* __restrict__ bits, uint64_t* __restrict__ nbase) {
@@ -135,8 +136,8 @@ __global__ void huff_node_kernel(const HuffNodeDev* __restrict__ nodes, const ui
     p += take;
   }
   const uint16_t c0 = nodes[v].child0, c1 = nodes[v].child1;
-  nbase[2 * v] = nodes[c0].leaf ? ~0ull : (nodes[c0].bv_pos - Dnext) - z;
-  nbase[2 * v + 1] = nodes[c1].leaf ? ~0ull : (nodes[c1].bv_pos - Dnext) - (start - z);
+  nbase[2 * v] = (nodes[c0].bv_pos - Dnext) - z;
+  nbase[2 * v + 1] = (nodes[c1].bv_pos - Dnext) - (start - z);
 }
 
 __global__ void __launch_bounds__(HUFF_THREADS)
@@ -167,13 +168,12 @@ __global__ void __launch_bounds__(HUFF_THREADS)
       const uint32_t zm = __ballot_sync(0xffffffffu, valid && !b);
       const uint64_t zb = z + __popc(zm & lt);  // zeros before symbol i
       z += __popc(zm);
-      if (valid) {
-        const uint64_t base = nbase[2 * s_node[x] + b];
-        if (base != ~0ull) {
-          const uint64_t dest = base + (b ? i - zb : zb);
-          if (dest < cnt_next) dst[dest] = x;
-          else bad = true;
-        }
+      // a symbol whose code ends at depth d + 1 reaches a leaf and leaves the
+      // sequence (bases are modular: no base value can mark a leaf child)
+      if (valid && (uint32_t)(s_path[x] >> 56) > (uint32_t)d + 1) {
+        const uint64_t dest = nbase[2 * s_node[x] + b] + (b ? i - zb : zb);
+        if (dest < cnt_next) dst[dest] = x;
+        else bad = true;
       }
     }
     if (__any_sync(0xffffffffu, bad) && lane == 0) atomicCAS(err, 0u, (uint32_t)DERR_BAD_INDEX);
