@@ -229,22 +229,22 @@ int wtg_rank_build_noalloc(const uint64_t* d_words, uint64_t size_bits, uint64_t
  * (wavelet/levelWT/WT.h:43) or of wt_int constructions
  * (wt_int/wt_int_par.hpp:368-406) plus init_support would give, one text per
  * call -- built in one persistent launch that pulls work items from a
- * device queue, replayed from a CUDA graph after the first run.  The items,
- * in phase order: (text, tile) key histograms, (text, level, tile) level
- * bits, (text, rank tile) rank_support_v entries and select samples, (text)
- * select_support_mcl finishing; each waits for its text's previous phase.
+ * device queue, replayed from a CUDA graph after the first run.  A text of
+ * at most `whole_max` symbols is one item, built by one CTA from histogram
+ * to select tables; a longer text is split into (text, tile) key
+ * histograms, (text, tile) level bits of every level, (text, rank tile)
+ * rank_support_v entries and select samples, and (text) select_support_mcl
+ * finishing, each waiting for its text's previous phase.
  *   lengths : symbols of each text (ntexts entries); texts are u8 symbols
  *             read through their low `levels` bits, concatenated in order
  *   levels  : 1..4
  *   flags   : WTG_RANK | WTG_SELECT1 | WTG_SELECT0 (select implies rank)
  *   stream  : the stream the batch runs on (NULL: the batch makes its own)
  * The plan allocates every output region (sizes follow from the lengths).
- * The first wtg_batch_run times each launch shape (symbols per histogram /
- * level-bits tile x symbols per thread per chunk) on the loaded input, keeps
- * the fastest and captures the build in a CUDA graph; later runs replay the
- * graph.  Per-text outputs have the single-sequence layouts
- * (wtg_tree_get_bits / _get_rank / _get_select of a tree built with the same
- * levels). */
+ * The first wtg_batch_run uploads the item list and captures the build in a
+ * CUDA graph; later runs replay the graph.  Per-text outputs have the
+ * single-sequence layouts (wtg_tree_get_bits / _get_rank / _get_select of a
+ * tree built with the same levels). */
 int wtg_batch_plan(const uint64_t* lengths, uint64_t ntexts, int levels, uint32_t flags, void* stream,
                    wtg_batch** out);
 /* device address and size of the input buffer (the concatenated texts) */
@@ -252,23 +252,24 @@ int wtg_batch_input(wtg_batch* b, void** d_input, uint64_t* nbytes);
 /* copy the concatenated texts from host memory into the input buffer */
 int wtg_batch_load(wtg_batch* b, const void* texts);
 int wtg_batch_run(wtg_batch* b);
-/* fix the launch shape instead of timing the candidates on the first run:
- * (symbols per tile, symbols per thread per chunk) one of (4096, 4),
- * (8192, 4), (4096, 8), (8192, 8), (16384, 8), (8192, 16), (16384, 16),
- * (32768, 16) */
-int wtg_batch_set_shape(wtg_batch* b, int tile, int items_per_thread);
+/* the shape of the work list (before the next run): `tile` symbols per
+ * split-text tile (a multiple of 8192, 8192 .. 2^24; default 65536) and the
+ * longest text built whole by one CTA (-1, the default: the total symbols
+ * over the resident CTAs, at least 65536; 0: every text split) */
+int wtg_batch_set_shape(wtg_batch* b, int tile, int64_t whole_max);
 int wtg_batch_sync(wtg_batch* b);
 int wtg_batch_free(wtg_batch* b);
 /* after wtg_batch_sync.  text info: n, levels, bit words, rank words, ones,
- * zeros, and the chosen symbols per tile and symbols per thread */
+ * zeros, symbols per split tile, and 1 if the text was built whole */
 int wtg_batch_text_info(wtg_batch* b, uint64_t t, uint64_t info[8]);
 /* select info[8] of text t, as wtg_tree_select_info */
 int wtg_batch_select_info(wtg_batch* b, uint64_t t, int t_b, uint64_t info[8]);
 int wtg_batch_get_bits(wtg_batch* b, uint64_t t, uint64_t* dst, uint64_t nwords);
 int wtg_batch_get_rank(wtg_batch* b, uint64_t t, uint64_t* dst, uint64_t nwords);
 int wtg_batch_get_select(wtg_batch* b, uint64_t t, int t_b, uint64_t* sb_words, uint64_t* desc, uint64_t* pool);
-/* the launch shape the first run chose, and the time of each candidate (ms) */
-int wtg_batch_tuning(wtg_batch* b, int* tile, int* items_per_thread, float ms[8]);
+/* after a run: the split tile, the whole-text bound in use, and how many
+ * texts were built whole */
+int wtg_batch_shape(wtg_batch* b, int* tile, int64_t* whole_max, uint64_t* whole_texts);
 
 /* ------------------------------------------------- suffix array and BWT
  * The first two steps of the reference's FM-index construction

@@ -41,8 +41,29 @@ def test_batch_matches_single_builds(wtg, L):
     b.run()
     b.sync()
     _compare(wtg, b, texts, L)
-    tile, ipt, ms = b.tuning()
-    assert tile in (4096, 8192, 16384, 32768) and ipt in (4, 8, 16) and (ms > 0).sum() >= 1
+    tile, whole_max, nwhole = b.shape()
+    assert tile == 65536 and whole_max >= 65536 and nwhole == len(texts)
+    assert all(b.text_info(t)["whole"] == 1 for t in range(len(texts)))
+
+
+@pytest.mark.parametrize("L", [1, 2, 3, 4])
+@pytest.mark.parametrize("whole_max", [0, 5000])
+def test_split_texts_match_single_builds(wtg, L, whole_max):
+    """Texts longer than the whole-text bound go through the tiled items
+    (histogram / level bits / rank tiles with look-back / select): the
+    smallest tile, so that many texts span several tiles and rank tiles."""
+    rng = np.random.default_rng(200 + L)
+    texts = _texts(rng, 60, L, max_log2=18)
+    texts.append(rng.integers(0, 1 << L, 600001).astype(np.uint8))
+    b = wtg.Batch.from_texts(texts, L)
+    b.set_shape(8192, whole_max)
+    b.run()
+    b.sync()
+    _compare(wtg, b, texts, L)
+    tile, wm, nwhole = b.shape()
+    assert (tile, wm) == (8192, whole_max)
+    assert nwhole == sum(len(s) <= whole_max for s in texts)
+    assert all(b.text_info(t)["whole"] == int(len(s) <= whole_max) for t, s in enumerate(texts))
 
 
 def test_sparse_texts_take_long_blocks(wtg):

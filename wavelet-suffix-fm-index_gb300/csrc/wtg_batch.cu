@@ -4,20 +4,20 @@
 //
 // The reference builds one sequence per WT() call (levelWT/WT.C:43-227,
 // driven by levelWT/WTTime.C:78-103); a batch there is a loop of calls.  Here
-// one persistent kernel pulls work items from a device queue.  The item list
-// is made at plan time, in phase order, each phase's items by decreasing text
-// length:
+// one persistent kernel pulls work items from a device queue, made at plan
+// time.  A text up to a size bound (at most its fair share of the batch: the
+// total symbols over the resident CTAs) is one item:
+//   X (text)              one CTA builds the whole text: key histogram, every
+//                         level's bits in one pass over the text, the rank
+//                         table and select marks tile by tile with the prefix
+//                         carried, then select_support_mcl -- no waits on
+//                         other CTAs.
+// A longer text is split over many CTAs, in phase order, each phase's items
+// by decreasing text length:
 //   H (text, tile)        the key histogram of one tile of the text;
 //                         the text's last H item to finish turns the tiles'
 //                         histograms into per-tile prefixes and totals
-//   W (text, level, tile) the tile's bits of one level.  Level l of a text is
-//                         the text stably sorted by the top l bits
-//                         (levelWT/WT.C:118-190), so the symbols of (level l,
-//                         key k) form one contiguous bit run starting at
-//                         l*n + (symbols whose key is below k), and a tile's
-//                         piece of it starts after the earlier tiles' members
-//                         (the H prefixes): every tile and level is written
-//                         from the text directly, no level-by-level passes
+//   W (text, tile)        the tile's bits of every level
 //   R (text, rank tile)   rank_support_v entries and select sample marks of
 //                         256 superblocks, the ones before the tile from a
 //                         decoupled look-back over the text's rank tiles
@@ -26,17 +26,34 @@
 //                         widths, pool offsets (block scan), mini blocks from
 //                         the samples, long blocks by rank-table search,
 //                         m_superblock packing.
-// An item first waits (bounded) until its text's previous phase is complete:
-// per-text counters, bumped after each item's writes are fenced.  Every item
-// waits only on items taken from the queue before it, by CTAs that are
-// running, so the launch always completes.  Data another CTA wrote is read
-// through L2 (ld.cg, or bulk copies).
+// The split items come first, then the X items by decreasing length.  A
+// split item first waits (bounded) until its text's previous phase is
+// complete: per-text counters, bumped after each item's writes are fenced.
+// Every item waits only on items taken from the queue before it, by CTAs
+// that are running, so the launch always completes.  Data another CTA wrote
+// is read through L2 (ld.cg, or bulk copies).
+//
+// Level bits.  Level l of a text is the text stably sorted by the top l bits
+// of its symbols (levelWT/WT.C:118-190), so the symbols of (level l, key k)
+// form one contiguous run starting at l*n + (symbols whose key is below k),
+// and a range's piece of it starts after the earlier ranges' members.  A warp
+// takes 32 rows of 32 symbols (a lane per symbol) staged in shared memory by
+// cp.async.bulk.  Per row: one ballot per bit plane; level 0 is the top plane
+// itself; for level l >= 1 each lane finds its place in the row stably sorted
+// by key (lanes of smaller keys plus lanes before it with its key, from the
+// planes by logic ops and popcounts) and one OR-reduction of bit << place
+// gives the row's sorted level word, in which every key's members are one
+// segment.  Lane r keeps row r's planes and words; the lanes then count each
+// key's members per row, scan them across the rows, and the CTA places the
+// warps' pieces after one exchange per chunk.  A warp's piece of a key is
+// assembled in shared memory from the rows' segments and stored: the words
+// inside it plainly, its first and last word (shared with neighbouring
+// pieces) with 32-bit atomic ORs on the zeroed bitvector.
 // Every output has the layout of the single-sequence build.  The pool region
 // of each text is sized by a bound that holds for any input (see plan), so
-// the layout is fixed by the text lengths alone.  The launch shape (symbols
-// per thread per chunk, chunks per W tile) is picked by timing the candidates
-// on the batch itself, and the memsets plus the launch are captured in a
-// CUDA graph that later runs replay.
+// the layout is fixed by the text lengths alone.  The memsets plus the launch
+// are captured in a CUDA graph that later runs replay.
+
 #include <algorithm>
 #include <numeric>
 #include <vector>
@@ -49,18 +66,20 @@ namespace wtg {
 WTG_WAIT_LIMIT_SETTER(batch)
 
 constexpr int BATCH_LMAX = 4;
-constexpr int BATCH_SLOTS = (1 << BATCH_LMAX) - 1;  // (level, key) pairs
 constexpr int BATCH_BINS = 1 << BATCH_LMAX;
-constexpr uint32_t BATCH_INVALID = 0xFFFFFFFFu;
-constexpr int BT = 256;                       // threads per CTA
-constexpr int BNW = BT / 32;                  // warps per CTA
-constexpr int BATCH_MAX_CHUNK = BT * 16;      // symbols per chunk of the widest launch shape
-constexpr int RT_ITER = 8;                    // rows of BT words per rank tile
-constexpr int RT_SB = RT_ITER * BT / 8;       // superblocks per rank tile (R item)
+constexpr int BATCH_NS = (1 << BATCH_LMAX) - 2;  // (level >= 1, key) slots: level l, key k is slot 2^l - 2 + k
+constexpr int BATCH_NP = BATCH_NS / 2;           // slot pairs (two 16-bit counts in a word)
+constexpr int BT = 256;                          // threads per CTA
+constexpr int BNW = BT / 32;                     // warps per CTA
+constexpr int ROWS = 32;                         // rows of 32 symbols per warp per chunk
+constexpr int WSYM = ROWS * 32;                  // symbols per warp per chunk
+constexpr int CH = BNW * WSYM;                   // symbols per chunk
+constexpr int RT_ITER = 8;                       // rows of BT words per rank tile
+constexpr int RT_SB = RT_ITER * BT / 8;          // superblocks per rank tile
 
-// work item: x = text, y = kind | level << 8, z = tile
-enum : uint32_t { IT_H = 0, IT_W = 1, IT_R = 2, IT_S = 3 };
-// per-text completion counters: done[4 t + DN_*]
+// work item: x = text, y = kind, z = tile
+enum : uint32_t { IT_H = 0, IT_W = 1, IT_R = 2, IT_S = 3, IT_X = 4 };
+// per-text completion counters of split texts: done[4 t + DN_*]
 enum : uint32_t { DN_H = 0, DN_HREADY = 1, DN_W = 2, DN_R = 3 };
 
 struct BatchArgs {
@@ -69,10 +88,10 @@ struct BatchArgs {
   uint64_t T;
   int L;
   uint32_t flags;
-  uint64_t tile;          // symbols per H / W tile
+  uint64_t tile;          // symbols per H / W tile of a split text (a multiple of CH)
   const uint4* items;
   uint32_t nitems;
-  const uint64_t* hb;     // first H tile of each text, T + 1
+  const uint64_t* hb;     // first H tile of each text, T + 1 (split texts only have tiles)
   uint32_t* thist;        // per H tile: BATCH_BINS counts, made exclusive prefixes by the text's last H item
   uint32_t* ttot;         // per text: BATCH_BINS totals
   const uint64_t* rb;     // first rank tile of each text, T + 1
@@ -101,20 +120,20 @@ struct BatchSmem {
   uint4 item[2];  // the item being processed and the next one (taken early)
   uint32_t hist[BATCH_BINS];
   uint32_t part[16][BATCH_BINS];
-  uint64_t base[BATCH_SLOTS];
-  uint64_t carry[BATCH_SLOTS];
-  uint32_t cnt[BNW][BATCH_SLOTS];
-  uint64_t start[BNW][BATCH_SLOTS];
+  uint64_t wbase[BATCH_NS];           // where the range's members of each slot start
+  uint32_t wcnt[2][BNW][BATCH_NP];    // per chunk parity and warp: members per slot pair
+  uint32_t scr[BNW][34];              // per warp: a piece being assembled (zero between uses)
   uint64_t wsum[BNW];
   uint64_t run;
+  uint64_t rcarry;
   uint32_t nlong;
   uint32_t flag;
   uint32_t sb[RT_SB];
   uint64_t prefix;
   uint64_t ent[BNW][64];
-  // W: two staging buffers for chunks of up to BATCH_MAX_CHUNK symbols (plus
-  // the text's offset from a 16-byte boundary), filled by cp.async.bulk
-  alignas(16) uint8_t stage[2][BATCH_MAX_CHUNK + 32];
+  // two staging buffers for chunks of CH symbols (plus the text's offset
+  // from a 16-byte boundary), filled by cp.async.bulk
+  alignas(16) uint8_t stage[2][CH + 32];
   alignas(8) uint64_t bar[2];
 };
 
@@ -209,73 +228,70 @@ __device__ __forceinline__ uint64_t batch_select_by_rank(int t_b, const uint64_t
   return 0;
 }
 
-// Run of (level l, key k) in a row: the valid lanes whose symbol's bits
-// above level l spell k (planes P[j] = ballot of bit j, V = valid lanes)
-template <int LL>
-__device__ __forceinline__ uint32_t batch_run_mask(const uint32_t* P, uint32_t V, int l, uint32_t k) {
-  uint32_t m = V;
-#pragma unroll
-  for (int j = LL - 1; j >= 0; --j)
-    if (j >= LL - l) m &= ((k >> (j - (LL - l))) & 1u) ? P[j] : ~P[j];
-  return m;
-}
-
-// ---- H item: the key histogram of symbols [c0, c1) of a text.  The order of
+// Adds the key histogram (bins 1 .. 2^L - 1) of cnt symbols at `in` to
+// sm.hist (zeroed by the caller; a barrier before reading it).  The order of
 // the symbols does not matter here, so each thread reads 16 at a time and
 // counts the low-L-bit values of a 32-bit word bit-sliced (L <= 2) or
 // bytewise (L = 3, 4); bin 0 is what remains.
-__device__ void batch_h_item(const BatchArgs& a, uint32_t t, uint32_t j, BatchSmem& sm) {
+__device__ void batch_count(const uint8_t* __restrict__ in, uint64_t cnt, int L, BatchSmem& sm) {
   const uint32_t tid = threadIdx.x, lane = tid & 31;
-  const int L = a.L;
   const uint32_t nbin = 1u << L, vmask = nbin - 1;
+  uint32_t c[BATCH_BINS];
+#pragma unroll
+  for (int b = 0; b < BATCH_BINS; ++b) c[b] = 0;
+  const uint32_t bmask = vmask * 0x01010101u;
+  auto count_word = [&](uint32_t w) {  // four symbols
+    const uint32_t x = w & bmask;
+    if (L == 1) {
+      c[1] += __popc(x);
+    } else if (L == 2) {
+      const uint32_t lo = x & 0x01010101u, hi = (x >> 1) & 0x01010101u, both = __popc(lo & hi);
+      c[1] += __popc(lo) - both;
+      c[2] += __popc(hi) - both;
+      c[3] += both;
+    } else {
+#pragma unroll
+      for (int b = 1; b < BATCH_BINS; ++b)
+        if ((uint32_t)b < nbin) c[b] += __popc(__vcmpeq4(x, (uint32_t)b * 0x01010101u)) >> 3;
+    }
+  };
+  const uint64_t head = min(cnt, (uint64_t)((16u - ((uintptr_t)in & 15u)) & 15u));  // bytes before a 16-byte boundary
+  const uint64_t nvec = (cnt - head) / 16;
+  const uint64_t rest = head + nvec * 16;
+  if (tid < head) count_word(in[tid]);
+  if (tid < cnt - rest) count_word(in[rest + tid]);
+  const uint4* vin = reinterpret_cast<const uint4*>(in + head);
+  uint64_t q = tid;
+  for (; q + BT < nvec; q += 2 * BT) {
+    const uint4 u = __ldg(vin + q), v = __ldg(vin + q + BT);
+    count_word(u.x); count_word(u.y); count_word(u.z); count_word(u.w);
+    count_word(v.x); count_word(v.y); count_word(v.z); count_word(v.w);
+  }
+  if (q < nvec) {
+    const uint4 u = __ldg(vin + q);
+    count_word(u.x); count_word(u.y); count_word(u.z); count_word(u.w);
+  }
+#pragma unroll
+  for (int b = 1; b < BATCH_BINS; ++b) {
+    if ((uint32_t)b >= nbin) continue;
+    const uint32_t s = __reduce_add_sync(0xffffffffu, c[b]);
+    if (lane == 0 && s) atomicAdd(&sm.hist[b], s);
+  }
+}
+
+// level of slot s (slots of level l: 2^l - 2 .. 2^(l+1) - 3)
+__host__ __device__ constexpr int slot_level(int s) { return s < 2 ? 1 : (s < 6 ? 2 : 3); }
+
+// ---- H item: the key histogram of symbols [c0, c1) of a split text
+__device__ void batch_h_item(const BatchArgs& a, uint32_t t, uint32_t j, BatchSmem& sm) {
+  const uint32_t tid = threadIdx.x;
+  const int L = a.L;
+  const uint32_t nbin = 1u << L;
   const uint64_t n = a.so[t + 1] - a.so[t];
   const uint64_t c0 = (uint64_t)j * a.tile, c1 = min(n, c0 + a.tile), cnt = c1 - c0;
-  const uint8_t* __restrict__ in = a.sym + a.so[t] + c0;
   if (tid < BATCH_BINS) sm.hist[tid] = 0;
   __syncthreads();
-  {
-    uint32_t c[BATCH_BINS];
-#pragma unroll
-    for (int b = 0; b < BATCH_BINS; ++b) c[b] = 0;
-    const uint32_t bmask = vmask * 0x01010101u;
-    auto count_word = [&](uint32_t w) {  // four symbols
-      const uint32_t x = w & bmask;
-      if (L == 1) {
-        c[1] += __popc(x);
-      } else if (L == 2) {
-        const uint32_t lo = x & 0x01010101u, hi = (x >> 1) & 0x01010101u, both = __popc(lo & hi);
-        c[1] += __popc(lo) - both;
-        c[2] += __popc(hi) - both;
-        c[3] += both;
-      } else {
-#pragma unroll
-        for (int b = 1; b < BATCH_BINS; ++b)
-          if ((uint32_t)b < nbin) c[b] += __popc(__vcmpeq4(x, (uint32_t)b * 0x01010101u)) >> 3;
-      }
-    };
-    const uint64_t head = min(cnt, (uint64_t)((16u - ((uintptr_t)in & 15u)) & 15u));  // bytes before a 16-byte boundary
-    const uint64_t nvec = (cnt - head) / 16;
-    const uint64_t rest = head + nvec * 16;
-    if (tid < head) count_word(in[tid]);
-    if (tid < cnt - rest) count_word(in[rest + tid]);
-    const uint4* vin = reinterpret_cast<const uint4*>(in + head);
-    uint64_t q = tid;
-    for (; q + BT < nvec; q += 2 * BT) {
-      const uint4 u = __ldg(vin + q), v = __ldg(vin + q + BT);
-      count_word(u.x); count_word(u.y); count_word(u.z); count_word(u.w);
-      count_word(v.x); count_word(v.y); count_word(v.z); count_word(v.w);
-    }
-    if (q < nvec) {
-      const uint4 u = __ldg(vin + q);
-      count_word(u.x); count_word(u.y); count_word(u.z); count_word(u.w);
-    }
-#pragma unroll
-    for (int b = 1; b < BATCH_BINS; ++b) {
-      if ((uint32_t)b >= nbin) continue;
-      const uint32_t s = __reduce_add_sync(0xffffffffu, c[b]);
-      if (lane == 0 && s) atomicAdd(&sm.hist[b], s);
-    }
-  }
+  batch_count(a.sym + a.so[t] + c0, cnt, L, sm);
   __syncthreads();
   uint32_t* __restrict__ th = a.thist + (a.hb[t] + j) * BATCH_BINS;
   if (tid < BATCH_BINS) {
@@ -319,179 +335,223 @@ __device__ void batch_h_item(const BatchArgs& a, uint32_t t, uint32_t j, BatchSm
   batch_signal(&a.done[4 * t + DN_HREADY]);
 }
 
-// ---- W item: the bits of level l for symbols [c0, c1) of a text.  Level 0
-// holds every symbol in order: a warp's row pair is one 64-bit word.  Level
-// l >= 1 has 2^l runs (keys); per chunk of BT * IPT symbols a warp counts
-// its rows' members of each run (one ballot per bit plane and row; run masks
-// from logic ops), the block places the warps' pieces after the run's carry,
-// and each warp appends its pieces, compacting the level's plane to the run
-// with one OR-reduction of 1 << rank per row.  Words a piece shares with a
-// neighbouring piece (its first and last) are ORed with 64-bit atomics;
-// words inside it are stored.
-template <int IPT, int LL>
-__device__ void batch_w_item(const BatchArgs& a, uint32_t t, int l, uint32_t j, BatchSmem& sm, uint32_t& phases) {
-  constexpr uint64_t CH = (uint64_t)BT * IPT;
-  static_assert(CH <= BATCH_MAX_CHUNK, "chunk larger than the staging buffers");
-  static_assert(IPT % 2 == 0, "level 0 rows are stored in pairs");
+// One chunk's rows of a warp (lane = symbol, row r = symbols r0 + 32 r ..):
+// lane r gets row r's bit planes kP, valid lanes kV, and level words kW
+// (kW[0] = the top plane; kW[l] = the level-l bits of the row stably sorted
+// by the l-bit key).
+template <int LL, bool FULL>
+__device__ __forceinline__ void batch_rows(const uint8_t* __restrict__ st, uint64_t r0, uint64_t ce, uint32_t lane,
+                                           uint32_t (&kP)[LL], uint32_t& kV, uint32_t (&kW)[LL]) {
+  const uint32_t lt = (1u << lane) - 1u;
+#pragma unroll
+  for (int r = 0; r < ROWS; ++r) {
+    const bool valid = FULL || r0 + 32 * r + lane < ce;
+    const uint32_t x = valid ? (uint32_t)st[32 * r + lane] : 0u;
+    uint32_t P[LL], W[LL];
+#pragma unroll
+    for (int j = 0; j < LL; ++j) P[j] = __ballot_sync(0xffffffffu, (x >> j) & 1u);
+    const uint32_t V = FULL ? 0xffffffffu : __ballot_sync(0xffffffffu, valid);
+    W[0] = P[LL - 1];
+    // E: valid lanes whose key so far equals this lane's; less: valid lanes
+    // whose key so far is smaller
+    uint32_t E = V, less = 0;
+#pragma unroll
+    for (int l = 1; l < LL; ++l) {
+      const int j = LL - l;  // the key bit level l adds
+      const uint32_t m = 0u - ((x >> j) & 1u);
+      less += __popc(E & ~P[j] & m);
+      E &= ~(P[j] ^ m);
+      const uint32_t place = less + __popc(E & lt);
+      W[l] = __reduce_or_sync(0xffffffffu, ((x >> (LL - 1 - l)) & 1u) << place);
+    }
+    if (lane == (uint32_t)r) {
+#pragma unroll
+      for (int j = 0; j < LL; ++j) {
+        kP[j] = P[j];
+        kW[j] = W[j];
+      }
+      kV = V;
+    }
+  }
+}
+
+// The level bits of symbols [cb, ce) of text t (cb a multiple of CH), every
+// level in one pass; sm.wbase[s] (set before a barrier) is where the range's
+// first member of slot s goes.
+template <int LL>
+__device__ void batch_w_range(const BatchArgs& a, uint32_t t, uint64_t cb, uint64_t ce, BatchSmem& sm,
+                              uint32_t& phases) {
+  constexpr int NSL = (1 << LL) - 2;  // slots of levels >= 1
+  constexpr int NP = (NSL + 1) / 2;   // their pairs
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const uint32_t vmask = (1u << LL) - 1, lt = (1u << lane) - 1;
   const uint64_t n = a.so[t + 1] - a.so[t];
   const uint8_t* __restrict__ in = a.sym + a.so[t];
-  uint64_t* __restrict__ bits = a.bits + a.bo[t];
-  const uint64_t cb = (uint64_t)j * a.tile, ce = min(n, cb + a.tile);
-  const int bs = LL - 1 - l;      // the bit plane of level l
-  const int q0 = (1 << l) - 1;    // first slot of level l
-  const int nk = 1 << l;          // its runs
-  // run starts: l * n + symbols of keys below k; the tile's piece after the earlier tiles' members
-  if (tid < (uint32_t)nk) {
-    const uint32_t* tot = a.ttot + (uint64_t)t * BATCH_BINS;
-    const uint32_t* pre = a.thist + (a.hb[t] + j) * BATCH_BINS;
-    uint64_t below = 0, mine = 0;
-    for (uint32_t b = 0; b < (1u << LL); ++b) {
-      const uint32_t key = b >> (LL - l);
-      if (key < tid) below += __ldcg(tot + b);
-      if (key == tid) mine += __ldcg(pre + b);
-    }
-    sm.base[q0 + tid] = (uint64_t)l * n + below;
-    sm.carry[q0 + tid] = mine;
-  }
-  // chunks are staged by thread 0 one ahead: from the 16-byte boundary at
-  // or below the chunk (the input has 16 bytes of padding after the last
-  // text, so the rounded-up tail stays inside it); tile starts are multiples
-  // of 16, so every chunk has the same offset from its boundary
+  uint32_t* __restrict__ bits32 = reinterpret_cast<uint32_t*>(a.bits + a.bo[t]);
+  uint32_t* __restrict__ scr = sm.scr[warp];
+  uint64_t run = 0;  // lane s < NSL: where the next chunk's members of slot s start
+  if (NSL > 0 && lane < (uint32_t)NSL) run = sm.wbase[lane];
+  // chunks are staged by thread 0 two ahead: from the 16-byte boundary at or
+  // below the chunk (the input has 16 bytes of padding after the last text,
+  // so the rounded-up tail stays inside it); chunk starts are multiples of
+  // 16 apart, so every chunk has the same offset from its boundary
   const uint32_t off = (uint32_t)((uintptr_t)in & 15u);
   auto stage_chunk = [&](uint64_t c, int buf) {
-    const uint64_t cnt = min(CH, ce - c);
+    const uint64_t cnt = min((uint64_t)CH, ce - c);
     const uint32_t bytes = (uint32_t)((off + cnt + 15) & ~15ull);
     fence_proxy_async_smem();
     mbar_expect_tx(&sm.bar[buf], bytes);
     bulk_g2s(sm.stage[buf], in + c - off, bytes, &sm.bar[buf]);
   };
-  __syncthreads();
+  if (tid == 0) {
+    if (cb < ce) stage_chunk(cb, 0);
+    if (cb + CH < ce) stage_chunk(cb + CH, 1);
+  }
   int cur = 0;
-  if (tid == 0 && ce > cb) stage_chunk(cb, 0);
   for (uint64_t c0 = cb; c0 < ce; c0 += CH, cur ^= 1) {
-    if (tid == 0 && c0 + CH < ce) stage_chunk(c0 + CH, cur ^ 1);  // its last readers passed the previous barrier
     mbar_wait(&sm.bar[cur], (phases >> cur) & 1u, a.err);
     phases ^= 1u << cur;
-    const uint8_t* const st = sm.stage[cur] + off;
-    const uint64_t s0 = c0 + (uint64_t)warp * 32 * IPT;
-    uint32_t v[IPT];
+    const uint64_t r0 = c0 + (uint64_t)warp * WSYM;
+    const uint8_t* const st = sm.stage[cur] + off + warp * WSYM;
+    uint32_t kP[LL], kV = 0, kW[LL];
 #pragma unroll
-    for (int r = 0; r < IPT; ++r) {
-      const uint64_t i = s0 + 32 * r + lane;
-      v[r] = i < ce ? (st[i - c0] & vmask) : BATCH_INVALID;
-    }
-    if (l == 0) {
-      // level 0: bit bs of every symbol, in order; rows 2h and 2h + 1 form
-      // the 64-bit word (s0 + 64 h) / 64 of the text's bits
+    for (int j = 0; j < LL; ++j) kP[j] = kW[j] = 0;
+    if (c0 + CH <= ce) batch_rows<LL, true>(st, r0, ce, lane, kP, kV, kW);
+    else batch_rows<LL, false>(st, r0, ce, lane, kP, kV, kW);
+    // lane r = row r: members of each slot in the row (cs) and where the
+    // key's segment starts in the row's sorted level word (as)
+    uint32_t cs[NSL > 0 ? NSL : 1], as[NSL > 0 ? NSL : 1];
+    if constexpr (NSL > 0) {
+      uint32_t M[NSL];
+      M[0] = kV & ~kP[LL - 1];
+      M[1] = kV & kP[LL - 1];
 #pragma unroll
-      for (int h = 0; h < IPT / 2; ++h) {
-        const bool va = v[2 * h] != BATCH_INVALID, vb = v[2 * h + 1] != BATCH_INVALID;
-        const uint32_t lo = __ballot_sync(0xffffffffu, va && ((v[2 * h] >> bs) & 1u));
-        const uint32_t hi = __ballot_sync(0xffffffffu, vb && ((v[2 * h + 1] >> bs) & 1u));
-        const uint64_t first = s0 + 64 * h;
-        if (lane == 0 && first < ce) {
-          const uint64_t wv = ((uint64_t)hi << 32) | lo;
-          // the text's last level-0 word may share bits with level 1
-          if (first + 64 <= n) bits[first >> 6] = wv;
-          else if (wv) atomicOr((unsigned long long*)&bits[first >> 6], (unsigned long long)wv);
+      for (int l = 2; l < LL; ++l)
+#pragma unroll
+        for (int k = 0; k < (1 << l); ++k)
+          M[(1 << l) - 2 + k] = M[(1 << (l - 1)) - 2 + (k >> 1)] & ((k & 1) ? kP[LL - l] : ~kP[LL - l]);
+#pragma unroll
+      for (int l = 1; l < LL; ++l) {
+        uint32_t acc = 0;
+#pragma unroll
+        for (int k = 0; k < (1 << l); ++k) {
+          const int s = (1 << l) - 2 + k;
+          cs[s] = __popc(M[s]);
+          as[s] = acc;
+          acc += cs[s];
         }
       }
-      __syncthreads();  // the staging buffer is refilled after every warp has read it
-      continue;
     }
-    constexpr int NKMAX = 1 << (LL - 1);  // keys of the deepest level
-    uint32_t cnt[NKMAX];
+    // row prefixes (rp) and warp totals (tot) per slot, two 16-bit counts per scan
+    uint32_t rp[NP > 0 ? NP : 1], tot[NP > 0 ? NP : 1];
 #pragma unroll
-    for (int k = 0; k < NKMAX; ++k) cnt[k] = 0;
+    for (int p = 0; p < NP; ++p) {
+      const uint32_t v = cs[2 * p] | ((2 * p + 1 < NSL) ? (cs[2 * p + 1] << 16) : 0u);
+      uint32_t inc = v;
 #pragma unroll
-    for (int r = 0; r < IPT; ++r) {
-      const bool valid = v[r] != BATCH_INVALID;
-      uint32_t P[LL];
-#pragma unroll
-      for (int jj = 0; jj < LL; ++jj) P[jj] = __ballot_sync(0xffffffffu, valid && ((v[r] >> jj) & 1u));
-      const uint32_t V = __ballot_sync(0xffffffffu, valid);
-#pragma unroll
-      for (int k = 0; k < NKMAX; ++k)
-        if (k < nk) cnt[k] += __popc(batch_run_mask<LL>(P, V, l, (uint32_t)k));
-    }
-    if (lane == 0) {
-#pragma unroll
-      for (int k = 0; k < NKMAX; ++k)
-        if (k < nk) sm.cnt[warp][q0 + k] = cnt[k];
-    }
-    __syncthreads();
-    if (tid < (uint32_t)nk) {
-      const int q = q0 + tid;
-      uint64_t run = sm.carry[q];
-      for (int w = 0; w < BNW; ++w) {
-        sm.start[w][q] = run;
-        run += sm.cnt[w][q];
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t q = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= (uint32_t)o) inc += q;
       }
-      sm.carry[q] = run;
+      rp[p] = inc - v;
+      tot[p] = __shfl_sync(0xffffffffu, inc, 31);
+      if (lane == 31) sm.wcnt[cur][warp][p] = inc;
     }
-    __syncthreads();
-    uint64_t acc[NKMAX], word[NKMAX];
-    uint32_t fill[NKMAX];
-    bool shared_word[NKMAX];
-#pragma unroll
-    for (int k = 0; k < NKMAX; ++k) {
-      const uint64_t dest = k < nk ? sm.base[q0 + k] + sm.start[warp][q0 + k] : 0;
-      word[k] = dest >> 6;
-      fill[k] = (uint32_t)(dest & 63);
-      shared_word[k] = fill[k] != 0;  // the first word may hold the previous piece's tail
-      acc[k] = 0;
+    // level 0: the rows' bits in order; a row reaching past the text's end
+    // shares its word with level 1
+    {
+      const uint64_t rs = r0 + 32 * lane;
+      if (rs < ce) {
+        if (rs + 32 <= n) bits32[rs >> 5] = kW[0];
+        else if (kW[0]) atomicOr(bits32 + (rs >> 5), kW[0]);
+      }
     }
+    __syncthreads();  // the chunk's counts are in; every warp has read the staging buffer
+    if (tid == 0 && c0 + 2 * CH < ce) stage_chunk(c0 + 2 * CH, cur);
+    if constexpr (NSL > 0) {
+      uint32_t before[NP], all[NP];
 #pragma unroll
-    for (int r = 0; r < IPT; ++r) {
-      const bool valid = v[r] != BATCH_INVALID;
-      uint32_t P[LL];
+      for (int p = 0; p < NP; ++p) {
+        uint32_t b = 0, s = 0;
 #pragma unroll
-      for (int jj = 0; jj < LL; ++jj) P[jj] = __ballot_sync(0xffffffffu, valid && ((v[r] >> jj) & 1u));
-      const uint32_t V = __ballot_sync(0xffffffffu, valid);
-      uint32_t plane = P[0];
+        for (int w = 0; w < BNW; ++w) {
+          const uint32_t x = sm.wcnt[cur][w][p];
+          b += (w < (int)warp) ? x : 0u;
+          s += x;
+        }
+        before[p] = b;
+        all[p] = s;
+      }
 #pragma unroll
-      for (int jj = 1; jj < LL; ++jj) plane = jj == bs ? P[jj] : plane;
-#pragma unroll
-      for (int k = 0; k < NKMAX; ++k) {
-        if (k >= nk) continue;
-        const uint32_t m = batch_run_mask<LL>(P, V, l, (uint32_t)k);
-        const uint32_t cm = __popc(m);
-        if (cm == 0) continue;
-        const uint32_t one = ((m & plane) >> lane) & 1u ? (1u << __popc(m & lt)) : 0u;
-        const uint32_t comp = __reduce_or_sync(0xffffffffu, one);
-        acc[k] |= (uint64_t)comp << fill[k];
-        if (fill[k] + cm >= 64) {
-          if (lane == 0 && acc[k]) {
-            if (shared_word[k]) atomicOr((unsigned long long*)&bits[word[k]], (unsigned long long)acc[k]);
-            else bits[word[k]] = acc[k];
+      for (int s = 0; s < NSL; ++s) {
+        const int l = slot_level(s);
+        const uint32_t sh = (s & 1) ? 16 : 0;
+        const uint32_t Ts = (tot[s >> 1] >> sh) & 0xFFFFu;
+        if (Ts == 0) continue;
+        const uint64_t d0 = __shfl_sync(0xffffffffu, run, s) + ((before[s >> 1] >> sh) & 0xFFFFu);
+        const uint32_t c = cs[s];
+        if (c) {
+          const uint64_t d = d0 + ((rp[s >> 1] >> sh) & 0xFFFFu);
+          const uint32_t seg = c == 32 ? kW[l] : (kW[l] >> as[s]) & ((1u << c) - 1u);
+          const uint32_t q = (uint32_t)((d >> 5) - (d0 >> 5)), o = (uint32_t)d & 31u;
+          atomicOr(scr + q, seg << o);
+          if (o + c > 32) atomicOr(scr + q + 1, seg >> (32 - o));
+        }
+        __syncwarp();
+        const uint32_t nw = (uint32_t)(((d0 + Ts + 31) >> 5) - (d0 >> 5));
+        for (uint32_t q = lane; q < nw; q += 32) {
+          const uint32_t v = scr[q];
+          scr[q] = 0;
+          uint32_t* g = bits32 + (d0 >> 5) + q;
+          if (q == 0 || q + 1 == nw) {
+            if (v) atomicOr(g, v);
+          } else {
+            *g = v;
           }
-          acc[k] = fill[k] ? ((uint64_t)comp >> (64 - fill[k])) : 0;
-          fill[k] = fill[k] + cm - 64;
-          ++word[k];
-          shared_word[k] = false;
-        } else {
-          fill[k] += cm;
         }
+        __syncwarp();
       }
-    }
-    // the piece's last (partial) word is shared with the next piece
+      uint32_t mine = 0;
 #pragma unroll
-    for (int k = 0; k < NKMAX; ++k)
-      if (k < nk && lane == 0 && fill[k] && acc[k])
-        atomicOr((unsigned long long*)&bits[word[k]], (unsigned long long)acc[k]);
-    __syncthreads();
+      for (int p = 0; p < NP; ++p)
+        if ((lane >> 1) == (uint32_t)p) mine = ((lane & 1) ? (all[p] >> 16) : all[p]) & 0xFFFFu;
+      run += mine;
+    }
   }
+}
+
+// ---- W item: every level's bits of tile j of a split text
+template <int LL>
+__device__ void batch_w_item(const BatchArgs& a, uint32_t t, uint32_t j, BatchSmem& sm, uint32_t& phases) {
+  constexpr int NSL = (1 << LL) - 2;
+  const uint32_t tid = threadIdx.x;
+  const uint64_t n = a.so[t + 1] - a.so[t];
+  const uint64_t cb = (uint64_t)j * a.tile, ce = min(n, cb + a.tile);
+  // slot (l, k): l * n + symbols of keys below k + the earlier tiles' members of key k
+  if (NSL > 0 && (int)tid < NSL) {
+    const int l = slot_level((int)tid);
+    const uint32_t k = tid - ((1u << l) - 2);
+    const uint32_t* tot = a.ttot + (uint64_t)t * BATCH_BINS;
+    const uint32_t* pre = a.thist + (a.hb[t] + j) * BATCH_BINS;
+    uint64_t below = 0, mine = 0;
+    for (uint32_t b = 0; b < (1u << LL); ++b) {
+      const uint32_t key = b >> (LL - l);
+      if (key < k) below += __ldcg(tot + b);
+      if (key == k) mine += __ldcg(pre + b);
+    }
+    sm.wbase[tid] = (uint64_t)l * n + below + mine;
+  }
+  __syncthreads();
+  batch_w_range<LL>(a, t, cb, ce, sm, phases);
   batch_signal(&a.done[4 * t + DN_W]);
 }
 
-// ---- R item: rank_support_v entries and select marks of rank tile r (RT_SB
-// superblocks) of a text's bitvector; the ones before the tile from a
-// decoupled look-back over the text's rank tiles (taken from the queue in
-// order, so every predecessor has started).  The tile holding the final
+// ---- rank tile r (RT_SB superblocks) of a text's bitvector: rank_support_v
+// entries and select marks.  The ones before the tile come from a decoupled
+// look-back over the text's rank tiles (split texts: the R items are taken
+// from the queue in order, so every predecessor has started) or from
+// sm.rcarry (one CTA taking the tiles in order).  The tile holding the final
 // superblock writes the arg counts; last args go to the text's info.
-__device__ void batch_r_item(const BatchArgs& a, uint32_t t, uint32_t r, BatchSmem& sm) {
+__device__ void batch_r_tile(const BatchArgs& a, uint32_t t, uint32_t r, BatchSmem& sm, bool lookback) {
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, g8 = lane & 7;
   const uint64_t n = a.so[t + 1] - a.so[t];
   const uint64_t size = (uint64_t)a.L * n;
@@ -553,7 +613,12 @@ __device__ void batch_r_item(const BatchArgs& a, uint32_t t, uint32_t r, BatchSm
     }
     const uint64_t total = __shfl_sync(0xffffffffu, incw, 31);
     uint64_t prefix = 0;
-    if (r == 0) {
+    if (!lookback) {
+      if (lane == 0) {
+        prefix = sm.rcarry;
+        sm.rcarry = prefix + total;
+      }
+    } else if (r == 0) {
       if (lane == 0) lb_publish(status, r, LB_FLAG_INC, total);
     } else {
       if (lane == 0) lb_publish(status, r, LB_FLAG_AGG, total);
@@ -598,7 +663,8 @@ __device__ void batch_r_item(const BatchArgs& a, uint32_t t, uint32_t r, BatchSm
   const uint64_t e0 = last_arg_end(words, last0, W, tailmask, 0);
   if (e1) atomicMax((unsigned long long*)&info[2], (unsigned long long)e1);
   if (e0) atomicMax((unsigned long long*)&info[3], (unsigned long long)e0);
-  batch_signal(&a.done[4 * t + DN_R]);
+  if (lookback) batch_signal(&a.done[4 * t + DN_R]);
+  else __syncthreads();  // sm.sb and sm.prefix are the next tile's
 }
 
 // ---- S item: select_support_mcl of each polarity of one text
@@ -708,9 +774,45 @@ __device__ void batch_s_item(const BatchArgs& a, uint32_t t, BatchSmem& sm) {
   }
 }
 
-template <int IPT>
-__global__ void __launch_bounds__(BT, 3) batch_build_kernel(BatchArgs a) {
+// ---- X item: the whole text t in this CTA
+template <int L>
+__device__ void batch_x_item(const BatchArgs& a, uint32_t t, BatchSmem& sm, uint32_t& phases) {
+  const uint32_t tid = threadIdx.x;
+  const uint64_t n = a.so[t + 1] - a.so[t];
+  if (tid < BATCH_BINS) sm.hist[tid] = 0;
+  __syncthreads();
+  batch_count(a.sym + a.so[t], n, L, sm);
+  __syncthreads();
+  // slot (l, k): level l starts at l * n, key k after the symbols of smaller keys
+  constexpr int NSL = (1 << L) - 2;
+  if (NSL > 0 && (int)tid < NSL) {
+    const int l = slot_level((int)tid);
+    const uint32_t k = tid - ((1u << l) - 2);
+    uint64_t below = 0, others = 0;
+    for (uint32_t b = 1; b < (1u << L); ++b) {
+      others += sm.hist[b];
+      if ((b >> (L - l)) < k) below += sm.hist[b];
+    }
+    if (k > 0) below += n - others;  // bin 0 has key 0
+    sm.wbase[tid] = (uint64_t)l * n + below;
+  }
+  __syncthreads();
+  batch_w_range<L>(a, t, 0, n, sm, phases);
+  __syncthreads();  // the bits are written (read back through L2 below)
+  if (a.flags & WTG_RANK) {
+    if (tid == 0) sm.rcarry = 0;
+    __syncthreads();
+    const uint32_t nt = (uint32_t)(a.rb[t + 1] - a.rb[t]);
+    for (uint32_t r = 0; r < nt; ++r) batch_r_tile(a, t, r, sm, false);
+  }
+  if (a.flags & (WTG_SELECT1 | WTG_SELECT0)) batch_s_item(a, t, sm);
+}
+
+// one instantiation per level count (the level pass keeps per-slot state in registers)
+template <int LL>
+__global__ void __launch_bounds__(BT, LL == 4 ? 2 : 3) batch_build_kernel(BatchArgs a) {
   __shared__ BatchSmem sm;
+  for (uint32_t i = threadIdx.x; i < BNW * 34; i += BT) (&sm.scr[0][0])[i] = 0;
   if (threadIdx.x == 0) {
     mbar_init(&sm.bar[0], 1);
     mbar_init(&sm.bar[1], 1);
@@ -729,47 +831,27 @@ __global__ void __launch_bounds__(BT, 3) batch_build_kernel(BatchArgs a) {
       const uint32_t q = atomicAdd(a.queue, 1u);
       sm.item[1] = q < a.nitems ? a.items[q] : make_uint4(0, 0xFFFFFFFFu, 0, 0);
     }
-    const uint32_t t = it.x, kind = it.y & 0xFF, level = it.y >> 8, tile = it.z;
-    const uint64_t n = a.so[t + 1] - a.so[t];
+    const uint32_t t = it.x, kind = it.y, tile = it.z;
     const uint32_t J = (uint32_t)(a.hb[t + 1] - a.hb[t]);
-    if (kind == IT_H) {
+    if (kind == IT_X) {
+      batch_x_item<LL>(a, t, sm, phases);
+    } else if (kind == IT_H) {
       batch_h_item(a, t, tile, sm);
     } else if (kind == IT_W) {
       batch_wait(&a.done[4 * t + DN_HREADY], 1, a.err);
-      switch (a.L) {
-        case 1: batch_w_item<IPT, 1>(a, t, (int)level, tile, sm, phases); break;
-        case 2: batch_w_item<IPT, 2>(a, t, (int)level, tile, sm, phases); break;
-        case 3: batch_w_item<IPT, 3>(a, t, (int)level, tile, sm, phases); break;
-        default: batch_w_item<IPT, 4>(a, t, (int)level, tile, sm, phases); break;
-      }
+      batch_w_item<LL>(a, t, tile, sm, phases);
     } else if (kind == IT_R) {
-      batch_wait(&a.done[4 * t + DN_W], (uint32_t)a.L * J, a.err);
-      batch_r_item(a, t, tile, sm);
+      batch_wait(&a.done[4 * t + DN_W], J, a.err);
+      batch_r_tile(a, t, tile, sm, true);
     } else {
       batch_wait(&a.done[4 * t + DN_R], (uint32_t)(a.rb[t + 1] - a.rb[t]), a.err);
       batch_s_item(a, t, sm);
     }
-    (void)n;
     __syncthreads();
   }
 }
 
 // ------------------------------------------------------------------ host
-
-struct BatchVariant {
-  int ipt;       // symbols per thread per chunk (chunk = BT * ipt symbols)
-  int cpt;       // chunks per H / W tile
-  void (*kernel)(BatchArgs);
-  uint64_t tile() const { return (uint64_t)BT * ipt * cpt; }
-};
-
-static const BatchVariant kBatchVariants[] = {
-    {4, 4, batch_build_kernel<4>},   {4, 8, batch_build_kernel<4>},   {8, 2, batch_build_kernel<8>},
-    {8, 4, batch_build_kernel<8>},   {8, 8, batch_build_kernel<8>},   {16, 2, batch_build_kernel<16>},
-    {16, 4, batch_build_kernel<16>}, {16, 8, batch_build_kernel<16>},
-};
-constexpr int kNumBatchVariants = sizeof(kBatchVariants) / sizeof(kBatchVariants[0]);
-constexpr uint64_t kMinTile = (uint64_t)BT * 4 * 4;  // the smallest tile of the variants
 
 struct BatchImpl {
   uint64_t T = 0;
@@ -783,10 +865,12 @@ struct BatchImpl {
   DevBuf in, d_so, d_bo, d_ro, d_sao, d_mo, d_deo, d_sbo, d_poo[2], d_rb, d_hb, d_items;
   DevBuf bits, rank, samples, marks, desc[2], sbw[2], pool[2], info, queue, err, thist, ttot, rstat, done;
   uint32_t nitems = 0;
-  int items_variant = -1;  // the variant the uploaded items and H tiles follow
+  bool items_valid = false;
+  uint64_t tile = 65536;      // symbols per H / W tile of a split text
+  int64_t whole_req = -1;     // texts up to this many symbols are X items (-1: automatic)
+  uint64_t whole_max = 0;     // the bound in use
+  uint64_t nwhole = 0;        // texts built whole
   std::vector<uint64_t> h_info;
-  int variant = -1;
-  float tune_ms[kNumBatchVariants] = {0};
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   bool info_valid = false;
@@ -807,50 +891,78 @@ static uint64_t pool_bound(uint64_t size) {
   return nsb * logn + (logn4 ? size / logn4 : 0) * 64 * logn + 1;
 }
 
-// The work list of one launch shape, in phase order (each phase's items by
-// decreasing text length), and the texts' first H tiles.
-static int batch_items(BatchImpl& b, int variant) {
+static void (*batch_kernel(int L))(BatchArgs) {
+  switch (L) {
+    case 1: return batch_build_kernel<1>;
+    case 2: return batch_build_kernel<2>;
+    case 3: return batch_build_kernel<3>;
+    default: return batch_build_kernel<4>;
+  }
+}
+
+// CTAs of the persistent grid: every one resident at once
+static int batch_grid_size(int L) {
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel(L), BT, 0);
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return std::max(1, per_sm) * std::max(1, sms);
+}
+
+// The work list: split texts' items in phase order (each phase by decreasing
+// text length), then one X item per other text by decreasing length; and the
+// split texts' first H tiles.  A text is built whole when it holds at most
+// the bound: by default its fair share of the batch (the total over the
+// resident CTAs), at least 65536 symbols.
+static int batch_items(BatchImpl& b) {
   int rc;
-  if (b.items_variant == variant) return WTG_OK;
-  const uint64_t tile = kBatchVariants[variant].tile();
+  if (b.items_valid) return WTG_OK;
+  const uint64_t total = b.so[b.T];
+  b.whole_max = b.whole_req >= 0 ? (uint64_t)b.whole_req
+                                 : std::max<uint64_t>(65536, total / (uint64_t)batch_grid_size(b.L));
+  const uint64_t tile = b.tile;
   const bool supports = (b.flags & (WTG_RANK | WTG_SELECT1 | WTG_SELECT0)) != 0;
   const bool sel = (b.flags & (WTG_SELECT1 | WTG_SELECT0)) != 0;
   std::vector<uint64_t> hb(b.T + 1, 0);
-  for (uint64_t t = 0; t < b.T; ++t) hb[t + 1] = hb[t] + (b.n[t] + tile - 1) / tile;
+  std::vector<uint32_t> split, whole;
+  for (uint32_t t : b.order) (b.n[t] > b.whole_max ? split : whole).push_back(t);
+  for (uint64_t t = 0; t < b.T; ++t) hb[t + 1] = hb[t] + (b.n[t] > b.whole_max ? (b.n[t] + tile - 1) / tile : 0);
   std::vector<uint4> items;
-  items.reserve(hb[b.T] * (1 + b.L) + 2 * b.T + b.rtiles);
-  for (uint32_t t : b.order)
+  items.reserve(hb[b.T] * 2 + 2 * b.T + b.rtiles);
+  for (uint32_t t : split)
     for (uint64_t j = 0; j < hb[t + 1] - hb[t]; ++j) items.push_back(make_uint4(t, IT_H, (uint32_t)j, 0));
-  for (uint32_t t : b.order)
-    for (int l = 0; l < b.L; ++l)
-      for (uint64_t j = 0; j < hb[t + 1] - hb[t]; ++j)
-        items.push_back(make_uint4(t, IT_W | ((uint32_t)l << 8), (uint32_t)j, 0));
+  for (uint32_t t : split)
+    for (uint64_t j = 0; j < hb[t + 1] - hb[t]; ++j) items.push_back(make_uint4(t, IT_W, (uint32_t)j, 0));
   if (supports)
-    for (uint32_t t : b.order)
+    for (uint32_t t : split)
       for (uint64_t r = 0; r < b.rb[t + 1] - b.rb[t]; ++r) items.push_back(make_uint4(t, IT_R, (uint32_t)r, 0));
   if (sel)
-    for (uint32_t t : b.order) items.push_back(make_uint4(t, IT_S, 0, 0));
+    for (uint32_t t : split) items.push_back(make_uint4(t, IT_S, 0, 0));
+  for (uint32_t t : whole) items.push_back(make_uint4(t, IT_X, 0, 0));
   if (items.size() >= 0xFFFFFFFFull) return fail(WTG_ERR_INVALID, "too many work items");
   cudaStream_t s = b.stream;
   if ((rc = b.d_items.ensure(std::max<size_t>(items.size(), 1) * sizeof(uint4), s))) return rc;
   if ((rc = b.d_hb.ensure((b.T + 1) * 8, s))) return rc;
+  if ((rc = b.thist.ensure(std::max<uint64_t>(hb[b.T], 1) * BATCH_BINS * sizeof(uint32_t), s))) return rc;
   if (!items.empty())
     WTG_CK(cudaMemcpyAsync(b.d_items.p, items.data(), items.size() * sizeof(uint4), cudaMemcpyHostToDevice, s));
   WTG_CK(cudaMemcpyAsync(b.d_hb.p, hb.data(), (b.T + 1) * 8, cudaMemcpyHostToDevice, s));
   WTG_CK(cudaStreamSynchronize(s));  // the host vectors must outlive the copies
   b.nitems = (uint32_t)items.size();
-  b.items_variant = variant;
+  b.nwhole = whole.size();
+  b.items_valid = true;
   return WTG_OK;
 }
 
-static BatchArgs batch_args(BatchImpl& b, int variant) {
+static BatchArgs batch_args(BatchImpl& b) {
   BatchArgs a;
   a.sym = b.in.as<uint8_t>();
   a.so = b.d_so.as<uint64_t>();
   a.T = b.T;
   a.L = b.L;
   a.flags = b.flags;
-  a.tile = kBatchVariants[variant].tile();
+  a.tile = b.tile;
   a.items = b.d_items.as<uint4>();
   a.nitems = b.nitems;
   a.hb = b.d_hb.as<uint64_t>();
@@ -881,29 +993,18 @@ static BatchArgs batch_args(BatchImpl& b, int variant) {
   return a;
 }
 
-// every CTA of the persistent grid resident at once
-static int batch_grid(const BatchVariant& v, uint32_t nitems) {
-  int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, v.kernel, BT, 0);
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const uint64_t g = (uint64_t)std::max(1, per_sm) * (uint64_t)std::max(1, sms);
-  return (int)std::max<uint64_t>(1, std::min<uint64_t>(g, std::max<uint32_t>(nitems, 1)));
-}
-
 // the whole build: clear the outputs, counters and the queue, run the
-// persistent kernel (the item list of the variant is uploaded beforehand)
-static int batch_enqueue(BatchImpl& b, int variant) {
+// persistent kernel (the item list is uploaded beforehand)
+static int batch_enqueue(BatchImpl& b) {
   cudaStream_t s = b.stream;
-  const BatchVariant& v = kBatchVariants[variant];
   WTG_CK(cudaMemsetAsync(b.bits.p, 0, b.bits_words * sizeof(uint64_t), s));
   WTG_CK(cudaMemsetAsync(b.queue.p, 0, sizeof(uint32_t), s));
   WTG_CK(cudaMemsetAsync(b.done.p, 0, b.T * 4 * sizeof(uint32_t), s));
   WTG_CK(cudaMemsetAsync(b.rstat.p, 0, std::max<uint64_t>(b.rtiles, 1) * sizeof(uint64_t), s));
   WTG_CK(cudaMemsetAsync(b.info.p, 0, b.T * 8 * sizeof(uint64_t), s));
   count_launch();
-  v.kernel<<<batch_grid(v, b.nitems), BT, 0, s>>>(batch_args(b, variant));
+  const int grid = (int)std::min<uint64_t>((uint64_t)batch_grid_size(b.L), std::max<uint32_t>(b.nitems, 1));
+  batch_kernel(b.L)<<<grid, BT, 0, s>>>(batch_args(b));
   WTG_CK(cudaGetLastError());
   return WTG_OK;
 }
@@ -949,7 +1050,6 @@ int batch_plan(BatchImpl& b, const uint64_t* lengths, uint64_t T, int L, uint32_
   b.poo[0].assign(T + 1, 0);
   b.poo[1].assign(T + 1, 0);
   b.rb.assign(T + 1, 0);
-  uint64_t max_htiles = 0;
   for (uint64_t t = 0; t < T; ++t) {
     const uint64_t n = b.n[t];
     if (n >= (1ull << 31) / (uint64_t)L) return fail(WTG_ERR_INVALID, "a text's bits must stay below 2^31");
@@ -968,7 +1068,6 @@ int batch_plan(BatchImpl& b, const uint64_t* lengths, uint64_t T, int L, uint32_
     b.poo[0][t + 1] = b.poo[0][t] + pb;
     b.poo[1][t + 1] = b.poo[1][t] + pb;
     b.rb[t + 1] = b.rb[t] + ((W >> 3) + 1 + RT_SB - 1) / RT_SB;  // rank tiles of RT_SB superblocks
-    max_htiles += (n + kMinTile - 1) / kMinTile;
   }
   b.bits_words = b.bo[T];
   b.rank_words = b.ro[T];
@@ -976,7 +1075,7 @@ int batch_plan(BatchImpl& b, const uint64_t* lengths, uint64_t T, int L, uint32_
   b.order.resize(T);
   std::iota(b.order.begin(), b.order.end(), 0u);
   std::stable_sort(b.order.begin(), b.order.end(), [&](uint32_t x, uint32_t y) { return b.n[x] > b.n[y]; });
-  b.items_variant = -1;
+  b.items_valid = false;
 
   auto up = [&](DevBuf& d, const void* h, size_t bytes) -> int {
     int r;
@@ -1007,7 +1106,6 @@ int batch_plan(BatchImpl& b, const uint64_t* lengths, uint64_t T, int L, uint32_
   if ((rc = b.info.ensure(T * 8 * 8, s))) return rc;
   if ((rc = b.queue.ensure(8, s))) return rc;
   if ((rc = b.err.ensure(8, s))) return rc;
-  if ((rc = b.thist.ensure(std::max<uint64_t>(max_htiles, 1) * BATCH_BINS * sizeof(uint32_t), s))) return rc;
   if ((rc = b.ttot.ensure(T * BATCH_BINS * sizeof(uint32_t), s))) return rc;
   if ((rc = b.rstat.ensure(std::max<uint64_t>(b.rtiles, 1) * sizeof(uint64_t), s))) return rc;
   if ((rc = b.done.ensure(T * 4 * sizeof(uint32_t), s))) return rc;
@@ -1021,9 +1119,9 @@ int batch_plan(BatchImpl& b, const uint64_t* lengths, uint64_t T, int L, uint32_
 static int batch_capture(BatchImpl& b) {
   int rc;
   cudaStream_t s = b.stream;
-  if ((rc = batch_items(b, b.variant))) return rc;
+  if ((rc = batch_items(b))) return rc;
   WTG_CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-  rc = batch_enqueue(b, b.variant);
+  rc = batch_enqueue(b);
   cudaGraph_t g = nullptr;
   const cudaError_t ce = cudaStreamEndCapture(s, &g);
   if (rc) {
@@ -1036,59 +1134,24 @@ static int batch_capture(BatchImpl& b) {
   return WTG_OK;
 }
 
-// Times every launch shape once (after one warm-up run of each) on the
-// batch's own input and keeps the fastest; then captures the build in a graph.
-static int batch_tune_and_capture(BatchImpl& b) {
-  int rc;
-  cudaStream_t s = b.stream;
-  cudaEvent_t e0, e1;
-  WTG_CK(cudaEventCreate(&e0));
-  WTG_CK(cudaEventCreate(&e1));
-  float best = 1e30f;
-  int best_v = 0;
-  for (int v = 0; v < kNumBatchVariants; ++v) {
-    if ((rc = batch_items(b, v))) break;
-    if ((rc = batch_enqueue(b, v))) break;
-    WTG_CK(cudaEventRecord(e0, s));
-    if ((rc = batch_enqueue(b, v))) break;
-    WTG_CK(cudaEventRecord(e1, s));
-    WTG_CK(cudaEventSynchronize(e1));
-    float ms = 0;
-    cudaEventElapsedTime(&ms, e0, e1);
-    b.tune_ms[v] = ms;
-    if (ms < best) {
-      best = ms;
-      best_v = v;
-    }
-  }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  if (rc) return rc;
-  b.variant = best_v;
-  return batch_capture(b);
-}
-
-int batch_set_shape(BatchImpl& b, int tile, int ipt) {
-  for (int v = 0; v < kNumBatchVariants; ++v) {
-    if ((int)kBatchVariants[v].tile() == tile && kBatchVariants[v].ipt == ipt) {
-      if (b.exec) cudaGraphExecDestroy(b.exec);
-      if (b.graph) cudaGraphDestroy(b.graph);
-      b.exec = nullptr;
-      b.graph = nullptr;
-      b.variant = v;
-      return batch_capture(b);
-    }
-  }
-  return fail(WTG_ERR_INVALID,
-              "no such launch shape (symbols per tile / per thread: 4096/4, 8192/4, 4096/8, 8192/8, 16384/8, "
-              "8192/16, 16384/16, 32768/16)");
+int batch_set_shape(BatchImpl& b, int tile, int64_t whole_max) {
+  if (tile < CH || tile > (1 << 24) || tile % CH) return fail(WTG_ERR_INVALID, "tile must be a multiple of 8192 in 8192 .. 2^24");
+  if (whole_max < -1) return fail(WTG_ERR_INVALID, "whole_max must be -1 (automatic) or >= 0");
+  if (b.exec) cudaGraphExecDestroy(b.exec);
+  if (b.graph) cudaGraphDestroy(b.graph);
+  b.exec = nullptr;
+  b.graph = nullptr;
+  b.tile = (uint64_t)tile;
+  b.whole_req = whole_max;
+  b.items_valid = false;
+  return WTG_OK;
 }
 
 int batch_run(BatchImpl& b) {
   int rc;
   b.info_valid = false;
   if (!b.exec) {
-    if ((rc = batch_tune_and_capture(b))) return rc;
+    if ((rc = batch_capture(b))) return rc;
   }
   count_launch();
   WTG_CK(cudaGraphLaunch(b.exec, b.stream));
@@ -1117,8 +1180,8 @@ int batch_text_info(const BatchImpl& b, uint64_t t, uint64_t info[8]) {
   info[3] = b.ro[t + 1] - b.ro[t];
   info[4] = b.h_info[8 * t + 0];
   info[5] = b.h_info[8 * t + 1];
-  info[6] = b.variant >= 0 ? kBatchVariants[b.variant].tile() : 0;
-  info[7] = b.variant >= 0 ? (uint64_t)kBatchVariants[b.variant].ipt : 0;
+  info[6] = b.tile;
+  info[7] = b.n[t] <= b.whole_max ? 1 : 0;
   return WTG_OK;
 }
 
@@ -1181,11 +1244,11 @@ void* batch_input(BatchImpl& b) { return b.in.p; }
 cudaStream_t batch_stream(const BatchImpl& b) { return b.stream; }
 uint64_t batch_total_symbols(const BatchImpl& b) { return b.so[b.T]; }
 
-int batch_tuning(const BatchImpl& b, int* tile, int* ipt, float* ms, int nms) {
-  if (b.variant < 0) return fail(WTG_ERR_INVALID, "the batch has not run yet");
-  *tile = (int)kBatchVariants[b.variant].tile();
-  *ipt = kBatchVariants[b.variant].ipt;
-  for (int v = 0; v < nms && v < kNumBatchVariants; ++v) ms[v] = b.tune_ms[v];
+int batch_shape(const BatchImpl& b, int* tile, int64_t* whole_max, uint64_t* whole_texts) {
+  if (!b.items_valid) return fail(WTG_ERR_INVALID, "the batch has not run yet");
+  *tile = (int)b.tile;
+  *whole_max = (int64_t)b.whole_max;
+  *whole_texts = b.nwhole;
   return WTG_OK;
 }
 

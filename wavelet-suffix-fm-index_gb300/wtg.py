@@ -104,7 +104,7 @@ _SIGS = {
     "wtg_batch_input": ([vp, vp, vp], i32),
     "wtg_batch_load": ([vp, vp], i32),
     "wtg_batch_run": ([vp], i32),
-    "wtg_batch_set_shape": ([vp, i32, i32], i32),
+    "wtg_batch_set_shape": ([vp, i32, ctypes.c_int64], i32),
     "wtg_batch_sync": ([vp], i32),
     "wtg_batch_free": ([vp], i32),
     "wtg_batch_text_info": ([vp, u64, vp], i32),
@@ -112,7 +112,7 @@ _SIGS = {
     "wtg_batch_get_bits": ([vp, u64, vp, u64], i32),
     "wtg_batch_get_rank": ([vp, u64, vp, u64], i32),
     "wtg_batch_get_select": ([vp, u64, i32, vp, vp, vp], i32),
-    "wtg_batch_tuning": ([vp, vp, vp, vp], i32),
+    "wtg_batch_shape": ([vp, vp, vp, vp], i32),
     "wtg_remap_alphabet": ([vp, u64, i32, vp], i32),
     "wtg_rank_build_noalloc": ([vp, u64, vp, vp], i32),
     "wtg_profile_enable": ([i32], i32),
@@ -768,9 +768,10 @@ class Batch:
     def run(self):
         _ck(lib().wtg_batch_run(self.h))
 
-    def set_shape(self, tile, items_per_thread):
-        """Fix the launch shape: symbols per H / W work item and per thread per chunk."""
-        _ck(lib().wtg_batch_set_shape(self.h, tile, items_per_thread))
+    def set_shape(self, tile=65536, whole_max=-1):
+        """Work-list shape for the next run: symbols per split-text tile, and
+        the longest text one CTA builds whole (-1 automatic, 0 split all)."""
+        _ck(lib().wtg_batch_set_shape(self.h, tile, whole_max))
 
     def sync(self):
         _ck(lib().wtg_batch_sync(self.h))
@@ -789,7 +790,7 @@ class Batch:
     def text_info(self, t):
         a = np.zeros(8, dtype=np.uint64)
         _ck(lib().wtg_batch_text_info(self.h, t, _p(a)))
-        return dict(zip(("n", "levels", "bit_words", "rank_words", "ones", "zeros", "tile", "ipt"),
+        return dict(zip(("n", "levels", "bit_words", "rank_words", "ones", "zeros", "tile", "whole"),
                         (int(x) for x in a)))
 
     def bits(self, t):
@@ -811,11 +812,11 @@ class Batch:
         _ck(lib().wtg_batch_get_select(self.h, t, t_b, _p(sb), _p(desc), _p(pool)))
         return _SelectTables(info, sb[: int(info[6])], desc[: int(info[4])], pool[: int(info[7])])
 
-    def tuning(self):
-        th, ipt = ctypes.c_int(0), ctypes.c_int(0)
-        ms = np.zeros(8, dtype=np.float32)
-        _ck(lib().wtg_batch_tuning(self.h, ctypes.byref(th), ctypes.byref(ipt), _p(ms)))
-        return th.value, ipt.value, ms
+    def shape(self):
+        """(split tile, whole-text bound in use, texts built whole) after a run."""
+        th, wm, nw = ctypes.c_int(0), ctypes.c_int64(0), ctypes.c_uint64(0)
+        _ck(lib().wtg_batch_shape(self.h, ctypes.byref(th), ctypes.byref(wm), ctypes.byref(nw)))
+        return th.value, wm.value, nw.value
 
 
 def rank_build_noalloc(d_words_ptr, size_bits, d_rank_ptr, stream=0):
