@@ -129,6 +129,7 @@ struct BatchSmem {
   uint32_t nlong;
   uint32_t flag;
   uint32_t sb[RT_SB];
+  uint32_t lastw[2];  // rank tile: last word + 1 holding a one / a zero
   uint64_t prefix;
   uint64_t ent[BNW][64];
   // two staging buffers for chunks of CH symbols (plus the text's offset
@@ -335,6 +336,88 @@ __device__ void batch_h_item(const BatchArgs& a, uint32_t t, uint32_t j, BatchSm
   batch_signal(&a.done[4 * t + DN_HREADY]);
 }
 
+// Bits of x at the set bits of m, packed to the low end in order: the
+// published compress ("generalized extract") of Warren, Hacker's Delight,
+// 2nd ed., section 7-4 -- five rounds, round i moving each kept bit right by
+// 2^i where bit i of its count of dropped bits below it is set.
+__device__ __forceinline__ uint32_t compress32(uint32_t x, uint32_t m) {
+  x &= m;
+  uint32_t mk = ~m << 1;
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+    uint32_t mp = mk ^ (mk << 1);  // parity of the dropped bits below each bit
+    mp ^= mp << 2;
+    mp ^= mp << 4;
+    mp ^= mp << 8;
+    mp ^= mp << 16;
+    const uint32_t mv = mp & m;  // kept bits that move this round
+    m = (m ^ mv) | (mv >> (1 << i));
+    const uint32_t t = x & mv;
+    x = (x ^ t) | (t >> (1 << i));
+    mk &= ~mp;
+  }
+  return x;
+}
+
+// Bit J of each of 32 bytes (w[k] holds bytes 4k .. 4k + 3) as one word.
+// Per byte pair of words, a = the J-th bits of w[k] (at bits 0, 8, 16, 24)
+// and b those of w[k + 1] moved up by 4: the product with 0x01020408 lifts
+// a's four bits to bits 24..27 and b's to 28..31 (every other partial
+// product lands once below bit 24, so no carry reaches them).
+template <int J>
+__device__ __forceinline__ uint32_t byte_plane(const uint32_t (&w)[8]) {
+  uint32_t p = 0;
+#pragma unroll
+  for (int k = 0; k < 8; k += 2) {
+    const uint32_t a = (w[k] >> J) & 0x01010101u, b = (w[k + 1] >> J) & 0x01010101u;
+    p |= (((a + (b << 4)) * 0x01020408u) >> 24) << (4 * k);
+  }
+  return p;
+}
+
+// Lane r's own row (symbols r0 + 32 r .. + 31, staged at byte off + 32 r of
+// the warp's 16-byte aligned stage region st16) as eight words of four
+// symbols: three aligned 16-byte loads, then a funnel shift by the offset.
+template <int Q>
+__device__ __forceinline__ void batch_row_words(const uint8_t* __restrict__ st16, uint32_t lane, uint32_t sh,
+                                                uint32_t (&w)[8]) {
+  const uint4* p = reinterpret_cast<const uint4*>(st16 + 32 * lane);
+  const uint4 q0 = p[0], q1 = p[1], q2 = p[2];
+  const uint32_t u[12] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x, q2.y, q2.z, q2.w};
+#pragma unroll
+  for (int k = 0; k < 8; ++k) w[k] = __funnelshift_r(u[k + Q], u[k + Q + 1], sh);
+}
+
+// Lane r's row for 1 or 2 levels: its valid symbols V, level-0 word w0 (the
+// top plane) and, for two levels, the members (cs) and level-1 bits (seg,
+// compressed to the low end) of key 0 and key 1.
+template <int LL>
+__device__ __forceinline__ void batch_row_swar(const uint8_t* __restrict__ st16, uint32_t off, uint64_t rs,
+                                               uint64_t ce, uint32_t lane, uint32_t& w0, uint32_t (&cs)[2],
+                                               uint32_t (&seg)[2]) {
+  uint32_t w[8];
+  const uint32_t sh = 8 * (off & 3);
+  switch (off >> 2) {
+    case 0: batch_row_words<0>(st16, lane, sh, w); break;
+    case 1: batch_row_words<1>(st16, lane, sh, w); break;
+    case 2: batch_row_words<2>(st16, lane, sh, w); break;
+    default: batch_row_words<3>(st16, lane, sh, w); break;
+  }
+  const uint64_t left = rs < ce ? ce - rs : 0;
+  const uint32_t V = left >= 32 ? 0xffffffffu : (1u << (uint32_t)left) - 1u;
+  if constexpr (LL == 1) {
+    w0 = byte_plane<0>(w) & V;
+  } else {
+    const uint32_t p1 = byte_plane<1>(w) & V, p0 = byte_plane<0>(w);
+    w0 = p1;
+    const uint32_t m0 = V & ~p1;
+    cs[0] = __popc(m0);
+    cs[1] = __popc(p1);
+    seg[0] = compress32(p0, m0);
+    seg[1] = compress32(p0, p1);
+  }
+}
+
 // One chunk's rows of a warp (lane = symbol, row r = symbols r0 + 32 r ..):
 // lane r gets row r's bit planes kP, valid lanes kV, and level words kW
 // (kW[0] = the top plane; kW[l] = the level-l bits of the row stably sorted
@@ -412,15 +495,18 @@ __device__ void batch_w_range(const BatchArgs& a, uint32_t t, uint64_t cb, uint6
     phases ^= 1u << cur;
     const uint64_t r0 = c0 + (uint64_t)warp * WSYM;
     const uint8_t* const st = sm.stage[cur] + off + warp * WSYM;
-    uint32_t kP[LL], kV = 0, kW[LL];
+    // lane r = row r: its level-0 word, and per slot its members (cs) and
+    // their level bits compressed to the low end (seg)
+    uint32_t w0 = 0, cs[NSL > 0 ? NSL : 2], seg[NSL > 0 ? NSL : 2];
+    if constexpr (LL <= 2) {
+      batch_row_swar<LL>(sm.stage[cur] + warp * WSYM, off, r0 + 32 * lane, ce, lane, w0, cs, seg);
+    } else {
+      uint32_t kP[LL], kV = 0, kW[LL];
 #pragma unroll
-    for (int j = 0; j < LL; ++j) kP[j] = kW[j] = 0;
-    if (c0 + CH <= ce) batch_rows<LL, true>(st, r0, ce, lane, kP, kV, kW);
-    else batch_rows<LL, false>(st, r0, ce, lane, kP, kV, kW);
-    // lane r = row r: members of each slot in the row (cs) and where the
-    // key's segment starts in the row's sorted level word (as)
-    uint32_t cs[NSL > 0 ? NSL : 1], as[NSL > 0 ? NSL : 1];
-    if constexpr (NSL > 0) {
+      for (int j = 0; j < LL; ++j) kP[j] = kW[j] = 0;
+      if (c0 + CH <= ce) batch_rows<LL, true>(st, r0, ce, lane, kP, kV, kW);
+      else batch_rows<LL, false>(st, r0, ce, lane, kP, kV, kW);
+      w0 = kW[0];
       uint32_t M[NSL];
       M[0] = kV & ~kP[LL - 1];
       M[1] = kV & kP[LL - 1];
@@ -431,13 +517,13 @@ __device__ void batch_w_range(const BatchArgs& a, uint32_t t, uint64_t cb, uint6
           M[(1 << l) - 2 + k] = M[(1 << (l - 1)) - 2 + (k >> 1)] & ((k & 1) ? kP[LL - l] : ~kP[LL - l]);
 #pragma unroll
       for (int l = 1; l < LL; ++l) {
-        uint32_t acc = 0;
+        uint32_t acc = 0;  // where the key's segment starts in the row's sorted level word
 #pragma unroll
         for (int k = 0; k < (1 << l); ++k) {
-          const int s = (1 << l) - 2 + k;
-          cs[s] = __popc(M[s]);
-          as[s] = acc;
-          acc += cs[s];
+          const int q = (1 << l) - 2 + k;
+          cs[q] = __popc(M[q]);
+          seg[q] = cs[q] == 32 ? kW[l] : (kW[l] >> acc) & ((1u << cs[q]) - 1u);
+          acc += cs[q];
         }
       }
     }
@@ -461,8 +547,8 @@ __device__ void batch_w_range(const BatchArgs& a, uint32_t t, uint64_t cb, uint6
     {
       const uint64_t rs = r0 + 32 * lane;
       if (rs < ce) {
-        if (rs + 32 <= n) bits32[rs >> 5] = kW[0];
-        else if (kW[0]) atomicOr(bits32 + (rs >> 5), kW[0]);
+        if (rs + 32 <= n) bits32[rs >> 5] = w0;
+        else if (w0) atomicOr(bits32 + (rs >> 5), w0);
       }
     }
     __syncthreads();  // the chunk's counts are in; every warp has read the staging buffer
@@ -483,7 +569,6 @@ __device__ void batch_w_range(const BatchArgs& a, uint32_t t, uint64_t cb, uint6
       }
 #pragma unroll
       for (int s = 0; s < NSL; ++s) {
-        const int l = slot_level(s);
         const uint32_t sh = (s & 1) ? 16 : 0;
         const uint32_t Ts = (tot[s >> 1] >> sh) & 0xFFFFu;
         if (Ts == 0) continue;
@@ -491,10 +576,9 @@ __device__ void batch_w_range(const BatchArgs& a, uint32_t t, uint64_t cb, uint6
         const uint32_t c = cs[s];
         if (c) {
           const uint64_t d = d0 + ((rp[s >> 1] >> sh) & 0xFFFFu);
-          const uint32_t seg = c == 32 ? kW[l] : (kW[l] >> as[s]) & ((1u << c) - 1u);
           const uint32_t q = (uint32_t)((d >> 5) - (d0 >> 5)), o = (uint32_t)d & 31u;
-          atomicOr(scr + q, seg << o);
-          if (o + c > 32) atomicOr(scr + q + 1, seg >> (32 - o));
+          atomicOr(scr + q, seg[s] << o);
+          if (o + c > 32) atomicOr(scr + q + 1, seg[s] >> (32 - o));
         }
         __syncwarp();
         const uint32_t nw = (uint32_t)(((d0 + Ts + 31) >> 5) - (d0 >> 5));
@@ -571,10 +655,21 @@ __device__ void batch_r_tile(const BatchArgs& a, uint32_t t, uint32_t r, BatchSm
   uint64_t* __restrict__ info = a.info + 8 * (uint64_t)t;
   uint64_t* __restrict__ status = a.rstat + a.rb[t];
   const uint64_t wbase = (uint64_t)r * (RT_ITER * BT);
+  // rows of BT words the tile needs: through the word of the final
+  // superblock's entry (word 8 NB, past the data when W is a multiple of 8)
+  const uint64_t wend = max(W, 8 * NB + 1);
+  const int nrows = (int)min((uint64_t)RT_ITER, (wend - wbase + BT - 1) / BT);
+  if (tid < 2) sm.lastw[tid] = 0;
   uint64_t w[RT_ITER];
   uint32_t c[RT_ITER], inc[RT_ITER];
 #pragma unroll
   for (int i = 0; i < RT_ITER; ++i) {
+    if (i >= nrows) {
+      w[i] = 0;
+      c[i] = inc[i] = 0;
+      if (g8 == 7) sm.sb[i * (BT / 8) + warp * 4 + (lane >> 3)] = 0;
+      continue;
+    }
     const uint64_t wi = wbase + i * BT + tid;
     uint64_t x = wi < W ? __ldcg(words + wi) : 0ull;  // written by the W items of other CTAs
     if (wi == W - 1) x &= tailmask;
@@ -633,6 +728,7 @@ __device__ void batch_r_tile(const BatchArgs& a, uint32_t t, uint32_t r, BatchSm
   uint64_t last1 = 0, last0 = 0;
 #pragma unroll
   for (int i = 0; i < RT_ITER; ++i) {
+    if (i >= nrows) break;
     const uint32_t sbl = i * (BT / 8) + warp * 4 + (lane >> 3);
     const uint64_t b = (uint64_t)r * RT_SB + sbl;  // superblock
     const uint64_t wi = wbase + i * BT + tid;
@@ -659,10 +755,19 @@ __device__ void batch_r_tile(const BatchArgs& a, uint32_t t, uint32_t r, BatchSm
       word_marks(w[i], c[i], sb_before + excl, wi, wi == W - 1 ? tailmask : ~0ull, sel1, sel0, samples, samp_last,
                  starts1, starts0, ends1, ends0, last1, last0);
   }
-  const uint64_t e1 = last_arg_end(words, last1, W, tailmask, 1);
-  const uint64_t e0 = last_arg_end(words, last0, W, tailmask, 0);
-  if (e1) atomicMax((unsigned long long*)&info[2], (unsigned long long)e1);
-  if (e0) atomicMax((unsigned long long*)&info[3], (unsigned long long)e0);
+  // the tile's last word holding a one / a zero (word indices < 2^26), then
+  // the position after its last one / zero, once per tile
+  const uint32_t l1 = __reduce_max_sync(0xffffffffu, (uint32_t)last1);
+  const uint32_t l0 = __reduce_max_sync(0xffffffffu, (uint32_t)last0);
+  if (lane == 0) {
+    if (l1) atomicMax(&sm.lastw[0], l1);
+    if (l0) atomicMax(&sm.lastw[1], l0);
+  }
+  __syncthreads();
+  if (tid < 2 && sm.lastw[tid]) {
+    const uint64_t e = last_arg_end(words, sm.lastw[tid], W, tailmask, 1 - (int)tid);
+    atomicMax((unsigned long long*)&info[2 + tid], (unsigned long long)e);
+  }
   if (lookback) batch_signal(&a.done[4 * t + DN_R]);
   else __syncthreads();  // sm.sb and sm.prefix are the next tile's
 }
