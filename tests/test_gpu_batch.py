@@ -47,14 +47,17 @@ def test_batch_matches_single_builds(wtg, L):
 
 
 @pytest.mark.parametrize("L", [1, 2, 3, 4])
-@pytest.mark.parametrize("whole_max", [0, 5000])
+@pytest.mark.parametrize("whole_max", [0, 5000, 1 << 20])
 def test_split_texts_match_single_builds(wtg, L, whole_max):
     """Texts longer than the whole-text bound go through the tiled items
     (histogram / level bits / rank tiles with look-back / select): the
-    smallest tile, so that many texts span several tiles and rank tiles."""
+    smallest tile, so that many texts span several tiles and rank tiles.
+    With the bound at 2^20 every text is built whole, the longest over
+    several rounds of the rank pass and many select superblocks."""
     rng = np.random.default_rng(200 + L)
     texts = _texts(rng, 60, L, max_log2=18)
     texts.append(rng.integers(0, 1 << L, 600001).astype(np.uint8))
+    texts.append(np.minimum(rng.geometric(0.6, 300007), (1 << L) - 1).astype(np.uint8))  # skewed: long select blocks
     b = wtg.Batch.from_texts(texts, L)
     b.set_shape(8192, whole_max)
     b.run()

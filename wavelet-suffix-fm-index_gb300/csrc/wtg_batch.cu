@@ -125,11 +125,12 @@ struct BatchSmem {
   uint32_t scr[BNW][34];              // per warp: a piece being assembled (zero between uses)
   uint64_t wsum[BNW];
   uint64_t run;
-  uint64_t rcarry;
   uint32_t nlong;
   uint32_t flag;
   uint32_t sb[RT_SB];
   uint32_t lastw[2];  // rank tile: last word + 1 holding a one / a zero
+  uint32_t wsum32[BNW];
+  uint8_t lut[256 * 8];  // lut[byte * 8 + r] = position of the r-th set bit of byte
   uint64_t prefix;
   uint64_t ent[BNW][64];
   // two staging buffers for chunks of CH symbols (plus the text's offset
@@ -263,12 +264,16 @@ __device__ void batch_count(const uint8_t* __restrict__ in, uint64_t cnt, int L,
   if (tid < cnt - rest) count_word(in[rest + tid]);
   const uint4* vin = reinterpret_cast<const uint4*>(in + head);
   uint64_t q = tid;
-  for (; q + BT < nvec; q += 2 * BT) {
-    const uint4 u = __ldg(vin + q), v = __ldg(vin + q + BT);
-    count_word(u.x); count_word(u.y); count_word(u.z); count_word(u.w);
-    count_word(v.x); count_word(v.y); count_word(v.z); count_word(v.w);
+  for (; q + 3 * BT < nvec; q += 4 * BT) {  // four 16-byte loads in flight per thread
+    uint4 u[4];
+#pragma unroll
+    for (int h = 0; h < 4; ++h) u[h] = __ldg(vin + q + h * BT);
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+      count_word(u[h].x); count_word(u[h].y); count_word(u[h].z); count_word(u[h].w);
+    }
   }
-  if (q < nvec) {
+  for (; q < nvec; q += BT) {
     const uint4 u = __ldg(vin + q);
     count_word(u.x); count_word(u.y); count_word(u.z); count_word(u.w);
   }
@@ -458,12 +463,27 @@ __device__ __forceinline__ void batch_rows(const uint8_t* __restrict__ st, uint6
   }
 }
 
+// Stages the chunk of text t at symbol c (up to ce) into staging buffer buf
+// (thread 0): from the 16-byte boundary at or below the chunk -- the input has
+// 16 bytes of padding after the last text, so the rounded-up tail stays inside
+// it; chunk starts are multiples of 16 apart, so every chunk of a text has the
+// same offset from its boundary.
+__device__ __forceinline__ void batch_stage(BatchSmem& sm, const uint8_t* in, uint64_t c, uint64_t ce, int buf) {
+  const uint32_t off = (uint32_t)((uintptr_t)in & 15u);
+  const uint64_t cnt = min((uint64_t)CH, ce - c);
+  const uint32_t bytes = (uint32_t)((off + cnt + 15) & ~15ull);
+  fence_proxy_async_smem();
+  mbar_expect_tx(&sm.bar[buf], bytes);
+  bulk_g2s(sm.stage[buf], in + c - off, bytes, &sm.bar[buf]);
+}
+
 // The level bits of symbols [cb, ce) of text t (cb a multiple of CH), every
 // level in one pass; sm.wbase[s] (set before a barrier) is where the range's
-// first member of slot s goes.
+// first member of slot s goes.  Chunks are staged two ahead; `staged`: the
+// caller has already staged the first two.
 template <int LL>
 __device__ void batch_w_range(const BatchArgs& a, uint32_t t, uint64_t cb, uint64_t ce, BatchSmem& sm,
-                              uint32_t& phases) {
+                              uint32_t& phases, bool staged) {
   constexpr int NSL = (1 << LL) - 2;  // slots of levels >= 1
   constexpr int NP = (NSL + 1) / 2;   // their pairs
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -471,23 +491,14 @@ __device__ void batch_w_range(const BatchArgs& a, uint32_t t, uint64_t cb, uint6
   const uint8_t* __restrict__ in = a.sym + a.so[t];
   uint32_t* __restrict__ bits32 = reinterpret_cast<uint32_t*>(a.bits + a.bo[t]);
   uint32_t* __restrict__ scr = sm.scr[warp];
-  uint64_t run = 0;  // lane s < NSL: where the next chunk's members of slot s start
-  if (NSL > 0 && lane < (uint32_t)NSL) run = sm.wbase[lane];
-  // chunks are staged by thread 0 two ahead: from the 16-byte boundary at or
-  // below the chunk (the input has 16 bytes of padding after the last text,
-  // so the rounded-up tail stays inside it); chunk starts are multiples of
-  // 16 apart, so every chunk has the same offset from its boundary
+  // lane s < NSL: where the next chunk's members of slot s start (a text's
+  // bits are below 2^31)
+  uint32_t run = 0;
+  if (NSL > 0 && lane < (uint32_t)NSL) run = (uint32_t)sm.wbase[lane];
   const uint32_t off = (uint32_t)((uintptr_t)in & 15u);
-  auto stage_chunk = [&](uint64_t c, int buf) {
-    const uint64_t cnt = min((uint64_t)CH, ce - c);
-    const uint32_t bytes = (uint32_t)((off + cnt + 15) & ~15ull);
-    fence_proxy_async_smem();
-    mbar_expect_tx(&sm.bar[buf], bytes);
-    bulk_g2s(sm.stage[buf], in + c - off, bytes, &sm.bar[buf]);
-  };
-  if (tid == 0) {
-    if (cb < ce) stage_chunk(cb, 0);
-    if (cb + CH < ce) stage_chunk(cb + CH, 1);
+  if (tid == 0 && !staged) {
+    if (cb < ce) batch_stage(sm, in, cb, ce, 0);
+    if (cb + CH < ce) batch_stage(sm, in, cb + CH, ce, 1);
   }
   int cur = 0;
   for (uint64_t c0 = cb; c0 < ce; c0 += CH, cur ^= 1) {
@@ -552,7 +563,7 @@ __device__ void batch_w_range(const BatchArgs& a, uint32_t t, uint64_t cb, uint6
       }
     }
     __syncthreads();  // the chunk's counts are in; every warp has read the staging buffer
-    if (tid == 0 && c0 + 2 * CH < ce) stage_chunk(c0 + 2 * CH, cur);
+    if (tid == 0 && c0 + 2 * CH < ce) batch_stage(sm, in, c0 + 2 * CH, ce, cur);
     if constexpr (NSL > 0) {
       uint32_t before[NP], all[NP];
 #pragma unroll
@@ -572,16 +583,16 @@ __device__ void batch_w_range(const BatchArgs& a, uint32_t t, uint64_t cb, uint6
         const uint32_t sh = (s & 1) ? 16 : 0;
         const uint32_t Ts = (tot[s >> 1] >> sh) & 0xFFFFu;
         if (Ts == 0) continue;
-        const uint64_t d0 = __shfl_sync(0xffffffffu, run, s) + ((before[s >> 1] >> sh) & 0xFFFFu);
+        const uint32_t d0 = __shfl_sync(0xffffffffu, run, s) + ((before[s >> 1] >> sh) & 0xFFFFu);
         const uint32_t c = cs[s];
         if (c) {
-          const uint64_t d = d0 + ((rp[s >> 1] >> sh) & 0xFFFFu);
-          const uint32_t q = (uint32_t)((d >> 5) - (d0 >> 5)), o = (uint32_t)d & 31u;
+          const uint32_t d = d0 + ((rp[s >> 1] >> sh) & 0xFFFFu);
+          const uint32_t q = (d >> 5) - (d0 >> 5), o = d & 31u;
           atomicOr(scr + q, seg[s] << o);
           if (o + c > 32) atomicOr(scr + q + 1, seg[s] >> (32 - o));
         }
         __syncwarp();
-        const uint32_t nw = (uint32_t)(((d0 + Ts + 31) >> 5) - (d0 >> 5));
+        const uint32_t nw = ((d0 + Ts + 31) >> 5) - (d0 >> 5);
         for (uint32_t q = lane; q < nw; q += 32) {
           const uint32_t v = scr[q];
           scr[q] = 0;
@@ -625,17 +636,60 @@ __device__ void batch_w_item(const BatchArgs& a, uint32_t t, uint32_t j, BatchSm
     sm.wbase[tid] = (uint64_t)l * n + below + mine;
   }
   __syncthreads();
-  batch_w_range<LL>(a, t, cb, ce, sm, phases);
+  batch_w_range<LL>(a, t, cb, ce, sm, phases, false);
   batch_signal(&a.done[4 * t + DN_W]);
 }
 
-// ---- rank tile r (RT_SB superblocks) of a text's bitvector: rank_support_v
-// entries and select marks.  The ones before the tile come from a decoupled
-// look-back over the text's rank tiles (split texts: the R items are taken
-// from the queue in order, so every predecessor has started) or from
-// sm.rcarry (one CTA taking the tiles in order).  The tile holding the final
-// superblock writes the arg counts; last args go to the text's info.
-__device__ void batch_r_tile(const BatchArgs& a, uint32_t t, uint32_t r, BatchSmem& sm, bool lookback) {
+// Select marks of word wi of a batch text (its bits are below 2^31, so
+// every position and count fits 32 bits): the same marks as word_marks() in
+// wtg_select.cuh -- for select1 (x) and select0 (~x) every 64th arg, every
+// superblock start (arg 4096q) and end (arg 4096q + 4095).  K1 = ones before
+// the word; the next multiple of 64 is d1 = (-K1) & 63 ones into it and
+// d0 = K1 & 63 zeros into it, so one select serves both polarities.
+__device__ __forceinline__ void batch_word_marks(uint64_t x, uint32_t c, uint32_t K1, uint32_t wi, uint64_t zmask,
+                                                 bool sel1, bool sel0, uint32_t* __restrict__ samples,
+                                                 uint32_t samp_last, uint64_t* __restrict__ starts1,
+                                                 uint64_t* __restrict__ starts0, uint64_t* __restrict__ ends1,
+                                                 uint64_t* __restrict__ ends0, uint32_t& lastw1, uint32_t& lastw0) {
+  const uint64_t z = ~x & zmask;
+  const uint32_t cz = __popcll(z);
+  const uint32_t base = wi << 6;
+  const uint32_t K0 = base - K1;
+  const uint32_t d1 = (0u - K1) & 63u, d0 = K1 & 63u;
+  const bool s1 = sel1 && d1 < c, s0 = sel0 && d0 < cz;
+  if (s1 || s0) {
+    const uint32_t pos = base + sel64_0(s1 ? x : z, s1 ? d1 : d0);
+    if (s1) {
+      const uint32_t k = K1 + d1;
+      samples[k >> 6] = pos;
+      if ((k & 4095) == 0) starts1[k >> 12] = pos;
+    }
+    if (s0) {
+      const uint32_t pos0 = s1 ? base + (uint32_t)(__ffsll((long long)z) - 1) : pos;
+      const uint32_t k = K0 + d0;
+      samples[samp_last - (k >> 6)] = pos0;
+      if ((k & 4095) == 0) starts0[k >> 12] = pos0;
+    }
+  }
+  if (sel1) {
+    const uint32_t e = 4095u - (K1 & 4095u);
+    if (e < c) ends1[(K1 + e) >> 12] = base + sel64_0(x, e);
+    lastw1 = c ? wi + 1 : lastw1;
+  }
+  if (sel0) {
+    const uint32_t e = 4095u - (K0 & 4095u);
+    if (e < cz) ends0[(K0 + e) >> 12] = base + sel64_0(z, e);
+    lastw0 = cz ? wi + 1 : lastw0;
+  }
+}
+
+// ---- R item: rank tile r (RT_SB superblocks) of a split text's bitvector:
+// rank_support_v entries and select marks.  The ones before the tile come
+// from a decoupled look-back over the text's rank tiles (the R items are
+// taken from the queue in order, so every predecessor has started).  The
+// tile holding the final superblock writes the arg counts; last args go to
+// the text's info.
+__device__ void batch_r_tile(const BatchArgs& a, uint32_t t, uint32_t r, BatchSmem& sm) {
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, g8 = lane & 7;
   const uint64_t n = a.so[t + 1] - a.so[t];
   const uint64_t size = (uint64_t)a.L * n;
@@ -708,12 +762,7 @@ __device__ void batch_r_tile(const BatchArgs& a, uint32_t t, uint32_t r, BatchSm
     }
     const uint64_t total = __shfl_sync(0xffffffffu, incw, 31);
     uint64_t prefix = 0;
-    if (!lookback) {
-      if (lane == 0) {
-        prefix = sm.rcarry;
-        sm.rcarry = prefix + total;
-      }
-    } else if (r == 0) {
+    if (r == 0) {
       if (lane == 0) lb_publish(status, r, LB_FLAG_INC, total);
     } else {
       if (lane == 0) lb_publish(status, r, LB_FLAG_AGG, total);
@@ -723,42 +772,43 @@ __device__ void batch_r_tile(const BatchArgs& a, uint32_t t, uint32_t r, BatchSm
     if (lane == 0) sm.prefix = prefix;
   }
   __syncthreads();
-  const uint64_t tprefix = sm.prefix;
-  const uint64_t r_last = W - 8 * NB;  // words of the final superblock
-  uint64_t last1 = 0, last0 = 0;
+  const uint32_t tprefix = (uint32_t)sm.prefix;  // a text's bits are below 2^31
+  const uint32_t r_last = (uint32_t)(W - 8 * NB);  // words of the final superblock
+  const uint32_t W32 = (uint32_t)W, NB32 = (uint32_t)NB, slast = (uint32_t)samp_last;
+  uint32_t last1 = 0, last0 = 0;
 #pragma unroll
   for (int i = 0; i < RT_ITER; ++i) {
     if (i >= nrows) break;
     const uint32_t sbl = i * (BT / 8) + warp * 4 + (lane >> 3);
-    const uint64_t b = (uint64_t)r * RT_SB + sbl;  // superblock
-    const uint64_t wi = wbase + i * BT + tid;
-    const uint64_t sb_before = tprefix + sm.sb[sbl];
+    const uint32_t b = r * RT_SB + sbl;  // superblock
+    const uint32_t wi = (uint32_t)wbase + i * BT + tid;
+    const uint32_t sb_before = tprefix + sm.sb[sbl];
     const uint32_t excl = inc[i] - c[i];
     const uint32_t sbt = __shfl_sync(0xffffffffu, inc[i], (lane & ~7u) + 7);
     if (flags & WTG_RANK) {
       // field k (1..7) = count before block k; the final superblock writes
       // only fields 1..max(r,1), r = its words (rank_support_v_par.hpp:99-108)
-      const uint32_t kmax = (b < NB) ? 7u : (r_last > 1 ? (uint32_t)r_last : 1u);
+      const uint32_t kmax = (b < NB32) ? 7u : (r_last > 1 ? r_last : 1u);
       uint64_t part = (g8 >= 1 && g8 <= kmax) ? ((uint64_t)excl << (63 - 9 * g8)) : 0ull;
 #pragma unroll
       for (int o = 1; o < 8; o <<= 1) part |= __shfl_xor_sync(0xffffffffu, part, o);
-      if (g8 == 0 && b <= NB) {
-        rank[2 * b] = sb_before;
-        rank[2 * b + 1] = part;
+      if (g8 == 0 && b <= NB32) {
+        rank[2 * (uint64_t)b] = sb_before;
+        rank[2 * (uint64_t)b + 1] = part;
       }
     }
-    if (b == NB && g8 == 0) {
+    if (b == NB32 && g8 == 0) {
       info[0] = sb_before + sbt;
       info[1] = size - (sb_before + sbt);
     }
-    if (wi < W)
-      word_marks(w[i], c[i], sb_before + excl, wi, wi == W - 1 ? tailmask : ~0ull, sel1, sel0, samples, samp_last,
-                 starts1, starts0, ends1, ends0, last1, last0);
+    if (wi < W32)
+      batch_word_marks(w[i], c[i], sb_before + excl, wi, wi == W32 - 1 ? tailmask : ~0ull, sel1, sel0, samples,
+                       slast, starts1, starts0, ends1, ends0, last1, last0);
   }
   // the tile's last word holding a one / a zero (word indices < 2^26), then
   // the position after its last one / zero, once per tile
-  const uint32_t l1 = __reduce_max_sync(0xffffffffu, (uint32_t)last1);
-  const uint32_t l0 = __reduce_max_sync(0xffffffffu, (uint32_t)last0);
+  const uint32_t l1 = __reduce_max_sync(0xffffffffu, last1);
+  const uint32_t l0 = __reduce_max_sync(0xffffffffu, last0);
   if (lane == 0) {
     if (l1) atomicMax(&sm.lastw[0], l1);
     if (l0) atomicMax(&sm.lastw[1], l0);
@@ -768,8 +818,7 @@ __device__ void batch_r_tile(const BatchArgs& a, uint32_t t, uint32_t r, BatchSm
     const uint64_t e = last_arg_end(words, sm.lastw[tid], W, tailmask, 1 - (int)tid);
     atomicMax((unsigned long long*)&info[2 + tid], (unsigned long long)e);
   }
-  if (lookback) batch_signal(&a.done[4 * t + DN_R]);
-  else __syncthreads();  // sm.sb and sm.prefix are the next tile's
+  batch_signal(&a.done[4 * t + DN_R]);
 }
 
 // ---- S item: select_support_mcl of each polarity of one text
@@ -879,14 +928,214 @@ __device__ void batch_s_item(const BatchArgs& a, uint32_t t, BatchSmem& sm) {
   }
 }
 
+// d-th (0-based) set bit of v; cl = popcount of its low 32 bits.  Halving
+// by popcounts down to a byte, then the in-byte table.
+__device__ __forceinline__ uint32_t batch_sel64(uint64_t v, uint32_t d, uint32_t cl, const uint8_t* __restrict__ lut) {
+  const bool up = d >= cl;
+  uint32_t w = up ? (uint32_t)(v >> 32) : (uint32_t)v;
+  d -= up ? cl : 0u;
+  uint32_t pos = up ? 32u : 0u;
+  const uint32_t c16 = __popc(w & 0xFFFFu);
+  const bool u16 = d >= c16;
+  w = u16 ? (w >> 16) : w;
+  d -= u16 ? c16 : 0u;
+  pos += u16 ? 16u : 0u;
+  const uint32_t c8 = __popc(w & 0xFFu);
+  const bool u8 = d >= c8;
+  w = u8 ? (w >> 8) : w;
+  d -= u8 ? c8 : 0u;
+  pos += u8 ? 8u : 0u;
+  return pos + lut[((w & 0xFFu) << 3) | (d & 7u)];
+}
+
+// ---- the rank table and select marks of a whole text in this CTA (its bits
+// were written by this CTA): a thread per 512-bit superblock, BT
+// superblocks per round; the ones before a superblock from a block scan of
+// the round's superblock counts plus the rounds before.  Per word at most
+// one in-word select (the next 64th one or zero: the select1 samples of a
+// superblock are consecutive from index ceil(ones before / 64), the select0
+// samples descend from the back from ceil(zeros before / 64)); superblock
+// ends (at most one per polarity in 512 bits) and the last args once per
+// superblock.  A text's bits are below 2^31: 32-bit positions and counts.
+__device__ void batch_r_whole(const BatchArgs& a, uint32_t t, BatchSmem& sm) {
+  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint64_t n = a.so[t + 1] - a.so[t];
+  const uint32_t size = (uint32_t)((uint64_t)a.L * n);
+  const uint32_t W = (size + 63) / 64, NB = W >> 3;
+  const uint32_t r_last = W - 8 * NB;  // words of the final superblock
+  const uint64_t tailmask = (size & 63) ? ((1ull << (size & 63)) - 1) : ~0ull;
+  const uint32_t flags = a.flags;
+  const bool sel1 = flags & WTG_SELECT1, sel0 = flags & WTG_SELECT0, sel = sel1 || sel0;
+  const uint64_t* __restrict__ words = a.bits + a.bo[t];
+  uint64_t* __restrict__ rank = a.rank + a.ro[t];
+  uint32_t* __restrict__ samples = a.samples + a.sao[t];
+  const uint32_t samp_last = W + 1;
+  const uint64_t nsbc = size / 4096 + 2;
+  uint64_t* __restrict__ starts1 = a.marks + a.mo[t];
+  uint64_t* __restrict__ starts0 = starts1 + nsbc;
+  uint64_t* __restrict__ ends1 = starts0 + nsbc;
+  uint64_t* __restrict__ ends0 = ends1 + nsbc;
+  uint64_t* __restrict__ info = a.info + 8 * (uint64_t)t;
+  const uint8_t* __restrict__ lut = sm.lut;
+  if (tid < 2) sm.lastw[tid] = 0;
+  uint32_t carry = 0;                       // ones before the round
+  uint32_t last_sb1 = ~0u, last_sb0 = ~0u;  // last superblocks holding a one / a zero
+  for (uint32_t b0 = 0; b0 <= NB; b0 += BT) {
+    const uint32_t b = b0 + tid;  // this thread's superblock
+    const bool live = b <= NB;
+    const bool tail = 8 * b + 8 >= W;  // holds the last data word, or lies past it
+    uint64_t w[8];
+    if (!tail) {
+      const ulonglong2* p = reinterpret_cast<const ulonglong2*>(words + 8 * (uint64_t)b);
+      const ulonglong2 q0 = __ldcg(p), q1 = __ldcg(p + 1), q2 = __ldcg(p + 2), q3 = __ldcg(p + 3);
+      w[0] = q0.x; w[1] = q0.y; w[2] = q1.x; w[3] = q1.y; w[4] = q2.x; w[5] = q2.y; w[6] = q3.x; w[7] = q3.y;
+    } else {
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const uint32_t wi = 8 * b + j;
+        w[j] = (live && wi < W) ? (__ldcg(words + wi) & (wi == W - 1 ? tailmask : ~0ull)) : 0ull;
+      }
+    }
+    uint32_t cnt[8], tot = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      cnt[j] = __popcll(w[j]);
+      tot += cnt[j];
+    }
+    // block exclusive scan of the superblock counts
+    uint32_t inc = tot;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t q = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= (uint32_t)o) inc += q;
+    }
+    if (lane == 31) sm.wsum32[warp] = inc;
+    __syncthreads();
+    uint32_t before = 0, all = 0;
+#pragma unroll
+    for (int v = 0; v < BNW; ++v) {
+      const uint32_t x = sm.wsum32[v];
+      before += v < (int)warp ? x : 0u;
+      all += x;
+    }
+    __syncthreads();
+    const uint32_t sb_before = carry + before + inc - tot;  // ones before the superblock
+    carry += all;
+    if (!live) continue;
+    const uint32_t bits_in = tail ? (size > 512 * b ? min(512u, size - 512 * b) : 0u) : 512u;  // its data bits
+    const uint32_t zb = 512 * b - sb_before;                 // zeros before it
+    uint32_t* __restrict__ p1 = samples + ((sb_before + 63) >> 6);
+    uint32_t* __restrict__ p0 = samples + (samp_last - ((zb + 63) >> 6));
+    uint32_t excl = 0, n1 = 0, n0 = 0;
+    uint64_t part = 0;
+    const uint32_t kmax = b < NB ? 7u : (r_last > 1 ? r_last : 1u);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const uint64_t x = w[j];
+      const uint32_t cj = cnt[j];
+      if (j && (uint32_t)j <= kmax) part |= (uint64_t)excl << (63 - 9 * j);
+      if (sel) {
+        const uint32_t vb = tail ? min(64u, (uint32_t)max(0, (int)(size - 512 * b - 64 * j))) : 64u;
+        const uint32_t czj = vb - cj;  // zeros of the word's data bits
+        const uint32_t cl = __popc((uint32_t)x);
+        const uint32_t K1 = sb_before + excl, K0 = zb + 64u * j - excl;
+        const uint32_t d1 = (0u - K1) & 63u, d0 = K1 & 63u;
+        const bool s1 = sel1 && d1 < cj, s0 = sel0 && d0 < czj;
+        const uint32_t off = batch_sel64(s1 ? x : ~x, s1 ? d1 : d0, s1 ? cl : 32u - cl, lut);
+        // both polarities only when K1 % 64 == 0: the word's first one and first zero
+        const uint32_t off0 = s1 ? (uint32_t)(__ffsll((long long)~x) - 1) : off;
+        const uint32_t pos = 512 * b + 64u * j;
+        if (s1) p1[n1] = pos + off;
+        if (s0) *(p0 - n0) = pos + off0;
+        if (s1 && ((K1 + d1) & 4095u) == 0) starts1[(K1 + d1) >> 12] = pos + off;
+        if (s0 && ((K0 + d0) & 4095u) == 0) starts0[(K0 + d0) >> 12] = pos + off0;
+        n1 += s1;
+        n0 += s0;
+      }
+      excl += cj;
+    }
+    if (flags & WTG_RANK) reinterpret_cast<ulonglong2*>(rank)[b] = make_ulonglong2(sb_before, part);
+    if (b == NB) {
+      info[0] = sb_before + excl;
+      info[1] = size - (sb_before + excl);
+    }
+    if (sel) {
+      // superblock ends: arg 4095 of a 4096-arg superblock, at most one per
+      // polarity in 512 bits; the rare superblock that ends one of each takes
+      // a second round
+      const uint32_t cz = bits_in - excl;
+      const uint32_t e1 = 4095u - (sb_before & 4095u), e0 = 4095u - (zb & 4095u);
+      bool h1 = sel1 && e1 < excl, h0 = sel0 && e0 < cz;
+      const uint32_t act = __activemask();
+      while (__any_sync(act, h1 || h0)) {
+        const bool t1 = h1;
+        const uint32_t e = t1 ? e1 : e0;
+        uint32_t bef = 0, r = 0, jj = 0;
+        uint64_t xx = 0;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const uint32_t vb = tail ? min(64u, (uint32_t)max(0, (int)(size - 512 * b - 64 * j))) : 64u;
+          const uint32_t cj = t1 ? cnt[j] : vb - cnt[j];
+          const bool here = bef <= e && e < bef + cj;
+          xx = here ? w[j] : xx;
+          r = here ? e - bef : r;
+          jj = here ? (uint32_t)j : jj;
+          bef += cj;
+        }
+        xx = t1 ? xx : ~xx;
+        const uint32_t pos = 512 * b + 64 * jj + batch_sel64(xx, r, __popc((uint32_t)xx), lut);
+        if (h1) ends1[(sb_before + e1) >> 12] = pos;
+        else if (h0) ends0[(zb + e0) >> 12] = pos;
+        if (h1) h1 = false;
+        else h0 = false;
+      }
+      last_sb1 = excl ? b : last_sb1;
+      last_sb0 = cz ? b : last_sb0;
+    }
+  }
+  if (sel) {
+    // position after the last one / zero: the last word holding one in the
+    // last superblock holding one
+    uint32_t e[2] = {0, 0};
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const uint32_t sb = q == 0 ? last_sb1 : last_sb0;
+      if (sb == ~0u) continue;
+      for (int j = 7; j >= 0; --j) {
+        const uint32_t wi = 8 * sb + j;
+        if (wi >= W) continue;
+        uint64_t x = __ldcg(words + wi);
+        if (q) x = ~x & (wi == W - 1 ? tailmask : ~0ull);
+        if (x) {
+          e[q] = (wi << 6) + hi64(x) + 1;
+          break;
+        }
+      }
+    }
+    const uint32_t m1 = __reduce_max_sync(0xffffffffu, e[0]), m0 = __reduce_max_sync(0xffffffffu, e[1]);
+    if (lane == 0) {
+      if (m1) atomicMax(&sm.lastw[0], m1);
+      if (m0) atomicMax(&sm.lastw[1], m0);
+    }
+  }
+  __syncthreads();
+  if (tid < 2 && sel) info[2 + tid] = sm.lastw[tid];
+  __syncthreads();  // the select pass reads the arg counts and last args next
+}
+
 // ---- X item: the whole text t in this CTA
 template <int L>
 __device__ void batch_x_item(const BatchArgs& a, uint32_t t, BatchSmem& sm, uint32_t& phases) {
   const uint32_t tid = threadIdx.x;
   const uint64_t n = a.so[t + 1] - a.so[t];
+  const uint8_t* in = a.sym + a.so[t];
+  if (tid == 0) {  // the level pass's first chunks load while the histogram runs
+    if (n > 0) batch_stage(sm, in, 0, n, 0);
+    if (n > CH) batch_stage(sm, in, CH, n, 1);
+  }
   if (tid < BATCH_BINS) sm.hist[tid] = 0;
   __syncthreads();
-  batch_count(a.sym + a.so[t], n, L, sm);
+  batch_count(in, n, L, sm);
   __syncthreads();
   // slot (l, k): level l starts at l * n, key k after the symbols of smaller keys
   constexpr int NSL = (1 << L) - 2;
@@ -902,14 +1151,9 @@ __device__ void batch_x_item(const BatchArgs& a, uint32_t t, BatchSmem& sm, uint
     sm.wbase[tid] = (uint64_t)l * n + below;
   }
   __syncthreads();
-  batch_w_range<L>(a, t, 0, n, sm, phases);
+  batch_w_range<L>(a, t, 0, n, sm, phases, true);
   __syncthreads();  // the bits are written (read back through L2 below)
-  if (a.flags & WTG_RANK) {
-    if (tid == 0) sm.rcarry = 0;
-    __syncthreads();
-    const uint32_t nt = (uint32_t)(a.rb[t + 1] - a.rb[t]);
-    for (uint32_t r = 0; r < nt; ++r) batch_r_tile(a, t, r, sm, false);
-  }
+  if (a.flags & WTG_RANK) batch_r_whole(a, t, sm);
   if (a.flags & (WTG_SELECT1 | WTG_SELECT0)) batch_s_item(a, t, sm);
 }
 
@@ -918,6 +1162,18 @@ template <int LL>
 __global__ void __launch_bounds__(BT, LL == 4 ? 2 : 3) batch_build_kernel(BatchArgs a) {
   __shared__ BatchSmem sm;
   for (uint32_t i = threadIdx.x; i < BNW * 34; i += BT) (&sm.scr[0][0])[i] = 0;
+  for (uint32_t e = threadIdx.x; e < 256 * 8; e += BT) {
+    uint32_t byte = e >> 3, r = e & 7, pos = 0;
+    for (uint32_t k = 0; k < 8; ++k)
+      if ((byte >> k) & 1u) {
+        if (r == 0) {
+          pos = k;
+          break;
+        }
+        --r;
+      }
+    sm.lut[e] = (uint8_t)pos;
+  }
   if (threadIdx.x == 0) {
     mbar_init(&sm.bar[0], 1);
     mbar_init(&sm.bar[1], 1);
@@ -947,7 +1203,7 @@ __global__ void __launch_bounds__(BT, LL == 4 ? 2 : 3) batch_build_kernel(BatchA
       batch_w_item<LL>(a, t, tile, sm, phases);
     } else if (kind == IT_R) {
       batch_wait(&a.done[4 * t + DN_W], J, a.err);
-      batch_r_tile(a, t, tile, sm, true);
+      batch_r_tile(a, t, tile, sm);
     } else {
       batch_wait(&a.done[4 * t + DN_R], (uint32_t)(a.rb[t + 1] - a.rb[t]), a.err);
       batch_s_item(a, t, sm);
