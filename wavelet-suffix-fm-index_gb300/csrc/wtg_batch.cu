@@ -112,6 +112,8 @@ struct BatchArgs {
   uint64_t* pool[2];
   const uint64_t* poo[2];  // T + 1 entries: region bounds
   uint64_t* info;          // 8 per text: m1, m0, last1, last0, pool1, pool0, nlong1, nlong0
+  uint32_t* kstream;       // 2 levels: per text, the level-1 key-1 run of a whole text before it is moved
+  const uint64_t* ko;      // its word offset per text
   uint32_t* queue;
   uint32_t* err;
 };
@@ -133,6 +135,8 @@ struct BatchSmem {
   uint8_t lut[256 * 8];  // lut[byte * 8 + r] = position of the r-th set bit of byte
   uint64_t prefix;
   uint64_t ent[BNW][64];
+  uint64_t sdesc[BT];  // select pass: descriptors of the chunk's superblocks
+  uint32_t wend[BATCH_NS];  // level pass: where each slot's run ended
   // two staging buffers for chunks of CH symbols (plus the text's offset
   // from a 16-byte boundary), filled by cp.async.bulk
   alignas(16) uint8_t stage[2][CH + 32];
@@ -479,11 +483,13 @@ __device__ __forceinline__ void batch_stage(BatchSmem& sm, const uint8_t* in, ui
 
 // The level bits of symbols [cb, ce) of text t (cb a multiple of CH), every
 // level in one pass; sm.wbase[s] (set before a barrier) is where the range's
-// first member of slot s goes.  Chunks are staged two ahead; `staged`: the
-// caller has already staged the first two.
+// first member of slot s goes, and sm.wend[s] gets where its run ended.
+// Chunks are staged two ahead; `staged`: the caller has already staged the
+// first two.  slot1, if given, takes slot 1's run (positions from its own
+// bit 0) in place of the text's bits.
 template <int LL>
 __device__ void batch_w_range(const BatchArgs& a, uint32_t t, uint64_t cb, uint64_t ce, BatchSmem& sm,
-                              uint32_t& phases, bool staged) {
+                              uint32_t& phases, bool staged, uint32_t* __restrict__ slot1 = nullptr) {
   constexpr int NSL = (1 << LL) - 2;  // slots of levels >= 1
   constexpr int NP = (NSL + 1) / 2;   // their pairs
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -596,7 +602,7 @@ __device__ void batch_w_range(const BatchArgs& a, uint32_t t, uint64_t cb, uint6
         for (uint32_t q = lane; q < nw; q += 32) {
           const uint32_t v = scr[q];
           scr[q] = 0;
-          uint32_t* g = bits32 + (d0 >> 5) + q;
+          uint32_t* g = ((s == 1 && slot1) ? slot1 : bits32) + (d0 >> 5) + q;
           if (q == 0 || q + 1 == nw) {
             if (v) atomicOr(g, v);
           } else {
@@ -612,6 +618,7 @@ __device__ void batch_w_range(const BatchArgs& a, uint32_t t, uint64_t cb, uint6
       run += mine;
     }
   }
+  if (NSL > 0 && warp == 0 && lane < (uint32_t)NSL) sm.wend[lane] = run;
 }
 
 // ---- W item: every level's bits of tile j of a split text
@@ -876,28 +883,34 @@ __device__ void batch_s_item(const BatchArgs& a, uint32_t t, BatchSmem& sm) {
       if (i < nsb) {
         if (off + sz > pool_cap) atomicCAS(a.err, 0u, (uint32_t)DERR_SELECT_OVERFLOW);
         desc[i] = (off << 8) | d;
+        sm.sdesc[tid] = (off << 8) | d;
       }
       __syncthreads();
       if (tid == 0) sm.run += total;
       // fill: warp per superblock of this chunk
       for (uint64_t j = warp; j < (uint64_t)BT && i0 + j < nsb; j += BNW) {
         const uint64_t si = i0 + j;
-        const uint64_t dd = desc[si];
+        const uint64_t dd = sm.sdesc[j];
         const uint64_t poff = dd >> 8;
         const uint32_t wdt = (uint32_t)(dd & 127);
         if (poff + ((dd >> 7) & 1 ? 64ull * wdt : wdt) > pool_cap) continue;
         if (!((dd >> 7) & 1)) {
-          const uint32_t start = t_b ? __ldcg(samples + 64 * si) : __ldcg(samples + samp_last - 64 * si);
+          // the superblock's samples (every 64th arg), relative to its first
+          // (entry 0, arg 4096 si < m): one round of loads
+          uint32_t sp[2];
 #pragma unroll
           for (int h = 0; h < 2; ++h) {
             const uint32_t e = lane + 32 * h;
             const uint64_t k = 4096 * si + 64 * (uint64_t)e;
-            uint64_t ent = 0;  // entries past the arg count stay zero; their samples do not exist
-            if (k < m) {
-              const uint32_t sp = t_b ? __ldcg(samples + 64 * si + e) : __ldcg(samples + samp_last - (64 * si + e));
-              ent = (uint64_t)(uint32_t)(sp - start);
-            }
-            sm.ent[warp][e] = ent;
+            sp[h] = k < m ? (t_b ? __ldcg(samples + 64 * si + e) : __ldcg(samples + samp_last - (64 * si + e))) : 0u;
+          }
+          const uint32_t start = __shfl_sync(0xffffffffu, sp[0], 0);
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const uint32_t e = lane + 32 * h;
+            const uint64_t k = 4096 * si + 64 * (uint64_t)e;
+            // entries past the arg count stay zero; their samples do not exist
+            sm.ent[warp][e] = k < m ? (uint64_t)(uint32_t)(sp[h] - start) : 0ull;
           }
           __syncwarp();
           if (lane < wdt) pool[poff + lane] = packed_word(lane, wdt, 64, [&](uint64_t e) { return sm.ent[warp][e]; });
@@ -1133,25 +1146,55 @@ __device__ void batch_x_item(const BatchArgs& a, uint32_t t, BatchSmem& sm, uint
     if (n > 0) batch_stage(sm, in, 0, n, 0);
     if (n > CH) batch_stage(sm, in, CH, n, 1);
   }
-  if (tid < BATCH_BINS) sm.hist[tid] = 0;
-  __syncthreads();
-  batch_count(in, n, L, sm);
-  __syncthreads();
-  // slot (l, k): level l starts at l * n, key k after the symbols of smaller keys
-  constexpr int NSL = (1 << L) - 2;
-  if (NSL > 0 && (int)tid < NSL) {
-    const int l = slot_level((int)tid);
-    const uint32_t k = tid - ((1u << l) - 2);
-    uint64_t below = 0, others = 0;
-    for (uint32_t b = 1; b < (1u << L); ++b) {
-      others += sm.hist[b];
-      if ((b >> (L - l)) < k) below += sm.hist[b];
+  if constexpr (L == 2) {
+    // no histogram: level 1's key-0 run starts at n; the key-1 run (at n + the
+    // key-0 members, unknown until the pass ends) goes to the text's stream
+    // from its bit 0 and is moved into place after the pass
+    uint32_t* __restrict__ ks = a.kstream + a.ko[t];
+    const uint64_t kw = (n + 31) / 32 + 1;
+    for (uint64_t i = tid; i < kw; i += BT) ks[i] = 0;
+    if (tid == 0) {
+      sm.wbase[0] = n;
+      sm.wbase[1] = 0;
     }
-    if (k > 0) below += n - others;  // bin 0 has key 0
-    sm.wbase[tid] = (uint64_t)l * n + below;
+    __syncthreads();
+    batch_w_range<2>(a, t, 0, n, sm, phases, true, ks);
+    __syncthreads();
+    // move the key-1 run (m bits) to bit p = n + (key-0 members) of the text:
+    // word j of the bits takes the stream's bits from 32 j - p on
+    const uint32_t p = sm.wend[0], m = (uint32_t)(2 * n) - p;
+    uint32_t* __restrict__ bits32 = reinterpret_cast<uint32_t*>(a.bits + a.bo[t]);
+    if (m > 0) {
+      const uint32_t j0 = p >> 5, j1 = (p + m - 1) >> 5, o = p & 31u;
+      for (uint32_t j = j0 + tid; j <= j1; j += BT) {
+        const uint32_t q = j - j0;
+        const uint32_t hi = __ldcg(ks + q), lo = q ? __ldcg(ks + q - 1) : 0u;
+        const uint32_t v = o ? ((hi << o) | (lo >> (32 - o))) : hi;
+        if (j == j0) bits32[j] |= v;  // its low bits are key 0's (or level 0's)
+        else bits32[j] = v;
+      }
+    }
+  } else {
+    if (tid < BATCH_BINS) sm.hist[tid] = 0;
+    __syncthreads();
+    batch_count(in, n, L, sm);
+    __syncthreads();
+    // slot (l, k): level l starts at l * n, key k after the symbols of smaller keys
+    constexpr int NSL = (1 << L) - 2;
+    if (NSL > 0 && (int)tid < NSL) {
+      const int l = slot_level((int)tid);
+      const uint32_t k = tid - ((1u << l) - 2);
+      uint64_t below = 0, others = 0;
+      for (uint32_t b = 1; b < (1u << L); ++b) {
+        others += sm.hist[b];
+        if ((b >> (L - l)) < k) below += sm.hist[b];
+      }
+      if (k > 0) below += n - others;  // bin 0 has key 0
+      sm.wbase[tid] = (uint64_t)l * n + below;
+    }
+    __syncthreads();
+    batch_w_range<L>(a, t, 0, n, sm, phases, true);
   }
-  __syncthreads();
-  batch_w_range<L>(a, t, 0, n, sm, phases, true);
   __syncthreads();  // the bits are written (read back through L2 below)
   if (a.flags & WTG_RANK) batch_r_whole(a, t, sm);
   if (a.flags & (WTG_SELECT1 | WTG_SELECT0)) batch_s_item(a, t, sm);
@@ -1220,11 +1263,12 @@ struct BatchImpl {
   uint32_t flags = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
-  std::vector<uint64_t> n, so, bo, ro, sao, mo, deo, sbo, poo[2], rb;
+  std::vector<uint64_t> n, so, bo, ro, sao, mo, deo, sbo, poo[2], rb, ko;
   std::vector<uint32_t> order;  // texts by decreasing length
   uint64_t bits_words = 0, rank_words = 0, rtiles = 0;
   DevBuf in, d_so, d_bo, d_ro, d_sao, d_mo, d_deo, d_sbo, d_poo[2], d_rb, d_hb, d_items;
   DevBuf bits, rank, samples, marks, desc[2], sbw[2], pool[2], info, queue, err, thist, ttot, rstat, done;
+  DevBuf kstream, d_ko;
   uint32_t nitems = 0;
   bool items_valid = false;
   uint64_t tile = 65536;      // symbols per H / W tile of a split text
@@ -1349,6 +1393,8 @@ static BatchArgs batch_args(BatchImpl& b) {
     a.poo[t] = b.d_poo[t].as<uint64_t>();
   }
   a.info = b.info.as<uint64_t>();
+  a.kstream = b.kstream.as<uint32_t>();
+  a.ko = b.d_ko.as<uint64_t>();
   a.queue = b.queue.as<uint32_t>();
   a.err = b.err.as<uint32_t>();
   return a;
@@ -1381,7 +1427,7 @@ void batch_delete(BatchImpl* b) {
                     &b->d_sbo,   &b->d_poo[0], &b->d_poo[1], &b->d_rb,   &b->d_hb,   &b->d_items, &b->bits,
                     &b->rank,    &b->samples, &b->marks,   &b->desc[0], &b->desc[1], &b->sbw[0], &b->sbw[1],
                     &b->pool[0], &b->pool[1], &b->info,    &b->queue,  &b->err,    &b->thist,  &b->ttot,
-                    &b->rstat,   &b->done};
+                    &b->rstat,   &b->done,    &b->kstream, &b->d_ko};
   for (DevBuf* d : bufs) d->release(s);
   cudaStreamSynchronize(s);
   if (b->own_stream) cudaStreamDestroy(s);
@@ -1411,6 +1457,7 @@ int batch_plan(BatchImpl& b, const uint64_t* lengths, uint64_t T, int L, uint32_
   b.poo[0].assign(T + 1, 0);
   b.poo[1].assign(T + 1, 0);
   b.rb.assign(T + 1, 0);
+  b.ko.assign(T + 1, 0);
   for (uint64_t t = 0; t < T; ++t) {
     const uint64_t n = b.n[t];
     if (n >= (1ull << 31) / (uint64_t)L) return fail(WTG_ERR_INVALID, "a text's bits must stay below 2^31");
@@ -1428,6 +1475,8 @@ int batch_plan(BatchImpl& b, const uint64_t* lengths, uint64_t T, int L, uint32_
     const uint64_t pb = pool_bound(size);
     b.poo[0][t + 1] = b.poo[0][t] + pb;
     b.poo[1][t + 1] = b.poo[1][t] + pb;
+    // 2 levels: the whole-text pass's key-1 stream, n bits and a zero word (in 32-bit words)
+    b.ko[t + 1] = b.ko[t] + (L == 2 ? (n + 31) / 32 + 1 : 0);
     b.rb[t + 1] = b.rb[t] + ((W >> 3) + 1 + RT_SB - 1) / RT_SB;  // rank tiles of RT_SB superblocks
   }
   b.bits_words = b.bo[T];
@@ -1455,6 +1504,8 @@ int batch_plan(BatchImpl& b, const uint64_t* lengths, uint64_t T, int L, uint32_
   if ((rc = up(b.d_sbo, b.sbo.data(), (T + 1) * 8))) return rc;
   if ((rc = up(b.d_poo[0], b.poo[0].data(), (T + 1) * 8))) return rc;
   if ((rc = up(b.d_poo[1], b.poo[1].data(), (T + 1) * 8))) return rc;
+  if ((rc = up(b.d_ko, b.ko.data(), (T + 1) * 8))) return rc;
+  if ((rc = b.kstream.ensure(std::max<uint64_t>(b.ko[T], 2) * 4, s))) return rc;
   if ((rc = b.bits.ensure(b.bits_words * 8 + 64, s))) return rc;
   if ((rc = b.rank.ensure(b.rank_words * 8 + 64, s))) return rc;
   if ((rc = b.samples.ensure(b.sao[T] * 4 + 64, s))) return rc;
