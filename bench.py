@@ -412,7 +412,7 @@ def measure_batch(torch, wtg, stream, ntexts, reps=5, cpu_texts=0):
     b.load(texts)
     del texts
     t0 = time.perf_counter()
-    b.run()  # first run: item list upload + graph capture
+    b.run()  # first run: autotune + graph capture
     b.sync()
     first_s = time.perf_counter() - t0
     ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
@@ -427,7 +427,7 @@ def measure_batch(torch, wtg, stream, ntexts, reps=5, cpu_texts=0):
     b.sync()
     ms = e0.elapsed_time(e1) / reps
     step_bytes = sum(algorithmic_bytes(int(n), 2, 1) for n in lengths)
-    tile, whole_max, nwhole = b.shape()
+    tile, whole_max, spt, nwhole, tune_ms = b.shape()
     # the same texts, one single-sequence build each
     d_in, _ = b.input_device()
     offs = np.concatenate([[0], np.cumsum(lengths)]).astype(np.uint64)
@@ -476,7 +476,8 @@ def measure_batch(torch, wtg, stream, ntexts, reps=5, cpu_texts=0):
         "cpu_baseline": cpu,
         "texts": ntexts, "symbols": total, "algorithmic_bytes": step_bytes,
         "ms": ms, "gbs": step_bytes / (ms / 1e3) / 1e9, "first_run_s": first_s,
-        "work_list": {"split_tile_symbols": tile, "whole_text_max_symbols": whole_max, "texts_built_whole": nwhole},
+        "shape": {"split_tile_symbols": tile, "whole_text_max_symbols": whole_max, "symbols_per_thread": spt,
+                  "texts_built_whole": nwhole, "candidates_ms": [round(float(x), 3) for x in tune_ms[:6]]},
         "per_text_plain_ms": plain_s * 1e3, "per_text_plain_gbs": step_bytes / plain_s / 1e9,
         "speedup_vs_per_text": plain_s * 1e3 / ms, "exact_spot_check": bool(exact),
     }

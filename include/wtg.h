@@ -241,8 +241,10 @@ int wtg_rank_build_noalloc(const uint64_t* d_words, uint64_t size_bits, uint64_t
  *   flags   : WTG_RANK | WTG_SELECT1 | WTG_SELECT0 (select implies rank)
  *   stream  : the stream the batch runs on (NULL: the batch makes its own)
  * The plan allocates every output region (sizes follow from the lengths).
- * The first wtg_batch_run uploads the item list and captures the build in a
- * CUDA graph; later runs replay the graph.  Per-text outputs have the
+ * The first wtg_batch_run times the candidate shapes (symbols per thread of
+ * the level pass x split tile and whole-text bound) on the loaded input,
+ * keeps the fastest and captures the build in a CUDA graph; later runs
+ * replay the graph.  Per-text outputs have the
  * single-sequence layouts (wtg_tree_get_bits / _get_rank / _get_select of a
  * tree built with the same levels). */
 int wtg_batch_plan(const uint64_t* lengths, uint64_t ntexts, int levels, uint32_t flags, void* stream,
@@ -252,11 +254,13 @@ int wtg_batch_input(wtg_batch* b, void** d_input, uint64_t* nbytes);
 /* copy the concatenated texts from host memory into the input buffer */
 int wtg_batch_load(wtg_batch* b, const void* texts);
 int wtg_batch_run(wtg_batch* b);
-/* the shape of the work list (before the next run): `tile` symbols per
- * split-text tile (a multiple of 8192, 8192 .. 2^24; default 65536) and the
- * longest text built whole by one CTA (-1, the default: the total symbols
- * over the resident CTAs, at least 65536; 0: every text split) */
-int wtg_batch_set_shape(wtg_batch* b, int tile, int64_t whole_max);
+/* fix the shape instead of timing the candidates on the first run:
+ * `tile` symbols per split-text tile (a multiple of 256 x
+ * symbols_per_thread, up to 2^24), the longest text built whole by one CTA
+ * (-1: the total symbols over the resident CTAs, at least 65536; 0: every
+ * text split) and the level pass's symbols per thread (32, or 64 for 1-2
+ * levels) */
+int wtg_batch_set_shape(wtg_batch* b, int tile, int64_t whole_max, int symbols_per_thread);
 int wtg_batch_sync(wtg_batch* b);
 int wtg_batch_free(wtg_batch* b);
 /* after wtg_batch_sync.  text info: n, levels, bit words, rank words, ones,
@@ -267,9 +271,11 @@ int wtg_batch_select_info(wtg_batch* b, uint64_t t, int t_b, uint64_t info[8]);
 int wtg_batch_get_bits(wtg_batch* b, uint64_t t, uint64_t* dst, uint64_t nwords);
 int wtg_batch_get_rank(wtg_batch* b, uint64_t t, uint64_t* dst, uint64_t nwords);
 int wtg_batch_get_select(wtg_batch* b, uint64_t t, int t_b, uint64_t* sb_words, uint64_t* desc, uint64_t* pool);
-/* after a run: the split tile, the whole-text bound in use, and how many
- * texts were built whole */
-int wtg_batch_shape(wtg_batch* b, int* tile, int64_t* whole_max, uint64_t* whole_texts);
+/* after a run: the shape in use (split tile, whole-text bound, symbols per
+ * thread), how many texts were built whole, and the first run's time of each
+ * candidate shape in ms (0: not tried; all 0 after wtg_batch_set_shape) */
+int wtg_batch_shape(wtg_batch* b, int* tile, int64_t* whole_max, int* symbols_per_thread, uint64_t* whole_texts,
+                    float ms[8]);
 
 /* ------------------------------------------------- suffix array and BWT
  * The first two steps of the reference's FM-index construction

@@ -72,8 +72,10 @@ constexpr int BATCH_NP = BATCH_NS / 2;           // slot pairs (two 16-bit count
 constexpr int BT = 256;                          // threads per CTA
 constexpr int BNW = BT / 32;                     // warps per CTA
 constexpr int ROWS = 32;                         // rows of 32 symbols per warp per chunk
-constexpr int WSYM = ROWS * 32;                  // symbols per warp per chunk
-constexpr int CH = BNW * WSYM;                   // symbols per chunk
+constexpr int WSYM = ROWS * 32;                  // symbols per warp per chunk (one row per lane)
+constexpr int CH = BNW * WSYM;                   // symbols per chunk (one row per lane)
+constexpr int RPL_MAX = 2;                       // rows of 32 symbols per lane, at most
+constexpr int CH_MAX = CH * RPL_MAX;
 constexpr int RT_ITER = 8;                       // rows of BT words per rank tile
 constexpr int RT_SB = RT_ITER * BT / 8;          // superblocks per rank tile
 
@@ -124,7 +126,7 @@ struct BatchSmem {
   uint32_t part[16][BATCH_BINS];
   uint64_t wbase[BATCH_NS];           // where the range's members of each slot start
   uint32_t wcnt[2][BNW][BATCH_NP];    // per chunk parity and warp: members per slot pair
-  uint32_t scr[BNW][34];              // per warp: a piece being assembled (zero between uses)
+  uint32_t scr[BNW][68];              // per warp: a piece being assembled (zero between uses)
   uint64_t wsum[BNW];
   uint64_t run;
   uint32_t nlong;
@@ -137,9 +139,10 @@ struct BatchSmem {
   uint64_t ent[BNW][64];
   uint64_t sdesc[BT];  // select pass: descriptors of the chunk's superblocks
   uint32_t wend[BATCH_NS];  // level pass: where each slot's run ended
-  // two staging buffers for chunks of CH symbols (plus the text's offset
-  // from a 16-byte boundary), filled by cp.async.bulk
-  alignas(16) uint8_t stage[2][CH + 32];
+  // two staging buffers for chunks of up to CH_MAX symbols (plus the text's
+  // offset from a 16-byte boundary and the last lane's over-read), filled by
+  // cp.async.bulk
+  alignas(16) uint8_t stage[2][CH_MAX + 32];
   alignas(8) uint64_t bar[2];
 };
 
@@ -374,7 +377,7 @@ __device__ __forceinline__ uint32_t compress32(uint32_t x, uint32_t m) {
 // a's four bits to bits 24..27 and b's to 28..31 (every other partial
 // product lands once below bit 24, so no carry reaches them).
 template <int J>
-__device__ __forceinline__ uint32_t byte_plane(const uint32_t (&w)[8]) {
+__device__ __forceinline__ uint32_t byte_plane(const uint32_t* w) {
   uint32_t p = 0;
 #pragma unroll
   for (int k = 0; k < 8; k += 2) {
@@ -384,46 +387,61 @@ __device__ __forceinline__ uint32_t byte_plane(const uint32_t (&w)[8]) {
   return p;
 }
 
-// Lane r's own row (symbols r0 + 32 r .. + 31, staged at byte off + 32 r of
-// the warp's 16-byte aligned stage region st16) as eight words of four
-// symbols: three aligned 16-byte loads, then a funnel shift by the offset.
-template <int Q>
+// Lane r's own rows (RPL rows of 32 symbols from symbol 32 RPL r of the
+// warp's part of the chunk, staged at byte off + 32 RPL r of the warp's
+// 16-byte aligned stage region st16) as 8 RPL words of four symbols: 2 RPL + 1
+// aligned 16-byte loads, then a funnel shift by the offset.
+template <int Q, int RPL>
 __device__ __forceinline__ void batch_row_words(const uint8_t* __restrict__ st16, uint32_t lane, uint32_t sh,
-                                                uint32_t (&w)[8]) {
-  const uint4* p = reinterpret_cast<const uint4*>(st16 + 32 * lane);
-  const uint4 q0 = p[0], q1 = p[1], q2 = p[2];
-  const uint32_t u[12] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x, q2.y, q2.z, q2.w};
+                                                uint32_t (&w)[8 * RPL]) {
+  const uint4* p = reinterpret_cast<const uint4*>(st16 + 32 * RPL * lane);
+  uint32_t u[8 * RPL + 4];
 #pragma unroll
-  for (int k = 0; k < 8; ++k) w[k] = __funnelshift_r(u[k + Q], u[k + Q + 1], sh);
+  for (int v = 0; v < 2 * RPL + 1; ++v) {
+    const uint4 q = p[v];
+    u[4 * v] = q.x;
+    u[4 * v + 1] = q.y;
+    u[4 * v + 2] = q.z;
+    u[4 * v + 3] = q.w;
+  }
+#pragma unroll
+  for (int k = 0; k < 8 * RPL; ++k) w[k] = __funnelshift_r(u[k + Q], u[k + Q + 1], sh);
 }
 
-// Lane r's row for 1 or 2 levels: its valid symbols V, level-0 word w0 (the
-// top plane) and, for two levels, the members (cs) and level-1 bits (seg,
-// compressed to the low end) of key 0 and key 1.
-template <int LL>
+// Lane r's rows for 1 or 2 levels (rs = the first row's first symbol): per
+// row its level-0 word w0 (the top plane, valid symbols only) and, for two
+// levels, per key the members (cs) and level-1 bits (seg, compressed to the
+// low end, the rows' bits one after another).
+template <int LL, int RPL>
 __device__ __forceinline__ void batch_row_swar(const uint8_t* __restrict__ st16, uint32_t off, uint64_t rs,
-                                               uint64_t ce, uint32_t lane, uint32_t& w0, uint32_t (&cs)[2],
-                                               uint32_t (&seg)[2]) {
-  uint32_t w[8];
+                                               uint64_t ce, uint32_t lane, uint32_t (&w0)[RPL], uint32_t (&cs)[2],
+                                               uint64_t (&seg)[2]) {
+  uint32_t w[8 * RPL];
   const uint32_t sh = 8 * (off & 3);
   switch (off >> 2) {
-    case 0: batch_row_words<0>(st16, lane, sh, w); break;
-    case 1: batch_row_words<1>(st16, lane, sh, w); break;
-    case 2: batch_row_words<2>(st16, lane, sh, w); break;
-    default: batch_row_words<3>(st16, lane, sh, w); break;
+    case 0: batch_row_words<0, RPL>(st16, lane, sh, w); break;
+    case 1: batch_row_words<1, RPL>(st16, lane, sh, w); break;
+    case 2: batch_row_words<2, RPL>(st16, lane, sh, w); break;
+    default: batch_row_words<3, RPL>(st16, lane, sh, w); break;
   }
-  const uint64_t left = rs < ce ? ce - rs : 0;
-  const uint32_t V = left >= 32 ? 0xffffffffu : (1u << (uint32_t)left) - 1u;
-  if constexpr (LL == 1) {
-    w0 = byte_plane<0>(w) & V;
-  } else {
-    const uint32_t p1 = byte_plane<1>(w) & V, p0 = byte_plane<0>(w);
-    w0 = p1;
-    const uint32_t m0 = V & ~p1;
-    cs[0] = __popc(m0);
-    cs[1] = __popc(p1);
-    seg[0] = compress32(p0, m0);
-    seg[1] = compress32(p0, p1);
+  cs[0] = cs[1] = 0;
+  seg[0] = seg[1] = 0;
+#pragma unroll
+  for (int h = 0; h < RPL; ++h) {
+    const uint64_t r = rs + 32 * h;
+    const uint64_t left = r < ce ? ce - r : 0;
+    const uint32_t V = left >= 32 ? 0xffffffffu : (1u << (uint32_t)left) - 1u;
+    if constexpr (LL == 1) {
+      w0[h] = byte_plane<0>(w + 8 * h) & V;
+    } else {
+      const uint32_t p1 = byte_plane<1>(w + 8 * h) & V, p0 = byte_plane<0>(w + 8 * h);
+      w0[h] = p1;
+      const uint32_t m0 = V & ~p1;
+      seg[0] |= (uint64_t)compress32(p0, m0) << cs[0];
+      seg[1] |= (uint64_t)compress32(p0, p1) << cs[1];
+      cs[0] += __popc(m0);
+      cs[1] += __popc(p1);
+    }
   }
 }
 
@@ -472,26 +490,30 @@ __device__ __forceinline__ void batch_rows(const uint8_t* __restrict__ st, uint6
 // 16 bytes of padding after the last text, so the rounded-up tail stays inside
 // it; chunk starts are multiples of 16 apart, so every chunk of a text has the
 // same offset from its boundary.
-__device__ __forceinline__ void batch_stage(BatchSmem& sm, const uint8_t* in, uint64_t c, uint64_t ce, int buf) {
+__device__ __forceinline__ void batch_stage(BatchSmem& sm, const uint8_t* in, uint64_t c, uint64_t ce, int buf,
+                                            uint32_t chunk) {
   const uint32_t off = (uint32_t)((uintptr_t)in & 15u);
-  const uint64_t cnt = min((uint64_t)CH, ce - c);
+  const uint64_t cnt = min((uint64_t)chunk, ce - c);
   const uint32_t bytes = (uint32_t)((off + cnt + 15) & ~15ull);
   fence_proxy_async_smem();
   mbar_expect_tx(&sm.bar[buf], bytes);
   bulk_g2s(sm.stage[buf], in + c - off, bytes, &sm.bar[buf]);
 }
 
-// The level bits of symbols [cb, ce) of text t (cb a multiple of CH), every
-// level in one pass; sm.wbase[s] (set before a barrier) is where the range's
+// The level bits of symbols [cb, ce) of text t (cb a multiple of the chunk,
+// RPL rows of 32 symbols per lane: CH RPL symbols), every level in one pass; sm.wbase[s] (set before a barrier) is where the range's
 // first member of slot s goes, and sm.wend[s] gets where its run ended.
 // Chunks are staged two ahead; `staged`: the caller has already staged the
 // first two.  slot1, if given, takes slot 1's run (positions from its own
 // bit 0) in place of the text's bits.
-template <int LL>
+template <int LL, int RPL>
 __device__ void batch_w_range(const BatchArgs& a, uint32_t t, uint64_t cb, uint64_t ce, BatchSmem& sm,
                               uint32_t& phases, bool staged, uint32_t* __restrict__ slot1 = nullptr) {
   constexpr int NSL = (1 << LL) - 2;  // slots of levels >= 1
   constexpr int NP = (NSL + 1) / 2;   // their pairs
+  constexpr int WS = WSYM * RPL;      // symbols per warp per chunk
+  constexpr uint32_t CHR = CH * RPL;  // symbols per chunk
+  static_assert(RPL == 1 || LL <= 2, "two rows per lane only for 1-2 levels");
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint64_t n = a.so[t + 1] - a.so[t];
   const uint8_t* __restrict__ in = a.sym + a.so[t];
@@ -503,27 +525,28 @@ __device__ void batch_w_range(const BatchArgs& a, uint32_t t, uint64_t cb, uint6
   if (NSL > 0 && lane < (uint32_t)NSL) run = (uint32_t)sm.wbase[lane];
   const uint32_t off = (uint32_t)((uintptr_t)in & 15u);
   if (tid == 0 && !staged) {
-    if (cb < ce) batch_stage(sm, in, cb, ce, 0);
-    if (cb + CH < ce) batch_stage(sm, in, cb + CH, ce, 1);
+    if (cb < ce) batch_stage(sm, in, cb, ce, 0, CHR);
+    if (cb + CHR < ce) batch_stage(sm, in, cb + CHR, ce, 1, CHR);
   }
   int cur = 0;
-  for (uint64_t c0 = cb; c0 < ce; c0 += CH, cur ^= 1) {
+  for (uint64_t c0 = cb; c0 < ce; c0 += CHR, cur ^= 1) {
     mbar_wait(&sm.bar[cur], (phases >> cur) & 1u, a.err);
     phases ^= 1u << cur;
-    const uint64_t r0 = c0 + (uint64_t)warp * WSYM;
-    const uint8_t* const st = sm.stage[cur] + off + warp * WSYM;
-    // lane r = row r: its level-0 word, and per slot its members (cs) and
-    // their level bits compressed to the low end (seg)
-    uint32_t w0 = 0, cs[NSL > 0 ? NSL : 2], seg[NSL > 0 ? NSL : 2];
+    const uint64_t r0 = c0 + (uint64_t)warp * WS;
+    // lane r: its rows' level-0 words, and per slot their members (cs) and
+    // level bits compressed to the low end (seg)
+    uint32_t w0[RPL], cs[NSL > 0 ? NSL : 2];
+    uint64_t seg[NSL > 0 ? NSL : 2];
     if constexpr (LL <= 2) {
-      batch_row_swar<LL>(sm.stage[cur] + warp * WSYM, off, r0 + 32 * lane, ce, lane, w0, cs, seg);
+      batch_row_swar<LL, RPL>(sm.stage[cur] + warp * WS, off, r0 + 32 * RPL * lane, ce, lane, w0, cs, seg);
     } else {
+      const uint8_t* const st = sm.stage[cur] + off + warp * WS;
       uint32_t kP[LL], kV = 0, kW[LL];
 #pragma unroll
       for (int j = 0; j < LL; ++j) kP[j] = kW[j] = 0;
       if (c0 + CH <= ce) batch_rows<LL, true>(st, r0, ce, lane, kP, kV, kW);
       else batch_rows<LL, false>(st, r0, ce, lane, kP, kV, kW);
-      w0 = kW[0];
+      w0[0] = kW[0];
       uint32_t M[NSL];
       M[0] = kV & ~kP[LL - 1];
       M[1] = kV & kP[LL - 1];
@@ -561,15 +584,16 @@ __device__ void batch_w_range(const BatchArgs& a, uint32_t t, uint64_t cb, uint6
     }
     // level 0: the rows' bits in order; a row reaching past the text's end
     // shares its word with level 1
-    {
-      const uint64_t rs = r0 + 32 * lane;
+#pragma unroll
+    for (int h = 0; h < RPL; ++h) {
+      const uint64_t rs = r0 + 32 * (RPL * lane + h);
       if (rs < ce) {
-        if (rs + 32 <= n) bits32[rs >> 5] = w0;
-        else if (w0) atomicOr(bits32 + (rs >> 5), w0);
+        if (rs + 32 <= n) bits32[rs >> 5] = w0[h];
+        else if (w0[h]) atomicOr(bits32 + (rs >> 5), w0[h]);
       }
     }
     __syncthreads();  // the chunk's counts are in; every warp has read the staging buffer
-    if (tid == 0 && c0 + 2 * CH < ce) batch_stage(sm, in, c0 + 2 * CH, ce, cur);
+    if (tid == 0 && c0 + 2 * CHR < ce) batch_stage(sm, in, c0 + 2 * CHR, ce, cur, CHR);
     if constexpr (NSL > 0) {
       uint32_t before[NP], all[NP];
 #pragma unroll
@@ -594,8 +618,10 @@ __device__ void batch_w_range(const BatchArgs& a, uint32_t t, uint64_t cb, uint6
         if (c) {
           const uint32_t d = d0 + ((rp[s >> 1] >> sh) & 0xFFFFu);
           const uint32_t q = (d >> 5) - (d0 >> 5), o = d & 31u;
-          atomicOr(scr + q, seg[s] << o);
-          if (o + c > 32) atomicOr(scr + q + 1, seg[s] >> (32 - o));
+          const uint64_t v = seg[s] << o;  // c <= 32 RPL bits from bit o: up to three words
+          atomicOr(scr + q, (uint32_t)v);
+          if (o + c > 32) atomicOr(scr + q + 1, (uint32_t)(v >> 32));
+          if (RPL > 1 && o + c > 64) atomicOr(scr + q + 2, (uint32_t)(seg[s] >> (64 - o)));
         }
         __syncwarp();
         const uint32_t nw = ((d0 + Ts + 31) >> 5) - (d0 >> 5);
@@ -622,7 +648,7 @@ __device__ void batch_w_range(const BatchArgs& a, uint32_t t, uint64_t cb, uint6
 }
 
 // ---- W item: every level's bits of tile j of a split text
-template <int LL>
+template <int LL, int RPL>
 __device__ void batch_w_item(const BatchArgs& a, uint32_t t, uint32_t j, BatchSmem& sm, uint32_t& phases) {
   constexpr int NSL = (1 << LL) - 2;
   const uint32_t tid = threadIdx.x;
@@ -643,7 +669,7 @@ __device__ void batch_w_item(const BatchArgs& a, uint32_t t, uint32_t j, BatchSm
     sm.wbase[tid] = (uint64_t)l * n + below + mine;
   }
   __syncthreads();
-  batch_w_range<LL>(a, t, cb, ce, sm, phases, false);
+  batch_w_range<LL, RPL>(a, t, cb, ce, sm, phases, false);
   batch_signal(&a.done[4 * t + DN_W]);
 }
 
@@ -1137,14 +1163,14 @@ __device__ void batch_r_whole(const BatchArgs& a, uint32_t t, BatchSmem& sm) {
 }
 
 // ---- X item: the whole text t in this CTA
-template <int L>
+template <int L, int RPL>
 __device__ void batch_x_item(const BatchArgs& a, uint32_t t, BatchSmem& sm, uint32_t& phases) {
   const uint32_t tid = threadIdx.x;
   const uint64_t n = a.so[t + 1] - a.so[t];
   const uint8_t* in = a.sym + a.so[t];
   if (tid == 0) {  // the level pass's first chunks load while the histogram runs
-    if (n > 0) batch_stage(sm, in, 0, n, 0);
-    if (n > CH) batch_stage(sm, in, CH, n, 1);
+    if (n > 0) batch_stage(sm, in, 0, n, 0, CH * RPL);
+    if (n > CH * RPL) batch_stage(sm, in, CH * RPL, n, 1, CH * RPL);
   }
   if constexpr (L == 2) {
     // no histogram: level 1's key-0 run starts at n; the key-1 run (at n + the
@@ -1158,7 +1184,7 @@ __device__ void batch_x_item(const BatchArgs& a, uint32_t t, BatchSmem& sm, uint
       sm.wbase[1] = 0;
     }
     __syncthreads();
-    batch_w_range<2>(a, t, 0, n, sm, phases, true, ks);
+    batch_w_range<2, RPL>(a, t, 0, n, sm, phases, true, ks);
     __syncthreads();
     // move the key-1 run (m bits) to bit p = n + (key-0 members) of the text:
     // word j of the bits takes the stream's bits from 32 j - p on
@@ -1193,18 +1219,19 @@ __device__ void batch_x_item(const BatchArgs& a, uint32_t t, BatchSmem& sm, uint
       sm.wbase[tid] = (uint64_t)l * n + below;
     }
     __syncthreads();
-    batch_w_range<L>(a, t, 0, n, sm, phases, true);
+    batch_w_range<L, RPL>(a, t, 0, n, sm, phases, true);
   }
   __syncthreads();  // the bits are written (read back through L2 below)
   if (a.flags & WTG_RANK) batch_r_whole(a, t, sm);
   if (a.flags & (WTG_SELECT1 | WTG_SELECT0)) batch_s_item(a, t, sm);
 }
 
-// one instantiation per level count (the level pass keeps per-slot state in registers)
-template <int LL>
+// one instantiation per level count (the level pass keeps per-slot state in
+// registers) and rows per lane
+template <int LL, int RPL>
 __global__ void __launch_bounds__(BT, LL == 4 ? 2 : 3) batch_build_kernel(BatchArgs a) {
   __shared__ BatchSmem sm;
-  for (uint32_t i = threadIdx.x; i < BNW * 34; i += BT) (&sm.scr[0][0])[i] = 0;
+  for (uint32_t i = threadIdx.x; i < BNW * 68; i += BT) (&sm.scr[0][0])[i] = 0;
   for (uint32_t e = threadIdx.x; e < 256 * 8; e += BT) {
     uint32_t byte = e >> 3, r = e & 7, pos = 0;
     for (uint32_t k = 0; k < 8; ++k)
@@ -1238,12 +1265,12 @@ __global__ void __launch_bounds__(BT, LL == 4 ? 2 : 3) batch_build_kernel(BatchA
     const uint32_t t = it.x, kind = it.y, tile = it.z;
     const uint32_t J = (uint32_t)(a.hb[t + 1] - a.hb[t]);
     if (kind == IT_X) {
-      batch_x_item<LL>(a, t, sm, phases);
+      batch_x_item<LL, RPL>(a, t, sm, phases);
     } else if (kind == IT_H) {
       batch_h_item(a, t, tile, sm);
     } else if (kind == IT_W) {
       batch_wait(&a.done[4 * t + DN_HREADY], 1, a.err);
-      batch_w_item<LL>(a, t, tile, sm, phases);
+      batch_w_item<LL, RPL>(a, t, tile, sm, phases);
     } else if (kind == IT_R) {
       batch_wait(&a.done[4 * t + DN_W], J, a.err);
       batch_r_tile(a, t, tile, sm);
@@ -1273,8 +1300,13 @@ struct BatchImpl {
   bool items_valid = false;
   uint64_t tile = 65536;      // symbols per H / W tile of a split text
   int64_t whole_req = -1;     // texts up to this many symbols are X items (-1: automatic)
+  int rpl = 1;                // rows of 32 symbols per lane in the level pass
+  bool shape_fixed = false;   // set_shape was called: no tuning
   uint64_t whole_max = 0;     // the bound in use
   uint64_t nwhole = 0;        // texts built whole
+  uint64_t items_tile = 0;    // the shape the uploaded items follow
+  int64_t items_whole = -2;
+  float tune_ms[8] = {0};
   std::vector<uint64_t> h_info;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -1296,19 +1328,19 @@ static uint64_t pool_bound(uint64_t size) {
   return nsb * logn + (logn4 ? size / logn4 : 0) * 64 * logn + 1;
 }
 
-static void (*batch_kernel(int L))(BatchArgs) {
+static void (*batch_kernel(int L, int rpl))(BatchArgs) {
   switch (L) {
-    case 1: return batch_build_kernel<1>;
-    case 2: return batch_build_kernel<2>;
-    case 3: return batch_build_kernel<3>;
-    default: return batch_build_kernel<4>;
+    case 1: return rpl == 2 ? batch_build_kernel<1, 2> : batch_build_kernel<1, 1>;
+    case 2: return rpl == 2 ? batch_build_kernel<2, 2> : batch_build_kernel<2, 1>;
+    case 3: return batch_build_kernel<3, 1>;
+    default: return batch_build_kernel<4, 1>;
   }
 }
 
 // CTAs of the persistent grid: every one resident at once
-static int batch_grid_size(int L) {
+static int batch_grid_size(int L, int rpl) {
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel(L), BT, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel(L, rpl), BT, 0);
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -1322,10 +1354,10 @@ static int batch_grid_size(int L) {
 // resident CTAs), at least 65536 symbols.
 static int batch_items(BatchImpl& b) {
   int rc;
-  if (b.items_valid) return WTG_OK;
+  if (b.items_valid && b.items_tile == b.tile && b.items_whole == b.whole_req) return WTG_OK;
   const uint64_t total = b.so[b.T];
   b.whole_max = b.whole_req >= 0 ? (uint64_t)b.whole_req
-                                 : std::max<uint64_t>(65536, total / (uint64_t)batch_grid_size(b.L));
+                                 : std::max<uint64_t>(65536, total / (uint64_t)batch_grid_size(b.L, 1));
   const uint64_t tile = b.tile;
   const bool supports = (b.flags & (WTG_RANK | WTG_SELECT1 | WTG_SELECT0)) != 0;
   const bool sel = (b.flags & (WTG_SELECT1 | WTG_SELECT0)) != 0;
@@ -1357,6 +1389,8 @@ static int batch_items(BatchImpl& b) {
   b.nitems = (uint32_t)items.size();
   b.nwhole = whole.size();
   b.items_valid = true;
+  b.items_tile = b.tile;
+  b.items_whole = b.whole_req;
   return WTG_OK;
 }
 
@@ -1410,8 +1444,8 @@ static int batch_enqueue(BatchImpl& b) {
   WTG_CK(cudaMemsetAsync(b.rstat.p, 0, std::max<uint64_t>(b.rtiles, 1) * sizeof(uint64_t), s));
   WTG_CK(cudaMemsetAsync(b.info.p, 0, b.T * 8 * sizeof(uint64_t), s));
   count_launch();
-  const int grid = (int)std::min<uint64_t>((uint64_t)batch_grid_size(b.L), std::max<uint32_t>(b.nitems, 1));
-  batch_kernel(b.L)<<<grid, BT, 0, s>>>(batch_args(b));
+  const int grid = (int)std::min<uint64_t>((uint64_t)batch_grid_size(b.L, b.rpl), std::max<uint32_t>(b.nitems, 1));
+  batch_kernel(b.L, b.rpl)<<<grid, BT, 0, s>>>(batch_args(b));
   WTG_CK(cudaGetLastError());
   return WTG_OK;
 }
@@ -1546,16 +1580,80 @@ static int batch_capture(BatchImpl& b) {
   return WTG_OK;
 }
 
-int batch_set_shape(BatchImpl& b, int tile, int64_t whole_max) {
-  if (tile < CH || tile > (1 << 24) || tile % CH) return fail(WTG_ERR_INVALID, "tile must be a multiple of 8192 in 8192 .. 2^24");
-  if (whole_max < -1) return fail(WTG_ERR_INVALID, "whole_max must be -1 (automatic) or >= 0");
+// The autotuner's candidates: symbols per thread of the level pass (one or
+// two 32-symbol rows per lane; two only for 1-2 levels) x (split tile,
+// whole-text bound): the automatic bound, and every text split into tiles
+// of 32768 or 131072 symbols.
+struct BatchShape {
+  int rpl;
+  uint64_t tile;
+  int64_t whole;
+};
+static const BatchShape kBatchShapes[] = {
+    {1, 65536, -1}, {2, 65536, -1}, {1, 32768, 0}, {2, 32768, 0}, {1, 131072, 0}, {2, 131072, 0},
+};
+constexpr int kNumBatchShapes = sizeof(kBatchShapes) / sizeof(kBatchShapes[0]);
+
+static void batch_drop_graph(BatchImpl& b) {
   if (b.exec) cudaGraphExecDestroy(b.exec);
   if (b.graph) cudaGraphDestroy(b.graph);
   b.exec = nullptr;
   b.graph = nullptr;
+}
+
+// Times every candidate shape once (after one warm-up run) on the batch's
+// own input and keeps the fastest.
+static int batch_tune(BatchImpl& b) {
+  int rc = WTG_OK;
+  cudaStream_t s = b.stream;
+  cudaEvent_t e0, e1;
+  WTG_CK(cudaEventCreate(&e0));
+  WTG_CK(cudaEventCreate(&e1));
+  float best = 1e30f;
+  int best_v = 0;
+  for (int v = 0; v < kNumBatchShapes; ++v) {
+    b.tune_ms[v] = 0;
+    if (kBatchShapes[v].rpl > 1 && b.L > 2) continue;
+    b.rpl = kBatchShapes[v].rpl;
+    b.tile = kBatchShapes[v].tile;
+    b.whole_req = kBatchShapes[v].whole;
+    if ((rc = batch_items(b))) break;
+    if ((rc = batch_enqueue(b))) break;
+    WTG_CK(cudaEventRecord(e0, s));
+    if ((rc = batch_enqueue(b))) break;
+    WTG_CK(cudaEventRecord(e1, s));
+    WTG_CK(cudaEventSynchronize(e1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    b.tune_ms[v] = ms;
+    if (ms < best) {
+      best = ms;
+      best_v = v;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  b.rpl = kBatchShapes[best_v].rpl;
+  b.tile = kBatchShapes[best_v].tile;
+  b.whole_req = kBatchShapes[best_v].whole;
+  return WTG_OK;
+}
+
+int batch_set_shape(BatchImpl& b, int tile, int64_t whole_max, int symbols_per_thread) {
+  if (symbols_per_thread != 32 && symbols_per_thread != 64)
+    return fail(WTG_ERR_INVALID, "symbols_per_thread must be 32 or 64");
+  if (symbols_per_thread == 64 && b.L > 2) return fail(WTG_ERR_INVALID, "64 symbols per thread need 1-2 levels");
+  const int chunk = CH * (symbols_per_thread / 32);
+  if (tile < chunk || tile > (1 << 24) || tile % chunk)
+    return fail(WTG_ERR_INVALID, "tile must be a multiple of 256 x symbols_per_thread in that .. 2^24");
+  if (whole_max < -1) return fail(WTG_ERR_INVALID, "whole_max must be -1 (automatic) or >= 0");
+  batch_drop_graph(b);
   b.tile = (uint64_t)tile;
   b.whole_req = whole_max;
-  b.items_valid = false;
+  b.rpl = symbols_per_thread / 32;
+  b.shape_fixed = true;
+  for (float& m : b.tune_ms) m = 0;
   return WTG_OK;
 }
 
@@ -1563,6 +1661,7 @@ int batch_run(BatchImpl& b) {
   int rc;
   b.info_valid = false;
   if (!b.exec) {
+    if (!b.shape_fixed && (rc = batch_tune(b))) return rc;
     if ((rc = batch_capture(b))) return rc;
   }
   count_launch();
@@ -1656,11 +1755,14 @@ void* batch_input(BatchImpl& b) { return b.in.p; }
 cudaStream_t batch_stream(const BatchImpl& b) { return b.stream; }
 uint64_t batch_total_symbols(const BatchImpl& b) { return b.so[b.T]; }
 
-int batch_shape(const BatchImpl& b, int* tile, int64_t* whole_max, uint64_t* whole_texts) {
+int batch_shape(const BatchImpl& b, int* tile, int64_t* whole_max, int* symbols_per_thread, uint64_t* whole_texts,
+                float* ms, int nms) {
   if (!b.items_valid) return fail(WTG_ERR_INVALID, "the batch has not run yet");
   *tile = (int)b.tile;
   *whole_max = (int64_t)b.whole_max;
+  *symbols_per_thread = 32 * b.rpl;
   *whole_texts = b.nwhole;
+  for (int v = 0; v < nms; ++v) ms[v] = v < kNumBatchShapes ? b.tune_ms[v] : 0.f;
   return WTG_OK;
 }
 

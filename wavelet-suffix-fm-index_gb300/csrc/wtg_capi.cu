@@ -885,9 +885,9 @@ int wtg_batch_load(wtg_batch* B, const void* texts) {
   return WTG_OK;
 }
 
-int wtg_batch_set_shape(wtg_batch* B, int tile, int64_t whole_max) {
+int wtg_batch_set_shape(wtg_batch* B, int tile, int64_t whole_max, int symbols_per_thread) {
   if (!B) return fail(WTG_ERR_INVALID, "null batch");
-  return batch_set_shape(*B->b, tile, whole_max);
+  return batch_set_shape(*B->b, tile, whole_max, symbols_per_thread);
 }
 
 int wtg_batch_run(wtg_batch* B) {
@@ -943,9 +943,11 @@ int wtg_batch_get_select(wtg_batch* B, uint64_t t, int t_b, uint64_t* sb_words, 
   return batch_get(*B->b, t, 4, t_b, pool, si[7]);
 }
 
-int wtg_batch_shape(wtg_batch* B, int* tile, int64_t* whole_max, uint64_t* whole_texts) {
-  if (!B || !tile || !whole_max || !whole_texts) return fail(WTG_ERR_INVALID, "null argument");
-  return batch_shape(*B->b, tile, whole_max, whole_texts);
+int wtg_batch_shape(wtg_batch* B, int* tile, int64_t* whole_max, int* symbols_per_thread, uint64_t* whole_texts,
+                    float ms[8]) {
+  if (!B || !tile || !whole_max || !symbols_per_thread || !whole_texts || !ms)
+    return fail(WTG_ERR_INVALID, "null argument");
+  return batch_shape(*B->b, tile, whole_max, symbols_per_thread, whole_texts, ms, 8);
 }
 
 // ------------------------------------------------ Huffman-shaped trees

@@ -127,7 +127,7 @@ void batch_delete(BatchImpl* b);
 int batch_plan(BatchImpl& b, const uint64_t* lengths, uint64_t T, int L, uint32_t flags, cudaStream_t s,
                bool own_stream);
 int batch_run(BatchImpl& b);
-int batch_set_shape(BatchImpl& b, int tile, int64_t whole_max);
+int batch_set_shape(BatchImpl& b, int tile, int64_t whole_max, int symbols_per_thread);
 int batch_sync(BatchImpl& b, uint32_t* err_out);
 int batch_text_info(const BatchImpl& b, uint64_t t, uint64_t info[8]);
 int batch_select_info(const BatchImpl& b, uint64_t t, int t_b, uint64_t info[8]);
@@ -136,7 +136,8 @@ int batch_get(const BatchImpl& b, uint64_t t, int what, int t_b, void* dst, uint
 void* batch_input(BatchImpl& b);
 cudaStream_t batch_stream(const BatchImpl& b);
 uint64_t batch_total_symbols(const BatchImpl& b);
-int batch_shape(const BatchImpl& b, int* tile, int64_t* whole_max, uint64_t* whole_texts);
+int batch_shape(const BatchImpl& b, int* tile, int64_t* whole_max, int* symbols_per_thread, uint64_t* whole_texts,
+                float* ms, int nms);
 
 // Huffman-shaped wavelet tree of a byte text (wtg_huff.cu)
 struct HuffImpl;

@@ -104,7 +104,7 @@ _SIGS = {
     "wtg_batch_input": ([vp, vp, vp], i32),
     "wtg_batch_load": ([vp, vp], i32),
     "wtg_batch_run": ([vp], i32),
-    "wtg_batch_set_shape": ([vp, i32, ctypes.c_int64], i32),
+    "wtg_batch_set_shape": ([vp, i32, ctypes.c_int64, i32], i32),
     "wtg_batch_sync": ([vp], i32),
     "wtg_batch_free": ([vp], i32),
     "wtg_batch_text_info": ([vp, u64, vp], i32),
@@ -112,7 +112,7 @@ _SIGS = {
     "wtg_batch_get_bits": ([vp, u64, vp, u64], i32),
     "wtg_batch_get_rank": ([vp, u64, vp, u64], i32),
     "wtg_batch_get_select": ([vp, u64, i32, vp, vp, vp], i32),
-    "wtg_batch_shape": ([vp, vp, vp, vp], i32),
+    "wtg_batch_shape": ([vp, vp, vp, vp, vp, vp], i32),
     "wtg_remap_alphabet": ([vp, u64, i32, vp], i32),
     "wtg_rank_build_noalloc": ([vp, u64, vp, vp], i32),
     "wtg_profile_enable": ([i32], i32),
@@ -768,10 +768,11 @@ class Batch:
     def run(self):
         _ck(lib().wtg_batch_run(self.h))
 
-    def set_shape(self, tile=65536, whole_max=-1):
-        """Work-list shape for the next run: symbols per split-text tile, and
-        the longest text one CTA builds whole (-1 automatic, 0 split all)."""
-        _ck(lib().wtg_batch_set_shape(self.h, tile, whole_max))
+    def set_shape(self, tile=65536, whole_max=-1, symbols_per_thread=32):
+        """Fix the shape instead of tuning it on the first run: symbols per
+        split-text tile, the longest text one CTA builds whole (-1 automatic,
+        0 split all), and the level pass's symbols per thread (32 or 64)."""
+        _ck(lib().wtg_batch_set_shape(self.h, tile, whole_max, symbols_per_thread))
 
     def sync(self):
         _ck(lib().wtg_batch_sync(self.h))
@@ -813,10 +814,13 @@ class Batch:
         return _SelectTables(info, sb[: int(info[6])], desc[: int(info[4])], pool[: int(info[7])])
 
     def shape(self):
-        """(split tile, whole-text bound in use, texts built whole) after a run."""
-        th, wm, nw = ctypes.c_int(0), ctypes.c_int64(0), ctypes.c_uint64(0)
-        _ck(lib().wtg_batch_shape(self.h, ctypes.byref(th), ctypes.byref(wm), ctypes.byref(nw)))
-        return th.value, wm.value, nw.value
+        """After a run: (split tile, whole-text bound in use, symbols per
+        thread, texts built whole, candidate times in ms)."""
+        th, wm, spt, nw = ctypes.c_int(0), ctypes.c_int64(0), ctypes.c_int(0), ctypes.c_uint64(0)
+        ms = np.zeros(8, dtype=np.float32)
+        _ck(lib().wtg_batch_shape(self.h, ctypes.byref(th), ctypes.byref(wm), ctypes.byref(spt), ctypes.byref(nw),
+                                  _p(ms)))
+        return th.value, wm.value, spt.value, nw.value, ms
 
 
 def rank_build_noalloc(d_words_ptr, size_bits, d_rank_ptr, stream=0):
