@@ -54,11 +54,11 @@ def algorithmic_bytes(n, L, w, sel_words=0):
 
 
 # DRAM bytes (read + write) per symbol of one uint32 partitioning level pass,
-# from ncu's dram__bytes_read.sum + dram__bytes_write.sum over levels 9-11 of
-# an n=2^26 build (491.9 MB per launch: 269.6 MB read, 222.3 MB written, the
-# rest of the writes still in L2 when the launch ends); traffic grows
+# from ncu's dram__bytes_read.sum + dram__bytes_write.sum over three level
+# launches (levels 9-11) of an n=2^28 build: 2137.7 MB per launch (1079.0 MB
+# read, 1058.7 MB written) against 2181.0 MB algorithmic; traffic grows
 # linearly with n, so a full launch's traffic is this figure times n.
-LEVEL_DRAM_BYTES_PER_SYMBOL_U32 = 491.9e6 / 2 ** 26
+LEVEL_DRAM_BYTES_PER_SYMBOL_U32 = 2137.7e6 / 2 ** 28
 
 
 def level_launch_bytes(n, w):
@@ -708,7 +708,7 @@ def run_wtg(args, rank, world, local_rank):
         e_s = slowest_rank(dist, torch, time.perf_counter() - t0, dev)
         e2e = {"value": job_throughput(world, e_steps, e2e_bytes, e_s), "unit": "GB/s",
                "h2d_bytes_per_step": 4 * n, "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e_s / e_steps,
-               "step_ms": [round(x, 2) for x in step_ms]}
+               "median_ms_per_step": round(float(np.median(step_ms)), 3), "step_ms": [round(x, 2) for x in step_ms]}
         t_e.free()
         del outs, host_in, t_e
         torch.cuda.empty_cache()
