@@ -397,7 +397,7 @@ def b_texts_host(texts_seed, ntexts):
     return [concat[offs[t]:offs[t + 1]] for t in range(ntexts)]
 
 
-def measure_batch(torch, wtg, stream, ntexts, reps=5, cpu_texts=0):
+def measure_batch(torch, wtg, stream, ntexts, reps=5, cpu_texts=0, shape=None):
     """Batched build of ntexts DNA-like texts (lengths floor(2^U[10,20]),
     i.i.d. uniform over 4 symbols, 2 levels, rank + select1 + select0): one
     persistent launch replayed from a CUDA graph, against the same texts
@@ -411,8 +411,10 @@ def measure_batch(torch, wtg, stream, ntexts, reps=5, cpu_texts=0):
     b = wtg.Batch(lengths, 2, wtg.ALL, stream.cuda_stream)
     b.load(texts)
     del texts
+    if shape:  # (split tile, whole-text bound, symbols per thread) instead of the tuner's choice
+        b.set_shape(*shape)
     t0 = time.perf_counter()
-    b.run()  # first run: autotune + graph capture
+    b.run()  # first run: autotune (unless the shape is fixed) + graph capture
     b.sync()
     first_s = time.perf_counter() - t0
     ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
@@ -586,8 +588,8 @@ def measure_select(torch, wtg, tree, n, L, dev, stream, log2_q, reps=5, cpu_log2
         exact = exact and ok
         learned.append({
             "segments_per_level": segs, "mqs": 2 * nq / (ms / 1e3) / 1e6, "ms": ms, "speedup": plain_ms / ms,
-            "exact": bool(ok), "space_bits_per_bit": 8 * info["model_bytes"] / bits,
-            "model_bytes": info["model_bytes"], "segments": info["segments"],
+            "exact": bool(ok), "space_bits_per_bit": 8 * info["index_bytes"] / bits,
+            "index_bytes": info["index_bytes"], "segments": info["segments"],
             "fallback_segments": info["fallback_segments"], "max_window": info["max_window"],
             "mean_window": info["window_sum"] / max(1, info["segments"] - info["fallback_segments"]),
             "misses": info["misses"], "build_ms": b0.elapsed_time(b1),
@@ -772,7 +774,8 @@ def run_wtg(args, rank, world, local_rank):
                                 cpu_log2=24 if cpu_on else 0)
         queries = measure_queries(torch, tree, seq, n, dev, stream, args.select_log2)
     if args.batch_texts:
-        batch = measure_batch(torch, wtg, stream, args.batch_texts, cpu_texts=512 if cpu_on else 0)
+        shape = tuple(int(x) for x in args.batch_shape.split(",")) if args.batch_shape else None
+        batch = measure_batch(torch, wtg, stream, args.batch_texts, cpu_texts=512 if cpu_on else 0, shape=shape)
     if args.bytes_log2:
         byte_text = measure_byte_text(torch, wtg, dev, args.bytes_log2, cpu=cpu_on)
     fm = None
@@ -852,6 +855,8 @@ def main():
     ap.add_argument("--fm-cpu-log2", type=int, default=22)
     ap.add_argument("--bytes-log2", type=int, default=24,
                     help="byte-text build (Zipf bytes, 8 levels, rank) of 2^k symbols; 0 skips")
+    ap.add_argument("--batch-shape", default=None,
+                    help="fix the batch's shape as tile,whole_max,symbols_per_thread (default: autotuned)")
     ap.add_argument("--batch-texts", type=int, default=4096,
                     help="texts of the batched-build comparison (0: skip it)")
     ap.add_argument("--select-log2", type=int, default=26,

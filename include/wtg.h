@@ -327,19 +327,24 @@ int wtg_tree_level_select_device(wtg_tree* t, int t_b, const uint64_t* d_level, 
  * `segments` segments of 2^g args; each gets a line fitted on the GPU by
  * least squares to `samples` (k, select(k)) pairs taken from the plain
  * select, and an error window that holds for every k of the segment.  A
- * query predicts the position and searches the window exactly through the
- * rank_support_v superblocks; segments whose window exceeds max_window
- * positions are answered by the plain select.  Answers equal
+ * query predicts the position and searches the window exactly through a
+ * rank directory of the superblocks (per 8192 bits the ones before them,
+ * per 512-bit superblock an int8 residual against the line between: 24
+ * bytes per 8192 bits, small enough to stay in L2), then reads the
+ * superblock's one 64-byte line; segments whose window exceeds max_window
+ * positions, and blocks whose residuals overflow int8, are answered by the
+ * plain select.  Answers equal
  * wtg_tree_level_select's.  The index reads the tree's bitvector, rank and
  * select tables: it is valid until the tree is rebuilt or freed (queries
  * after a rebuild return WTG_ERR_INVALID).  Needs a tree built with WTG_ALL.
  * Builds on the tree's stream and waits for it. */
 int wtg_lsel_build(wtg_tree* t, uint32_t segments, uint32_t samples, uint32_t max_window, wtg_lsel** out);
 int wtg_lsel_free(wtg_lsel* m);
-/* info[8]: segments (both polarities), model bytes, segments answered by the
- * plain select, largest window of the others, sum of their windows, searches
- * that fell back since the build (0 unless the tables are inconsistent),
- * segments and samples parameters */
+/* info[8]: segments (both polarities), index bytes (segment records and
+ * the rank directory), segments answered by the plain select, largest
+ * window of the others, sum of their windows, searches that fell back since
+ * the build (0 unless the tables are inconsistent), segments and samples
+ * parameters */
 int wtg_lsel_info(wtg_lsel* m, uint64_t info[8]);
 /* one level's model: lvl_info = {args before the level, args in it, g,
  * segments}; rec (may be NULL) receives 4 u32 per segment: base, slope

@@ -967,26 +967,6 @@ __device__ void batch_s_item(const BatchArgs& a, uint32_t t, BatchSmem& sm) {
   }
 }
 
-// d-th (0-based) set bit of v; cl = popcount of its low 32 bits.  Halving
-// by popcounts down to a byte, then the in-byte table.
-__device__ __forceinline__ uint32_t batch_sel64(uint64_t v, uint32_t d, uint32_t cl, const uint8_t* __restrict__ lut) {
-  const bool up = d >= cl;
-  uint32_t w = up ? (uint32_t)(v >> 32) : (uint32_t)v;
-  d -= up ? cl : 0u;
-  uint32_t pos = up ? 32u : 0u;
-  const uint32_t c16 = __popc(w & 0xFFFFu);
-  const bool u16 = d >= c16;
-  w = u16 ? (w >> 16) : w;
-  d -= u16 ? c16 : 0u;
-  pos += u16 ? 16u : 0u;
-  const uint32_t c8 = __popc(w & 0xFFu);
-  const bool u8 = d >= c8;
-  w = u8 ? (w >> 8) : w;
-  d -= u8 ? c8 : 0u;
-  pos += u8 ? 8u : 0u;
-  return pos + lut[((w & 0xFFu) << 3) | (d & 7u)];
-}
-
 // ---- the rank table and select marks of a whole text in this CTA (its bits
 // were written by this CTA): a thread per 512-bit superblock, BT
 // superblocks per round; the ones before a superblock from a block scan of
@@ -1080,7 +1060,7 @@ __device__ void batch_r_whole(const BatchArgs& a, uint32_t t, BatchSmem& sm) {
         const uint32_t K1 = sb_before + excl, K0 = zb + 64u * j - excl;
         const uint32_t d1 = (0u - K1) & 63u, d0 = K1 & 63u;
         const bool s1 = sel1 && d1 < cj, s0 = sel0 && d0 < czj;
-        const uint32_t off = batch_sel64(s1 ? x : ~x, s1 ? d1 : d0, s1 ? cl : 32u - cl, lut);
+        const uint32_t off = sel64_lut(s1 ? x : ~x, s1 ? d1 : d0, s1 ? cl : 32u - cl, lut);
         // both polarities only when K1 % 64 == 0: the word's first one and first zero
         const uint32_t off0 = s1 ? (uint32_t)(__ffsll((long long)~x) - 1) : off;
         const uint32_t pos = 512 * b + 64u * j;
@@ -1122,7 +1102,7 @@ __device__ void batch_r_whole(const BatchArgs& a, uint32_t t, BatchSmem& sm) {
           bef += cj;
         }
         xx = t1 ? xx : ~xx;
-        const uint32_t pos = 512 * b + 64 * jj + batch_sel64(xx, r, __popc((uint32_t)xx), lut);
+        const uint32_t pos = 512 * b + 64 * jj + sel64_lut(xx, r, __popc((uint32_t)xx), lut);
         if (h1) ends1[(sb_before + e1) >> 12] = pos;
         else if (h0) ends0[(zb + e0) >> 12] = pos;
         if (h1) h1 = false;
@@ -1232,18 +1212,7 @@ template <int LL, int RPL>
 __global__ void __launch_bounds__(BT, LL == 4 ? 2 : 3) batch_build_kernel(BatchArgs a) {
   __shared__ BatchSmem sm;
   for (uint32_t i = threadIdx.x; i < BNW * 68; i += BT) (&sm.scr[0][0])[i] = 0;
-  for (uint32_t e = threadIdx.x; e < 256 * 8; e += BT) {
-    uint32_t byte = e >> 3, r = e & 7, pos = 0;
-    for (uint32_t k = 0; k < 8; ++k)
-      if ((byte >> k) & 1u) {
-        if (r == 0) {
-          pos = k;
-          break;
-        }
-        --r;
-      }
-    sm.lut[e] = (uint8_t)pos;
-  }
+  sel_lut_init(sm.lut);
   if (threadIdx.x == 0) {
     mbar_init(&sm.bar[0], 1);
     mbar_init(&sm.bar[1], 1);

@@ -151,6 +151,17 @@ __global__ void __launch_bounds__(BV_THREADS)
   }
 }
 
+// position after the last one (t_b = 1) or zero (t_b = 0) of superblock sb
+// (eight words, all inside the bitvector); read through L2
+__device__ __forceinline__ uint64_t last_arg_end_sb(const uint64_t* __restrict__ words, uint64_t sb, int t_b) {
+  for (int j = 7; j >= 0; --j) {
+    uint64_t x = __ldcg(words + 8 * sb + j);
+    if (!t_b) x = ~x;
+    if (x) return ((8 * sb + j) << 6) + hi64(x) + 1;
+  }
+  return 0;
+}
+
 // Rank table and select samples of a wavelet tree's concatenated bitvector
 // when n % 512 == 0: superblock b is chunk c of level l (b = l * n/512 + c),
 // and the zeros before it are the zeros of the levels before l (lvl_zb) plus
@@ -167,36 +178,6 @@ __global__ void __launch_bounds__(BV_THREADS)
 // holds at most one superblock end per polarity (512 < 4096 args), resolved
 // once per superblock; the last word holding a one / a zero is resolved once
 // per thread from the last such superblock.
-__device__ __forceinline__ uint32_t sel64_lut(uint64_t v, uint32_t d, uint32_t cl, const uint8_t* __restrict__ lut) {
-  // d-th (0-based) set bit of v; cl = popcount of its low 32 bits
-  const bool up = d >= cl;
-  uint32_t w = up ? (uint32_t)(v >> 32) : (uint32_t)v;
-  d -= up ? cl : 0u;
-  uint32_t pos = up ? 32u : 0u;
-  const uint32_t c16 = __popc(w & 0xFFFFu);
-  const bool u16 = d >= c16;
-  w = u16 ? (w >> 16) : w;
-  d -= u16 ? c16 : 0u;
-  pos += u16 ? 16u : 0u;
-  const uint32_t c8 = __popc(w & 0xFFu);
-  const bool u8 = d >= c8;
-  w = u8 ? (w >> 8) : w;
-  d -= u8 ? c8 : 0u;
-  pos += u8 ? 8u : 0u;
-  return pos + lut[((w & 0xFFu) << 3) | (d & 7u)];
-}
-
-// position after the last one (t_b = 1) or zero (t_b = 0) of superblock sb
-// (eight words, all inside the bitvector); read through L2
-__device__ __forceinline__ uint64_t last_arg_end_sb(const uint64_t* __restrict__ words, uint64_t sb, int t_b) {
-  for (int j = 7; j >= 0; --j) {
-    uint64_t x = __ldcg(words + 8 * sb + j);
-    if (!t_b) x = ~x;
-    if (x) return ((8 * sb + j) << 6) + hi64(x) + 1;
-  }
-  return 0;
-}
-
 __global__ void __launch_bounds__(256)
     rs_levels_kernel(const uint64_t* __restrict__ words, int L, uint64_t chunks_per_level,
                      const uint32_t* __restrict__ chunkpre, uint64_t prestride, const uint64_t* __restrict__ lvl_zb,
@@ -204,15 +185,7 @@ __global__ void __launch_bounds__(256)
                      uint64_t* __restrict__ starts1, uint64_t* __restrict__ starts0, uint64_t* __restrict__ ends1,
                      uint64_t* __restrict__ ends0, unsigned long long* info) {
   __shared__ uint8_t lut[256 * 8];  // lut[byte * 8 + r] = position of the r-th set bit of byte
-  for (uint32_t e = threadIdx.x; e < 256 * 8; e += blockDim.x) {
-    uint32_t byte = e >> 3, r = e & 7, pos = 0;
-    for (uint32_t k = 0; k < 8; ++k)
-      if ((byte >> k) & 1u) {
-        if (r == 0) { pos = k; break; }
-        --r;
-      }
-    lut[e] = (uint8_t)pos;
-  }
+  sel_lut_init(lut);
   __syncthreads();
   const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;

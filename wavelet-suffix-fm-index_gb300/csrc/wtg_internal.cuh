@@ -88,6 +88,45 @@ __device__ __forceinline__ uint32_t sel64_0(uint64_t x, uint32_t r) {
 // position of the i-th (1-based) set bit of x (bits::sel semantics); i <= popc(x)
 __device__ __forceinline__ uint32_t sel64(uint64_t x, uint32_t i) { return sel64_0(x, i - 1); }
 
+// d-th (0-based) set bit of v, d < popc(v); cl = popcount of its low 32
+// bits.  Halving by popcounts down to a byte, then a 256 x 8 table of
+// in-byte selects (lut[byte * 8 + r] = position of the r-th set bit of
+// byte), kept in shared memory by the caller (sel_lut_init).
+__device__ __forceinline__ uint32_t sel64_lut(uint64_t v, uint32_t d, uint32_t cl, const uint8_t* __restrict__ lut) {
+  const bool up = d >= cl;
+  uint32_t w = up ? (uint32_t)(v >> 32) : (uint32_t)v;
+  d -= up ? cl : 0u;
+  uint32_t pos = up ? 32u : 0u;
+  const uint32_t c16 = __popc(w & 0xFFFFu);
+  const bool u16 = d >= c16;
+  w = u16 ? (w >> 16) : w;
+  d -= u16 ? c16 : 0u;
+  pos += u16 ? 16u : 0u;
+  const uint32_t c8 = __popc(w & 0xFFu);
+  const bool u8 = d >= c8;
+  w = u8 ? (w >> 8) : w;
+  d -= u8 ? c8 : 0u;
+  pos += u8 ? 8u : 0u;
+  return pos + lut[((w & 0xFFu) << 3) | (d & 7u)];
+}
+
+// fills the in-byte select table (every thread of the block takes part; a
+// barrier must follow before the first use)
+__device__ __forceinline__ void sel_lut_init(uint8_t* lut) {
+  for (uint32_t e = threadIdx.x; e < 256 * 8; e += blockDim.x) {
+    uint32_t byte = e >> 3, r = e & 7, pos = 0;
+    for (uint32_t k = 0; k < 8; ++k)
+      if ((byte >> k) & 1u) {
+        if (r == 0) {
+          pos = k;
+          break;
+        }
+        --r;
+      }
+    lut[e] = (uint8_t)pos;
+  }
+}
+
 // sdsl bits::hi (0 for x == 0)
 __host__ __device__ __forceinline__ uint32_t hi64(uint64_t x) {
 #ifdef __CUDA_ARCH__

@@ -14,12 +14,20 @@
 // select (lsel_fit_kernel), and signed bounds dlo_j <= select(k) - pred(k)
 // <= dhi_j that hold for EVERY k of the segment: lsel_bound_kernel derives
 // them from each word's first and last arg and the rank table, so no pair is
-// left unchecked.  A query reads its segment record, probes rank_support_v
-// superblocks inside [pred + dlo, pred + dhi] (two interpolation steps, then
-// bisection), takes the word from the superblock's 9-bit counts and selects
-// inside it.  Segments whose window exceeds max_window, and any search that
-// does not close, are answered by the plain select, so every answer is the
-// plain select's answer.
+// left unchecked.
+//
+// The window is searched through a rank directory small enough to stay in
+// L2 (lsel_dir_kernel, from the rank_support_v table): per 8192-bit block of
+// the concatenated bitvector the exact ones before it (u64), and per 512-bit
+// superblock an int8 residual against the line between its block's two
+// counts -- 24 bytes per 8192 bits.  A query reads its segment record, the
+// block counts inside [pred + dlo, pred + dhi] (L2), its block's sixteen
+// residuals (L2), which give the superblock exactly, and then the
+// superblock's eight words: one 64-byte line from DRAM, where plain select
+// reads a mini-block entry and then the data.  Segments whose window
+// exceeds max_window, blocks whose residuals do not fit int8, and any search
+// that does not close are answered by the plain select, so every answer is
+// the plain select's answer.
 #include <algorithm>
 #include <vector>
 
@@ -34,6 +42,8 @@ struct LselLevel {
   uint32_t g;        // log2 of args per segment
   uint32_t nseg;     // segments of this level
   uint64_t rec_off;  // index of the level's first segment record
+  uint64_t off;      // the level's first bit in the concatenated bitvector
+  uint64_t pad;
 };
 
 // segment record (uint4): x = base (level position), y = slope (16.16 fixed,
@@ -48,16 +58,49 @@ struct LselImpl {
   std::vector<LselLevel> lv_host[2];
   SelView plain_host[2];
   DevBuf lv[2], rec[2], plain[2], stats;  // plain: the SelView of the fallback
+  DevBuf dbase, dres;                     // rank directory: block counts, superblock residuals
+  uint64_t dblocks = 0;
 };
 
 namespace {
 
 constexpr int LSEL_FRAC = 16;
 constexpr int LSEL_MAX_PROBES = 40;
-constexpr int LSEL_INTERP_PROBES = 5;
 constexpr long long LSEL_SAT = 1ll << 30;
 // stats words per polarity: fallback segments, max window, window sum, misses
 constexpr int LSEL_ST = 4;
+constexpr int LSEL_DIR_SB = 16;          // superblocks per directory block (8192 bits)
+constexpr int8_t LSEL_DIR_OVER = -128;   // residual 0 of a block whose residuals do not fit int8
+
+// L2 cache policies for the query's loads (per load, no device state): the
+// index (segment records, directory) evict-last, the data lines evict-first
+__device__ __forceinline__ uint64_t l2_policy_last() {
+  uint64_t p;
+  asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t l2_policy_first() {
+  uint64_t p;
+  asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t ld_u64_pol(const uint64_t* a, uint64_t pol) {
+  uint64_t v;
+  asm volatile("ld.global.nc.L2::cache_hint.u64 %0, [%1], %2;" : "=l"(v) : "l"(a), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ uint4 ld_v4_pol(const void* a, uint64_t pol) {
+  uint4 v;
+  asm volatile("ld.global.nc.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
+               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+               : "l"(a), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ ulonglong2 ld_v2u64_pol(const void* a, uint64_t pol) {
+  ulonglong2 v;
+  asm volatile("ld.global.nc.L2::cache_hint.v2.u64 {%0, %1}, [%2], %3;" : "=l"(v.x), "=l"(v.y) : "l"(a), "l"(pol));
+  return v;
+}
 
 __device__ __forceinline__ uint64_t lsel_pred(uint32_t base, uint32_t slope, uint64_t x) {
   return (uint64_t)base + (((uint64_t)slope * x) >> LSEL_FRAC);
@@ -263,10 +306,55 @@ __global__ void lsel_stats_kernel(const uint4* __restrict__ rec, uint64_t nseg, 
   }
 }
 
+// Rank directory: thread per block j of LSEL_DIR_SB superblocks: base[j] =
+// ones before superblock 16 j, base[nblocks] = all ones (the rank table's
+// last entry NB counts the ones before superblock NB, which still holds data
+// when the words are not a multiple of 8: its words are added), res[j][i] =
+// ones before superblock 16 j + i minus base[j] + floor((base[j + 1] -
+// base[j]) i / 16).  Residual 0 is always 0; a block with a residual outside
+// int8 stores LSEL_DIR_OVER there instead.
+__global__ void lsel_dir_kernel(const uint64_t* __restrict__ tbl, const uint64_t* __restrict__ words, uint64_t W,
+                                uint64_t nblocks, uint64_t* __restrict__ base, int8_t* __restrict__ res,
+                                unsigned long long* __restrict__ over) {
+  const uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j > nblocks) return;
+  const uint64_t NB = W >> 3;
+  auto ones_before = [&](uint64_t sb) -> uint64_t {  // superblock sb <= NB, or all ones past it
+    if (sb <= NB) return __ldg(tbl + 2 * sb);
+    uint64_t c = __ldg(tbl + 2 * NB);
+    for (uint64_t w = 8 * NB; w < W; ++w) c += __popcll(__ldg(words + w));
+    return c;
+  };
+  const uint64_t b0 = ones_before(LSEL_DIR_SB * j);
+  base[j] = b0;
+  if (j == nblocks) return;
+  const uint64_t b1 = ones_before(LSEL_DIR_SB * (j + 1));
+  int8_t r[LSEL_DIR_SB];
+  bool bad = false;
+#pragma unroll
+  for (int i = 0; i < LSEL_DIR_SB; ++i) {
+    const uint64_t sb = LSEL_DIR_SB * j + i;
+    long long d = 0;
+    if (sb <= NB) d = (long long)__ldg(tbl + 2 * sb) - (long long)(b0 + (((b1 - b0) * (uint64_t)i) >> 4));
+    bad = bad || d < -127 || d > 127;
+    r[i] = (int8_t)d;
+  }
+  if (bad) {
+    r[0] = LSEL_DIR_OVER;
+    atomicAdd(over, 1ull);
+  }
+  int4* dst = reinterpret_cast<int4*>(res + LSEL_DIR_SB * j);
+  *dst = *reinterpret_cast<const int4*>(r);
+}
+
 struct LselView {
   const uint64_t* words;
   const uint64_t* tbl;
   uint64_t nwords;  // data words of the concatenated bitvector
+  uint64_t total;   // its bits
+  const uint64_t* dbase;
+  const int8_t* dres;
+  uint64_t dblocks;
   uint64_t n;
   int L;
   uint32_t max_window;
@@ -284,75 +372,123 @@ __device__ __noinline__ uint64_t lsel_plain(const SelView* v, uint64_t K, uint64
 }
 
 // Learned search for query (l, k).  Returns the answer, or sets *fallback
-// when the plain select must answer (window above max_window, or a search
-// that did not close).
+// when the plain select must answer (window above max_window, a block whose
+// residuals overflow, or a search that did not close).
 template <int T_B>
 __device__ __forceinline__ uint64_t lsel_search(const LselView& v, uint64_t l, uint64_t k, bool* fallback) {
   if (l >= (uint64_t)v.L) return NONE64;
   const LselLevel d = v.lv[l];
   if (k == 0 || k > d.m) return NONE64;
-  const uint64_t off = l * v.n;
-  const uint64_t K = d.A + k;
-  const uint64_t j = (k - 1) >> d.g;
-  const uint4 r = __ldg(v.rec + d.rec_off + j);
-  const long long dlo = (int)r.z, dhi = (int)r.w;
-  if (dhi < dlo || dhi - dlo > (long long)v.max_window) {
+  const uint64_t keep = l2_policy_last(), stream = l2_policy_first();
+  const uint64_t off = d.off, K = d.A + k, km = k - 1;
+  const uint64_t j = km >> d.g;
+  const uint4 r = ld_v4_pol(v.rec + d.rec_off + j, keep);
+  const int dlo = (int)r.z, dhi = (int)r.w;
+  if (dhi < dlo || (uint32_t)(dhi - dlo) > v.max_window) {
     *fallback = true;
     return 0;
   }
-  const long long pred = (long long)lsel_pred(r.x, r.y, (k - 1) - (j << d.g));
+  const long long pred = (long long)r.x + (long long)(((uint64_t)r.y * (km - (j << d.g))) >> LSEL_FRAC);
   const long long lo = max(pred + dlo, 0ll), hi = min(pred + dhi, (long long)v.n - 1);
-  // superblock indices fit 32 bits: n * L < 2^32 * 24 bits
-  uint32_t s_lo = (uint32_t)((off + (uint64_t)lo) >> 9), s_hi = (uint32_t)((off + (uint64_t)hi) >> 9);
-  uint32_t s = (uint32_t)((off + (uint64_t)min(max(pred, lo), hi)) >> 9);
-  const uint64_t slope = r.y;
-  const uint32_t last_word = (uint32_t)(v.nwords - 1);
-  const ulonglong2* __restrict__ tbl2 = reinterpret_cast<const ulonglong2*>(v.tbl);
-  for (int probe = 0; s_lo <= s_hi && probe < LSEL_MAX_PROBES; ++probe) {
-    const ulonglong2 e = __ldg(tbl2 + s);
-    const uint64_t R = T_B ? e.x : ((uint64_t)s << 9) - e.x;
-    if (R >= K) {  // the answer lies before superblock s
-      if (s == s_lo) break;
-      s_hi = s - 1;
-      if (probe < LSEL_INTERP_PROBES) {
-        const uint64_t back = 1 + ((umin64(R - K + 1, (uint64_t)1 << 31) * slope) >> (LSEL_FRAC + 9));
-        s -= (uint32_t)umin64(back, s - s_lo);
-      } else {
-        s = (s_lo + s_hi) >> 1;
-      }
-      continue;
-    }
-    const uint32_t need = (uint32_t)umin64(K - R, 0xFFFFFFFFu);
-    // counts of the words before word q (q = 1..7) hold only for data words;
-    // the last superblock's fields past its data are zero
-    const uint32_t qmax = min(7u, last_word - (s << 3));
-    uint32_t jw = 0, cb = 0;
+  // directory blocks the window touches; args of this polarity before block
+  // b: ones = dbase[b], zeros = its first bit (clamped to the end) - ones
+  uint64_t b_lo = (off + (uint64_t)lo) >> 13, b_hi = (off + (uint64_t)hi) >> 13;
+  if (b_hi >= v.dblocks) b_hi = v.dblocks - 1;
+  if (b_lo > b_hi) b_lo = b_hi;
+  auto before = [&](uint64_t b, uint64_t ones) -> uint64_t {
+    return T_B ? ones : umin64(b << 13, v.total) - ones;
+  };
+  // the block holding arg K: the last b in [b_lo, b_hi] with before(b) < K;
+  // its first candidate's two counts and residuals load in one round
+  uint64_t c_lo = ld_u64_pol(v.dbase + b_lo, keep), c_hi = ld_u64_pol(v.dbase + b_lo + 1, keep);
+  uint4 rv = ld_v4_pol(reinterpret_cast<const uint4*>(v.dres) + b_lo, keep);
+  if (before(b_lo, c_lo) >= K) {
+    atomicAdd(v.misses, 1ull);
+    *fallback = true;
+    return 0;
+  }
+  uint64_t bb = b_lo;
+  for (int probe = 0; bb < b_hi && probe < LSEL_MAX_PROBES && before(bb + 1, c_hi) < K; ++probe) {
+    ++bb;
+    c_lo = c_hi;
+    c_hi = ld_u64_pol(v.dbase + bb + 1, keep);
+    rv = ld_v4_pol(reinterpret_cast<const uint4*>(v.dres) + bb, keep);
+  }
+  if (before(bb + 1, c_hi) < K) {  // not inside the window's blocks
+    atomicAdd(v.misses, 1ull);
+    *fallback = true;
+    return 0;
+  }
+  if ((int8_t)(rv.x & 0xFFu) == LSEL_DIR_OVER) {
+    *fallback = true;
+    return 0;
+  }
+  // inside the block (32-bit): args before its superblock i are a(i) = t(i)
+  // (ones) or 512 i - t(i) (zeros), t(i) = floor(span i / 16) + residual i;
+  // a rises with i, so a branch-free binary search finds the last
+  // superblock that starts inside the data with a(i) < need (a(0) = 0)
+  const uint32_t span = (uint32_t)(c_hi - c_lo);
+  const uint32_t need_blk = (uint32_t)(K - before(bb, c_lo));
+  const uint64_t bit0 = bb << 13;
+  const uint32_t nvalid = (uint32_t)umin64(LSEL_DIR_SB, (v.total - bit0 + 511) >> 9);  // superblocks with data
+  auto args_before = [&](uint32_t i) -> uint32_t {
+    const uint32_t wsel = (i & 8) ? ((i & 4) ? rv.w : rv.z) : ((i & 4) ? rv.y : rv.x);
+    const int32_t rr = (int32_t)(int8_t)(uint8_t)(wsel >> (8 * (i & 3)));
+    const uint32_t t = ((span * i) >> 4) + (uint32_t)rr;
+    return T_B ? t : 512u * i - t;
+  };
+  uint32_t si = 0;
 #pragma unroll
-    for (int q = 1; q < 8; ++q) {
-      const uint32_t c1 = (uint32_t)(e.y >> (63 - 9 * q)) & 0x1FFu;
-      const uint32_t c = T_B ? c1 : (uint32_t)(64 * q) - c1;
-      if ((uint32_t)q <= qmax && c < need) {
-        jw = (uint32_t)q;
-        cb = c;
-      }
+  for (uint32_t step = 8; step; step >>= 1) {
+    const uint32_t c = si + step;
+    if (c < nvalid && args_before(c) < need_blk) si = c;
+  }
+  const uint32_t need = need_blk - args_before(si);  // 1 .. args in superblock si
+  const uint64_t sb = (bb << 4) + si;
+  // its eight words: one 64-byte line, the four 16-byte loads issued at once
+  // (evict first); a line that is not all data (the bitvector's last one)
+  // takes the guarded path
+  const uint64_t w0 = sb << 3;
+  const bool whole = w0 + 8 < v.nwords || (w0 + 8 == v.nwords && (v.total & 63) == 0);
+  uint64_t wv[8];
+  if (whole) {
+    const ulonglong2* p2 = reinterpret_cast<const ulonglong2*>(v.words + w0);
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+      const ulonglong2 x = ld_v2u64_pol(p2 + h, stream);
+      wv[2 * h] = T_B ? x.x : ~x.x;
+      wv[2 * h + 1] = T_B ? x.y : ~x.y;
     }
-    const uint32_t wi = (s << 3) + jw;
-    uint64_t word = __ldg(v.words + wi);
-    if (!T_B) word = ~word;
-    const uint32_t cnt = (uint32_t)__popcll(word);
-    if (cb + cnt >= need) return ((uint64_t)wi << 6) + sel64(word, need - cb) - off;
-    if (s == s_hi) break;  // the answer lies after superblock s
-    s_lo = s + 1;
-    if (probe < LSEL_INTERP_PROBES) {
-      const uint64_t fwd = ((uint64_t)(need - cb - cnt) * slope) >> (LSEL_FRAC + 9);
-      s = s + 1 + (uint32_t)umin64(fwd, s_hi - s - 1);
-    } else {
-      s = (s_lo + s_hi) >> 1;
+  } else {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const uint64_t wi = w0 + q;
+      uint64_t x = wi < v.nwords ? ld_u64_pol(v.words + wi, stream) : 0ull;
+      if (!T_B) {
+        x = wi < v.nwords ? ~x : 0ull;
+        if (wi == v.nwords - 1 && (v.total & 63)) x &= (1ull << (v.total & 63)) - 1;
+      }
+      wv[q] = x;
     }
   }
-  atomicAdd(v.misses, 1ull);
-  *fallback = true;
-  return 0;
+  // the word holding the need-th arg: the words whose counts before them
+  // are below need, less one
+  uint32_t acc = __popcll(wv[0]), jq = 0, bq = 0;
+  uint64_t wsel = wv[0];
+#pragma unroll
+  for (int q = 1; q < 8; ++q) {
+    const bool past = acc < need;
+    jq += past;
+    bq = past ? acc : bq;
+    wsel = past ? wv[q] : wsel;
+    acc += __popcll(wv[q]);
+  }
+  if (acc < need) {
+    atomicAdd(v.misses, 1ull);
+    *fallback = true;
+    return 0;
+  }
+  return ((w0 + jq) << 6) + sel64(wsel, need - bq) - off;
 }
 
 template <int T_B>
@@ -366,7 +502,7 @@ __global__ void __launch_bounds__(256) lsel_query_kernel(LselView v, const uint6
   uint64_t res = lsel_search<T_B>(v, l, k, &fallback);
   if (fallback) {
     const LselLevel d = v.lv[l];
-    res = lsel_plain(v.plain, d.A + k, l * v.n);
+    res = lsel_plain(v.plain, d.A + k, d.off);
   }
   out[q] = res;
 }
@@ -445,6 +581,8 @@ void lsel_delete(LselImpl* m) {
     m->plain[t].release(nullptr);
   }
   m->stats.release(nullptr);
+  m->dbase.release(nullptr);
+  m->dres.release(nullptr);
   cudaDeviceSynchronize();
   delete m;
 }
@@ -487,6 +625,7 @@ int lsel_build(LselImpl& m, TreeImpl& t, uint32_t segments, uint32_t samples, ui
       d.g = g;
       d.nseg = (uint32_t)((d.m + (1ull << g) - 1) >> g);
       d.rec_off = off;
+      d.off = (uint64_t)l * n;
       off += d.nseg;
     }
     m.nseg[tb] = off;
@@ -499,8 +638,9 @@ int lsel_build(LselImpl& m, TreeImpl& t, uint32_t segments, uint32_t samples, ui
     if ((rc = m.plain[tb].ensure(sizeof(SelView), s))) return rc;
     WTG_CK(cudaMemcpyAsync(m.plain[tb].p, &m.plain_host[tb], sizeof(SelView), cudaMemcpyHostToDevice, s));
   }
-  if ((rc = m.stats.ensure(2 * LSEL_ST * sizeof(uint64_t), s))) return rc;
-  WTG_CK(cudaMemsetAsync(m.stats.p, 0, 2 * LSEL_ST * sizeof(uint64_t), s));
+  // stats: LSEL_ST words per polarity, then the directory's overflow blocks
+  if ((rc = m.stats.ensure((2 * LSEL_ST + 1) * sizeof(uint64_t), s))) return rc;
+  WTG_CK(cudaMemsetAsync(m.stats.p, 0, (2 * LSEL_ST + 1) * sizeof(uint64_t), s));
 
   const int sms = 152;
   for (int tb = 0; tb < 2; ++tb) {
@@ -518,6 +658,19 @@ int lsel_build(LselImpl& m, TreeImpl& t, uint32_t segments, uint32_t samples, ui
         m.lv[1].as<LselLevel>(), m.rec[0].as<uint4>(), m.rec[1].as<uint4>());
     WTG_CK(cudaGetLastError());
   }
+  {
+    // the rank directory over the concatenated bitvector's superblocks 0..NB
+    const uint64_t NB = t.bit_words >> 3;
+    m.dblocks = NB / LSEL_DIR_SB + 1;  // blocks 0 .. NB / 16: every superblock with data
+    if ((rc = m.dbase.ensure((m.dblocks + 1) * sizeof(uint64_t), s))) return rc;
+    if ((rc = m.dres.ensure(m.dblocks * LSEL_DIR_SB, s))) return rc;
+    count_launch();
+    lsel_dir_kernel<<<grid_of(m.dblocks + 1, 256, 1u << 30), 256, 0, s>>>(
+        t.bv.rank.as<uint64_t>(), t.bits.as<uint64_t>(), t.bit_words, m.dblocks, m.dbase.as<uint64_t>(),
+        m.dres.as<int8_t>(),
+        m.stats.as<unsigned long long>() + 2 * LSEL_ST);
+    WTG_CK(cudaGetLastError());
+  }
   for (int tb = 0; tb < 2; ++tb) {
     if (!m.nseg[tb]) continue;
     count_launch();
@@ -530,12 +683,14 @@ int lsel_build(LselImpl& m, TreeImpl& t, uint32_t segments, uint32_t samples, ui
 }
 
 int lsel_info(const LselImpl& m, uint64_t info[8], cudaStream_t s) {
-  uint64_t st[2 * LSEL_ST];
+  uint64_t st[2 * LSEL_ST + 1];
   WTG_CK(cudaMemcpyAsync(st, m.stats.p, sizeof(st), cudaMemcpyDeviceToHost, s));
   WTG_CK(cudaStreamSynchronize(s));
   const uint64_t segs = m.nseg[0] + m.nseg[1];
   info[0] = segs;
-  info[1] = segs * sizeof(uint4) + 2 * (uint64_t)m.L * sizeof(LselLevel);
+  // the index's bytes: segment records, level records and the rank directory
+  info[1] = segs * sizeof(uint4) + 2 * (uint64_t)m.L * sizeof(LselLevel) + (m.dblocks + 1) * sizeof(uint64_t) +
+            m.dblocks * LSEL_DIR_SB;
   info[2] = st[0] + st[LSEL_ST + 0];
   info[3] = std::max(st[1], st[LSEL_ST + 1]);
   info[4] = st[2] + st[LSEL_ST + 2];
@@ -575,6 +730,10 @@ int launch_lsel_query(LselImpl& m, int t_b, const uint64_t* level, const uint64_
   v.words = t.bits.as<uint64_t>();
   v.tbl = t.bv.rank.as<uint64_t>();
   v.nwords = t.bit_words;
+  v.total = t.n * (uint64_t)t.levels;
+  v.dbase = m.dbase.as<uint64_t>();
+  v.dres = m.dres.as<int8_t>();
+  v.dblocks = m.dblocks;
 
   v.n = t.n;
   v.L = t.levels;

@@ -540,7 +540,7 @@ class LearnedSelect:
     def info(self):
         a = np.zeros(8, dtype=np.uint64)
         _ck(lib().wtg_lsel_info(self.h, _p(a)))
-        keys = ("segments", "model_bytes", "fallback_segments", "max_window", "window_sum", "misses",
+        keys = ("segments", "index_bytes", "fallback_segments", "max_window", "window_sum", "misses",
                 "segments_param", "samples_param")
         return {k: int(v) for k, v in zip(keys, a)}
 
