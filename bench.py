@@ -67,6 +67,14 @@ def level_launch_bytes(n, w):
     return 2 * n * w + n / 8
 
 
+def init_ranks(dist, backend, timeout_s):
+    """The process group of a multi-rank run, with a short timeout: a rank
+    that fails or leaves between steps ends the others' next collective with
+    an error instead of a hang."""
+    import datetime
+    dist.init_process_group(backend, timeout=datetime.timedelta(seconds=timeout_s))
+
+
 def slowest_rank(dist, torch, seconds, device):
     """The job's time: the maximum of one value over all ranks (identity
     without a process group)."""
@@ -646,7 +654,7 @@ def run_wtg(args, rank, world, local_rank):
     dist = None
     if world > 1:
         import torch.distributed as dist
-        dist.init_process_group("nccl")
+        init_ranks(dist, "nccl", args.rank_timeout)
     dev = torch.device("cuda", local_rank)
     n = 1 << args.n_log2
     L = LEVELS
@@ -855,6 +863,8 @@ def main():
     ap.add_argument("--fm-cpu-log2", type=int, default=22)
     ap.add_argument("--bytes-log2", type=int, default=24,
                     help="byte-text build (Zipf bytes, 8 levels, rank) of 2^k symbols; 0 skips")
+    ap.add_argument("--rank-timeout", type=float, default=600,
+                    help="seconds a collective waits for the other ranks before it fails")
     ap.add_argument("--batch-shape", default=None,
                     help="fix the batch's shape as tile,whole_max,symbols_per_thread (default: autotuned)")
     ap.add_argument("--batch-texts", type=int, default=4096,

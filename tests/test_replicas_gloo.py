@@ -4,7 +4,9 @@ one independent sequence per rank, no collective on the data path), joined
 by the job-time reduction (maximum over ranks) and the whole-job throughput;
 and two gloo ranks that each drive libwtg's C ABI in their own process
 (a real build checked against the oracle where a GPU is present, the
-no-GPU, argument and injected-allocation-failure paths otherwise)."""
+no-GPU, argument and injected-allocation-failure paths otherwise); and a
+rank that fails between steps: the other rank's next collective ends with
+an error within the process group's timeout instead of hanging."""
 import os
 import socket
 
@@ -129,3 +131,39 @@ def test_two_gloo_ranks_through_libwtg():
                 assert codes[1:3] == [3, 3]  # ERR_CUDA: no GPU, no CPU fallback
         if has_gpu:
             assert out[0][0][-1] != out[0][1][-1]  # independent sequences
+
+
+def _failing_rank(rank, world, port, out):
+    import sys
+    import time
+    for p in (ROOT,):
+        if p not in sys.path:
+            sys.path.insert(0, p)
+    import bench
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world))
+    bench.init_ranks(dist, "gloo", 5)
+    bench.slowest_rank(dist, torch, 1.0, torch.device("cpu"))  # step 1: both ranks
+    if rank == 1:
+        raise RuntimeError("rank 1 fails between steps")
+    t0 = time.perf_counter()
+    try:
+        bench.slowest_rank(dist, torch, 2.0, torch.device("cpu"))  # step 2: the peer is gone
+        out[rank] = ("no error", time.perf_counter() - t0)
+    except Exception as e:  # the collective reports the lost peer
+        out[rank] = (type(e).__name__, time.perf_counter() - t0)
+
+
+def test_failed_rank_ends_the_next_collective():
+    ctx = mp.get_context("spawn")
+    port = _free_port()
+    with ctx.Manager() as m:
+        out = m.dict()
+        procs = [ctx.Process(target=_failing_rank, args=(r, 2, port, out)) for r in range(2)]
+        for p in procs:
+            p.start()
+        for p in procs:
+            p.join(120)
+        assert procs[1].exitcode != 0  # the failing rank
+        assert procs[0].exitcode == 0
+        kind, waited = out[0]
+        assert kind != "no error" and waited < 60
