@@ -96,10 +96,12 @@ __device__ __forceinline__ uint4 ld_v4_pol(const void* a, uint64_t pol) {
                : "l"(a), "l"(pol));
   return v;
 }
-__device__ __forceinline__ ulonglong2 ld_v2u64_pol(const void* a, uint64_t pol) {
-  ulonglong2 v;
-  asm volatile("ld.global.nc.L2::cache_hint.v2.u64 {%0, %1}, [%2], %3;" : "=l"(v.x), "=l"(v.y) : "l"(a), "l"(pol));
-  return v;
+// one 32-byte sector (32-byte aligned) in a single load
+__device__ __forceinline__ void ld_v4u64_pol(const void* a, uint64_t pol, uint64_t& x, uint64_t& y, uint64_t& z,
+                                             uint64_t& w) {
+  asm volatile("ld.global.nc.L2::cache_hint.v4.u64 {%0, %1, %2, %3}, [%4], %5;"
+               : "=l"(x), "=l"(y), "=l"(z), "=l"(w)
+               : "l"(a), "l"(pol));
 }
 
 __device__ __forceinline__ uint64_t lsel_pred(uint32_t base, uint32_t slope, uint64_t x) {
@@ -445,19 +447,18 @@ __device__ __forceinline__ uint64_t lsel_search(const LselView& v, uint64_t l, u
   }
   const uint32_t need = need_blk - args_before(si);  // 1 .. args in superblock si
   const uint64_t sb = (bb << 4) + si;
-  // its eight words: one 64-byte line, the four 16-byte loads issued at once
-  // (evict first); a line that is not all data (the bitvector's last one)
-  // takes the guarded path
+  // its eight words: one 64-byte line, its two 32-byte sectors loaded at
+  // once (evict first); a line that is not all data (the bitvector's last
+  // one) takes the guarded path
   const uint64_t w0 = sb << 3;
   const bool whole = w0 + 8 < v.nwords || (w0 + 8 == v.nwords && (v.total & 63) == 0);
   uint64_t wv[8];
   if (whole) {
-    const ulonglong2* p2 = reinterpret_cast<const ulonglong2*>(v.words + w0);
+    ld_v4u64_pol(v.words + w0, stream, wv[0], wv[1], wv[2], wv[3]);
+    ld_v4u64_pol(v.words + w0 + 4, stream, wv[4], wv[5], wv[6], wv[7]);
+    if (!T_B) {
 #pragma unroll
-    for (int h = 0; h < 4; ++h) {
-      const ulonglong2 x = ld_v2u64_pol(p2 + h, stream);
-      wv[2 * h] = T_B ? x.x : ~x.x;
-      wv[2 * h + 1] = T_B ? x.y : ~x.y;
+      for (int q = 0; q < 8; ++q) wv[q] = ~wv[q];
     }
   } else {
 #pragma unroll
