@@ -373,139 +373,159 @@ __device__ __noinline__ uint64_t lsel_plain(const SelView* v, uint64_t K, uint64
   return p == NONE64 ? NONE64 : p - off;
 }
 
-// Learned search for query (l, k).  Returns the answer, or sets *fallback
-// when the plain select must answer (window above max_window, a block whose
-// residuals overflow, or a search that did not close).
-template <int T_B>
-__device__ __forceinline__ uint64_t lsel_search(const LselView& v, uint64_t l, uint64_t k, bool* fallback) {
-  if (l >= (uint64_t)v.L) return NONE64;
-  const LselLevel d = v.lv[l];
-  if (k == 0 || k > d.m) return NONE64;
+// The learned search, NQ queries per thread taken stage by stage so that
+// each stage's loads for all of them are in flight together: inputs; level
+// and segment records; the window's directory block (counts and residuals);
+// the superblock (branch-free binary search over the residuals) and its one
+// 64-byte line; the word and the in-word select.  A query whose window
+// exceeds max_window, whose block's residuals overflow, or whose search does
+// not close is answered by the plain select, so every answer is the plain
+// select's answer.
+template <int T_B, int NQ>
+__global__ void __launch_bounds__(256) lsel_query_kernel_nq(LselView v, const uint64_t* __restrict__ lev,
+                                                            const uint64_t* __restrict__ kq, uint64_t nq,
+                                                            uint64_t* __restrict__ out) {
   const uint64_t keep = l2_policy_last(), stream = l2_policy_first();
-  const uint64_t off = d.off, K = d.A + k, km = k - 1;
-  const uint64_t j = km >> d.g;
-  const uint4 r = ld_v4_pol(v.rec + d.rec_off + j, keep);
-  const int dlo = (int)r.z, dhi = (int)r.w;
-  if (dhi < dlo || (uint32_t)(dhi - dlo) > v.max_window) {
-    *fallback = true;
-    return 0;
+  const uint64_t q0 = (uint64_t)blockIdx.x * blockDim.x * NQ + threadIdx.x;
+  uint64_t l[NQ], k[NQ], res[NQ];
+  int st[NQ];  // 0 searching, 1 done, 2 fallback
+#pragma unroll
+  for (int i = 0; i < NQ; ++i) {
+    const uint64_t q = q0 + (uint64_t)i * blockDim.x;
+    st[i] = q < nq ? 0 : 1;
+    l[i] = q < nq ? lev[q] : 0;
+    k[i] = q < nq ? kq[q] : 0;
+    res[i] = NONE64;
   }
-  const long long pred = (long long)r.x + (long long)(((uint64_t)r.y * (km - (j << d.g))) >> LSEL_FRAC);
-  const long long lo = max(pred + dlo, 0ll), hi = min(pred + dhi, (long long)v.n - 1);
-  // directory blocks the window touches; args of this polarity before block
-  // b: ones = dbase[b], zeros = its first bit (clamped to the end) - ones
-  uint64_t b_lo = (off + (uint64_t)lo) >> 13, b_hi = (off + (uint64_t)hi) >> 13;
-  if (b_hi >= v.dblocks) b_hi = v.dblocks - 1;
-  if (b_lo > b_hi) b_lo = b_hi;
+  LselLevel d[NQ];
+  uint4 r[NQ];
+  uint64_t K[NQ];
+#pragma unroll
+  for (int i = 0; i < NQ; ++i) {
+    if (st[i] == 0 && (l[i] >= (uint64_t)v.L)) st[i] = 1;
+    if (st[i] == 0) {
+      d[i] = v.lv[l[i]];
+      if (k[i] == 0 || k[i] > d[i].m) st[i] = 1;
+    }
+    if (st[i] == 0) {
+      K[i] = d[i].A + k[i];
+      const uint64_t j = (k[i] - 1) >> d[i].g;
+      r[i] = ld_v4_pol(v.rec + d[i].rec_off + j, keep);
+    }
+  }
+  uint64_t b_lo[NQ], b_hi[NQ], c_lo[NQ], c_hi[NQ];
+  uint4 rv[NQ];
+#pragma unroll
+  for (int i = 0; i < NQ; ++i) {
+    if (st[i] != 0) continue;
+    const int dlo = (int)r[i].z, dhi = (int)r[i].w;
+    if (dhi < dlo || (uint32_t)(dhi - dlo) > v.max_window) {
+      st[i] = 2;
+      continue;
+    }
+    const uint64_t km = k[i] - 1, j = km >> d[i].g;
+    const long long pred = (long long)r[i].x + (long long)(((uint64_t)r[i].y * (km - (j << d[i].g))) >> LSEL_FRAC);
+    const long long lo = max(pred + dlo, 0ll), hi = min(pred + dhi, (long long)v.n - 1);
+    b_lo[i] = (d[i].off + (uint64_t)lo) >> 13;
+    b_hi[i] = (d[i].off + (uint64_t)hi) >> 13;
+    if (b_hi[i] >= v.dblocks) b_hi[i] = v.dblocks - 1;
+    if (b_lo[i] > b_hi[i]) b_lo[i] = b_hi[i];
+    c_lo[i] = ld_u64_pol(v.dbase + b_lo[i], keep);
+    c_hi[i] = ld_u64_pol(v.dbase + b_lo[i] + 1, keep);
+    rv[i] = ld_v4_pol(reinterpret_cast<const uint4*>(v.dres) + b_lo[i], keep);
+  }
   auto before = [&](uint64_t b, uint64_t ones) -> uint64_t {
     return T_B ? ones : umin64(b << 13, v.total) - ones;
   };
-  // the block holding arg K: the last b in [b_lo, b_hi] with before(b) < K;
-  // its first candidate's two counts and residuals load in one round
-  uint64_t c_lo = ld_u64_pol(v.dbase + b_lo, keep), c_hi = ld_u64_pol(v.dbase + b_lo + 1, keep);
-  uint4 rv = ld_v4_pol(reinterpret_cast<const uint4*>(v.dres) + b_lo, keep);
-  if (before(b_lo, c_lo) >= K) {
-    atomicAdd(v.misses, 1ull);
-    *fallback = true;
-    return 0;
-  }
-  uint64_t bb = b_lo;
-  for (int probe = 0; bb < b_hi && probe < LSEL_MAX_PROBES && before(bb + 1, c_hi) < K; ++probe) {
-    ++bb;
-    c_lo = c_hi;
-    c_hi = ld_u64_pol(v.dbase + bb + 1, keep);
-    rv = ld_v4_pol(reinterpret_cast<const uint4*>(v.dres) + bb, keep);
-  }
-  if (before(bb + 1, c_hi) < K) {  // not inside the window's blocks
-    atomicAdd(v.misses, 1ull);
-    *fallback = true;
-    return 0;
-  }
-  if ((int8_t)(rv.x & 0xFFu) == LSEL_DIR_OVER) {
-    *fallback = true;
-    return 0;
-  }
-  // inside the block (32-bit): args before its superblock i are a(i) = t(i)
-  // (ones) or 512 i - t(i) (zeros), t(i) = floor(span i / 16) + residual i;
-  // a rises with i, so a branch-free binary search finds the last
-  // superblock that starts inside the data with a(i) < need (a(0) = 0)
-  const uint32_t span = (uint32_t)(c_hi - c_lo);
-  const uint32_t need_blk = (uint32_t)(K - before(bb, c_lo));
-  const uint64_t bit0 = bb << 13;
-  const uint32_t nvalid = (uint32_t)umin64(LSEL_DIR_SB, (v.total - bit0 + 511) >> 9);  // superblocks with data
-  auto args_before = [&](uint32_t i) -> uint32_t {
-    const uint32_t wsel = (i & 8) ? ((i & 4) ? rv.w : rv.z) : ((i & 4) ? rv.y : rv.x);
-    const int32_t rr = (int32_t)(int8_t)(uint8_t)(wsel >> (8 * (i & 3)));
-    const uint32_t t = ((span * i) >> 4) + (uint32_t)rr;
-    return T_B ? t : 512u * i - t;
-  };
-  uint32_t si = 0;
+  uint64_t w0[NQ];
+  uint32_t need[NQ];
+  uint64_t wv[NQ][8];
 #pragma unroll
-  for (uint32_t step = 8; step; step >>= 1) {
-    const uint32_t c = si + step;
-    if (c < nvalid && args_before(c) < need_blk) si = c;
-  }
-  const uint32_t need = need_blk - args_before(si);  // 1 .. args in superblock si
-  const uint64_t sb = (bb << 4) + si;
-  // its eight words: one 64-byte line, its two 32-byte sectors loaded at
-  // once (evict first); a line that is not all data (the bitvector's last
-  // one) takes the guarded path
-  const uint64_t w0 = sb << 3;
-  const bool whole = w0 + 8 < v.nwords || (w0 + 8 == v.nwords && (v.total & 63) == 0);
-  uint64_t wv[8];
-  if (whole) {
-    ld_v4u64_pol(v.words + w0, stream, wv[0], wv[1], wv[2], wv[3]);
-    ld_v4u64_pol(v.words + w0 + 4, stream, wv[4], wv[5], wv[6], wv[7]);
-    if (!T_B) {
-#pragma unroll
-      for (int q = 0; q < 8; ++q) wv[q] = ~wv[q];
+  for (int i = 0; i < NQ; ++i) {
+    if (st[i] != 0) continue;
+    if (before(b_lo[i], c_lo[i]) >= K[i]) {
+      atomicAdd(v.misses, 1ull);
+      st[i] = 2;
+      continue;
     }
-  } else {
+    uint64_t bb = b_lo[i];
+    for (int probe = 0; bb < b_hi[i] && probe < LSEL_MAX_PROBES && before(bb + 1, c_hi[i]) < K[i]; ++probe) {
+      ++bb;
+      c_lo[i] = c_hi[i];
+      c_hi[i] = ld_u64_pol(v.dbase + bb + 1, keep);
+      rv[i] = ld_v4_pol(reinterpret_cast<const uint4*>(v.dres) + bb, keep);
+    }
+    if (before(bb + 1, c_hi[i]) < K[i] || (int8_t)(rv[i].x & 0xFFu) == LSEL_DIR_OVER) {
+      st[i] = 2;
+      continue;
+    }
+    const uint32_t span = (uint32_t)(c_hi[i] - c_lo[i]);
+    const uint32_t need_blk = (uint32_t)(K[i] - before(bb, c_lo[i]));
+    const uint32_t nvalid = (uint32_t)umin64(LSEL_DIR_SB, (v.total - (bb << 13) + 511) >> 9);
+    const uint4 R = rv[i];
+    auto args_before = [&](uint32_t c) -> uint32_t {
+      const uint32_t wsel = (c & 8) ? ((c & 4) ? R.w : R.z) : ((c & 4) ? R.y : R.x);
+      const int32_t rr = (int32_t)(int8_t)(uint8_t)(wsel >> (8 * (c & 3)));
+      const uint32_t t = ((span * c) >> 4) + (uint32_t)rr;
+      return T_B ? t : 512u * c - t;
+    };
+    uint32_t si = 0;
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      const uint64_t wi = w0 + q;
-      uint64_t x = wi < v.nwords ? ld_u64_pol(v.words + wi, stream) : 0ull;
+    for (uint32_t step = 8; step; step >>= 1) {
+      const uint32_t c = si + step;
+      if (c < nvalid && args_before(c) < need_blk) si = c;
+    }
+    need[i] = need_blk - args_before(si);
+    w0[i] = ((bb << 4) + si) << 3;
+    const bool whole = w0[i] + 8 < v.nwords || (w0[i] + 8 == v.nwords && (v.total & 63) == 0);
+    if (whole) {
+      ld_v4u64_pol(v.words + w0[i], stream, wv[i][0], wv[i][1], wv[i][2], wv[i][3]);
+      ld_v4u64_pol(v.words + w0[i] + 4, stream, wv[i][4], wv[i][5], wv[i][6], wv[i][7]);
       if (!T_B) {
-        x = wi < v.nwords ? ~x : 0ull;
-        if (wi == v.nwords - 1 && (v.total & 63)) x &= (1ull << (v.total & 63)) - 1;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) wv[i][q] = ~wv[i][q];
       }
-      wv[q] = x;
+    } else {
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const uint64_t wi = w0[i] + q;
+        uint64_t x = wi < v.nwords ? ld_u64_pol(v.words + wi, stream) : 0ull;
+        if (!T_B) {
+          x = wi < v.nwords ? ~x : 0ull;
+          if (wi == v.nwords - 1 && (v.total & 63)) x &= (1ull << (v.total & 63)) - 1;
+        }
+        wv[i][q] = x;
+      }
     }
   }
-  // the word holding the need-th arg: the words whose counts before them
-  // are below need, less one
-  uint32_t acc = __popcll(wv[0]), jq = 0, bq = 0;
-  uint64_t wsel = wv[0];
 #pragma unroll
-  for (int q = 1; q < 8; ++q) {
-    const bool past = acc < need;
-    jq += past;
-    bq = past ? acc : bq;
-    wsel = past ? wv[q] : wsel;
-    acc += __popcll(wv[q]);
+  for (int i = 0; i < NQ; ++i) {
+    if (st[i] != 0) continue;
+    uint32_t acc = __popcll(wv[i][0]), jq = 0, bq = 0;
+    uint64_t wsel = wv[i][0];
+#pragma unroll
+    for (int q = 1; q < 8; ++q) {
+      const bool past = acc < need[i];
+      jq += past;
+      bq = past ? acc : bq;
+      wsel = past ? wv[i][q] : wsel;
+      acc += __popcll(wv[i][q]);
+    }
+    if (acc < need[i]) {
+      atomicAdd(v.misses, 1ull);
+      st[i] = 2;
+      continue;
+    }
+    res[i] = ((w0[i] + jq) << 6) + sel64(wsel, need[i] - bq) - d[i].off;
+    st[i] = 1;
   }
-  if (acc < need) {
-    atomicAdd(v.misses, 1ull);
-    *fallback = true;
-    return 0;
+#pragma unroll
+  for (int i = 0; i < NQ; ++i) {
+    const uint64_t q = q0 + (uint64_t)i * blockDim.x;
+    if (q >= nq) continue;
+    if (st[i] == 2) res[i] = lsel_plain(v.plain, d[i].A + k[i], d[i].off);
+    out[q] = res[i];
   }
-  return ((w0 + jq) << 6) + sel64(wsel, need - bq) - off;
-}
-
-template <int T_B>
-__global__ void __launch_bounds__(256) lsel_query_kernel(LselView v, const uint64_t* __restrict__ lev,
-                                                         const uint64_t* __restrict__ kq, uint64_t nq,
-                                                         uint64_t* __restrict__ out) {
-  const uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= nq) return;
-  const uint64_t l = lev[q], k = kq[q];
-  bool fallback = false;
-  uint64_t res = lsel_search<T_B>(v, l, k, &fallback);
-  if (fallback) {
-    const LselLevel d = v.lv[l];
-    res = lsel_plain(v.plain, d.A + k, d.off);
-  }
-  out[q] = res;
 }
 
 unsigned grid_of(uint64_t items, unsigned per_block, unsigned cap) {
@@ -743,12 +763,13 @@ int launch_lsel_query(LselImpl& m, int t_b, const uint64_t* level, const uint64_
   v.rec = m.rec[t_b].as<uint4>();
   v.plain = m.plain[t_b].as<SelView>();
   v.misses = m.stats.as<unsigned long long>() + t_b * LSEL_ST + 3;
-  const unsigned grid = (unsigned)((nq + 255) / 256);
+  constexpr int NQ = 2;  // queries per thread (1, 2, 4 measured: 2 is fastest)
+  const unsigned grid = (unsigned)((nq + 256 * NQ - 1) / (256 * NQ));
   count_launch();
   if (t_b)
-    lsel_query_kernel<1><<<grid, 256, 0, s>>>(v, level, k, nq, out);
+    lsel_query_kernel_nq<1, NQ><<<grid, 256, 0, s>>>(v, level, k, nq, out);
   else
-    lsel_query_kernel<0><<<grid, 256, 0, s>>>(v, level, k, nq, out);
+    lsel_query_kernel_nq<0, NQ><<<grid, 256, 0, s>>>(v, level, k, nq, out);
   WTG_CK(cudaGetLastError());
   return WTG_OK;
 }
