@@ -352,6 +352,7 @@ def measure_fm(torch, wtg, oracle_mod, dev, log2_n, log2_q, cpu_log2):
     qid = torch.repeat_interleave(torch.arange(nq, device=dev), lens)
     pos = starts[qid] + (torch.arange(total, device=dev) - off[:-1][qid])
     pat = tcodes[pos].contiguous()
+    patb = text[pos].contiguous()  # the same patterns as bytes, for the Huffman-shaped tree
     del qid, pos
     dC = torch.from_numpy(fm.C.view(np.int64)).to(dev)
     out = torch.empty(nq, dtype=torch.int64, device=dev)
@@ -366,6 +367,34 @@ def measure_fm(torch, wtg, oracle_mod, dev, log2_n, log2_q, cpu_log2):
     torch.cuda.synchronize()
     q_ms = e0.elapsed_time(e1) / 3
     zero = int((out < 1).sum().item())
+    # the reference FM-index's own tree (fm-index/par/WT.C:44): wt_huff over
+    # the BWT's bytes; the same patterns must give the same counts
+    hf = wtg.HuffmanTree.from_device(bw.data_ptr(), n, wtg.ALL, sp)
+    hf.free()
+    e0, e1 = ev(), ev()
+    e0.record(stream)
+    hf = wtg.HuffmanTree.from_device(bw.data_ptr(), n, wtg.ALL, sp)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    huff_ms = e0.elapsed_time(e1)
+    hist = torch.bincount(text.long(), minlength=256)
+    dCb = torch.zeros(256, dtype=torch.int64, device=dev)
+    dCb[1:] = torch.cumsum(hist, 0)[:-1]
+    outh = torch.empty(nq, dtype=torch.int64, device=dev)
+    runh = lambda: hf.fm_count_device(dCb.data_ptr(), patb.data_ptr(), off.data_ptr(), nq, outh.data_ptr(), sp)  # noqa: E731
+    runh()
+    torch.cuda.synchronize()
+    e0, e1 = ev(), ev()
+    e0.record(stream)
+    for _ in range(3):
+        runh()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    hq_ms = e0.elapsed_time(e1) / 3
+    huff = {"build_ms": huff_ms, "bits": hf.size, "nodes": hf.num_nodes, "count_ms": hq_ms,
+            "count_mqs": nq / (hq_ms / 1e3) / 1e6, "counts_equal_balanced_tree": bool(torch.equal(out, outh))}
+    hf.free()
+    del patb, outh, dCb
     # sorted-order spot check of the suffix array: adjacent suffixes compare
     # by first symbol, then by the inverse array one position on
     s_h = text.cpu().numpy()
@@ -390,7 +419,7 @@ def measure_fm(torch, wtg, oracle_mod, dev, log2_n, log2_q, cpu_log2):
            "n": n, "sigma": sigma, "sa_bwt_ms": sa_ms, "sa_rounds": rounds,
            "sa_msym_per_s": n / (sa_ms / 1e3) / 1e6, "wt_ms": wt_ms, "fm_build_ms": sa_ms + wt_ms,
            "count_queries": nq, "count_ms": q_ms, "count_mqs": nq / (q_ms / 1e3) / 1e6,
-           "counts_below_1": zero, "sa_order_exact": sa_exact, "cpu_suffix_array": cpu}
+           "counts_below_1": zero, "sa_order_exact": sa_exact, "huff": huff, "cpu_suffix_array": cpu}
     del text, sa, bw, codes, tcodes, pat, fm
     torch.cuda.empty_cache()
     return res

@@ -399,6 +399,10 @@ int wtg_huff_select(wtg_huff* h, const uint64_t* i, const uint64_t* sym, uint64_
 int wtg_huff_inverse_select(wtg_huff* h, const uint64_t* idx, uint64_t nq, uint64_t* rank_out, uint64_t* sym_out);
 int wtg_huff_fm_count(wtg_huff* h, const uint64_t* C, const uint8_t* pat, const uint64_t* off, uint64_t npat,
                       uint64_t* out);
+/* the same on device arrays, enqueued on `stream` (offsets must not
+ * decrease; they are not checked on the host) */
+int wtg_huff_fm_count_device(wtg_huff* h, const uint64_t* d_C, const uint8_t* d_pat, const uint64_t* d_off,
+                             uint64_t npat, uint64_t* d_out, void* stream);
 
 /* ---------------------------------------------- sdsl serialize() streams
  * The byte streams sdsl's serialize() writes (what sdsl::store_to_file puts

@@ -131,3 +131,27 @@ def test_fm_index_counts(wtg, oracle):
             k = s.find(pb, k + 1)
         assert got[q] == exp, q
     t.free()
+
+
+def test_fm_count_device_matches_host(wtg, oracle):
+    torch = pytest.importorskip("torch")
+    text = datagen.dna_markov(100000, seed=43)
+    text = np.concatenate([text, np.frombuffer(b"$", np.uint8)])
+    b = oracle.bwt(text, oracle.suffix_array(text))
+    t = wtg.HuffmanTree(b)
+    counts = np.bincount(text, minlength=256).astype(np.uint64)
+    C = np.concatenate([[0], np.cumsum(counts)[:-1]]).astype(np.uint64)
+    rng = np.random.default_rng(5)
+    pats = [text[i:i + m] for i, m in zip(rng.integers(0, text.size - 40, 300), rng.integers(1, 33, 300))]
+    off = np.concatenate([[0], np.cumsum([p.size for p in pats])]).astype(np.uint64)
+    pat = np.concatenate(pats)
+    host = t.fm_count(C, pat, off)
+    dev = torch.device("cuda")
+    dC = torch.from_numpy(C.view(np.int64)).to(dev)
+    dpat = torch.from_numpy(pat).to(dev)
+    doff = torch.from_numpy(off.view(np.int64)).to(dev)
+    dout = torch.empty(len(pats), dtype=torch.int64, device=dev)
+    t.fm_count_device(dC.data_ptr(), dpat.data_ptr(), doff.data_ptr(), len(pats), dout.data_ptr())
+    torch.cuda.synchronize()
+    assert np.array_equal(dout.cpu().numpy().view(np.uint64), host)
+    t.free()

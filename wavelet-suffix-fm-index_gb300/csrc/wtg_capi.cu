@@ -1123,6 +1123,13 @@ int wtg_huff_fm_count(wtg_huff* H, const uint64_t* C, const uint8_t* pat, const 
   return sync_and_check(s, huff_err(h));
 }
 
+int wtg_huff_fm_count_device(wtg_huff* H, const uint64_t* d_C, const uint8_t* d_pat, const uint64_t* d_off,
+                             uint64_t npat, uint64_t* d_out, void* stream) {
+  if (!H || !d_C || (npat && (!d_off || !d_out))) return fail(WTG_ERR_INVALID, "null argument");
+  if (npat == 0) return WTG_OK;
+  return launch_huff_fm_count(*H->h, d_C, d_pat, d_off, npat, d_out, (cudaStream_t)stream);
+}
+
 // ------------------------------------------------ sdsl serialize() streams
 
 int wtg_tree_serialize(wtg_tree* T, void* dst, uint64_t cap, uint64_t* len) {

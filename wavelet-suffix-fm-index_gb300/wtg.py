@@ -131,6 +131,7 @@ _SIGS = {
     "wtg_huff_select": ([vp, vp, vp, u64, vp], i32),
     "wtg_huff_inverse_select": ([vp, vp, u64, vp, vp], i32),
     "wtg_huff_fm_count": ([vp, vp, vp, vp, u64, vp], i32),
+    "wtg_huff_fm_count_device": ([vp, vp, vp, vp, u64, vp, vp], i32),
     "wtg_tree_serialize": ([vp, vp, u64, vp], i32),
     "wtg_tree_sigma": ([vp, vp], i32),
     "wtg_bv_serialize": ([vp, ctypes.c_uint32, vp, u64, vp], i32),
@@ -736,6 +737,11 @@ class HuffmanTree:
         out = np.zeros(off.size - 1, dtype=np.uint64)
         _ck(lib().wtg_huff_fm_count(self.h, _p(C), _p(pat) if pat.size else None, _p(off), out.size, _p(out)))
         return out
+
+    def fm_count_device(self, d_C, d_pat, d_off, npat, d_out, stream=0):
+        """fm_count on device arrays (256 u64 C, u8 patterns, npat + 1 u64
+        offsets, npat u64 counts), enqueued on `stream`."""
+        _ck(lib().wtg_huff_fm_count_device(self.h, vp(d_C), vp(d_pat), vp(d_off), int(npat), vp(d_out), vp(stream)))
 
 
 class Batch:
