@@ -138,7 +138,8 @@ struct BatchSmem {
   uint16_t ctab[256];    // nibble compress table (compress32_tab)
   uint64_t prefix;
   uint64_t ent[BNW][64];
-  uint64_t sdesc[BT];  // select pass: descriptors of the chunk's superblocks
+  uint64_t sdesc[BT];  // select pass: descriptors of the chunk's superblocks (a half block each)
+  uint64_t hwsum[2][BNW / 2];  // select pass: per half, its warps' sums
   uint32_t wend[BATCH_NS];  // level pass: where each slot's run ended
   // two staging buffers for chunks of up to CH_MAX symbols (plus the text's
   // offset from a 16-byte boundary and the last lane's over-read), filled by
@@ -884,7 +885,39 @@ __device__ void batch_r_tile(const BatchArgs& a, uint32_t t, uint32_t r, BatchSm
   batch_signal(&a.done[4 * t + DN_R]);
 }
 
-// ---- S item: select_support_mcl of each polarity of one text
+// ---- S item: select_support_mcl of both polarities of one text, at once:
+// warps 0-3 build select1, warps 4-7 select0, each half with its own named
+// barrier and scan, so that a text pays the phase's latency chain once
+__device__ __forceinline__ void batch_half_sync(uint32_t half) {
+  static_assert(BT == 256, "named barriers of 128 threads");
+  if (half) asm volatile("bar.sync 2, 128;" ::: "memory");  // constant ids: ptxas reserves barriers 0-2 only
+  else asm volatile("bar.sync 1, 128;" ::: "memory");
+}
+
+// exclusive scan of one u64 per thread over a half block; the half's total
+// through *total
+__device__ __forceinline__ uint64_t half_excl_scan(uint64_t v, uint32_t half, BatchSmem& sm, uint64_t* total) {
+  const uint32_t lane = threadIdx.x & 31, hwarp = (threadIdx.x >> 5) & 3;
+  uint64_t inc = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint64_t t = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= (uint32_t)o) inc += t;
+  }
+  if (lane == 31) sm.hwsum[half][hwarp] = inc;
+  batch_half_sync(half);
+  uint64_t before = 0, all = 0;
+#pragma unroll
+  for (int w = 0; w < 4; ++w) {
+    const uint64_t x = sm.hwsum[half][w];
+    before += (w < (int)hwarp) ? x : 0;
+    all += x;
+  }
+  batch_half_sync(half);
+  *total = all;
+  return before + inc - v;
+}
+
 __device__ void batch_s_item(const BatchArgs& a, uint32_t t, BatchSmem& sm) {
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint64_t n = a.so[t + 1] - a.so[t];
@@ -906,8 +939,10 @@ __device__ void batch_s_item(const BatchArgs& a, uint32_t t, BatchSmem& sm) {
   const uint64_t last1 = __ldcg(info + 2), last0 = __ldcg(info + 3);
   const uint32_t logn = (uint32_t)batch_logn(size);
   const uint64_t logn4 = (uint64_t)(uint32_t)(logn * logn * logn * logn);
-  for (int t_b = 1; t_b >= 0; --t_b) {
-    if (!(t_b ? sel1 : sel0)) continue;
+  constexpr uint32_t HT = BT / 2, HNW = BNW / 2;  // threads and warps per half
+  const uint32_t half = warp >> 2, htid = tid & (HT - 1), hwarp = warp & (HNW - 1);
+  const int t_b = half ? 0 : 1;
+  if (t_b ? sel1 : sel0) {
     const uint64_t m = t_b ? m1 : m0;
     const uint64_t nsb = (m + 4095) >> 12;
     const uint64_t last = t_b ? last1 : last0;
@@ -916,13 +951,11 @@ __device__ void batch_s_item(const BatchArgs& a, uint32_t t, BatchSmem& sm) {
     uint64_t* __restrict__ desc = a.desc[t_b] + a.deo[t];
     uint64_t* __restrict__ pool = a.pool[t_b] + a.poo[t_b][t];
     const uint64_t pool_cap = a.poo[t_b][t + 1] - a.poo[t_b][t];
-    if (tid == 0) {
-      sm.run = 0;
-      sm.nlong = 0;
-    }
-    __syncthreads();
-    for (uint64_t i0 = 0; i0 < nsb; i0 += BT) {
-      const uint64_t i = i0 + tid;
+    uint64_t* __restrict__ sdesc = sm.sdesc + half * HT;
+    uint64_t run = 0;  // pool words of the chunks before (the same in every thread of the half)
+    uint32_t nlong = 0;
+    for (uint64_t i0 = 0; i0 < nsb; i0 += HT) {
+      const uint64_t i = i0 + htid;
       uint64_t sz = 0, d = 0;
       if (i < nsb) {
         const uint64_t start = __ldcg(st + i);
@@ -932,21 +965,21 @@ __device__ void batch_s_item(const BatchArgs& a, uint32_t t, BatchSmem& sm) {
         const uint64_t wdt = lng ? hi64(end) + 1 : hi64(span) + 1;
         d = (lng << 7) | wdt;
         sz = lng ? 64 * wdt : wdt;
-        if (lng) atomicAdd(&sm.nlong, 1u);
       }
+      nlong += __popc(__ballot_sync(0xffffffffu, (d >> 7) & 1));  // per warp; summed below
       uint64_t total;
-      const uint64_t off = sm.run + block_excl_scan(sz, sm, &total);
+      const uint64_t off = run + half_excl_scan(sz, half, sm, &total);
       if (i < nsb) {
         if (off + sz > pool_cap) atomicCAS(a.err, 0u, (uint32_t)DERR_SELECT_OVERFLOW);
         desc[i] = (off << 8) | d;
-        sm.sdesc[tid] = (off << 8) | d;
+        sdesc[htid] = (off << 8) | d;
       }
-      __syncthreads();
-      if (tid == 0) sm.run += total;
+      batch_half_sync(half);
+      run += total;
       // fill: warp per superblock of this chunk
-      for (uint64_t j = warp; j < (uint64_t)BT && i0 + j < nsb; j += BNW) {
+      for (uint64_t j = hwarp; j < (uint64_t)HT && i0 + j < nsb; j += HNW) {
         const uint64_t si = i0 + j;
-        const uint64_t dd = sm.sdesc[j];
+        const uint64_t dd = sdesc[j];
         const uint64_t poff = dd >> 8;
         const uint32_t wdt = (uint32_t)(dd & 127);
         if (poff + ((dd >> 7) & 1 ? 64ull * wdt : wdt) > pool_cap) continue;
@@ -992,20 +1025,24 @@ __device__ void batch_s_item(const BatchArgs& a, uint32_t t, BatchSmem& sm) {
             });
         }
       }
-      __syncthreads();
+      batch_half_sync(half);  // sdesc is the next chunk's
     }
     // m_superblock
     uint64_t* __restrict__ sbw = a.sbw[t_b] + a.sbo[t];
     const uint64_t sb_nwords = (nsb * logn + 63) / 64;
-    for (uint64_t q = tid; q < sb_nwords; q += BT)
+    for (uint64_t q = htid; q < sb_nwords; q += HT)
       sbw[q] = packed_word(q, logn, nsb, [&](uint64_t i) { return __ldcg(st + i); });
-    __syncthreads();
-    if (tid == 0) {
-      info[4 + (1 - t_b)] = sm.run;
-      info[6 + (1 - t_b)] = sm.nlong;
+    // long superblocks: every warp of the half counted its lanes' chunks
+    if (lane == 0) sm.hwsum[half][hwarp] = nlong;
+    batch_half_sync(half);
+    if (htid == 0) {
+      uint64_t nl = 0;
+      for (int w = 0; w < (int)HNW; ++w) nl += sm.hwsum[half][w];
+      info[4 + (1 - t_b)] = run;
+      info[6 + (1 - t_b)] = nl;
     }
-    __syncthreads();
   }
+  __syncthreads();
 }
 
 // ---- the rank table and select marks of a whole text in this CTA (its bits
