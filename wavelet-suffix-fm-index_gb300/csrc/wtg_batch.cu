@@ -127,9 +127,6 @@ struct BatchSmem {
   uint64_t wbase[BATCH_NS];           // where the range's members of each slot start
   uint32_t wcnt[2][BNW][BATCH_NP];    // per chunk parity and warp: members per slot pair
   uint32_t scr[BNW][68];              // per warp: a piece being assembled (zero between uses)
-  uint64_t wsum[BNW];
-  uint64_t run;
-  uint32_t nlong;
   uint32_t flag;
   uint32_t sb[RT_SB];
   uint32_t lastw[2];  // rank tile: last word + 1 holding a one / a zero
@@ -184,29 +181,6 @@ __device__ __forceinline__ uint32_t batch_signal(uint32_t* ctr) {
     prev = atomicAdd(ctr, 1u);
   }
   return prev;
-}
-
-// block-wide exclusive scan of one u64 per thread; returns the prefix and
-// the block total through *total
-__device__ __forceinline__ uint64_t block_excl_scan(uint64_t v, BatchSmem& sm, uint64_t* total) {
-  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint64_t inc = v;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint64_t t = __shfl_up_sync(0xffffffffu, inc, o);
-    if (lane >= (uint32_t)o) inc += t;
-  }
-  if (lane == 31) sm.wsum[warp] = inc;
-  __syncthreads();
-  uint64_t before = 0, all = 0;
-  for (int w = 0; w < BNW; ++w) {
-    const uint64_t x = sm.wsum[w];
-    before += (w < (int)warp) ? x : 0;
-    all += x;
-  }
-  __syncthreads();
-  *total = all;
-  return before + inc - v;
 }
 
 // k-th (0-based) arg of a bitvector, found by binary search over the rank
@@ -350,34 +324,13 @@ __device__ void batch_h_item(const BatchArgs& a, uint32_t t, uint32_t j, BatchSm
   batch_signal(&a.done[4 * t + DN_HREADY]);
 }
 
-// Bits of x at the set bits of m, packed to the low end in order: the
-// published compress ("generalized extract") of Warren, Hacker's Delight,
-// 2nd ed., section 7-4 -- five rounds, round i moving each kept bit right by
-// 2^i where bit i of its count of dropped bits below it is set.
-__device__ __forceinline__ uint32_t compress32(uint32_t x, uint32_t m) {
-  x &= m;
-  uint32_t mk = ~m << 1;
-#pragma unroll
-  for (int i = 0; i < 5; ++i) {
-    uint32_t mp = mk ^ (mk << 1);  // parity of the dropped bits below each bit
-    mp ^= mp << 2;
-    mp ^= mp << 4;
-    mp ^= mp << 8;
-    mp ^= mp << 16;
-    const uint32_t mv = mp & m;  // kept bits that move this round
-    m = (m ^ mv) | (mv >> (1 << i));
-    const uint32_t t = x & mv;
-    x = (x ^ t) | (t >> (1 << i));
-    mk &= ~mp;
-  }
-  return x;
-}
-
-// The same compress by nibbles from a table: entry (m4 << 4) | x4 holds the
-// kept bits of nibble x4 under mask nibble m4, and (bit 8 up) 2^(bits kept).
+// Bits of x at the set bits of m, packed to the low end in order
+// ("compress"), by nibbles from a table: entry (m4 << 4) | x4 holds the kept
+// bits of nibble x4 under mask nibble m4, and (bit 8 up) 2^(bits kept).
 // Each nibble's bits land at the running product of those powers: one
-// shared load and two multiply-adds per nibble instead of the 5 x 17
-// logic ops above.
+// shared load and two multiply-adds per nibble, off the integer logic pipe
+// (the logic-op form of Warren, Hacker's Delight, 2nd ed., section 7-4,
+// takes five rounds of about 17 ops).
 __device__ __forceinline__ uint32_t compress32_tab(uint32_t x, uint32_t m, const uint16_t* __restrict__ tab) {
   const uint32_t lo = (x & 0x0F0F0F0Fu) | ((m & 0x0F0F0F0Fu) << 4);
   const uint32_t hi = ((x >> 4) & 0x0F0F0F0Fu) | (m & 0xF0F0F0F0u);
