@@ -948,10 +948,10 @@ __device__ void batch_s_item(const BatchArgs& a, uint32_t t, BatchSmem& sm) {
           }
           const uint32_t start = __shfl_sync(0xffffffffu, sp[0], 0);
           // the block is exactly wdt words (64 entries of wdt bits, wdt <= 32
-          // for a mini block): zero them, OR each entry in at bit e * wdt
-          // (a word and perhaps the next), then store
-          unsigned long long* blk = reinterpret_cast<unsigned long long*>(sm.ent[warp]);
-          if (lane < wdt) blk[lane] = 0;
+          // for a mini block): zero them, OR each entry in at bit e * wdt as
+          // 32-bit halves (a half and perhaps the next), then store
+          uint32_t* blk = reinterpret_cast<uint32_t*>(sm.ent[warp]);
+          if (lane < wdt) blk[2 * lane] = blk[2 * lane + 1] = 0;
           __syncwarp();
 #pragma unroll
           for (int h = 0; h < 2; ++h) {
@@ -959,14 +959,14 @@ __device__ void batch_s_item(const BatchArgs& a, uint32_t t, BatchSmem& sm) {
             const uint64_t k = 4096 * si + 64 * (uint64_t)e;
             // entries past the arg count stay zero; their samples do not exist
             const uint64_t val = k < m ? (uint64_t)(uint32_t)(sp[h] - start) : 0ull;
-            const uint32_t bit = e * wdt, wq = bit >> 6, sh = bit & 63u;
+            const uint32_t bit = e * wdt, wq = bit >> 5, sh = bit & 31u;
             if (val) {
-              atomicOr(blk + wq, (unsigned long long)(val << sh));
-              if (sh + wdt > 64) atomicOr(blk + wq + 1, (unsigned long long)(val >> (64 - sh)));
+              atomicOr(blk + wq, (uint32_t)(val << sh));
+              if (sh + wdt > 32) atomicOr(blk + wq + 1, (uint32_t)(val >> (32 - sh)));
             }
           }
           __syncwarp();
-          if (lane < wdt) pool[poff + lane] = blk[lane];
+          if (lane < wdt) pool[poff + lane] = (uint64_t)blk[2 * lane] | ((uint64_t)blk[2 * lane + 1] << 32);
           __syncwarp();
         } else {
           const uint64_t plo = __ldcg(st + si) >> 9;
