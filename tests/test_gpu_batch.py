@@ -145,3 +145,29 @@ def test_large_texts(wtg, L):
     b.run()
     b.sync()
     _compare(wtg, b, texts, L)
+
+
+@pytest.mark.parametrize("sel", ["select1", "select0"])
+@pytest.mark.parametrize("whole_max", [-1, 0])
+def test_one_select_polarity(wtg, sel, whole_max):
+    """Only one select structure asked for: the other half of the select
+    phase sits out; rank and the asked-for tables equal the single builds',
+    the other polarity is refused."""
+    rng = np.random.default_rng(17)
+    texts = _texts(rng, 50, 2, max_log2=17)
+    flag = wtg.SELECT1 if sel == "select1" else wtg.SELECT0
+    t_b = 1 if sel == "select1" else 0
+    b = wtg.Batch.from_texts(texts, 2, flags=wtg.RANK | flag)
+    b.set_shape(16384, whole_max, 64)
+    b.run()
+    b.sync()
+    for t, s in enumerate(texts):
+        ref = wtg.WaveletTree(np.asarray(s, dtype=np.uint8), levels=2, flags=wtg.ALL)
+        assert np.array_equal(b.bits(t), ref.bits()), t
+        assert np.array_equal(b.rank_table(t), ref.rank_table()), t
+        g, r = b.select_tables(t, t_b), ref.select_tables(t_b)
+        assert np.array_equal(g.sb_words, r.sb_words) and np.array_equal(g.desc, r.desc), t
+        assert np.array_equal(g.pool, r.pool), t
+        with pytest.raises(wtg.WtgError):
+            b.select_tables(t, 1 - t_b)
+        ref.free()
