@@ -7,11 +7,14 @@
 // one persistent kernel pulls work items from a device queue, made at plan
 // time.  A text up to a size bound (at most its fair share of the batch: the
 // total symbols over the resident CTAs) is one item:
-//   X (text)              one CTA builds the whole text: key histogram, every
-//                         level's bits in one pass over the text, the rank
-//                         table and select marks tile by tile with the prefix
-//                         carried, then select_support_mcl -- no waits on
-//                         other CTAs.
+//   X (text)              one CTA builds the whole text: every level's bits in
+//                         one pass over the text (after a key histogram; for
+//                         2 levels none: the level-1 key-1 run goes to a
+//                         per-text stream and is moved into place once the
+//                         key-0 count is known), the rank table and select
+//                         marks a superblock per thread with the prefix
+//                         carried over rounds, then select_support_mcl --
+//                         no waits on other CTAs.
 // A longer text is split over many CTAs, in phase order, each phase's items
 // by decreasing text length:
 //   H (text, tile)        the key histogram of one tile of the text;
@@ -22,10 +25,10 @@
 //                         256 superblocks, the ones before the tile from a
 //                         decoupled look-back over the text's rank tiles
 //                         (the reference layout and final-superblock rule)
-//   S (text)              select_support_mcl per polarity: long/mini choice,
-//                         widths, pool offsets (block scan), mini blocks from
-//                         the samples, long blocks by rank-table search,
-//                         m_superblock packing.
+//   S (text)              select_support_mcl, both polarities at once (a
+//                         half block each): long/mini choice, widths, pool
+//                         offsets (scan), mini blocks from the samples, long
+//                         blocks by rank-table search, m_superblock packing.
 // The split items come first, then the X items by decreasing length.  A
 // split item first waits (bounded) until its text's previous phase is
 // complete: per-text counters, bumped after each item's writes are fenced.
@@ -36,23 +39,27 @@
 // Level bits.  Level l of a text is the text stably sorted by the top l bits
 // of its symbols (levelWT/WT.C:118-190), so the symbols of (level l, key k)
 // form one contiguous run starting at l*n + (symbols whose key is below k),
-// and a range's piece of it starts after the earlier ranges' members.  A warp
-// takes 32 rows of 32 symbols (a lane per symbol) staged in shared memory by
-// cp.async.bulk.  Per row: one ballot per bit plane; level 0 is the top plane
-// itself; for level l >= 1 each lane finds its place in the row stably sorted
-// by key (lanes of smaller keys plus lanes before it with its key, from the
-// planes by logic ops and popcounts) and one OR-reduction of bit << place
-// gives the row's sorted level word, in which every key's members are one
-// segment.  Lane r keeps row r's planes and words; the lanes then count each
-// key's members per row, scan them across the rows, and the CTA places the
-// warps' pieces after one exchange per chunk.  A warp's piece of a key is
-// assembled in shared memory from the rows' segments and stored: the words
-// inside it plainly, its first and last word (shared with neighbouring
-// pieces) with 32-bit atomic ORs on the zeroed bitvector.
+// and a range's piece of it starts after the earlier ranges' members.  A
+// chunk of the text is staged in shared memory by cp.async.bulk; a lane
+// takes one or two rows of 32 symbols.  For 1-2 levels the lane reads its
+// own rows' bytes, forms each bit plane by a multiply-gather (level 0 is the
+// top plane) and compresses the level-1 bits of each key by a nibble table;
+// for 3-4 levels a warp takes 32 rows a lane per symbol: one ballot per bit
+// plane and row, and for level l >= 1 each lane's place in the row stably
+// sorted by key (lanes of smaller keys plus lanes before it with its key,
+// from the planes by logic ops and popcounts), one OR-reduction of
+// bit << place giving the row's sorted level word.  The lanes then count
+// each key's members per row, scan them across the rows, and the CTA places
+// the warps' pieces after one exchange per chunk.  A warp's piece of a key
+// is assembled in shared memory from the rows' segments and stored: the
+// words inside it plainly, its first and last word (shared with
+// neighbouring pieces) with 32-bit atomic ORs on the zeroed bitvector.
 // Every output has the layout of the single-sequence build.  The pool region
 // of each text is sized by a bound that holds for any input (see plan), so
-// the layout is fixed by the text lengths alone.  The memsets plus the launch
-// are captured in a CUDA graph that later runs replay.
+// the layout is fixed by the text lengths alone.  The first run times the
+// candidate shapes (symbols per thread x split tile and whole-text bound)
+// on the batch itself; the memsets plus the launch of the fastest are
+// captured in a CUDA graph that later runs replay.
 
 #include <algorithm>
 #include <numeric>
