@@ -428,6 +428,7 @@ int huff_build(HuffImpl& h, const uint8_t* d_text, uint64_t n, uint32_t flags) {
   WTG_CK(cudaStreamSynchronize(s));
   huff_shape(h, counts);
   const int nn = (int)h.nodes.size();
+  if (nn > HUFF_MAX_NODES) return fail(WTG_ERR_INVALID, "a byte alphabet's Huffman shape has at most 511 nodes");
   const uint64_t W = (h.size + 63) / 64;
   if ((rc = h.bits.ensure((W + 2) * sizeof(uint64_t), s))) return rc;
   WTG_CK(cudaMemsetAsync(h.bits.p, 0, (W + 2) * sizeof(uint64_t), s));
