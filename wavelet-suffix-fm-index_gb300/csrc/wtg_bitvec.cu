@@ -415,8 +415,21 @@ __global__ void __launch_bounds__(256)
   if (ql == 0) desc[i] = (off << 8) | (d & 255);
   if ((d >> 7) & 1) return;  // long block
   const uint32_t wdt = (uint32_t)(d & 127);
-  for (uint32_t q = ql; q < wdt; q += 16)
-    pool[off + q] = packed_word(q, wdt, 64, [&](uint64_t j) { return ent[warp][h][j]; });
+  // entry indices of a word's first and last bit: floor(x / wdt) for
+  // x < 2^11 by one multiply with ceil(2^26 / wdt) (exact for x < 2^20,
+  // wdt <= 64), not two divisions per word
+  const uint64_t rcp = ((1ull << 26) + wdt - 1) / wdt;
+  for (uint32_t q = ql; q < wdt; q += 16) {
+    const uint32_t lo = q * 64;
+    const uint32_t j0 = (uint32_t)(((uint64_t)lo * rcp) >> 26), j1 = (uint32_t)(((uint64_t)(lo + 63) * rcp) >> 26);
+    uint64_t out = 0;
+    for (uint32_t j = j0; j <= j1 && j < 64; ++j) {
+      const uint64_t v = ent[warp][h][j];  // < 2^wdt
+      const int32_t sh = (int32_t)(j * wdt) - (int32_t)lo;
+      out |= sh >= 0 ? (v << sh) : (v >> (-sh));
+    }
+    pool[off + q] = out;
+  }
 }
 
 // m_superblock: entry i = position of arg 4096*i, width logn
