@@ -72,7 +72,10 @@ CASES = [("exp20", 300001, 20, 1024), ("exp20", 1 << 18, 20, 1024), ("zipf8", 10
          ("bin1", 65, 1, 1024), ("tiny5", 37, 5, 4), ("u16_12", 77777, 12, 64), ("allsame", 4099, 3, 1024),
          # n % 512 == 0: the levels start on superblocks and queries go through the compact rank directory
          ("zipf8", 1 << 17, 8, 1024), ("u16_12", 153600, 12, 64), ("bin1", 512, 1, 1024),
-         ("exp20", 1 << 20, 20, 65536), ("tiny5", 1024, 5, 4), ("allsame", 4096, 3, 1024)]
+         ("exp20", 1 << 20, 20, 65536), ("tiny5", 1024, 5, 4), ("allsame", 4096, 3, 1024),
+         # runs of 4096 equal bits: every 8192-bit directory block is half zeros, half ones, so
+         # its superblock residuals overflow int8 and those queries take the plain select
+         ("runs", 1 << 17, 1, 1024), ("runs", 300001, 2, 64)]
 
 
 def _gen(kind, n, seed):
@@ -89,6 +92,8 @@ def _gen(kind, n, seed):
         return rng.integers(0, 4096, n).astype(np.uint16)
     if kind == "allsame":
         return np.full(n, 5, dtype=np.uint8)
+    if kind == "runs":
+        return ((np.arange(n) // 4096) % 4).astype(np.uint8)
     raise ValueError(kind)
 
 
