@@ -83,8 +83,10 @@ int wtg_tree_build(const void* seq, uint64_t n, int elem_bytes, int levels, uint
 
 /* Same as wtg_tree_build, and copies the level bitvector (bit words) and the
  * rank table (rank words, see wtg_tree_info) to host memory while the build
- * runs: the bits of each level leave as soon as its pass is done and the
- * rank table beside the select finishing kernels.  Either destination may be
+ * runs: the bits of each level leave as soon as its pass is done, and the
+ * rank entries of each level as soon as the rank/select pass has covered it
+ * (n % 512 == 0 and a page-locked rank_dst; otherwise the whole rank table
+ * beside the select finishing kernels).  Either destination may be
  * NULL; levels must be given (not 0).  With page-locked destinations the
  * copies overlap the kernels; pageable ones work but wait for each copy.
  * Returns once the build and the copies are complete.  No counterpart in the

@@ -166,8 +166,8 @@ __device__ __forceinline__ uint64_t last_arg_end_sb(const uint64_t* __restrict__
 // when n % 512 == 0: superblock b is chunk c of level l (b = l * n/512 + c),
 // and the zeros before it are the zeros of the levels before l (lvl_zb) plus
 // the chunk's prefix within its level (the level passes' chunk counts,
-// scanned) -- no scan over the bits.  Thread per superblock, grid-stride
-// over each level's superblocks.
+// scanned) -- no scan over the bits.  Levels l0..l1-1; thread per
+// superblock, grid-stride over each level's superblocks.
 //
 // Per word, the work is one in-word select at most (the next 64th one or
 // zero, see word_marks) in 32-bit arithmetic on per-superblock 64-bit bases:
@@ -179,7 +179,7 @@ __device__ __forceinline__ uint64_t last_arg_end_sb(const uint64_t* __restrict__
 // once per superblock; the last word holding a one / a zero is resolved once
 // per thread from the last such superblock.
 __global__ void __launch_bounds__(256)
-    rs_levels_kernel(const uint64_t* __restrict__ words, int L, uint64_t chunks_per_level,
+    rs_levels_kernel(const uint64_t* __restrict__ words, int l0, int l1, uint64_t chunks_per_level,
                      const uint32_t* __restrict__ chunkpre, uint64_t prestride, const uint64_t* __restrict__ lvl_zb,
                      uint32_t flags, uint64_t* __restrict__ rank, uint32_t* __restrict__ samples, uint64_t samp_last,
                      uint64_t* __restrict__ starts1, uint64_t* __restrict__ starts0, uint64_t* __restrict__ ends1,
@@ -193,7 +193,7 @@ __global__ void __launch_bounds__(256)
   uint64_t last_sb1 = ~0ull, last_sb0 = ~0ull;  // last superblocks holding a one / a zero
   // thread per 512-bit superblock: its eight words in four 16-byte loads,
   // counts and fields in registers, one 16-byte rank entry
-  for (int l = 0; l < L; ++l) {
+  for (int l = l0; l < l1; ++l) {
     const uint64_t zl = lvl_zb[l];
     const uint32_t* __restrict__ pre = chunkpre + (uint64_t)l * prestride;
     for (uint64_t c = tid; c < chunks_per_level; c += nthreads) {
@@ -298,25 +298,27 @@ __global__ void rs_levels_totals_kernel(const uint64_t* lvl_zb, int L, uint64_t 
   }
 }
 
-// zeros before every level: lvl_zb[l + 1] = lvl_zb[l] + zeros of level l
+// zeros before levels l0+1..l1: lvl_zb[l + 1] = lvl_zb[l] + zeros of level l,
+// from lvl_zb[l0] (0 for l0 == 0)
 __global__ void level_zeros_kernel(const uint32_t* __restrict__ chunkcnt, const uint32_t* __restrict__ chunkpre,
-                                   uint64_t stride, uint64_t nchunks, int L, uint64_t* __restrict__ lvl_zb) {
-  uint64_t acc = 0;
-  lvl_zb[0] = 0;
-  for (int l = 0; l < L; ++l) {
+                                   uint64_t stride, uint64_t nchunks, int l0, int l1, uint64_t* __restrict__ lvl_zb) {
+  if (l0 == 0) lvl_zb[0] = 0;
+  uint64_t acc = lvl_zb[l0];
+  for (int l = l0; l < l1; ++l) {
     acc += (uint64_t)chunkpre[l * stride + nchunks - 1] + chunkcnt[l * stride + nchunks - 1];
     lvl_zb[l + 1] = acc;
   }
 }
 
-int bv_from_levels(BvSupport& bv, const uint64_t* d_words, uint64_t n, int L, const uint32_t* chunkcnt,
-                   const uint32_t* chunkpre, uint64_t stride, uint64_t nchunks, uint64_t* lvl_zb, uint32_t flags,
-                   uint32_t* d_err, cudaStream_t s) {
-  int rc;
-  const uint64_t size = n * (uint64_t)L;
-  if ((rc = bv_prepare(bv, d_words, size, flags, s))) return rc;
-  const uint64_t W = size / 64, NB = W >> 3, samp_n = W + 2;
-  level_zeros_kernel<<<1, 1, 0, s>>>(chunkcnt, chunkpre, stride, nchunks, L, lvl_zb);
+int bv_levels_begin(BvSupport& bv, const uint64_t* d_words, uint64_t n, int L, uint32_t flags, cudaStream_t s) {
+  return bv_prepare(bv, d_words, n * (uint64_t)L, flags, s);
+}
+
+int bv_levels_pass(BvSupport& bv, uint64_t n, int l0, int l1, const uint32_t* chunkcnt, const uint32_t* chunkpre,
+                   uint64_t stride, uint64_t nchunks, uint64_t* lvl_zb, cudaStream_t s) {
+  if (l1 <= l0) return WTG_OK;
+  const uint64_t samp_n = bv.size / 64 + 2;
+  level_zeros_kernel<<<1, 1, 0, s>>>(chunkcnt, chunkpre, stride, nchunks, l0, l1, lvl_zb);
   count_launch();
   WTG_CK(cudaGetLastError());
   static int sms = 0;
@@ -331,13 +333,19 @@ int bv_from_levels(BvSupport& bv, const uint64_t* d_words, uint64_t n, int L, co
       1, std::min<uint64_t>((per_level + 255) / 256, (uint64_t)sms * 8));
   prof_begin(PROF_BVPASS, s);
   rs_levels_kernel<<<grid, 256, 0, s>>>(
-      d_words, L, n / 512, chunkpre, stride, lvl_zb, flags, bv.rank.as<uint64_t>(), bv.samples.as<uint32_t>(),
-      samp_n - 1, bv.sel[1].starts.as<uint64_t>(), bv.sel[0].starts.as<uint64_t>(), bv.sel[1].ends.as<uint64_t>(),
-      bv.sel[0].ends.as<uint64_t>(), bv.info.as<unsigned long long>());
+      bv.words, l0, l1, n / 512, chunkpre, stride, lvl_zb, bv.flags, bv.rank.as<uint64_t>(),
+      bv.samples.as<uint32_t>(), samp_n - 1, bv.sel[1].starts.as<uint64_t>(), bv.sel[0].starts.as<uint64_t>(),
+      bv.sel[1].ends.as<uint64_t>(), bv.sel[0].ends.as<uint64_t>(), bv.info.as<unsigned long long>());
   prof_end(PROF_BVPASS, s);
   count_launch();
   WTG_CK(cudaGetLastError());
-  rs_levels_totals_kernel<<<1, 1, 0, s>>>(lvl_zb, L, size, NB, (flags & WTG_RANK) ? bv.rank.as<uint64_t>() : nullptr,
+  return WTG_OK;
+}
+
+int bv_levels_end(BvSupport& bv, int L, const uint64_t* lvl_zb, uint32_t* d_err, cudaStream_t s) {
+  const uint64_t NB = bv.size / 512;
+  rs_levels_totals_kernel<<<1, 1, 0, s>>>(lvl_zb, L, bv.size, NB,
+                                         (bv.flags & WTG_RANK) ? bv.rank.as<uint64_t>() : nullptr,
                                          bv.info.as<unsigned long long>());
   count_launch();
   WTG_CK(cudaGetLastError());

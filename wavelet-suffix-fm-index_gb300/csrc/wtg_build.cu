@@ -817,6 +817,16 @@ static void launch_prepass(const void* s, uint64_t n, int L, int K, uint32_t* ti
 
 static uint64_t tile_elems(int) { return CHUNK; }  // counts are kept per 512-symbol chunk
 
+// host memory the device copies to without staging (page-locked or registered)
+static bool page_locked(const void* p) {
+  cudaPointerAttributes pa{};
+  if (cudaPointerGetAttributes(&pa, p) != cudaSuccess) {
+    cudaGetLastError();  // clear the query's error
+    return false;
+  }
+  return pa.type == cudaMemoryTypeHost;
+}
+
 int tree_levels_from_max(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int* levels) {
   cudaStream_t s = t.stream;
   int rc;
@@ -919,6 +929,27 @@ int tree_build(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int L, uint32
   // and (from level K on) its node tables.  With n % 512 == 0 the chunk
   // counts of every level also give the rank/select pass its prefixes.
   const bool rs_from_levels = flags && n > 0 && (n % CHUNK) == 0;
+  // When the rank table goes to page-locked host memory during the build,
+  // the rank/select pass runs level by level after each level pass, and each
+  // level's rank entries are copied while the later levels are built (a copy
+  // to pageable memory would hold the host until it ends); otherwise it is
+  // one launch over all levels after the last pass.
+  const bool rs_by_level = rs_from_levels && t.host_rank && (flags & WTG_RANK) && page_locked(t.host_rank);
+  uint64_t* lvl_zb = nullptr;
+  if (rs_from_levels) {
+    if ((rc = t.scratch.ensure(((uint64_t)L + 1) * sizeof(uint64_t), s))) return rc;
+    lvl_zb = t.scratch.as<uint64_t>();
+    if ((rc = bv_levels_begin(t.bv, t.bits.as<uint64_t>(), n, L, flags, s))) return rc;
+  }
+  const uint64_t rank_words_per_level = 2 * (n / CHUNK);  // rank entries of one level when n % 512 == 0
+  auto copy_rank_level = [&](int l) -> int {
+    const uint64_t off = (uint64_t)l * rank_words_per_level;
+    WTG_CK(cudaEventRecord(t.copy_ev, s));
+    WTG_CK(cudaStreamWaitEvent(t.copy_stream, t.copy_ev, 0));
+    WTG_CK(cudaMemcpyAsync(t.host_rank + off, t.bv.rank.as<uint64_t>() + off, rank_words_per_level * 8,
+                           cudaMemcpyDeviceToHost, t.copy_stream));
+    return WTG_OK;
+  };
   if (n) {
     if (L > 1) {
       if ((rc = t.lvl[0].ensure(n * eb + 16, s))) return rc;
@@ -999,6 +1030,11 @@ int tree_build(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int L, uint32
         count_launch();
         WTG_CK(cudaGetLastError());
       }
+      // a scattering level's chunk prefixes were scanned before its pass
+      if (rs_by_level && l < L - 1) {
+        if ((rc = bv_levels_pass(t.bv, n, l, l + 1, tilecnt, tilepre_all, tst, tiles, lvl_zb, s))) return rc;
+        if ((rc = copy_rank_level(l))) return rc;
+      }
     }
   }
 
@@ -1008,21 +1044,23 @@ int tree_build(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int L, uint32
     uint32_t* last_cnt = tilecnt + (uint64_t)(L - 1) * tst;
     uint32_t* last_pre = tilepre_all + (uint64_t)(L - 1) * tst;
     if ((rc = scan_exclusive_u32(last_cnt, last_pre, tiles, t.scan_tmp, d_err, s))) return rc;
-    if ((rc = t.scratch.ensure(((uint64_t)L + 1) * sizeof(uint64_t), s))) return rc;
-    if ((rc = bv_from_levels(t.bv, t.bits.as<uint64_t>(), n, L, tilecnt, tilepre_all, tst, tiles,
-                             t.scratch.as<uint64_t>(), flags, d_err, s)))
+    if ((rc = bv_levels_pass(t.bv, n, rs_by_level ? L - 1 : 0, L, tilecnt, tilepre_all, tst, tiles, lvl_zb, s)))
       return rc;
+    if (rs_by_level && (rc = copy_rank_level(L - 1))) return rc;
+    if ((rc = bv_levels_end(t.bv, L, lvl_zb, d_err, s))) return rc;
   } else if (flags) {
     if ((rc = bv_build(t.bv, t.bits.as<uint64_t>(), n * (uint64_t)L, flags, d_err, s))) return rc;
   }
   if (t.bv.rank_done) {
-    // the rank table was complete before the select finishing kernels
-    // started; its copy runs beside them
+    // the rank table (level by level: the rest, its final pair) was complete
+    // before the select finishing kernels started; its copy runs beside them
     const uint64_t size = n * (uint64_t)L;
     const uint64_t cap = (size + 63) / 64 * 64;
     const uint64_t rank_words = size ? ((cap >> 9) + 1) * 2 : 2;
+    const uint64_t from = rs_by_level ? rank_words - 2 : 0;
     WTG_CK(cudaStreamWaitEvent(t.copy_stream, t.bv.rank_done, 0));
-    WTG_CK(cudaMemcpyAsync(t.host_rank, t.bv.rank.p, rank_words * 8, cudaMemcpyDeviceToHost, t.copy_stream));
+    WTG_CK(cudaMemcpyAsync(t.host_rank + from, t.bv.rank.as<uint64_t>() + from, (rank_words - from) * 8,
+                           cudaMemcpyDeviceToHost, t.copy_stream));
     t.bv.rank_done = nullptr;
   }
   return WTG_OK;

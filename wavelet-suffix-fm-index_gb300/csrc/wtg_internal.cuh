@@ -392,10 +392,14 @@ int bv_pass(BvSupport& bv, uint32_t* d_err, cudaStream_t s);
 int bv_finish(BvSupport& bv, uint32_t* d_err, cudaStream_t s);
 // for a wavelet tree's bits with n % 512 == 0: the same structures from the
 // level passes' per-chunk zero counts (chunkcnt) and their scans (chunkpre),
-// both [L][stride]; lvl_zb receives L + 1 words
-int bv_from_levels(BvSupport& bv, const uint64_t* d_words, uint64_t n, int L, const uint32_t* chunkcnt,
-                   const uint32_t* chunkpre, uint64_t stride, uint64_t nchunks, uint64_t* lvl_zb, uint32_t flags,
-                   uint32_t* d_err, cudaStream_t s);
+// both [L][stride], in three steps: allocate and clear; the pass over levels
+// l0..l1-1 (once over all levels, or level by level in order as each level's
+// bits and chunk prefixes are final), which extends lvl_zb (L + 1 words, the
+// zeros before each level) to l1; the totals and the select finishing kernels
+int bv_levels_begin(BvSupport& bv, const uint64_t* d_words, uint64_t n, int L, uint32_t flags, cudaStream_t s);
+int bv_levels_pass(BvSupport& bv, uint64_t n, int l0, int l1, const uint32_t* chunkcnt, const uint32_t* chunkpre,
+                   uint64_t stride, uint64_t nchunks, uint64_t* lvl_zb, cudaStream_t s);
+int bv_levels_end(BvSupport& bv, int L, const uint64_t* lvl_zb, uint32_t* d_err, cudaStream_t s);
 void bv_release(BvSupport& bv, cudaStream_t s);
 
 }  // namespace wtg
