@@ -17,7 +17,8 @@
  *            in heap order, with 4-byte (uintT) or 8-byte (-DLONG) fields and
  *            UINT_T_MAX for absent links (wavelet/levelWT/WT.h:30-35).  Node
  *            records the reference never writes are zero here.
- *   rank   : rank_support_v<1> m_basic_block, ((capacity>>9)+1)*2 words
+ *   rank   : rank_support_v<1> m_basic_block, ((capacity>>9)+1)*2 words, with
+ *            capacity = the bit count rounded up to a multiple of 64
  *            (rank/rank_support_v_par.hpp:78-113).
  *   select : select_support_mcl<t_b> as three flat arrays:
  *            sb_words = the int_vector<0> data of m_superblock (width logn);
@@ -86,7 +87,9 @@ int wtg_tree_build(const void* seq, uint64_t n, int elem_bytes, int levels, uint
  * runs: the bits of each level leave as soon as its pass is done, and the
  * rank entries of each level as soon as the rank/select pass has covered it
  * (n % 512 == 0 and a page-locked rank_dst; otherwise the whole rank table
- * beside the select finishing kernels).  Either destination may be
+ * beside the select finishing kernels).  A page-locked input of at least
+ * 2^22 symbols is copied in eight pieces, and the build's first pass counts
+ * each piece as it lands.  Either destination may be
  * NULL; levels must be given (not 0).  With page-locked destinations the
  * copies overlap the kernels; pageable ones work but wait for each copy.
  * Returns once the build and the copies are complete.  No counterpart in the

@@ -76,12 +76,12 @@ struct LvShape {
 
 template <typename T>
 __global__ void __launch_bounds__(LV_THREADS) prepass_kernel(const T* __restrict__ s, uint64_t n, int L, int K,
-                                                             int vec_ok, uint32_t* __restrict__ chunkcnt,
+                                                             int vec_ok, uint64_t c_begin, uint64_t c_end,
+                                                             uint32_t* __restrict__ chunkcnt,
                                                              uint32_t* __restrict__ hist) {
   const uint32_t lane = threadIdx.x & 31;
   const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-  const uint64_t nchunks = (n + CHUNK - 1) / CHUNK;
   const int top = L - 1;
   const int top2 = K > 1 ? L - 2 : 0;
   uint32_t c1 = 0, c2 = 0, c12 = 0, cnt = 0;  // top bit set, second bit set, both, symbols
@@ -117,11 +117,11 @@ __global__ void __launch_bounds__(LV_THREADS) prepass_kernel(const T* __restrict
     const uint32_t wz = __reduce_add_sync(0xffffffffu, ones);
     if (lane == 0) chunkcnt[c] = cv - wz;  // zeros of level 0 in this chunk
   };
-  // two chunks per step, both loaded before either is counted
-  for (uint64_t c = gw; c < nchunks; c += 2 * nwarps) {
+  // chunks c_begin..c_end-1, two per step, both loaded before either is counted
+  for (uint64_t c = c_begin + gw; c < c_end; c += 2 * nwarps) {
     const uint64_t cb = c + nwarps;
     const bool fa = vec_ok && (c + 1) * CHUNK <= n;
-    const bool fb = vec_ok && cb < nchunks && (cb + 1) * CHUNK <= n;
+    const bool fb = vec_ok && cb < c_end && (cb + 1) * CHUNK <= n;
     uint4 va[NV], vb[NV];
     if (fa) {
       const uint4* q = (const uint4*)(s + c * CHUNK);
@@ -134,7 +134,7 @@ __global__ void __launch_bounds__(LV_THREADS) prepass_kernel(const T* __restrict
       for (int j = 0; j < NV; ++j) vb[j] = __ldg(&q[j * 32 + lane]);
     }
     chunk(c, fa, va);
-    if (cb < nchunks) chunk(cb, fb, vb);
+    if (cb < c_end) chunk(cb, fb, vb);
   }
   // bins of the top K bits (K = 1: bins 0/1 = top bit 0/1)
   uint32_t h[4] = {cnt - c1 - c2 + c12, c2 - c12, c1 - c12, c12};
@@ -798,13 +798,13 @@ static void launch_level(const LevelArgs& a, cudaStream_t st) {
 }
 
 template <typename T>
-static void launch_prepass(const void* s, uint64_t n, int L, int K, uint32_t* tilecnt, uint32_t* hist,
-                           cudaStream_t st) {
-  const uint64_t chunks = (n + CHUNK - 1) / CHUNK;
+static void launch_prepass(const void* s, uint64_t n, int L, int K, uint64_t c_begin, uint64_t c_end,
+                           uint32_t* tilecnt, uint32_t* hist, cudaStream_t st) {
+  const uint64_t chunks = c_end - c_begin;
   unsigned grid = (unsigned)std::min<uint64_t>((chunks + 7) / 8, (uint64_t)sm_count() * 8);
   if (grid == 0) grid = 1;
   const int vec_ok = ((uintptr_t)s % 16) == 0;
-  prepass_kernel<T><<<grid, LV_THREADS, 0, st>>>((const T*)s, n, L, K, vec_ok, tilecnt, hist);
+  prepass_kernel<T><<<grid, LV_THREADS, 0, st>>>((const T*)s, n, L, K, vec_ok, c_begin, c_end, tilecnt, hist);
 }
 
 #define WTG_DISPATCH(eb, fn, ...)                       \
@@ -817,8 +817,9 @@ static void launch_prepass(const void* s, uint64_t n, int L, int K, uint32_t* ti
 
 static uint64_t tile_elems(int) { return CHUNK; }  // counts are kept per 512-symbol chunk
 
-// host memory the device copies to without staging (page-locked or registered)
-static bool page_locked(const void* p) {
+// host memory the device copies to and from without staging (page-locked or
+// registered)
+bool host_page_locked(const void* p) {
   cudaPointerAttributes pa{};
   if (cudaPointerGetAttributes(&pa, p) != cudaSuccess) {
     cudaGetLastError();  // clear the query's error
@@ -897,11 +898,27 @@ int tree_build(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int L, uint32
   if (n) WTG_CK(cudaMemsetAsync(tilecnt, 0, (uint64_t)L * tst * sizeof(uint32_t), s));
 
   if (n) {
+    const uint64_t nchunks = (n + CHUNK - 1) / CHUNK;
     prof_begin(PROF_HIST, s);
-    WTG_DISPATCH(eb, launch_prepass, d_seq, n, L, K, tilecnt, S, s);
+    if (t.in_pieces > 0) {
+      // each piece of the input is counted once its copy has landed; the
+      // passes after the pre-pass see the whole input
+      for (int i = 0; i < t.in_pieces; ++i) {
+        const uint64_t c0 = std::min<uint64_t>(nchunks, (uint64_t)i * t.in_piece_chunks);
+        const uint64_t c1 = std::min<uint64_t>(nchunks, c0 + t.in_piece_chunks);
+        WTG_CK(cudaStreamWaitEvent(s, t.in_ev[i], 0));
+        if (c1 > c0) {
+          WTG_DISPATCH(eb, launch_prepass, d_seq, n, L, K, c0, c1, tilecnt, S, s);
+          count_launch();
+          WTG_CK(cudaGetLastError());
+        }
+      }
+    } else {
+      WTG_DISPATCH(eb, launch_prepass, d_seq, n, L, K, 0, nchunks, tilecnt, S, s);
+      count_launch();
+      WTG_CK(cudaGetLastError());
+    }
     prof_end(PROF_HIST, s);
-    count_launch();
-    WTG_CK(cudaGetLastError());
   }
   if ((rc = scan_exclusive_u32(S, S, (1ull << K) + 1, t.scan_tmp, d_err, s))) return rc;
   {
@@ -934,7 +951,7 @@ int tree_build(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int L, uint32
   // level's rank entries are copied while the later levels are built (a copy
   // to pageable memory would hold the host until it ends); otherwise it is
   // one launch over all levels after the last pass.
-  const bool rs_by_level = rs_from_levels && t.host_rank && (flags & WTG_RANK) && page_locked(t.host_rank);
+  const bool rs_by_level = rs_from_levels && t.host_rank && (flags & WTG_RANK) && host_page_locked(t.host_rank);
   uint64_t* lvl_zb = nullptr;
   if (rs_from_levels) {
     if ((rc = t.scratch.ensure(((uint64_t)L + 1) * sizeof(uint64_t), s))) return rc;
@@ -1088,6 +1105,16 @@ void tree_release(TreeImpl& t) {
   if (t.copy_ev) cudaEventDestroy(t.copy_ev);
   if (t.rank_ev) cudaEventDestroy(t.rank_ev);
   t.copy_ev = t.rank_ev = nullptr;
+  if (t.in_stream) {
+    cudaStreamSynchronize(t.in_stream);
+    cudaStreamDestroy(t.in_stream);
+    t.in_stream = nullptr;
+  }
+  for (cudaEvent_t& e : t.in_ev) {
+    if (e) cudaEventDestroy(e);
+    e = nullptr;
+  }
+  t.in_pieces = 0;
   lsel_detach_all(t);
   t.seq.release(s);
   t.lvl[0].release(s);

@@ -37,6 +37,8 @@ using namespace wtg;
 namespace {
 
 constexpr int MAX_LEVELS = 24;
+// inputs of at least this many symbols are copied in pieces by wtg_tree_build_out
+constexpr uint64_t IN_PIECE_MIN_SYMBOLS = 1ull << 22;
 
 int check_device() {
   int n = 0;
@@ -231,9 +233,39 @@ int wtg_tree_build_out(const void* seq, uint64_t n, int elem_bytes, int levels, 
     if (fresh) wtg_tree_free(T);
     return cuda_fail(e, "stream/event create");
   }
+  // a large page-locked input is copied in pieces on in_stream, and the
+  // build's pre-pass counts each piece as it lands (the levels are known, so
+  // nothing else reads the input before the pre-pass is done)
+  const int pieces = (levels > 0 && n >= IN_PIECE_MIN_SYMBOLS && host_page_locked(seq)) ? TreeImpl::IN_PIECES_MAX : 0;
+  if (e == cudaSuccess && pieces && !t.in_stream) e = cudaStreamCreateWithFlags(&t.in_stream, cudaStreamNonBlocking);
+  for (int i = 0; e == cudaSuccess && i < pieces; ++i)
+    if (!t.in_ev[i]) e = cudaEventCreateWithFlags(&t.in_ev[i], cudaEventDisableTiming);
+  if (e != cudaSuccess) {
+    if (fresh) wtg_tree_free(T);
+    return cuda_fail(e, "stream/event create");
+  }
   if ((rc = t.seq.ensure(n * elem_bytes, t.stream)) == WTG_OK) {
     cudaError_t ce = cudaSuccess;
-    if (n) ce = cudaMemcpyAsync(t.seq.p, seq, n * elem_bytes, cudaMemcpyHostToDevice, t.stream);
+    if (pieces) {
+      // the pieces start after everything queued on the build stream (the
+      // buffer's allocation, a previous build's reads of it)
+      const uint64_t nchunks = (n + 511) / 512;
+      const uint64_t per = (nchunks + pieces - 1) / pieces;
+      ce = cudaEventRecord(t.in_ev[0], t.stream);
+      if (ce == cudaSuccess) ce = cudaStreamWaitEvent(t.in_stream, t.in_ev[0], 0);
+      for (int i = 0; ce == cudaSuccess && i < pieces; ++i) {
+        const uint64_t lo = std::min<uint64_t>(n, (uint64_t)i * per * 512);
+        const uint64_t hi = std::min<uint64_t>(n, ((uint64_t)i + 1) * per * 512);
+        if (hi > lo)
+          ce = cudaMemcpyAsync((char*)t.seq.p + lo * elem_bytes, (const char*)seq + lo * elem_bytes,
+                               (hi - lo) * elem_bytes, cudaMemcpyHostToDevice, t.in_stream);
+        if (ce == cudaSuccess) ce = cudaEventRecord(t.in_ev[i], t.in_stream);
+      }
+      t.in_pieces = pieces;
+      t.in_piece_chunks = per;
+    } else if (n) {
+      ce = cudaMemcpyAsync(t.seq.p, seq, n * elem_bytes, cudaMemcpyHostToDevice, t.stream);
+    }
     if (ce != cudaSuccess) rc = cuda_fail(ce, "cudaMemcpyAsync(seq)");
   }
   t.host_bits = bits_dst;
@@ -241,12 +273,16 @@ int wtg_tree_build_out(const void* seq, uint64_t n, int elem_bytes, int levels, 
   if (rc == WTG_OK) rc = build_tree_common(T, t.seq.p, n, elem_bytes, levels, flags);
   t.host_bits = nullptr;
   t.host_rank = nullptr;
+  t.in_pieces = 0;
   if (rc == WTG_OK) rc = sync_and_check(t.stream, t.err.as<uint32_t>());
   if (rc == WTG_OK) {
     const cudaError_t ce = cudaStreamSynchronize(t.copy_stream);
     if (ce != cudaSuccess) rc = cuda_fail(ce, "copies of the outputs");
   }
   if (rc != WTG_OK) {
+    // a build that stopped before its pre-pass waited for every piece
+    // leaves no copy in flight into the tree's input buffer
+    if (pieces) cudaStreamSynchronize(t.in_stream);
     if (fresh) wtg_tree_free(T);
     return rc;
   }

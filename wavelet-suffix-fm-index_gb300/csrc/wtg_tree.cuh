@@ -42,10 +42,21 @@ struct TreeImpl {
   uint64_t* host_rank = nullptr;
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t copy_ev = nullptr, rank_ev = nullptr;
+  // input arriving in pieces (wtg_tree_build_out from page-locked memory):
+  // piece i holds chunks [i * in_piece_chunks, (i + 1) * in_piece_chunks) of
+  // 512 symbols and is on the device once in_ev[i] has fired; the pre-pass
+  // counts each piece as it lands.  in_pieces = 0: the input is resident.
+  static constexpr int IN_PIECES_MAX = 8;
+  cudaStream_t in_stream = nullptr;
+  cudaEvent_t in_ev[IN_PIECES_MAX] = {};
+  int in_pieces = 0;
+  uint64_t in_piece_chunks = 0;
   std::vector<LselImpl*> deps;  // learned select indexes reading this tree
 };
 
 int tree_levels_from_max(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int* levels);
+// page-locked or registered host memory (copies need no staging)
+bool host_page_locked(const void* p);
 int tree_build(TreeImpl& t, const void* d_seq, uint64_t n, int eb, int L, uint32_t flags);
 int tree_nodes(TreeImpl& t, int ib, uint64_t n_entries, void* d_out);
 void tree_release(TreeImpl& t);
